@@ -1,0 +1,406 @@
+"""Benchmark: split-field FDTD on the curvilinear strip-waveguide bend.
+
+Workload (the configuration the headline metric is quoted on): a silicon strip
+90-degree bend (R = 2 um, core 0.45 x 0.22 um, eps 12.11 in 2.085) in
+orthogonal curvilinear coordinates, 256 x 192 x 160 cells with nonuniform
+metric factors (15-25 nm), 12-cell split PML on all faces; a batch of 8
+excitations (2 ports x 4 guided modes, TE0/TM0/TE1/TM1 sheets); Gaussian pulse
+source; FP64-accumulated running DFT at 21 wavelengths (1.50-1.60 um) on both
+port planes.  Seeded synthetic structure (no dataset).
+
+One bench "step" = one Yee step (the reference main_calc) of every excitation
+of the batch.  Reported:
+  value      FP32 batched Gcell-updates/s, device-resident, K timed steps
+  e2e        the same metric through the C ABI from host buffers: plan creation
+             (host precompute + uploads), incident sheets, schedule, a full
+             8000-step run and the DFT read-back, per simulated step
+  fp64       the plain FP64 (bit-identical to the reference) kernel: Gcell/s
+  s_cols     S-matrix columns per second of full 8000-step runs, FP32 batched
+             and FP64 plain, and the max relative S-parameter error FP32 vs FP64
+  roofline   achieved HBM GB/s of the dominant kernel (the FP32 sweeps) from
+             algorithmic bytes / CUDA-event launch time, against MEASURED_PEAKS.json
+  cpu_baseline  the CPU oracle (a restatement of the reference main_calc) on a
+             bounded sample of the same workload on this host's cores
+
+`--impl reference` times the reference CPU implementation instead (the
+oracle; all host cores as independent processes, one excitation each).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s & S-cols/s: batched FP32 vs plain FP64 on 1 GB300 at stated error"
+LAMS = list(np.linspace(1.50, 1.60, 21))
+FULL_STEPS = 8000
+BATCH = 8
+WORKLOAD = ("bend 256x192x160 curvilinear (R=2um, Si strip in SiO2), 12-cell split PML on 6 faces, "
+            "batch 8 = 2 ports x 4 modes, Gaussian pulse, FP64 DFT at 21 wavelengths on 2 port planes")
+
+
+def algorithmic_bytes_per_step(n3, n_split, batch, s_f=4, coef_bytes=24):
+    """Compulsory HBM traffic of one step: every field component read and
+    written once per excitation (12*s_f per cell), the per-cell coefficients
+    once per step (shared by the batch), the aux slot of split cells read and
+    written per excitation; sigma tables and DFT samples excluded."""
+    return n3 * (12 * s_f * batch + coef_bytes) + n_split * 12 * s_f * batch
+
+
+class Clocks:
+    """nvidia-smi sampling in the background during the timed regions."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def make_workload(shape=(256, 192, 160)):
+    from smatranem_gb300 import workloads as W
+    bend = W.bend_structure(shape=shape)
+    pr = W.prepare(bend.s, dt_factor=1.0 / 0.99)
+    modes = W.mode_profiles(bend)
+    return bend, pr, modes
+
+
+def excitations(bend, modes):
+    """(port plane, inci_mode sign, Hinc, Einc) for 2 ports x 4 modes."""
+    out = []
+    for port, (plane, sign) in enumerate(((bend.iI, 1), (bend.iT - 2, -1))):
+        for Hinc, Einc in modes:
+            out.append((plane, sign, Hinc, Einc))
+    return out
+
+
+def make_plan(bend, pr, modes, precision, batch, nsteps, stream=None):
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    s = bend.s
+    p = F.Plan.create(s.L, s.iBc, (bend.iB, bend.iT, bend.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
+                      pr.sigma, precision=precision, batch=batch, stream=stream)
+    ex = excitations(bend, modes)
+    for b in range(batch):
+        plane, sign, Hinc, Einc = ex[b % len(ex)]
+        p.set_incident(b, Hinc, Einc)
+        p.set_source_plane(b, plane, sign)
+    src, ph = W.pulse_schedule(nsteps, pr.dt, lams_um=LAMS)
+    p.set_schedule(src, planes=(bend.iB, bend.iT), phase=ph)
+    return p
+
+
+def s_parameters(p, bend, modes, b):
+    """|S|^2-style complex overlaps: [port plane][lambda][mode]."""
+    from smatranem_gb300 import workloads as W
+    S = np.zeros((2, len(LAMS), len(modes)), np.complex128)
+    for q in range(2):
+        for f in range(len(LAMS)):
+            d = p.get_dft(b, f, q)
+            for m, (Hinc, Einc) in enumerate(modes):
+                S[q, f, m] = W.overlap(d, Hinc, Einc)
+    return S
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle) -- bounded samples
+# ---------------------------------------------------------------------------
+
+def _cpu_worker(args):
+    """One process: `nsteps` oracle main_calc steps of the full bend, one excitation."""
+    shape, nsteps, kind = args
+    import oracle
+    bend, pr, modes = make_workload(shape)
+    o = oracle.Oracle(kind)
+    Ah, Bh, Ae, Be = pr.coefficients()
+    s = bend.s
+    n3 = s.n3
+    pl = s.L[0] * s.L[1]
+    H = np.zeros(3 * (n3 + pr.lnotn + 1))
+    E = np.zeros_like(H)
+    Hinc, Einc = modes[0]
+    rng = np.random.default_rng(0)
+    H[:3 * n3] = rng.standard_normal(3 * n3) * 1e-3
+    mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+    t0 = time.perf_counter()
+    o.time_loop(s.L, Ah, Bh, Ae, Be, s.iBc, H, E, (bend.iB, bend.iT, bend.iI, 1), Hinc, Einc, pr.n2pi, (1, 1, 3),
+                0, nsteps, *mons, pr.cont, pr.addr)
+    return time.perf_counter() - t0, n3 * nsteps
+
+
+def cpu_rate(nproc, shape, nsteps, kind):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(nproc) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_worker, [(shape, nsteps, kind)] * nproc)
+        wall = time.perf_counter() - t0
+    cells = sum(r[1] for r in res)
+    tmax = max(r[0] for r in res)
+    return cells / tmax, tmax, wall
+
+
+def oracle_kind():
+    import oracle
+    oracle.build()
+    if oracle.reference_available():
+        try:
+            oracle.Oracle("reference")
+            return "reference"
+        except OSError:
+            pass
+    return "port"
+
+
+# ---------------------------------------------------------------------------
+# runs
+# ---------------------------------------------------------------------------
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+    return ws, rank, local
+
+
+def dist_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args):
+    ws, rank, local = dist_setup()
+    if rank != 0:
+        return
+    kind = oracle_kind()
+    nproc = os.cpu_count() or 1
+    shape = (256, 192, 160)
+    nsteps = args.ref_steps
+    t_all = time.perf_counter()
+    rate, tmax, wall = cpu_rate(nproc, shape, nsteps, kind)
+    g = rate / 1e9
+    sample = (f"{nproc} independent processes (one excitation each, the reference is single-threaded), "
+              f"{nsteps} main_calc steps of the full bend each; {tmax:.1f} s timed per process")
+    line = {"impl": "reference", "metric": METRIC, "value": g, "unit": "Gcell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmax / nsteps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": g, "unit": "Gcell-updates/s", "cores": nproc, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": g, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t_all}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    ws, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    from smatranem_gb300 import fdtd as F
+    clocks = Clocks(local)
+    bend, pr, modes = make_workload()
+    n3 = bend.s.n3
+    n_split = pr.lnotn
+    batch = args.batch
+    stream = torch.cuda.Stream()
+    # ---- FP32 batched, device resident: the headline value --------------
+    p32 = make_plan(bend, pr, modes, F.FP32, batch, FULL_STEPS, stream=stream.cuda_stream)
+    p32.run(0, args.warmup)
+    dist_barrier(ws)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    p32.run(args.warmup, args.warmup + args.steps, sync=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_ms = dist_max(ev0.elapsed_time(ev1), ws)
+    dist_barrier(ws)
+    value = ws * batch * n3 * args.steps / (t_ms * 1e-3) / 1e9
+    ms_step = t_ms / args.steps
+    # per-kernel launch times for the roofline (same stream, CUDA events)
+    kt = p32.time_kernels(args.warmup + args.steps, 64)
+    bytes_step = algorithmic_bytes_per_step(n3, n_split, batch)
+    sweep_ms = 0.5 * (kt[0] + kt[1])
+    achieved = (bytes_step / 2) / (sweep_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    launches = 2 * args.steps + 2 * math.ceil(args.steps / 32) + 1
+    # ---- full runs: S-matrix columns/s and the FP32-vs-FP64 S error -----
+    full = args.full_steps
+    p32b = make_plan(bend, pr, modes, F.FP32, batch, full, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p32b.run(0, full)
+    t_full32 = time.perf_counter() - t0
+    S32 = s_parameters(p32b, bend, modes, 0)
+    finite32 = p32b.check_finite()[0]
+    p32b.close()
+    p32.close()
+    p64 = make_plan(bend, pr, modes, F.FP64, 1, full, stream=stream.cuda_stream)
+    p64.run(0, 3)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    p64.run(3, 3 + args.steps64, sync=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t64_ms = ev0.elapsed_time(ev1)
+    fp64_rate = n3 * args.steps64 / (t64_ms * 1e-3) / 1e9
+    p64.close()
+    p64 = make_plan(bend, pr, modes, F.FP64, 1, full, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p64.run(0, full)
+    t_full64 = time.perf_counter() - t0
+    S64 = s_parameters(p64, bend, modes, 0)
+    p64.close()
+    clocks.stop()
+    big = np.abs(S64) > 1e-3 * np.abs(S64).max()
+    s_rel = float(np.max(np.abs(S32 - S64)[big] / np.abs(S64)[big]))
+    s_abs = float(np.max(np.abs(S32 - S64)) / np.abs(S64).max())
+    # ---- e2e through the C ABI from host buffers --------------------------
+    t0 = time.perf_counter()
+    pe = make_plan(bend, pr, modes, F.FP32, batch, full)
+    pe.run(0, full)
+    Se = [s_parameters(pe, bend, modes, b) for b in range(batch)]
+    pe.close()
+    t_e2e = time.perf_counter() - t0
+    pl = bend.s.L[0] * bend.s.L[1]
+    h2d = (8 * 3 * n3 * 4 + 2 * 3 * n3 * 4 + batch * 8 * pl * 8 + full * (6 + 4 * len(LAMS)) * 8 * 1.5)
+    d2h = batch * 2 * len(LAMS) * 4 * pl * 16
+    e2e = ws * batch * n3 * full / t_e2e / 1e9
+    # ---- CPU baseline (bounded sample, oracle) -----------------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        kind = oracle_kind()
+        rate, tmax, wall = cpu_rate(1, (256, 192, 160), args.cpu_steps, kind)
+        cpu = {"value": rate / 1e9, "unit": "Gcell-updates/s", "cores": 1, "kind": kind,
+               "sample": f"{args.cpu_steps} main_calc steps of the full bend, one excitation, "
+                         f"{tmax:.1f} s on 1 core"}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": n3, "split_cells": n_split, "batch": batch,
+                   "l2": "inputs larger than L2 (fields of 8 excitations: %.1f GB)" % (batch * 4 * 3 * n3 * 4 / 1e9),
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+        "e2e": {"value": e2e, "unit": "Gcell-updates/s", "h2d_bytes_per_step": h2d / full,
+                "d2h_bytes_per_step": d2h / full, "what": f"create+incident+schedule+{full} steps+DFT read-back, "
+                                                          f"{t_e2e:.2f} s"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None, "kernel": "k_sweep32 (H and E sweeps)",
+                     "bytes_per_launch": bytes_step / 2, "ms_per_launch": [kt[0], kt[1]],
+                     "ms_dft_flush_per_step": kt[2]},
+        "fp64_plain": {"value": fp64_rate, "unit": "Gcell-updates/s", "steps": args.steps64,
+                       "s_cols_per_s": 1.0 / t_full64, "full_run_s": t_full64},
+        "fp32_batched": {"s_cols_per_s": batch / t_full32, "full_run_s": t_full32, "full_steps": full,
+                         "finite": finite32},
+        "s_cols_speedup_fp32_vs_fp64": (batch / t_full32) / (1.0 / t_full64),
+        "s_param_rel_err_fp32_vs_fp64": {"max_rel": s_rel, "max_abs_over_max": s_abs,
+                                         "over": "2 ports x 21 wavelengths x 4 modes, excitation 0, |S| > 1e-3 max"},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--full-steps", type=int, default=FULL_STEPS)
+    ap.add_argument("--steps64", type=int, default=40)
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--ref-steps", type=int, default=4)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

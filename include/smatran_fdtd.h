@@ -1,0 +1,214 @@
+/*
+ * smatran_fdtd.h -- C ABI of the GB300 (sm_103a) split-field FDTD time loop.
+ *
+ * Drop-in replacement for the hot path of SMatrAnEM's FDTD solver,
+ * FDTDcalc/FDTDsplitfieldMetal.c.  The reference has no library interface:
+ * its time loop (main :146-167) calls main_calc (:242-329) once per step with
+ * host arrays.  This header exposes that seam:
+ *
+ *   smat_main_calc            one step with exactly main_calc's arguments (host
+ *                             buffers, stateless, slow: for binding-level parity)
+ *   smat_fdtd_create / ...    a plan that keeps the structure and the fields
+ *                             resident in HBM and runs many steps per call
+ *
+ * Conventions (all from the reference):
+ *   L[4] = {L0, L1, L2, L3}: cells along x, y, z and the number of outer
+ *       (port) layers at each z end (main :57).
+ *   cell index l = j0 + L0*j1 + L0*L1*j2; a 3-vector field component c of cell
+ *       l sits at c + 3*l ("reference layout"); complex arrays are interleaved
+ *       (re, im) doubles, i.e. C99 double complex.
+ *   H_t, E_t: 3*(L3D + Lnotn + 1) doubles, L3D = L0*L1*L2: the main field, then
+ *       the aux (split-PML "-" half or stable-form increment) slot of each
+ *       non-'n' cell at 3*L3D + 3*address_notn[l], then a zero sentinel.
+ *   Planes: HB/EB/HT/ET are 2*L0*L1 complex: component v (0 = x, 1 = y) of
+ *       pixel p = j0 + L0*j1 at v + 2*p (main_calc :318-328).
+ *
+ * Every function returns 0 on success or a negative SMAT_E* code; nothing
+ * calls exit().  smat_last_error() gives a message for the calling thread.
+ * Device memory, streams and kernels are owned by the library; the caller
+ * owns every host buffer.  One plan lives on one CUDA device and one stream.
+ */
+#ifndef SMATRAN_FDTD_H
+#define SMATRAN_FDTD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMAT_OK 0
+#define SMAT_EINVAL (-1)    /* bad argument or inconsistent sizes */
+#define SMAT_ECUDA (-2)     /* CUDA runtime error (message has the detail) */
+#define SMAT_ENOMEM (-3)    /* device or host allocation failed */
+#define SMAT_EMONITOR (-4)  /* a monitor plane holds a PML ('a') cell: the
+                               reference aborts with "iBTIin[m] error!" (:320) */
+#define SMAT_ESTATE (-5)    /* call not valid for this plan (precision, no schedule...) */
+#define SMAT_ENUMERIC (-6)  /* non-finite value detected in the fields */
+
+#define SMAT_FP64 0 /* fields and coefficients in FP64, same operation order as the
+                       reference: bit-identical results */
+#define SMAT_FP32 1 /* fields in FP32 (packed coefficient stream); DFT accumulated
+                       in FP64; results within a stated tolerance of FP64 */
+
+/* Structure of one simulation, at the level of the reference's precompute
+ * (main :62-143).  mu/epsi are the media AFTER remove_sigma (:76), i.e. real
+ * (or lossy) values times the metric factors; sigma is the per-axis stretch
+ * profile recovered by set_sigma (:75), 2*(L0+L1+L2) doubles laid out as
+ * sigma[h + 2*j0], sigma[2*L0 + h + 2*j1], sigma[2*(L0+L1) + h + 2*j2] with
+ * h = 0 for the H sub-point and h = 1 for the E sub-point. */
+typedef struct smat_fdtd_desc {
+    int L[4];
+    int iBc[3];          /* BoundaryCondition B0..B2 in {-1, 0, 1} (input.txt) */
+    int iBTIin[4];       /* {iB, iT, iI, inci_mode}: monitor planes, source plane,
+                            signed mode number (main :84) */
+    double invtau_R;     /* from set_tau (:515-524) */
+    double invtau_I;
+    const double *mu;    /* 3*L3D complex */
+    const double *epsi;  /* 3*L3D complex */
+    const double *sigma; /* 2*(L0+L1+L2) */
+    const unsigned char *pec; /* optional, L3D bytes: nonzero forces Ae = Be = 0 on
+                                 the E components of that (ordinary) cell */
+    int precision;       /* SMAT_FP64 or SMAT_FP32 */
+    int batch;           /* independent excitations sharing the structure, >= 1 */
+} smat_fdtd_desc;
+
+typedef struct smat_fdtd_plan smat_fdtd_plan;
+
+/* Message describing the last error on the calling thread ("" if none). */
+const char *smat_last_error(void);
+
+/* Host precompute, restating main :62-143.  Callable without a GPU. ------- */
+
+/* set_sigma :858-926: sigma (2*(L0+L1+L2), zeroed by the callee) from the
+ * stretched media. */
+int smat_set_sigma(const int L[4], const double *mu, const double *epsi, double *sigma);
+/* remove_sigma :822-853, in place.  SMAT_EINVAL where the reference exits. */
+int smat_remove_sigma(const int L[4], double *mu, double *epsi, const double *sigma);
+/* set_address :188-233: Cont[L3D] in {'n','a','h','e','b'}, address_notn[L3D];
+ * *Lnotn receives the number of non-'n' cells. */
+int smat_set_address(const int L[4], const double *sigma, const double *mu,
+                     const double *epsi, char *Cont, int *Lnotn, int *address_notn);
+/* coefficient build of main :106-143 into Ah, Bh, Ae, Be of 3*(L3D+Lnotn)
+ * doubles each (zeroed by the callee). */
+int smat_coefficients(const int L[4], int Lnotn, const double *sigma, const double *mu,
+                      const double *epsi, const char *Cont, const int *address_notn,
+                      double invtau_R, double invtau_I,
+                      double *Ah, double *Bh, double *Ae, double *Be);
+/* set_tau :515-524. */
+int smat_set_tau(double omega, double min_Dt, int *N_2pi, double *invtau_R, double *invtau_I);
+/* set_env :452-475; returns NaN where the reference exits ("f_env error!"). */
+double smat_set_env(int N_2pi, const int time_period[3], int j_half, int j_time, int j_period);
+
+/* The reference seam. ----------------------------------------------------- */
+
+/* One Yee step: same arguments, layouts and results as main_calc
+ * (FDTDsplitfieldMetal.c:242-329), ExpN2 being 2 complex.  All pointers are
+ * host memory; fields and DFT planes are updated in place.  Runs the FP64
+ * kernels on the current device; uploads and downloads everything per call. */
+int smat_main_calc(const int L[4], const double *Ah, const double *Bh,
+                   const double *Ae, const double *Be, const int iBc[3],
+                   double *H_t, double *E_t, const int iBTIin[4],
+                   const double *Hi, const double *Ei, const double *ExpN2,
+                   double *HB, double *EB, double *HT, double *ET,
+                   const char *Cont, const int *address_notn);
+
+/* Plans. ------------------------------------------------------------------ */
+
+/* Build a plan from the media (runs set_address and the coefficient build on
+ * the host, then uploads).  stream: a cudaStream_t, or NULL for a stream the
+ * plan creates and owns. */
+int smat_fdtd_create(const smat_fdtd_desc *desc, void *stream, smat_fdtd_plan **plan);
+
+/* Build an FP64 plan straight from main_calc's coefficient arrays
+ * (main :101-143 outputs), for callers that already ran the precompute. */
+int smat_fdtd_create_from_coeffs(const int L[4], const double *Ah, const double *Bh,
+                                 const double *Ae, const double *Be, const int iBc[3],
+                                 const char *Cont, const int *address_notn, int Lnotn,
+                                 const int iBTIin[4], int batch, void *stream,
+                                 smat_fdtd_plan **plan);
+
+int smat_fdtd_destroy(smat_fdtd_plan *plan);
+
+/* Geometry of a plan: L (4), Lnotn, precision, batch.  Any pointer may be NULL. */
+int smat_fdtd_info(const smat_fdtd_plan *plan, int L[4], int *Lnotn, int *precision,
+                   int *batch);
+
+/* Fields of excitation b in the reference layout (3*(L3D+Lnotn+1) doubles
+ * each).  FP32 plans convert on the way. */
+int smat_fdtd_set_fields(smat_fdtd_plan *plan, int b, const double *H_t, const double *E_t);
+int smat_fdtd_get_fields(smat_fdtd_plan *plan, int b, double *H_t, double *E_t);
+
+/* One step with explicit sheet sources (main_calc's Hi, Ei: 2*L0*L1 doubles,
+ * shared by every excitation) and DFT phases ExpN2 (2 complex).  Accumulates
+ * the reference DFT (frequency slot 0 on planes iB, iT). */
+int smat_fdtd_step(smat_fdtd_plan *plan, const double *Hi, const double *Ei,
+                   const double *ExpN2);
+
+/* Incident profile of excitation b: Hinc, Einc complex 2*L0*L1 each, the
+ * arrays set_incident (:479-511) builds. */
+int smat_fdtd_set_incident(smat_fdtd_plan *plan, int b, const double *Hinc,
+                           const double *Einc);
+
+/* Source plane and direction of excitation b (default: iBTIin[2] and the sign
+ * of iBTIin[3] for every excitation).  Lets one batch hold the excitations of
+ * several ports; the reference runs one (iI, inci_mode) per process. */
+int smat_fdtd_set_source_plane(smat_fdtd_plan *plan, int b, int iI, int inci_mode);
+
+/* The reference CW schedule: envelope set_env (:452-475) and phases ExpN
+ * (:93-99) for stop-period*N_2pi steps, with the reference DFT (one
+ * frequency, planes iB and iT, phases ExpN[(k+1)%N_2pi]) as frequency slot 0.
+ * Replaces any earlier schedule and DFT setup and zeroes the accumulators.
+ * SMAT_EMONITOR when iB or iT holds a PML cell (the reference exits, :320). */
+int smat_fdtd_set_cw_schedule(smat_fdtd_plan *plan, int N_2pi, const int time_period[3]);
+
+/* The reference CW run as a general schedule (what smat_fdtd_set_cw_schedule
+ * installs): src 6*stop-period*N_2pi doubles, phase 4*stop-period*N_2pi. */
+int smat_cw_schedule(int N_2pi, const int time_period[3], double *src, double *phase);
+
+/* A general schedule of nsteps steps.  src: 6 doubles per step
+ * {sE, cE, dE, sH, cH, dH}; the sheet sources of step k are
+ *   Ei = sE*(cE*Re(Einc) + dE*Im(Einc)),  Hi = sH*(cH*Re(Hinc) + dH*Im(Hinc)),
+ * the reference's 2*env*Re(conj(ExpN)*inc) with (cE, dE) = ExpN.
+ * DFT: nfreq frequencies on nplanes z-planes (planes[], at most 8), phases 4
+ * doubles per (step, frequency): the complex weight of H then of E at step k,
+ * laid out [k][f][4].  nfreq may be 0.  Zeroes the accumulators.  Unlike the
+ * reference DFT, a plane may cut the PML: split cells contribute their total
+ * field (main + aux), other cells their main slot as in main_calc :322-325. */
+int smat_fdtd_set_schedule(smat_fdtd_plan *plan, int nsteps, const double *src,
+                           int nfreq, int nplanes, const int *planes, const double *phase);
+
+/* Advance every excitation over global steps [k_begin, k_end) of the schedule.
+ * Asynchronous on the plan's stream; CUDA-graph captured in chunks. */
+int smat_fdtd_run(smat_fdtd_plan *plan, int k_begin, int k_end);
+
+/* Block until the plan's stream is idle; reports asynchronous errors. */
+int smat_fdtd_sync(smat_fdtd_plan *plan);
+
+/* Reference DFT planes of excitation b (frequency slot 0, planes iB/iT), in
+ * main_calc's layout.  Any pointer may be NULL. */
+int smat_fdtd_get_monitor(smat_fdtd_plan *plan, int b, double *HB, double *EB,
+                          double *HT, double *ET);
+
+/* DFT accumulator of excitation b, frequency f, schedule plane index q:
+ * out = 4*L0*L1 complex, components (Hx, Hy, Ex, Ey) each over L0*L1 pixels. */
+int smat_fdtd_get_dft(smat_fdtd_plan *plan, int b, int f, int q, double *out);
+
+/* Largest |field| over every excitation (a NaN/Inf check); *finite = 0 when a
+ * non-finite value is present. */
+int smat_fdtd_check_finite(smat_fdtd_plan *plan, int *finite, double *max_abs);
+
+/* Average device time per launch (ms) of the H sweep, the E sweep and the
+ * per-step DFT work (FP64: the DFT kernel; FP32: the ring flush amortised over
+ * its steps), measured with CUDA events on the plan's stream over steps
+ * [k_begin, k_begin+nsteps) of the schedule.  The steps are really taken. */
+int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double ms[3]);
+
+/* Launch shape of the FP32 sweeps: threads per block = 32 x block_y (1..8). */
+int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int block_y);
+
+/* Device bytes the plan holds. */
+long long smat_fdtd_device_bytes(const smat_fdtd_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

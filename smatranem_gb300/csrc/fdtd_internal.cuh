@@ -1,0 +1,116 @@
+/*
+ * Internal device-side data layout of a plan (shared by the kernel and the
+ * plan translation units).
+ *
+ * HBM layout, per excitation b of the batch (all structure-of-arrays, cell
+ * index l = j0 + L0*j1 + L0*L1*j2, x fastest so a warp reads 32 consecutive
+ * cells of one component):
+ *
+ *   FP64 (bit-identical path, the reference's representation):
+ *     H, E   [3][L3D] doubles    main slot (total field of ordinary cells)
+ *     Ha, Ea [3][Lnotn+1]        aux slot of each non-'n' cell, compact in
+ *                                 address_notn order, then a zero sentinel
+ *     coefficients: main [4][3][L3D] (Ah, Bh, Ae, Be), aux [4][3][Lnotn]
+ *     flags  [L3D] bytes: cell class + "a neighbour has an aux slot" bits
+ *
+ *   FP32 (bandwidth path): total-field form.
+ *     H, E   [3][L3D] floats     main + aux: what every neighbour's curl reads
+ *     Ha, Ea [3][L3D] floats     aux slot (dense; written only by non-'n' cells)
+ *     bh, be [3][L3D] floats     1/(tau_R^-1 * Re mu) (resp. epsi) per component:
+ *                                 the only per-cell coefficient of ordinary cells
+ *                                 (their A is exactly 1); split-PML cells scale it
+ *                                 by 1-D sigma tables; cells needing anything else
+ *                                 carry NaN in component 0 and a record index in
+ *                                 component 1 ("general" cells, a short list)
+ */
+#ifndef SMATRAN_FDTD_INTERNAL_CUH
+#define SMATRAN_FDTD_INTERNAL_CUH
+
+#include <cstdint>
+
+namespace smat {
+
+enum : uint8_t { CLS_N = 0, CLS_A = 1, CLS_H = 2, CLS_E = 3, CLS_B = 4 };
+constexpr uint8_t FL_BWD = 8;  /* a backward neighbour (wrapped) is non-'n' */
+constexpr uint8_t FL_FWD = 16; /* a forward neighbour (wrapped) is non-'n' */
+
+constexpr int MAX_PLANES = 8;
+
+struct Geo {
+    int L0, L1, L2, pl; /* pl = L0*L1 */
+    long long n3;       /* L0*L1*L2 */
+    int bc[3];          /* iBc */
+    int iI;             /* source plane */
+    double sgn;         /* iBTIin[3]/|iBTIin[3]| */
+};
+
+/* Per-step sources.  Step k of a launch = *base + rel. */
+struct Src {
+    const int *base;
+    const double *sched; /* [nsched][6] {sE, cE, dE, sH, cH, dH} */
+    const double *inc;   /* [batch][8*pl]: Hinc (2*pl complex) then Einc */
+    const double *xsrc;  /* explicit planes {Hi[2*pl], Ei[2*pl]} or null */
+    const int *iI;       /* [batch] source plane of each excitation (main :84 iI) */
+    const double *sgn;   /* [batch] its sign, inci_mode/|inci_mode| (:253) */
+};
+
+struct Dft {
+    int nfreq, nq;
+    int planes[MAX_PLANES];
+    const double *phase;  /* [nsched][nfreq][4] {pH re, im, pE re, im} */
+    const float *phase32; /* same in FP32 (for the deferred FP32 flush) */
+    const double *xphase; /* explicit {pH, pE} for smat_fdtd_step, or null */
+    const float *xphase32; /* the same in FP32 */
+    double *acc;          /* [batch][nfreq][nq][4][pl] complex */
+    int ringK;            /* FP32: samples kept per flush */
+    float *ring;          /* FP32: [batch][ringK][nq][4][pl] */
+};
+
+struct P64 {
+    Geo g;
+    int batch, lnotn;
+    const uint8_t *flags;
+    const int *addr;
+    const double *cm; /* [4][3][n3] */
+    const double *ca; /* [4][3][lnotn] */
+    double *H, *E;    /* [batch][3][n3] */
+    double *Ha, *Ea;  /* [batch][3][lnotn+1] */
+    Src s;
+    Dft d;
+};
+
+/* A cell the FP32 fast path does not cover by its three per-cell numbers. */
+struct Rec32 {
+    float A0[3], B0[3]; /* main slot ("+" half of a split cell) */
+    float A1[3], B1[3]; /* aux slot ("-" half, or the stable-form increment) */
+    int kind;
+    int pad[3];
+};
+enum : int { RK_N = 0, RK_A = 1, RK_STABLE = 2, RK_FROZEN = 3 };
+
+struct P32 {
+    Geo g;
+    int batch;
+    const float *bh, *be;
+    const Rec32 *hrec, *erec;
+    const float *tab;       /* [4][S]: A_h, G_h, A_e, G_e; S = L0+L1+L2 */
+    const uint8_t *pmask;   /* [S]: axis index lies in a PML (either half) */
+    float *H, *E, *Ha, *Ea; /* [batch][3][n3] */
+    Src s;
+    Dft d;
+};
+
+/* launchers (one translation unit per precision) */
+void launch_h64(const P64 &p, int rel, cudaStream_t st);
+void launch_e64(const P64 &p, int rel, cudaStream_t st);
+void launch_dft64(const P64 &p, int rel, cudaStream_t st);
+void launch_h32(const P32 &p, int rel, int by, cudaStream_t st);
+void launch_e32(const P32 &p, int rel, int by, cudaStream_t st);
+void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
+void launch_bump(int *base, int by, cudaStream_t st);
+void launch_set(int *base, int value, cudaStream_t st);
+void launch_maxabs(const void *x, long long n, int is_double, double *out, cudaStream_t st);
+
+} // namespace smat
+
+#endif

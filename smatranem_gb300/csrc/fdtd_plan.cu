@@ -1,0 +1,1045 @@
+/*
+ * Plans: device-resident state of one structure and its batch of excitations,
+ * the launch schedule (CUDA-graph captured chunks of steps) and the C ABI of
+ * include/smatran_fdtd.h.
+ *
+ * A plan replaces the reference time loop (FDTDcalc/FDTDsplitfieldMetal.c
+ * main :146-167) and its per-step main_calc (:242-329); the host precompute
+ * in host_precompute.c replaces main :62-143.
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "fdtd_internal.cuh"
+#include "host_internal.h"
+#include "smatran_fdtd.h"
+
+using namespace smat;
+
+namespace {
+
+constexpr int GRAPH_STEPS = 32; /* steps per captured graph (= FP32 ring length) */
+constexpr int RING_K = 32;
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    return smat_fail(SMAT_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                                                                                       \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);                                                            \
+    } while (0)
+
+/* zero-filled device allocation, ordered on stream st */
+template <class T> int dalloc(T **p, size_t n, cudaStream_t st)
+{
+    *p = nullptr;
+    if (n == 0) return SMAT_OK;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return smat_fail(SMAT_ENOMEM, "cudaMalloc of %zu bytes: %s", n * sizeof(T), cudaGetErrorString(e));
+    }
+    e = cudaMemsetAsync(*p, 0, n * sizeof(T), st);
+    if (e != cudaSuccess) return smat_fail(SMAT_ECUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    return SMAT_OK;
+}
+
+} // namespace
+
+struct smat_fdtd_plan {
+    int L[4], iBc[3], iBTIin[4];
+    int precision, batch, lnotn;
+    long long n3;
+    int pl;
+    double invtau_R = 0, invtau_I = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    long long dev_bytes = 0;
+    std::vector<char> cont;    /* host copy of the cell classes */
+    std::vector<int> addr;     /* host copy of address_notn */
+
+    /* common device state */
+    int *d_base = nullptr;
+    double *d_inc = nullptr;   /* [batch][8*pl] */
+    double *d_xsrc = nullptr;  /* explicit sheet planes */
+    double *d_xphase = nullptr;
+    float *d_xphase32 = nullptr;
+    double *d_sched = nullptr; /* [nsched][6] */
+    int nsched = 0;
+    double *d_phase = nullptr; /* [nsched][nfreq][4] */
+    float *d_phase32 = nullptr;
+    double *d_acc = nullptr;   /* [batch][nfreq][nq][4][pl] complex */
+    float *d_ring = nullptr;
+    int nfreq = 0, nq = 0, planes[MAX_PLANES] = {0};
+    bool ref_dft = false;      /* DFT slot 0 on planes (iB, iT) is the reference one */
+    bool ref_planes_ok = false; /* no PML cell on iB, iT (else the reference exits, :320) */
+    double *d_scratch = nullptr;
+    int *d_iI = nullptr;      /* [batch] source plane per excitation */
+    double *d_isgn = nullptr; /* [batch] its sign */
+
+    /* FP64 */
+    uint8_t *d_flags = nullptr;
+    int *d_addr = nullptr;
+    double *d_cm = nullptr, *d_ca = nullptr;
+    double *d_H64 = nullptr, *d_E64 = nullptr, *d_Ha64 = nullptr, *d_Ea64 = nullptr;
+
+    /* FP32 */
+    float *d_bh = nullptr, *d_be = nullptr, *d_tab = nullptr;
+    uint8_t *d_pmask = nullptr;
+    Rec32 *d_hrec = nullptr, *d_erec = nullptr;
+    float *d_H32 = nullptr, *d_E32 = nullptr, *d_Ha32 = nullptr, *d_Ea32 = nullptr;
+    int by32 = 8;
+
+    /* graphs: a chunk of GRAPH_STEPS steps, position independent via d_base */
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
+
+    std::vector<void *> allocations;
+
+    template <class T> int alloc(T **p, size_t n)
+    {
+        int rc = dalloc(p, n, stream);
+        if (rc == SMAT_OK && *p) {
+            allocations.push_back((void *)*p);
+            dev_bytes += (long long)(n * sizeof(T));
+        }
+        return rc;
+    }
+};
+
+namespace {
+
+Geo make_geo(const smat_fdtd_plan *p)
+{
+    Geo g;
+    g.L0 = p->L[0];
+    g.L1 = p->L[1];
+    g.L2 = p->L[2];
+    g.pl = p->pl;
+    g.n3 = p->n3;
+    for (int a = 0; a < 3; a++) g.bc[a] = p->iBc[a];
+    g.iI = p->iBTIin[2];
+    const int m = p->iBTIin[3];
+    g.sgn = (double)(m / (m < 0 ? -m : m));
+    return g;
+}
+
+Dft make_dft(const smat_fdtd_plan *p, bool explicit_phase)
+{
+    Dft d;
+    d.nfreq = p->nfreq;
+    d.nq = p->nq;
+    for (int i = 0; i < MAX_PLANES; i++) d.planes[i] = p->planes[i];
+    d.phase = p->d_phase;
+    d.phase32 = p->d_phase32;
+    d.xphase = explicit_phase ? p->d_xphase : nullptr;
+    d.xphase32 = explicit_phase ? p->d_xphase32 : nullptr;
+    d.acc = p->d_acc;
+    d.ringK = RING_K;
+    d.ring = p->d_ring;
+    return d;
+}
+
+Src make_src(const smat_fdtd_plan *p, bool explicit_src)
+{
+    Src s;
+    s.base = p->d_base;
+    s.sched = p->d_sched;
+    s.inc = p->d_inc;
+    s.xsrc = explicit_src ? p->d_xsrc : nullptr;
+    s.iI = p->d_iI;
+    s.sgn = p->d_isgn;
+    return s;
+}
+
+P64 make_p64(const smat_fdtd_plan *p, bool xp)
+{
+    P64 q;
+    q.g = make_geo(p);
+    q.batch = p->batch;
+    q.lnotn = p->lnotn;
+    q.flags = p->d_flags;
+    q.addr = p->d_addr;
+    q.cm = p->d_cm;
+    q.ca = p->d_ca;
+    q.H = p->d_H64;
+    q.E = p->d_E64;
+    q.Ha = p->d_Ha64;
+    q.Ea = p->d_Ea64;
+    q.s = make_src(p, xp);
+    q.d = make_dft(p, xp);
+    return q;
+}
+
+P32 make_p32(const smat_fdtd_plan *p, bool xp)
+{
+    P32 q;
+    q.g = make_geo(p);
+    q.batch = p->batch;
+    q.bh = p->d_bh;
+    q.be = p->d_be;
+    q.hrec = p->d_hrec;
+    q.erec = p->d_erec;
+    q.tab = p->d_tab;
+    q.pmask = p->d_pmask;
+    q.H = p->d_H32;
+    q.E = p->d_E32;
+    q.Ha = p->d_Ha32;
+    q.Ea = p->d_Ea32;
+    q.s = make_src(p, xp);
+    q.d = make_dft(p, xp);
+    return q;
+}
+
+/* the launches of steps rel0 .. rel0+n-1 relative to *d_base (no bump) */
+void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
+{
+    if (p->precision == SMAT_FP64) {
+        const P64 q = make_p64(p, xp);
+        for (int i = 0; i < n; i++) {
+            launch_h64(q, rel0 + i, p->stream);
+            launch_e64(q, rel0 + i, p->stream);
+            launch_dft64(q, rel0 + i, p->stream);
+        }
+    } else {
+        const P32 q = make_p32(p, xp);
+        for (int i = 0; i < n; i++) {
+            launch_h32(q, rel0 + i, p->by32, p->stream);
+            launch_e32(q, rel0 + i, p->by32, p->stream);
+        }
+        launch_flush32(q, rel0 + n, n, p->stream);
+    }
+}
+
+void drop_graph(smat_fdtd_plan *p)
+{
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    p->graph = nullptr;
+    p->graph_failed = false;
+}
+
+int build_graph(smat_fdtd_plan *p)
+{
+    if (p->graph || p->graph_failed) return SMAT_OK;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        p->graph_failed = true;
+        return SMAT_OK;
+    }
+    enqueue_steps(p, 0, GRAPH_STEPS, false);
+    launch_bump(p->d_base, GRAPH_STEPS, p->stream);
+    cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+    if (e != cudaSuccess || !g) {
+        cudaGetLastError();
+        p->graph_failed = true;
+        return SMAT_OK;
+    }
+    e = cudaGraphInstantiate(&p->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p->graph = nullptr;
+        p->graph_failed = true;
+    }
+    return SMAT_OK;
+}
+
+/* host flags of FP64 cells: class code and "a neighbour has an aux slot" */
+void build_flags(const smat_fdtd_plan *p, std::vector<uint8_t> &fl)
+{
+    const int L0 = p->L[0], L1 = p->L[1], L2 = p->L[2];
+    const long long n3 = p->n3;
+    fl.assign(n3, 0);
+    auto special = [&](long long l) { return p->cont[l] != 'n'; };
+    long long l = 0;
+    for (int j2 = 0; j2 < L2; j2++)
+        for (int j1 = 0; j1 < L1; j1++)
+            for (int j0 = 0; j0 < L0; j0++, l++) {
+                uint8_t c = CLS_N;
+                switch (p->cont[l]) {
+                case 'a': c = CLS_A; break;
+                case 'h': c = CLS_H; break;
+                case 'e': c = CLS_E; break;
+                case 'b': c = CLS_B; break;
+                default: c = CLS_N;
+                }
+                const long long xm = l + (j0 == 0 ? L0 - 1 : -1), xp = l + (j0 + 1 == L0 ? -(L0 - 1) : 1);
+                const long long sy = L0, sz = (long long)L0 * L1;
+                const long long ym = l + (j1 == 0 ? (L1 - 1) * sy : -sy), yp = l + (j1 + 1 == L1 ? -(L1 - 1) * sy : sy);
+                const long long zm = l + (j2 == 0 ? (L2 - 1) * sz : -sz), zp = l + (j2 + 1 == L2 ? -(L2 - 1) * sz : sz);
+                if (special(xm) || special(ym) || special(zm)) c |= FL_BWD;
+                if (special(xp) || special(yp) || special(zp)) c |= FL_FWD;
+                fl[l] = c;
+            }
+}
+
+int check_planes(const smat_fdtd_plan *p, int nq, const int *planes)
+{
+    for (int q = 0; q < nq; q++) {
+        const int z = planes[q];
+        if (z < 0 || z >= p->L[2]) return smat_fail(SMAT_EINVAL, "monitor plane %d outside 0..%d", z, p->L[2] - 1);
+        for (long long i = 0; i < p->pl; i++)
+            if (p->cont[i + (long long)p->pl * z] == 'a')
+                return smat_fail(SMAT_EMONITOR, "iBTIin error: monitor plane %d holds a PML cell", z);
+    }
+    return SMAT_OK;
+}
+
+/* (re)allocate DFT accumulators and the FP32 ring for nfreq x nq planes */
+int setup_dft(smat_fdtd_plan *p, int nfreq, int nq, const int *planes)
+{
+    if (nq > MAX_PLANES) return smat_fail(SMAT_EINVAL, "at most %d monitor planes", MAX_PLANES);
+    int rc;
+    for (int q = 0; q < nq; q++)
+        if (planes[q] < 0 || planes[q] >= p->L[2])
+            return smat_fail(SMAT_EINVAL, "monitor plane %d outside 0..%d", planes[q], p->L[2] - 1);
+    drop_graph(p);
+    const size_t acc_n = (size_t)p->batch * nfreq * nq * 4 * p->pl * 2;
+    const size_t ring_n = p->precision == SMAT_FP32 ? (size_t)p->batch * RING_K * nq * 4 * p->pl : 0;
+    const size_t old_acc = (size_t)p->batch * p->nfreq * p->nq * 4 * p->pl * 2;
+    const size_t old_ring = p->precision == SMAT_FP32 ? (size_t)p->batch * RING_K * p->nq * 4 * p->pl : 0;
+    if (acc_n != old_acc || !p->d_acc) {
+        if (p->d_acc) cudaFree(p->d_acc), p->dev_bytes -= old_acc * 8;
+        p->d_acc = nullptr;
+        if (acc_n) {
+            rc = dalloc(&p->d_acc, acc_n, p->stream);
+            if (rc) return rc;
+            p->dev_bytes += acc_n * 8;
+        }
+    }
+    if (ring_n != old_ring || (!p->d_ring && ring_n)) {
+        if (p->d_ring) cudaFree(p->d_ring), p->dev_bytes -= old_ring * 4;
+        p->d_ring = nullptr;
+        if (ring_n) {
+            rc = dalloc(&p->d_ring, ring_n, p->stream);
+            if (rc) return rc;
+            p->dev_bytes += ring_n * 4;
+        }
+    }
+    p->nfreq = nfreq;
+    p->nq = nq;
+    for (int i = 0; i < MAX_PLANES; i++) p->planes[i] = i < nq ? planes[i] : -1;
+    if (p->d_acc) CK(cudaMemsetAsync(p->d_acc, 0, acc_n * 8, p->stream));
+    return SMAT_OK;
+}
+
+int common_alloc(smat_fdtd_plan *p)
+{
+    int rc;
+    if ((rc = p->alloc(&p->d_base, 1))) return rc;
+    if ((rc = p->alloc(&p->d_inc, (size_t)p->batch * 8 * p->pl))) return rc;
+    if ((rc = p->alloc(&p->d_xsrc, (size_t)4 * p->pl))) return rc;
+    if ((rc = p->alloc(&p->d_xphase, 4))) return rc;
+    if ((rc = p->alloc(&p->d_xphase32, 4))) return rc;
+    if ((rc = p->alloc(&p->d_scratch, 4))) return rc;
+    if ((rc = p->alloc(&p->d_iI, p->batch)) || (rc = p->alloc(&p->d_isgn, p->batch))) return rc;
+    {
+        const int m = p->iBTIin[3];
+        std::vector<int> ii(p->batch, p->iBTIin[2]);
+        std::vector<double> sg(p->batch, (double)(m / (m < 0 ? -m : m)));
+        CK(cudaMemcpyAsync(p->d_iI, ii.data(), ii.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_isgn, sg.data(), sg.size() * 8, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+    }
+    /* the reference DFT: one frequency on planes iB and iT */
+    const int pls[2] = {p->iBTIin[0], p->iBTIin[1]};
+    rc = setup_dft(p, 1, 2, pls);
+    if (rc) return rc;
+    p->ref_dft = true;
+    p->ref_planes_ok = check_planes(p, 2, pls) == SMAT_OK;
+    smat_clear_error();
+    return SMAT_OK;
+}
+
+int validate_common(const int L[4], const int iBc[3], const int iBTIin[4], int batch)
+{
+    if (!L || L[0] <= 0 || L[1] <= 0 || L[2] <= 0 || L[3] < 0)
+        return smat_fail(SMAT_EINVAL, "L must be positive (got %d %d %d %d)", L ? L[0] : 0, L ? L[1] : 0, L ? L[2] : 0,
+                         L ? L[3] : 0);
+    if ((long long)L[0] * L[1] * L[2] >= (1LL << 31) / 3)
+        return smat_fail(SMAT_EINVAL, "grid too large for 32-bit reference indices");
+    if (!iBc || !iBTIin) return smat_fail(SMAT_EINVAL, "iBc and iBTIin are required");
+    for (int a = 0; a < 3; a++)
+        if (iBc[a] < -1 || iBc[a] > 1) return smat_fail(SMAT_EINVAL, "iBc[%d] = %d not in {-1,0,1}", a, iBc[a]);
+    if (iBTIin[3] == 0) return smat_fail(SMAT_EINVAL, "inci_mode = 0!");
+    for (int i = 0; i < 3; i++)
+        if (iBTIin[i] < 0 || iBTIin[i] >= L[2])
+            return smat_fail(SMAT_EINVAL, "plane iBTIin[%d] = %d outside 0..%d", i, iBTIin[i], L[2] - 1);
+    if (batch < 1) return smat_fail(SMAT_EINVAL, "batch must be >= 1");
+    return SMAT_OK;
+}
+
+smat_fdtd_plan *new_plan(const int L[4], const int iBc[3], const int iBTIin[4], int precision, int batch,
+                         void *stream)
+{
+    smat_fdtd_plan *p = new (std::nothrow) smat_fdtd_plan();
+    if (!p) return nullptr;
+    memcpy(p->L, L, sizeof p->L);
+    memcpy(p->iBc, iBc, sizeof p->iBc);
+    memcpy(p->iBTIin, iBTIin, sizeof p->iBTIin);
+    p->precision = precision;
+    p->batch = batch;
+    p->n3 = (long long)L[0] * L[1] * L[2];
+    p->pl = L[0] * L[1];
+    if (stream) {
+        p->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete p;
+            return nullptr;
+        }
+        p->own_stream = true;
+    }
+    return p;
+}
+
+/* FP64 device arrays from the reference coefficient arrays (AoS -> SoA) */
+int upload_f64(smat_fdtd_plan *p, const double *Ah, const double *Bh, const double *Ae, const double *Be)
+{
+    int rc;
+    const long long n3 = p->n3;
+    const int ln = p->lnotn;
+    std::vector<uint8_t> fl;
+    build_flags(p, fl);
+    if ((rc = p->alloc(&p->d_flags, n3))) return rc;
+    if ((rc = p->alloc(&p->d_addr, n3))) return rc;
+    if ((rc = p->alloc(&p->d_cm, 12 * (size_t)n3))) return rc;
+    if ((rc = p->alloc(&p->d_ca, 12 * (size_t)ln))) return rc;
+    const size_t fs = (size_t)p->batch * 3 * n3, as = (size_t)p->batch * 3 * (ln + 1);
+    if ((rc = p->alloc(&p->d_H64, fs)) || (rc = p->alloc(&p->d_E64, fs))) return rc;
+    if ((rc = p->alloc(&p->d_Ha64, as)) || (rc = p->alloc(&p->d_Ea64, as))) return rc;
+    std::vector<double> cm(12 * (size_t)n3), ca(12 * (size_t)ln);
+    const double *src[4] = {Ah, Bh, Ae, Be};
+    for (int w = 0; w < 4; w++)
+        for (int c = 0; c < 3; c++) {
+            for (long long l = 0; l < n3; l++) cm[((size_t)w * 3 + c) * n3 + l] = src[w][c + 3 * l];
+            for (int a = 0; a < ln; a++) ca[((size_t)w * 3 + c) * ln + a] = src[w][c + 3 * (n3 + a)];
+        }
+    CK(cudaMemcpyAsync(p->d_flags, fl.data(), n3, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_addr, p->addr.data(), n3 * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_cm, cm.data(), cm.size() * 8, cudaMemcpyHostToDevice, p->stream));
+    if (ln) CK(cudaMemcpyAsync(p->d_ca, ca.data(), ca.size() * 8, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+/* FP32 packed stream: per cell B = 1/(tR Re mu) (A == 1) for ordinary and
+ * separable split cells, records for everything else. */
+int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, const double *Bh, const double *Ae,
+               const double *Be)
+{
+    int rc;
+    const long long n3 = p->n3;
+    const double iR = d->invtau_R, iI = d->invtau_I;
+    const double *mu = d->mu, *ep = d->epsi;
+    std::vector<float> bh(3 * n3), be(3 * n3);
+    std::vector<Rec32> hrec, erec;
+    auto aux = [&](long long l, int c) { return (size_t)c + 3 * (size_t)(n3 + p->addr[l]); };
+    auto put_rec = [&](std::vector<float> &cf, std::vector<Rec32> &recs, long long l, const Rec32 &r) {
+        cf[l] = std::nanf("");
+        int idx = (int)recs.size();
+        float f;
+        memcpy(&f, &idx, 4);
+        cf[n3 + l] = f;
+        cf[2 * n3 + l] = 0.0f;
+        recs.push_back(r);
+    };
+    for (long long l = 0; l < n3; l++) {
+        const char k = p->cont[l];
+        const bool pec = d->pec && d->pec[l];
+        for (int side = 0; side < 2; side++) { /* 0: H (mu), 1: E (epsi) */
+            std::vector<float> &cf = side ? be : bh;
+            std::vector<Rec32> &recs = side ? erec : hrec;
+            const double *m = side ? ep : mu;
+            const double *A = side ? Ae : Ah, *B = side ? Be : Bh;
+            Rec32 r;
+            memset(&r, 0, sizeof r);
+            for (int c = 0; c < 3; c++) {
+                r.A0[c] = (float)A[c + 3 * l];
+                r.B0[c] = (float)B[c + 3 * l];
+                if (k != 'n') {
+                    r.A1[c] = (float)A[aux(l, c)];
+                    r.B1[c] = (float)B[aux(l, c)];
+                }
+            }
+            const bool lossless = m[2 * (3 * l + 0) + 1] == 0.0 && m[2 * (3 * l + 1) + 1] == 0.0 &&
+                                  m[2 * (3 * l + 2) + 1] == 0.0;
+            bool simple = false;
+            if (k == 'n') {
+                simple = lossless && !(side == 1 && pec) && r.A0[0] == 1.0f && r.A0[1] == 1.0f && r.A0[2] == 1.0f;
+                r.kind = RK_N;
+            } else if (k == 'a') {
+                simple = lossless;
+                r.kind = RK_A;
+            } else {
+                const bool stable_here = side == 0 ? (k == 'h' || k == 'b') : (k == 'e' || k == 'b');
+                r.kind = stable_here ? RK_STABLE : RK_FROZEN;
+            }
+            if (simple) {
+                for (int c = 0; c < 3; c++) cf[c * n3 + l] = (float)(1. / (iR * m[2 * (3 * l + c)]));
+            } else {
+                if (side == 1 && pec) {
+                    for (int c = 0; c < 3; c++) r.A0[c] = r.B0[c] = 0.0f;
+                }
+                put_rec(cf, recs, l, r);
+            }
+        }
+    }
+    /* 1-D sigma tables: rows A_h, G_h, A_e, G_e over the three axes */
+    const int S = p->L[0] + p->L[1] + p->L[2];
+    std::vector<float> tab(4 * (size_t)S);
+    std::vector<uint8_t> pmask(S);
+    const int aoff[3] = {0, p->L[0], p->L[0] + p->L[1]};
+    const int soff[3] = {0, 2 * p->L[0], 2 * (p->L[0] + p->L[1])};
+    for (int a = 0; a < 3; a++)
+        for (int j = 0; j < p->L[a]; j++) {
+            const double sh = d->sigma[soff[a] + 2 * j], se = d->sigma[soff[a] + 1 + 2 * j];
+            tab[0 * S + aoff[a] + j] = (float)((iR - iI * sh) / (iR + iI * sh));
+            tab[1 * S + aoff[a] + j] = (float)(iR / (iR + iI * sh));
+            tab[2 * S + aoff[a] + j] = (float)((iR - iI * se) / (iR + iI * se));
+            tab[3 * S + aoff[a] + j] = (float)(iR / (iR + iI * se));
+            pmask[aoff[a] + j] = std::fabs(sh) > 10.0 * 2.220446049250313e-16 || std::fabs(se) > 10.0 * 2.220446049250313e-16;
+        }
+    if ((rc = p->alloc(&p->d_bh, 3 * (size_t)n3)) || (rc = p->alloc(&p->d_be, 3 * (size_t)n3))) return rc;
+    if ((rc = p->alloc(&p->d_tab, 4 * (size_t)S)) || (rc = p->alloc(&p->d_pmask, (size_t)S))) return rc;
+    if ((rc = p->alloc(&p->d_hrec, hrec.size() + 1)) || (rc = p->alloc(&p->d_erec, erec.size() + 1))) return rc;
+    const size_t fs = (size_t)p->batch * 3 * n3;
+    if ((rc = p->alloc(&p->d_H32, fs)) || (rc = p->alloc(&p->d_E32, fs))) return rc;
+    if ((rc = p->alloc(&p->d_Ha32, fs)) || (rc = p->alloc(&p->d_Ea32, fs))) return rc;
+    CK(cudaMemcpyAsync(p->d_bh, bh.data(), bh.size() * 4, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_be, be.data(), be.size() * 4, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_pmask, pmask.data(), pmask.size(), cudaMemcpyHostToDevice, p->stream));
+    if (!hrec.empty())
+        CK(cudaMemcpyAsync(p->d_hrec, hrec.data(), hrec.size() * sizeof(Rec32), cudaMemcpyHostToDevice, p->stream));
+    if (!erec.empty())
+        CK(cudaMemcpyAsync(p->d_erec, erec.data(), erec.size() * sizeof(Rec32), cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+int finish_create(smat_fdtd_plan *p, int rc, smat_fdtd_plan **out)
+{
+    if (rc == SMAT_OK) rc = common_alloc(p);
+    if (rc == SMAT_OK) {
+        cudaError_t e = cudaStreamSynchronize(p->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "plan upload");
+    }
+    if (rc != SMAT_OK) {
+        smat_fdtd_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return SMAT_OK;
+}
+
+} // namespace
+
+/* ===================================================================== */
+
+extern "C" int smat_fdtd_create(const smat_fdtd_desc *d, void *stream, smat_fdtd_plan **out)
+{
+    smat_clear_error();
+    if (!d || !out || !d->mu || !d->epsi || !d->sigma) return smat_fail(SMAT_EINVAL, "create: null argument");
+    *out = nullptr;
+    int rc = validate_common(d->L, d->iBc, d->iBTIin, d->batch);
+    if (rc) return rc;
+    if (d->precision != SMAT_FP64 && d->precision != SMAT_FP32)
+        return smat_fail(SMAT_EINVAL, "precision must be SMAT_FP64 or SMAT_FP32");
+    if (!(d->invtau_R > 0) || !std::isfinite(d->invtau_I))
+        return smat_fail(SMAT_EINVAL, "invtau_R must be positive and invtau_I finite");
+    smat_fdtd_plan *p = new_plan(d->L, d->iBc, d->iBTIin, d->precision, d->batch, stream);
+    if (!p) return smat_fail(SMAT_ENOMEM, "plan allocation or stream creation failed");
+    p->invtau_R = d->invtau_R;
+    p->invtau_I = d->invtau_I;
+    const long long n3 = p->n3;
+    p->cont.resize(n3);
+    p->addr.resize(n3);
+    rc = smat_set_address(d->L, d->sigma, d->mu, d->epsi, p->cont.data(), &p->lnotn, p->addr.data());
+    if (rc) {
+        smat_fdtd_destroy(p);
+        return rc;
+    }
+    if (d->pec)
+        for (long long l = 0; l < n3; l++)
+            if (d->pec[l] && p->cont[l] != 'n') {
+                smat_fdtd_destroy(p);
+                return smat_fail(SMAT_EINVAL, "PEC cell %lld is not an ordinary ('n') cell", l);
+            }
+    const size_t nc = 3 * (size_t)(n3 + p->lnotn);
+    std::vector<double> Ah(nc), Bh(nc), Ae(nc), Be(nc);
+    rc = smat_coefficients(d->L, p->lnotn, d->sigma, d->mu, d->epsi, p->cont.data(), p->addr.data(), d->invtau_R,
+                           d->invtau_I, Ah.data(), Bh.data(), Ae.data(), Be.data());
+    if (rc) {
+        smat_fdtd_destroy(p);
+        return rc;
+    }
+    if (d->pec)
+        for (long long l = 0; l < n3; l++)
+            if (d->pec[l])
+                for (int c = 0; c < 3; c++) Ae[c + 3 * l] = Be[c + 3 * l] = 0.0;
+    rc = p->precision == SMAT_FP64 ? upload_f64(p, Ah.data(), Bh.data(), Ae.data(), Be.data())
+                                   : upload_f32(p, d, Ah.data(), Bh.data(), Ae.data(), Be.data());
+    return finish_create(p, rc, out);
+}
+
+extern "C" int smat_fdtd_create_from_coeffs(const int L[4], const double *Ah, const double *Bh, const double *Ae,
+                                            const double *Be, const int iBc[3], const char *Cont,
+                                            const int *address_notn, int Lnotn, const int iBTIin[4], int batch,
+                                            void *stream, smat_fdtd_plan **out)
+{
+    smat_clear_error();
+    if (!out || !Ah || !Bh || !Ae || !Be || !Cont || !address_notn)
+        return smat_fail(SMAT_EINVAL, "create_from_coeffs: null argument");
+    *out = nullptr;
+    int rc = validate_common(L, iBc, iBTIin, batch);
+    if (rc) return rc;
+    smat_fdtd_plan *p = new_plan(L, iBc, iBTIin, SMAT_FP64, batch, stream);
+    if (!p) return smat_fail(SMAT_ENOMEM, "plan allocation or stream creation failed");
+    const long long n3 = p->n3;
+    p->cont.assign(Cont, Cont + n3);
+    p->addr.assign(address_notn, address_notn + n3);
+    p->lnotn = Lnotn;
+    int count = 0;
+    for (long long l = 0; l < n3; l++) {
+        const char k = Cont[l];
+        if (k != 'n' && k != 'a' && k != 'h' && k != 'e' && k != 'b') {
+            smat_fdtd_destroy(p);
+            return smat_fail(SMAT_EINVAL, "Cont[%lld] = %d is not a cell class", l, (int)k);
+        }
+        const int a = address_notn[l];
+        if (k == 'n' ? a != Lnotn : (a < 0 || a >= Lnotn)) {
+            smat_fdtd_destroy(p);
+            return smat_fail(SMAT_EINVAL, "address_notn[%lld] = %d inconsistent with Cont/Lnotn", l, a);
+        }
+        count += k != 'n';
+    }
+    if (count != Lnotn) {
+        smat_fdtd_destroy(p);
+        return smat_fail(SMAT_EINVAL, "Lnotn = %d but %d non-'n' cells", Lnotn, count);
+    }
+    rc = upload_f64(p, Ah, Bh, Ae, Be);
+    return finish_create(p, rc, out);
+}
+
+extern "C" int smat_fdtd_destroy(smat_fdtd_plan *p)
+{
+    if (!p) return SMAT_OK;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    drop_graph(p);
+    for (void *a : p->allocations) cudaFree(a);
+    if (p->d_acc) cudaFree(p->d_acc);
+    if (p->d_ring) cudaFree(p->d_ring);
+    if (p->d_sched) cudaFree(p->d_sched);
+    if (p->d_phase) cudaFree(p->d_phase);
+    if (p->d_phase32) cudaFree(p->d_phase32);
+    if (p->own_stream && p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_info(const smat_fdtd_plan *p, int L[4], int *Lnotn, int *precision, int *batch)
+{
+    if (!p) return smat_fail(SMAT_EINVAL, "null plan");
+    if (L) memcpy(L, p->L, sizeof p->L);
+    if (Lnotn) *Lnotn = p->lnotn;
+    if (precision) *precision = p->precision;
+    if (batch) *batch = p->batch;
+    return SMAT_OK;
+}
+
+extern "C" long long smat_fdtd_device_bytes(const smat_fdtd_plan *p) { return p ? p->dev_bytes : 0; }
+
+extern "C" int smat_fdtd_set_fields(smat_fdtd_plan *p, int b, const double *H_t, const double *E_t)
+{
+    smat_clear_error();
+    if (!p || !H_t || !E_t || b < 0 || b >= p->batch) return smat_fail(SMAT_EINVAL, "set_fields: bad arguments");
+    const long long n3 = p->n3;
+    const int ln = p->lnotn;
+    for (int w = 0; w < 2; w++) {
+        const double *src = w ? E_t : H_t;
+        if (p->precision == SMAT_FP64) {
+            std::vector<double> m(3 * n3), a(3 * (size_t)(ln + 1), 0.0);
+            for (int c = 0; c < 3; c++) {
+                for (long long l = 0; l < n3; l++) m[c * n3 + l] = src[c + 3 * l];
+                for (int x = 0; x <= ln; x++) a[(size_t)c * (ln + 1) + x] = src[c + 3 * (n3 + x)];
+            }
+            double *dm = (w ? p->d_E64 : p->d_H64) + (size_t)b * 3 * n3;
+            double *da = (w ? p->d_Ea64 : p->d_Ha64) + (size_t)b * 3 * (ln + 1);
+            CK(cudaMemcpyAsync(dm, m.data(), m.size() * 8, cudaMemcpyHostToDevice, p->stream));
+            CK(cudaMemcpyAsync(da, a.data(), a.size() * 8, cudaMemcpyHostToDevice, p->stream));
+            CK(cudaStreamSynchronize(p->stream));
+        } else {
+            std::vector<float> t(3 * n3), a(3 * n3, 0.0f);
+            for (int c = 0; c < 3; c++)
+                for (long long l = 0; l < n3; l++) {
+                    double main = src[c + 3 * l], ax = 0.0;
+                    if (p->cont[l] != 'n') ax = src[c + 3 * (n3 + p->addr[l])];
+                    t[c * n3 + l] = (float)(main + ax);
+                    a[c * n3 + l] = (float)ax;
+                }
+            float *dt = (w ? p->d_E32 : p->d_H32) + (size_t)b * 3 * n3;
+            float *da = (w ? p->d_Ea32 : p->d_Ha32) + (size_t)b * 3 * n3;
+            CK(cudaMemcpyAsync(dt, t.data(), t.size() * 4, cudaMemcpyHostToDevice, p->stream));
+            CK(cudaMemcpyAsync(da, a.data(), a.size() * 4, cudaMemcpyHostToDevice, p->stream));
+            CK(cudaStreamSynchronize(p->stream));
+        }
+    }
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_get_fields(smat_fdtd_plan *p, int b, double *H_t, double *E_t)
+{
+    smat_clear_error();
+    if (!p || b < 0 || b >= p->batch) return smat_fail(SMAT_EINVAL, "get_fields: bad arguments");
+    const long long n3 = p->n3;
+    const int ln = p->lnotn;
+    for (int w = 0; w < 2; w++) {
+        double *dst = w ? E_t : H_t;
+        if (!dst) continue;
+        if (p->precision == SMAT_FP64) {
+            std::vector<double> m(3 * n3), a(3 * (size_t)(ln + 1));
+            const double *dm = (w ? p->d_E64 : p->d_H64) + (size_t)b * 3 * n3;
+            const double *da = (w ? p->d_Ea64 : p->d_Ha64) + (size_t)b * 3 * (ln + 1);
+            CK(cudaMemcpyAsync(m.data(), dm, m.size() * 8, cudaMemcpyDeviceToHost, p->stream));
+            CK(cudaMemcpyAsync(a.data(), da, a.size() * 8, cudaMemcpyDeviceToHost, p->stream));
+            CK(cudaStreamSynchronize(p->stream));
+            for (int c = 0; c < 3; c++) {
+                for (long long l = 0; l < n3; l++) dst[c + 3 * l] = m[c * n3 + l];
+                for (int x = 0; x <= ln; x++) dst[c + 3 * (n3 + x)] = a[(size_t)c * (ln + 1) + x];
+            }
+        } else {
+            std::vector<float> t(3 * n3), a(3 * n3);
+            const float *dt = (w ? p->d_E32 : p->d_H32) + (size_t)b * 3 * n3;
+            const float *da = (w ? p->d_Ea32 : p->d_Ha32) + (size_t)b * 3 * n3;
+            CK(cudaMemcpyAsync(t.data(), dt, t.size() * 4, cudaMemcpyDeviceToHost, p->stream));
+            CK(cudaMemcpyAsync(a.data(), da, a.size() * 4, cudaMemcpyDeviceToHost, p->stream));
+            CK(cudaStreamSynchronize(p->stream));
+            memset(dst, 0, sizeof(double) * 3 * (size_t)(n3 + ln + 1));
+            for (int c = 0; c < 3; c++)
+                for (long long l = 0; l < n3; l++) {
+                    if (p->cont[l] == 'n') {
+                        dst[c + 3 * l] = t[c * n3 + l];
+                    } else {
+                        const float ax = a[c * n3 + l];
+                        dst[c + 3 * l] = (double)(t[c * n3 + l] - ax);
+                        dst[c + 3 * (n3 + p->addr[l])] = ax;
+                    }
+                }
+        }
+    }
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_set_incident(smat_fdtd_plan *p, int b, const double *Hinc, const double *Einc)
+{
+    smat_clear_error();
+    if (!p || !Hinc || !Einc || b < 0 || b >= p->batch) return smat_fail(SMAT_EINVAL, "set_incident: bad arguments");
+    const size_t n = 4 * (size_t)p->pl;
+    CK(cudaMemcpyAsync(p->d_inc + (size_t)b * 8 * p->pl, Hinc, n * 8, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_inc + (size_t)b * 8 * p->pl + n, Einc, n * 8, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_set_source_plane(smat_fdtd_plan *p, int b, int iI, int inci_mode)
+{
+    smat_clear_error();
+    if (!p || b < 0 || b >= p->batch || iI < 0 || iI >= p->L[2] || inci_mode == 0)
+        return smat_fail(SMAT_EINVAL, "set_source_plane: bad arguments");
+    const double sg = (double)(inci_mode / (inci_mode < 0 ? -inci_mode : inci_mode));
+    CK(cudaMemcpyAsync(p->d_iI + b, &iI, sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemcpyAsync(p->d_isgn + b, &sg, 8, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_set_schedule(smat_fdtd_plan *p, int nsteps, const double *src, int nfreq, int nplanes,
+                                      const int *planes, const double *phase)
+{
+    smat_clear_error();
+    if (!p || nsteps <= 0 || !src || nfreq < 0 || (nfreq > 0 && (!phase || !planes || nplanes <= 0)))
+        return smat_fail(SMAT_EINVAL, "set_schedule: bad arguments");
+    int rc = setup_dft(p, nfreq, nfreq > 0 ? nplanes : 0, planes);
+    if (rc) return rc;
+    p->ref_dft = false;
+    if (p->d_sched) cudaFree(p->d_sched), p->d_sched = nullptr;
+    if (p->d_phase) cudaFree(p->d_phase), p->d_phase = nullptr;
+    if (p->d_phase32) cudaFree(p->d_phase32), p->d_phase32 = nullptr;
+    if ((rc = dalloc(&p->d_sched, 6 * (size_t)nsteps, p->stream))) return rc;
+    CK(cudaMemcpyAsync(p->d_sched, src, 6 * (size_t)nsteps * 8, cudaMemcpyHostToDevice, p->stream));
+    if (nfreq > 0) {
+        const size_t np = 4 * (size_t)nsteps * nfreq;
+        if ((rc = dalloc(&p->d_phase, np, p->stream))) return rc;
+        CK(cudaMemcpyAsync(p->d_phase, phase, np * 8, cudaMemcpyHostToDevice, p->stream));
+        if (p->precision == SMAT_FP32) {
+            std::vector<float> ph32(np);
+            for (size_t i = 0; i < np; i++) ph32[i] = (float)phase[i];
+            if ((rc = dalloc(&p->d_phase32, np, p->stream))) return rc;
+            CK(cudaMemcpyAsync(p->d_phase32, ph32.data(), np * 4, cudaMemcpyHostToDevice, p->stream));
+        }
+    }
+    p->nsched = nsteps;
+    CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+extern "C" int smat_cw_schedule(int N_2pi, const int tp[3], double *src, double *phase)
+{
+    smat_clear_error();
+    if (N_2pi <= 0 || !tp || tp[0] < 0 || tp[1] < 0 || tp[2] <= 0 || !src || !phase)
+        return smat_fail(SMAT_EINVAL, "cw_schedule: bad arguments");
+    return host_cw_schedule(N_2pi, tp, src, phase);
+}
+
+extern "C" int smat_fdtd_set_cw_schedule(smat_fdtd_plan *p, int N_2pi, const int tp[3])
+{
+    smat_clear_error();
+    if (!p || N_2pi <= 0 || !tp || tp[0] < 0 || tp[1] < 0 || tp[2] <= 0)
+        return smat_fail(SMAT_EINVAL, "set_cw_schedule: bad arguments");
+    if (!p->ref_planes_ok) {
+        const int pls[2] = {p->iBTIin[0], p->iBTIin[1]};
+        return check_planes(p, 2, pls);
+    }
+    const int nsteps = tp[2] * N_2pi;
+    std::vector<double> src(6 * (size_t)nsteps), ph(4 * (size_t)nsteps);
+    int rc = host_cw_schedule(N_2pi, tp, src.data(), ph.data());
+    if (rc) return rc;
+    const int planes[2] = {p->iBTIin[0], p->iBTIin[1]};
+    rc = smat_fdtd_set_schedule(p, nsteps, src.data(), 1, 2, planes, ph.data());
+    if (rc) return rc;
+    p->ref_dft = true;
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_step(smat_fdtd_plan *p, const double *Hi, const double *Ei, const double *ExpN2)
+{
+    smat_clear_error();
+    if (!p || !Hi || !Ei || !ExpN2) return smat_fail(SMAT_EINVAL, "step: bad arguments");
+    if (!p->ref_dft || p->nfreq < 1) return smat_fail(SMAT_ESTATE, "step: the reference DFT is not configured");
+    if (!p->ref_planes_ok) {
+        const int pls[2] = {p->iBTIin[0], p->iBTIin[1]};
+        return check_planes(p, 2, pls);
+    }
+    const int nf = p->nfreq;
+    p->nfreq = 1; /* explicit phases drive frequency slot 0 only */
+    const size_t n = 2 * (size_t)p->pl;
+    float x32[4] = {(float)ExpN2[0], (float)ExpN2[1], (float)ExpN2[2], (float)ExpN2[3]};
+    cudaError_t e = cudaMemcpyAsync(p->d_xsrc, Hi, n * 8, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_xsrc + n, Ei, n * 8, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_xphase, ExpN2, 4 * 8, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_xphase32, x32, 4 * 4, cudaMemcpyHostToDevice, p->stream);
+    if (e == cudaSuccess) {
+        launch_set(p->d_base, 0, p->stream);
+        enqueue_steps(p, 0, 1, true);
+        e = cudaStreamSynchronize(p->stream);
+    }
+    p->nfreq = nf;
+    if (e != cudaSuccess) return cuda_fail(e, "step");
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_run(smat_fdtd_plan *p, int k_begin, int k_end)
+{
+    smat_clear_error();
+    if (!p || k_begin < 0 || k_end < k_begin) return smat_fail(SMAT_EINVAL, "run: bad step range");
+    if (!p->d_sched) return smat_fail(SMAT_ESTATE, "run: no schedule (call set_cw_schedule or set_schedule)");
+    if (k_end > p->nsched) return smat_fail(SMAT_EINVAL, "run: k_end %d beyond the %d-step schedule", k_end, p->nsched);
+    launch_set(p->d_base, k_begin, p->stream);
+    int n = k_end - k_begin;
+    if (n >= GRAPH_STEPS) build_graph(p);
+    while (n >= GRAPH_STEPS) {
+        if (p->graph) {
+            CK(cudaGraphLaunch(p->graph, p->stream));
+        } else {
+            enqueue_steps(p, 0, GRAPH_STEPS, false);
+            launch_bump(p->d_base, GRAPH_STEPS, p->stream);
+        }
+        n -= GRAPH_STEPS;
+    }
+    if (n > 0) {
+        enqueue_steps(p, 0, n, false);
+        launch_bump(p->d_base, n, p->stream);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "run: launch");
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps, double *ms)
+{
+    smat_clear_error();
+    if (!p || !ms || nsteps <= 0 || k_begin < 0 || k_begin + nsteps > p->nsched)
+        return smat_fail(SMAT_EINVAL, "time_kernels: bad arguments");
+    cudaEvent_t ev[4];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    double acc[3] = {0, 0, 0};
+    float t;
+    launch_set(p->d_base, k_begin, p->stream);
+    const P64 q64 = make_p64(p, false);
+    const P32 q32 = make_p32(p, false);
+    for (int i = 0; i < nsteps; i++) {
+        CK(cudaEventRecord(ev[0], p->stream));
+        if (p->precision == SMAT_FP64) launch_h64(q64, i, p->stream);
+        else launch_h32(q32, i, p->by32, p->stream);
+        CK(cudaEventRecord(ev[1], p->stream));
+        if (p->precision == SMAT_FP64) launch_e64(q64, i, p->stream);
+        else launch_e32(q32, i, p->by32, p->stream);
+        CK(cudaEventRecord(ev[2], p->stream));
+        if (p->precision == SMAT_FP64) launch_dft64(q64, i, p->stream);
+        else if ((i + 1) % RING_K == 0 || i + 1 == nsteps) {
+            const int cnt = (i + 1) % RING_K == 0 ? RING_K : (i + 1) % RING_K;
+            launch_flush32(q32, i + 1, cnt, p->stream);
+        }
+        CK(cudaEventRecord(ev[3], p->stream));
+        CK(cudaEventSynchronize(ev[3]));
+        for (int k = 0; k < 3; k++) {
+            CK(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            acc[k] += t;
+        }
+    }
+    launch_bump(p->d_base, nsteps, p->stream);
+    CK(cudaStreamSynchronize(p->stream));
+    for (auto &e : ev) cudaEventDestroy(e);
+    ms[0] = acc[0] / nsteps;
+    ms[1] = acc[1] / nsteps;
+    ms[2] = acc[2] / nsteps;
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int block_y)
+{
+    if (!p || block_y < 1 || block_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
+    p->by32 = block_y;
+    drop_graph(p);
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_sync(smat_fdtd_plan *p)
+{
+    if (!p) return smat_fail(SMAT_EINVAL, "null plan");
+    CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+static int read_acc(smat_fdtd_plan *p, int b, int f, int q, std::vector<double> &out)
+{
+    const size_t n = 4 * (size_t)p->pl * 2;
+    out.resize(n);
+    const double *src = p->d_acc + (((size_t)b * p->nfreq + f) * p->nq + q) * n;
+    CK(cudaMemcpyAsync(out.data(), src, n * 8, cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_get_monitor(smat_fdtd_plan *p, int b, double *HB, double *EB, double *HT, double *ET)
+{
+    smat_clear_error();
+    if (!p || b < 0 || b >= p->batch) return smat_fail(SMAT_EINVAL, "get_monitor: bad arguments");
+    if (!p->ref_dft) return smat_fail(SMAT_ESTATE, "get_monitor: the reference DFT is not configured");
+    std::vector<double> a;
+    for (int q = 0; q < 2; q++) {
+        int rc = read_acc(p, b, 0, q, a);
+        if (rc) return rc;
+        double *Hd = q ? HT : HB, *Ed = q ? ET : EB;
+        for (long long px = 0; px < p->pl; px++)
+            for (int v = 0; v < 2; v++) {
+                if (Hd) {
+                    Hd[2 * (v + 2 * px)] = a[2 * (v * p->pl + px)];
+                    Hd[2 * (v + 2 * px) + 1] = a[2 * (v * p->pl + px) + 1];
+                }
+                if (Ed) {
+                    Ed[2 * (v + 2 * px)] = a[2 * ((2 + v) * p->pl + px)];
+                    Ed[2 * (v + 2 * px) + 1] = a[2 * ((2 + v) * p->pl + px) + 1];
+                }
+            }
+    }
+    return SMAT_OK;
+}
+
+/* preload the reference DFT accumulators (used by smat_main_calc, whose
+ * caller's HB..ET carry the running sums) */
+static int set_monitor(smat_fdtd_plan *p, const double *HB, const double *EB, const double *HT, const double *ET)
+{
+    const size_t n = 4 * (size_t)p->pl * 2;
+    std::vector<double> a(n);
+    for (int q = 0; q < 2; q++) {
+        const double *Hs = q ? HT : HB, *Es = q ? ET : EB;
+        for (long long px = 0; px < p->pl; px++)
+            for (int v = 0; v < 2; v++) {
+                a[2 * (v * p->pl + px)] = Hs[2 * (v + 2 * px)];
+                a[2 * (v * p->pl + px) + 1] = Hs[2 * (v + 2 * px) + 1];
+                a[2 * ((2 + v) * p->pl + px)] = Es[2 * (v + 2 * px)];
+                a[2 * ((2 + v) * p->pl + px) + 1] = Es[2 * (v + 2 * px) + 1];
+            }
+        CK(cudaMemcpyAsync(p->d_acc + q * n, a.data(), n * 8, cudaMemcpyHostToDevice, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+    }
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_get_dft(smat_fdtd_plan *p, int b, int f, int q, double *out)
+{
+    smat_clear_error();
+    if (!p || !out || b < 0 || b >= p->batch || f < 0 || f >= p->nfreq || q < 0 || q >= p->nq)
+        return smat_fail(SMAT_EINVAL, "get_dft: bad arguments");
+    std::vector<double> a;
+    int rc = read_acc(p, b, f, q, a);
+    if (rc) return rc;
+    memcpy(out, a.data(), a.size() * 8);
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_check_finite(smat_fdtd_plan *p, int *finite, double *max_abs)
+{
+    smat_clear_error();
+    if (!p) return smat_fail(SMAT_EINVAL, "null plan");
+    CK(cudaMemsetAsync(p->d_scratch, 0, 8, p->stream));
+    const bool d = p->precision == SMAT_FP64;
+    const long long nf = (long long)p->batch * 3 * p->n3;
+    const long long na = d ? (long long)p->batch * 3 * (p->lnotn + 1) : nf;
+    const void *arr[4] = {d ? (void *)p->d_H64 : (void *)p->d_H32, d ? (void *)p->d_E64 : (void *)p->d_E32,
+                          d ? (void *)p->d_Ha64 : (void *)p->d_Ha32, d ? (void *)p->d_Ea64 : (void *)p->d_Ea32};
+    for (int i = 0; i < 4; i++) launch_maxabs(arr[i], i < 2 ? nf : na, d, p->d_scratch, p->stream);
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, p->d_scratch, 8, cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    double m;
+    memcpy(&m, &bits, 8);
+    if (finite) *finite = std::isfinite(m) ? 1 : 0;
+    if (max_abs) *max_abs = m;
+    return SMAT_OK;
+}
+
+extern "C" int smat_main_calc(const int L[4], const double *Ah, const double *Bh, const double *Ae, const double *Be,
+                              const int iBc[3], double *H_t, double *E_t, const int iBTIin[4], const double *Hi,
+                              const double *Ei, const double *ExpN2, double *HB, double *EB, double *HT, double *ET,
+                              const char *Cont, const int *address_notn)
+{
+    smat_clear_error();
+    if (!L || !H_t || !E_t || !Hi || !Ei || !ExpN2 || !HB || !EB || !HT || !ET || !Cont || !address_notn)
+        return smat_fail(SMAT_EINVAL, "main_calc: null argument");
+    const long long n3 = (long long)L[0] * L[1] * L[2];
+    int lnotn = 0;
+    for (long long l = 0; l < n3; l++) lnotn += Cont[l] != 'n';
+    smat_fdtd_plan *p = nullptr;
+    int rc = smat_fdtd_create_from_coeffs(L, Ah, Bh, Ae, Be, iBc, Cont, address_notn, lnotn, iBTIin, 1, nullptr, &p);
+    if (rc) return rc;
+    rc = smat_fdtd_set_fields(p, 0, H_t, E_t);
+    if (!rc) rc = set_monitor(p, HB, EB, HT, ET);
+    if (!rc) rc = smat_fdtd_step(p, Hi, Ei, ExpN2);
+    if (!rc) rc = smat_fdtd_get_fields(p, 0, H_t, E_t);
+    if (!rc) rc = smat_fdtd_get_monitor(p, 0, HB, EB, HT, ET);
+    smat_fdtd_destroy(p);
+    return rc;
+}

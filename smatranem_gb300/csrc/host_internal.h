@@ -1,0 +1,22 @@
+/* Internal host-side helpers shared by the C and CUDA translation units. */
+#ifndef SMATRAN_HOST_INTERNAL_H
+#define SMATRAN_HOST_INTERNAL_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Records a printf-style message for smat_last_error() and returns code. */
+int smat_fail(int code, const char *fmt, ...);
+void smat_clear_error(void);
+
+/* exp(i*phi) table of main :93-99, 2*N complex into out (4*N doubles). */
+int host_expn(int N, double *out);
+/* The reference CW run as a schedule: src 6 doubles per step, phase 4 doubles
+ * per step, stop-period*N steps (main :153-167). */
+int host_cw_schedule(int N, const int time_period[3], double *src, double *phase);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

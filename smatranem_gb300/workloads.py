@@ -1,0 +1,362 @@
+"""Synthetic structures in the form the SMatrAnEM mesher chain hands the FDTD.
+
+The reference FDTD reads, per cell and component, the complex mu and epsi that
+Med3D -> BindData -> CorrF -> PMLgen leave in the Med files: material value
+times the metric factor fx_c = H_{c+1} H_{c+2} / H_c (H_j = du_j/dxi_j * h_j,
+MixedData/BindData.c:223-228), times the PML stretch s_{c+1} s_{c+2} / s_c
+with s = 1 + i*sigma (PMLset/PMLcalc.c:227-231), sigma graded as
+sigma_max * |depth/thickness|^p, sigma_max = -(p+1) ln(sqRef) / (4 omega d)
+(PMLset/PMLcalc.c:246-260).  The CFL bound written into each Med header is
+sqrt(min over cells of e00 e11 e22 m00 m11 m22 / ((e00+e11+e22)(m00+m11+m22)))
+(PMLset/PMLcalc.c:279-313); the FDTD takes min_Dt as its square root.
+
+Everything here is seeded numpy; no dataset is involved.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from . import fdtd
+
+
+@dataclasses.dataclass
+class Structure:
+    L: tuple            # (L0, L1, L2, L3)
+    mu: np.ndarray      # complex (n3, 3): stretched, as read from the Med files
+    epsi: np.ndarray
+    omega: float        # k/k0
+    min_dt: float       # the FDTD's min_Dt (sqrt of the Med-header "min Dt^2")
+    iBc: tuple = (1, 1, 1)
+    pec: np.ndarray | None = None  # uint8 (n3,), E coefficients forced to 0
+    name: str = ""
+
+    @property
+    def n3(self):
+        return self.L[0] * self.L[1] * self.L[2]
+
+
+@dataclasses.dataclass
+class Prepared:
+    """Outputs of the reference precompute (main :62-143)."""
+    s: Structure
+    sigma: np.ndarray
+    mu: np.ndarray      # after remove_sigma, complex (n3*3,)
+    epsi: np.ndarray
+    cont: np.ndarray
+    addr: np.ndarray
+    lnotn: int
+    n2pi: int
+    invtau_R: float
+    invtau_I: float
+
+    def coefficients(self):
+        return fdtd.coefficients(self.s.L, self.lnotn, self.sigma, self.mu, self.epsi, self.cont, self.addr,
+                                 self.invtau_R, self.invtau_I)
+
+    @property
+    def dt(self):
+        return 2 * math.pi / (self.s.omega * self.n2pi)
+
+
+def pml_sigma(n: int, lo: int, hi: int, omega: float, thick_lo: float, thick_hi: float,
+              sq_ref: float = 1e-12, power: int = 3):
+    """sigma at the H (h=0) and E (h=1) sub-points of n cells with lo/hi PML cells.
+
+    The H sub-point of cell j sits at j + 0.5 and the E sub-point at j + 1.0 in
+    cell units (the E component is half a cell forward of H along its own axis,
+    as the forward difference ope_R implies)."""
+    out = np.zeros((2, n))
+    for h, shift in ((0, 0.5), (1, 1.0)):
+        x = np.arange(n) + shift
+        if lo > 0:
+            smax = -(power + 1) * math.log(sq_ref) / (4 * omega * thick_lo)
+            d = np.clip((lo - x) / lo, 0, None)
+            out[h] += smax * d ** power
+        if hi > 0:
+            smax = -(power + 1) * math.log(sq_ref) / (4 * omega * thick_hi)
+            d = np.clip((x - (n - hi)) / hi, 0, None)
+            out[h] += smax * d ** power
+    return out
+
+
+def sigma_vector(L, sig_axes):
+    """Pack per-axis (2, L_a) profiles into the reference's 2*(L0+L1+L2) layout."""
+    parts = []
+    for a in range(3):
+        s = sig_axes[a]
+        v = np.zeros(2 * L[a])
+        v[0::2] = s[0]
+        v[1::2] = s[1]
+        parts.append(v)
+    return np.concatenate(parts)
+
+
+def stretch_media(L, mu_r, eps_r, sig_axes):
+    """Apply the PMLgen stretch: mu_c *= s_h(c+1) s_h(c+2) / s_e(c), epsi swapped."""
+    L0, L1, L2 = L[:3]
+    j = np.indices((L2, L1, L0)).reshape(3, -1)[::-1]  # j[0] fastest
+    s = []
+    for h in range(2):
+        s.append([1 + 1j * sig_axes[a][h][j[a]] for a in range(3)])
+    mu = np.array(mu_r, dtype=np.complex128, copy=True)
+    ep = np.array(eps_r, dtype=np.complex128, copy=True)
+    for c in range(3):
+        a1, a2 = (c + 1) % 3, (c + 2) % 3
+        mu[:, c] *= s[0][a1] * s[0][a2] / s[1][c]
+        ep[:, c] *= s[1][a1] * s[1][a2] / s[0][c]
+    return mu, ep
+
+
+def cfl_min_dt(mu_r, eps_r):
+    """min_Dt of the FDTD from real media (PMLcalc.c:279-313 then sqrt)."""
+    m = np.real(mu_r)
+    e = np.real(eps_r)
+    r = (e[:, 0] * e[:, 1] * e[:, 2] * m[:, 0] * m[:, 1] * m[:, 2]) / (e.sum(1) * m.sum(1))
+    r = r[np.isfinite(r) & (r > 0)]
+    return math.sqrt(math.sqrt(r.min()))
+
+
+def metric_fx(Hs):
+    """fx_c = H_{c+1} H_{c+2} / H_c from per-cell scale factors Hs (n3, 3)."""
+    fx = np.empty_like(Hs)
+    for c in range(3):
+        fx[:, c] = Hs[:, (c + 1) % 3] * Hs[:, (c + 2) % 3] / Hs[:, c]
+    return fx
+
+
+def random_structure(L, seed=0, pml=(2, 2, 2), pml_z_only=False, metals=0.0, lossy=0.0, pec=0.0,
+                     iBc=(1, 1, 1), omega=0.4, dx=0.2, aniso=0.15, sq_ref=1e-8):
+    """A small seeded structure exercising every cell class of the reference.
+
+    metals/lossy/pec are fractions of interior cells (outside the PML and off
+    the centre lines the FDTD reads sigma from) that become 'e'/'h'/'b' cells,
+    absorbing dielectrics, or PEC cells.  A metal component gets a Drude-like
+    epsi (Re < 0, Im > 0) or a mu with Re > 0, Im < 0; both have tan(arg) < 0,
+    the reference's test for its stable-form update.  That update is not
+    unconditionally stable (fields near such cells can grow), so tests that use
+    metals run few steps."""
+    rng = np.random.default_rng(seed)
+    L0, L1, L2, L3 = L
+    n3 = L0 * L1 * L2
+    Hs = dx * rng.uniform(1 - aniso, 1 + aniso, size=(n3, 3))
+    fx = metric_fx(Hs)
+    mu_r = fx * rng.uniform(0.9, 1.3, size=(n3, 3))
+    eps_r = fx * rng.uniform(1.0, 6.0, size=(n3, 3))
+    min_dt = cfl_min_dt(mu_r, eps_r)
+    j = np.indices((L2, L1, L0)).reshape(3, -1)[::-1]
+    p = pml
+    thick = [p[a] * dx for a in range(3)]
+    sig = []
+    for a, n in enumerate((L0, L1, L2)):
+        if pml_z_only and a < 2:
+            sig.append(np.zeros((2, n)))
+        else:
+            sig.append(pml_sigma(n, p[a], p[a], omega, max(thick[a], 1e-9), max(thick[a], 1e-9), sq_ref))
+    interior = np.ones(n3, bool)
+    for a, n in enumerate((L0, L1, L2)):
+        if not (pml_z_only and a < 2):
+            interior &= (j[a] >= p[a] + 1) & (j[a] < n - p[a] - 1)
+    # keep the centre lines the FDTD reads sigma from clean
+    c0, c1, c2 = L0 // 2, L1 // 2, L2 // 2
+    on_line = ((j[1] == c1) & (j[2] == c2)) | ((j[0] == c0) & (j[2] == c2)) | ((j[0] == c0) & (j[1] == c1))
+    cand = np.flatnonzero(interior & ~on_line)
+    rng.shuffle(cand)
+    nm, nl, npc = (int(round(f * len(cand))) for f in (metals, lossy, pec))
+    mcells, lcells, pcells = cand[:nm], cand[nm:nm + nl], cand[nm + nl:nm + nl + npc]
+    mu_c = mu_r.astype(np.complex128)
+    ep_c = eps_r.astype(np.complex128)
+    for i, l in enumerate(mcells):
+        kind = i % 3  # 'e', 'h', 'b'
+        comp = rng.integers(0, 3)
+        if kind in (0, 2):
+            ep_c[l, comp] = fx[l, comp] * (-rng.uniform(2, 20) + 1j * rng.uniform(0.5, 3))
+        if kind in (1, 2):
+            mu_c[l, comp] = fx[l, comp] * (rng.uniform(1, 2) - 1j * rng.uniform(0.1, 1))
+    for l in lcells:
+        ep_c[l] += 1j * fx[l] * rng.uniform(0.01, 0.5, size=3)
+    mu_s, ep_s = stretch_media(L, mu_c, ep_c, sig)
+    pec_mask = None
+    if npc:
+        pec_mask = np.zeros(n3, np.uint8)
+        pec_mask[pcells] = 1
+    return Structure(L=tuple(L), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=tuple(iBc), pec=pec_mask,
+                     name=f"random{tuple(L)}")
+
+
+def prepare(s: Structure, dt_factor: float = 1.0) -> Prepared:
+    """The reference precompute through the library (set_sigma .. set_tau)."""
+    mu = np.ascontiguousarray(s.mu.reshape(-1))
+    ep = np.ascontiguousarray(s.epsi.reshape(-1))
+    sigma = fdtd.set_sigma(s.L, mu, ep)
+    mu2, ep2 = fdtd.remove_sigma(s.L, mu, ep, sigma)
+    cont, addr, lnotn = fdtd.set_address(s.L, sigma, mu2, ep2)
+    n2pi, iR, iI = fdtd.set_tau(s.omega, s.min_dt / dt_factor)
+    return Prepared(s=s, sigma=sigma, mu=mu2, epsi=ep2, cont=cont, addr=addr, lnotn=lnotn, n2pi=n2pi,
+                    invtau_R=iR, invtau_I=iI)
+
+
+def random_fields(n, lnotn, seed=0, scale=1.0):
+    """Random H_t, E_t in the reference layout (sentinel zero)."""
+    rng = np.random.default_rng(seed)
+    m = 3 * (n + lnotn + 1)
+    H = rng.standard_normal(m) * scale
+    E = rng.standard_normal(m) * scale
+    H[-3:] = 0
+    E[-3:] = 0
+    return H, E
+
+
+def random_incident(pl, seed=0, real_e=True):
+    rng = np.random.default_rng(seed)
+    Hinc = rng.standard_normal(2 * pl) + 1j * rng.standard_normal(2 * pl)
+    Einc = rng.standard_normal(2 * pl) + (0 if real_e else 1j * rng.standard_normal(2 * pl))
+    return Hinc.astype(np.complex128), np.asarray(Einc, dtype=np.complex128)
+
+
+# ---------------------------------------------------------------------------
+# Curvilinear strip-waveguide bend (the bend benchmark structure)
+# ---------------------------------------------------------------------------
+
+INV_K0_UM = 0.1  # unit of length: 1/k0 = 0.1 um, as in the reference example deck
+
+
+def graded_spacing(n, center, fine, coarse, width):
+    """Cell sizes growing smoothly from `fine` at cell `center` to `coarse`."""
+    d = np.arange(n) + 0.5 - center
+    return fine + (coarse - fine) * (1.0 - np.exp(-(d / width) ** 2))
+
+
+@dataclasses.dataclass
+class Bend:
+    s: Structure
+    iB: int
+    iT: int
+    iI: int
+    pml: int
+    u0: np.ndarray   # cell-centre coordinates across (um), core centre at 0
+    u1: np.ndarray
+    n_eff: float = 2.4
+
+
+def bend_structure(shape=(256, 192, 160), pml=12, L3=16, radius_um=2.0, core=(0.45, 0.22), eps_core=12.11,
+                   eps_clad=2.085, lam0_um=1.55, cell_um=(0.015, 0.025), core_cell0=45, dt_factor=1.0 / 0.99,
+                   sq_ref=1e-12, power=3) -> Bend:
+    """Silicon strip 90-degree bend in orthogonal curvilinear coordinates.
+
+    u0 is the in-plane transverse (radial) coordinate, u1 the vertical one and
+    u2 the arc length along the bend; the bend (curvature 1/R) spans the
+    L2 - 2*L3 scatterer layers and the L3 outer layers at each end are straight
+    ports.  Metric: H0 = du0, H1 = du1, H2 = du2 * (1 + kappa*u0) (the scale
+    factor of polar coordinates), fx_c = H_{c+1} H_{c+2} / H_c per cell, so
+    every cell carries distinct coefficients.  Cell sizes du0, du1 grade from
+    15 nm at the core to 25 nm; du2 = quarter-circle length / bend layers.  The
+    core sits near the inner side of the bend (cell core_cell0 of L0) so that
+    1 + kappa*u0 stays above 0.5.  12-cell split PML on all six faces."""
+    L0, L1, L2 = shape
+    fine, coarse = (c / INV_K0_UM for c in cell_um)
+    du0 = graded_spacing(L0, core_cell0, fine, coarse, 40.0)
+    du1 = graded_spacing(L1, L1 / 2, fine, coarse, 30.0)
+    u0 = np.cumsum(du0) - 0.5 * du0
+    u0 = u0 - u0[core_cell0]
+    u1 = np.cumsum(du1) - 0.5 * du1
+    u1 = u1 - u1[L1 // 2]
+    R = radius_um / INV_K0_UM
+    nb = L2 - 2 * L3
+    du2 = np.full(L2, fine + 0.25 * (coarse - fine))
+    du2[L3:L2 - L3] = 0.5 * math.pi * R / nb
+    kappa = np.zeros(L2)
+    kappa[L3:L2 - L3] = 1.0 / R
+    omega = 2 * math.pi * INV_K0_UM / lam0_um
+    n3 = L0 * L1 * L2
+    j0 = np.tile(np.arange(L0), L1 * L2)
+    j1 = np.tile(np.repeat(np.arange(L1), L0), L2)
+    j2 = np.repeat(np.arange(L2), L0 * L1)
+    h2 = 1.0 + kappa[j2] * u0[j0]
+    Hs = np.stack([du0[j0], du1[j1], du2[j2] * h2], axis=1)
+    fx = metric_fx(Hs)
+    del Hs, h2
+    in_core = (np.abs(u0[j0]) <= 0.5 * core[0] / INV_K0_UM) & (np.abs(u1[j1]) <= 0.5 * core[1] / INV_K0_UM)
+    eps_r = np.where(in_core, eps_core, eps_clad)[:, None] * fx
+    mu_r = fx
+    min_dt = cfl_min_dt(mu_r, eps_r) / dt_factor * dt_factor  # header value; dt_factor applied in set_tau
+    sig = []
+    for a, (n, d) in enumerate(((L0, du0), (L1, du1), (L2, du2))):
+        th_lo, th_hi = float(d[:pml].sum()), float(d[n - pml:].sum())
+        sig.append(pml_sigma(n, pml, pml, omega, th_lo, th_hi, sq_ref, power))
+    mu_s, ep_s = stretch_media((L0, L1, L2), mu_r, eps_r, sig)
+    del mu_r, eps_r, fx
+    s = Structure(L=(L0, L1, L2, L3), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=(0, 0, 0),
+                  name=f"bend{L0}x{L1}x{L2}")
+    return Bend(s=s, iB=pml + 1, iT=L2 - pml - 2, iI=pml + 3, pml=pml, u0=u0 * INV_K0_UM, u1=u1 * INV_K0_UM)
+
+
+def mode_profiles(b: Bend, n_modes=4, w0_um=0.26, w1_um=0.16):
+    """Approximate guided-mode sheets of the strip: TE0, TM0, TE1, TM1.
+
+    Returns a list of (Hinc, Einc) complex planes (2*L0*L1, component v of pixel
+    p at v + 2p) for propagation along +u2: TE modes carry E_x with
+    H_y = n_eff E_x, TM modes E_y with H_x = -n_eff E_y.  Normalised to unit
+    overlap norm.  They stand in for the Mcalc eigenvectors (no mode solver in
+    this path)."""
+    L0, L1 = b.s.L[0], b.s.L[1]
+    x = b.u0[None, :] / w0_um
+    y = b.u1[:, None] / w1_um
+    g = np.exp(-x ** 2 - y ** 2)
+    shapes = [g, g, x * g, y * g]
+    out = []
+    for m in range(n_modes):
+        f = shapes[m].reshape(-1)
+        f = f / math.sqrt(2 * b.n_eff * float(np.sum(f * f)))
+        Hinc = np.zeros(2 * L0 * L1, np.complex128)
+        Einc = np.zeros(2 * L0 * L1, np.complex128)
+        if m % 2 == 0:  # TE: E_x, H_y
+            Einc[0::2] = f
+            Hinc[1::2] = b.n_eff * f
+        else:           # TM: E_y, H_x
+            Einc[1::2] = f
+            Hinc[0::2] = -b.n_eff * f
+        out.append((Hinc, Einc))
+    return out
+
+
+def pulse_schedule(nsteps, dt, lam0_um=1.55, bandwidth=0.2, lams_um=None, delay_sigmas=4.0):
+    """Gaussian-modulated sine sheet source and DFT phases at wavelengths lams_um.
+
+    Source: g(t) sin(omega0 t) with g a Gaussian whose spectral FWHM is
+    `bandwidth` * omega0; E sheets at t = (k+1/2) dt, H sheets at (k+1) dt (the
+    reference's half-step times).  DFT weights exp(i omega t) at the same times
+    as the reference's ExpN (main :93-99, :165)."""
+    w0 = 2 * math.pi * INV_K0_UM / lam0_um
+    sigma_w = bandwidth * w0 / 2.355
+    tau = 1.0 / sigma_w
+    t0 = delay_sigmas * tau
+    k = np.arange(nsteps)
+    tE, tH = (k + 0.5) * dt, (k + 1.0) * dt
+    src = np.zeros((nsteps, 6))
+    src[:, 0] = np.exp(-0.5 * ((tE - t0) / tau) ** 2)
+    src[:, 1] = np.sin(w0 * tE)
+    src[:, 3] = np.exp(-0.5 * ((tH - t0) / tau) ** 2)
+    src[:, 4] = np.sin(w0 * tH)
+    if lams_um is None:
+        lams_um = [lam0_um]
+    om = 2 * math.pi * INV_K0_UM / np.asarray(lams_um, dtype=np.float64)
+    ph = np.empty((nsteps, len(om), 4))
+    ph[:, :, 0] = np.cos(om[None] * tH[:, None])
+    ph[:, :, 1] = np.sin(om[None] * tH[:, None])
+    ph[:, :, 2] = np.cos(om[None] * (tH[:, None] + 0.5 * dt))
+    ph[:, :, 3] = np.sin(om[None] * (tH[:, None] + 0.5 * dt))
+    return src, ph
+
+
+def overlap(dft_plane, Hinc, Einc):
+    """Mode overlap of one DFT plane (4, pl: Hx, Hy, Ex, Ey) with a mode sheet:
+    sum conj(mode) . (Hx, Hy, -Ey, Ex), the vector S_calc projects
+    (FDTDsplitfieldMetal.c:437-445) with the mode in the same arrangement."""
+    mh = np.stack([Hinc[0::2], Hinc[1::2]])
+    me = np.stack([-Einc[1::2], Einc[0::2]])
+    v = np.stack([dft_plane[0], dft_plane[1], -dft_plane[3], dft_plane[2]])
+    m = np.concatenate([mh, me])
+    return complex(np.sum(np.conj(m) * v))

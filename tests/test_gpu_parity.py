@@ -1,0 +1,308 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the goldens.
+
+FP64 plans must reproduce the reference bit for bit (np.array_equal).  FP32
+plans are compared with a relative tolerance stated per test: the error of a
+field after n steps in FP32 against the FP64 result, measured as
+max|x32 - x64| / max|x64| over the array.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+
+
+def _fdtd():
+    from smatranem_gb300 import fdtd
+    return fdtd
+
+
+def _plan_from_golden(g, precision, batch=1):
+    f = _fdtd()
+    return f.Plan.create(g["L"], g["iBc"], g["iBTIin"], float(g["invtau_R"]), float(g["invtau_I"]), g["mu"],
+                         g["epsi"], g["sigma"], precision=precision, batch=batch)
+
+
+def _relerr(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_run_is_bit_identical_to_reference(built, name):
+    g = load_golden(name)
+    f = _fdtd()
+    n2, tp, nsteps = int(g["n2pi"]), g["time_period"], int(g["nsteps"])
+    with _plan_from_golden(g, f.FP64) as p:
+        p.set_fields(0, g["H0"], g["E0"])
+        p.set_incident(0, g["Hinc"], g["Einc"])
+        if int(g["ref_exits"]) > 0:
+            # a monitor plane holds a PML cell: the reference exits, so does the CW schedule
+            with pytest.raises(f.FdtdError) as ei:
+                p.set_cw_schedule(n2, tp)
+            assert ei.value.code == -4
+            src, ph = f.cw_schedule(n2, tp)
+            p.set_schedule(src, planes=(int(g["iBTIin"][0]), int(g["iBTIin"][1])), phase=ph)
+        else:
+            p.set_cw_schedule(n2, tp)
+        p.run(0, nsteps)
+        H, E = p.get_fields(0)
+        assert np.array_equal(H, g["H"])
+        assert np.array_equal(E, g["E"])
+        if int(g["ref_exits"]) == 0:
+            HB, EB, HT, ET = p.get_monitor(0)
+            for m, key in zip((HB, EB, HT, ET), ("HB", "EB", "HT", "ET")):
+                assert np.array_equal(m, g[key]), key
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_chunking_does_not_change_results(built, name):
+    """Graph-captured chunks, remainders and split run() calls give identical bits."""
+    g = load_golden(name)
+    f = _fdtd()
+    n2, tp = int(g["n2pi"]), g["time_period"]
+    src, ph = f.cw_schedule(n2, tp)
+    nsteps = min(75, src.shape[0])
+    planes = (int(g["iBTIin"][0]), int(g["iBTIin"][1]))
+    out = []
+    for cuts in ((0, nsteps), (0, 7, 40, nsteps)):
+        with _plan_from_golden(g, f.FP64) as p:
+            p.set_fields(0, g["H0"] * 1e-3, g["E0"] * 1e-3)
+            p.set_incident(0, g["Hinc"], g["Einc"])
+            p.set_schedule(src, planes=planes, phase=ph)
+            for a, b in zip(cuts[:-1], cuts[1:]):
+                p.run(a, b)
+            out.append((*p.get_fields(0), p.get_dft(0, 0, 0), p.get_dft(0, 0, 1)))
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["zpml_plain", "zpml_metal", "periodic_bc"])
+def test_step_api_and_main_calc_are_bit_identical(built, port, name):
+    """smat_fdtd_step (explicit Hi/Ei) and the stateless smat_main_calc."""
+    g = load_golden(name)
+    f = _fdtd()
+    L = g["L"]
+    pl = int(L[0] * L[1])
+    rng = np.random.default_rng(7)
+    steps = [(rng.standard_normal(2 * pl), rng.standard_normal(2 * pl), np.exp(1j * rng.uniform(0, 6, 2)))
+             for _ in range(3)]
+    coef = (g["Ah"], g["Bh"], g["Ae"], g["Be"])
+    # oracle
+    H, E = g["H0"].copy(), g["E0"].copy()
+    mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+    for Hi, Ei, z in steps:
+        assert port.main_calc(L, *coef, g["iBc"], H, E, g["iBTIin"], Hi, Ei, z, *mons, g["cont"], g["addr"]) == 0
+    # plan step API
+    with _plan_from_golden(g, f.FP64) as p:
+        p.set_fields(0, g["H0"], g["E0"])
+        for Hi, Ei, z in steps:
+            p.step(Hi, Ei, z)
+        H2, E2 = p.get_fields(0)
+        m2 = p.get_monitor(0)
+    assert np.array_equal(H2, H) and np.array_equal(E2, E)
+    for a, b in zip(m2, mons):
+        assert np.array_equal(a, b)
+    # stateless main_calc, same signature as the reference
+    H3, E3 = g["H0"].copy(), g["E0"].copy()
+    m3 = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+    for Hi, Ei, z in steps:
+        f.main_calc(L, *coef, g["iBc"], H3, E3, g["iBTIin"], Hi, Ei, z, *m3, g["cont"], g["addr"])
+    assert np.array_equal(H3, H) and np.array_equal(E3, E)
+    for a, b in zip(m3, mons):
+        assert np.array_equal(a, b)
+
+
+def test_from_coeffs_plan_and_batch(built, port):
+    """A plan built from main_calc's arrays; three excitations in one batch each
+    equal their own oracle run."""
+    g = load_golden("zpml_plain")
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    L, n2, tp = g["L"], int(g["n2pi"]), g["time_period"]
+    pl = int(L[0] * L[1])
+    n3 = int(np.prod(L[:3]))
+    ln = int(g["lnotn"])
+    coef = (g["Ah"], g["Bh"], g["Ae"], g["Be"])
+    nsteps = 45
+    excit = []
+    for b in range(3):
+        H0, E0 = W.random_fields(n3, ln, seed=30 + b, scale=1e-3)
+        Hinc, Einc = W.random_incident(pl, seed=40 + b)
+        excit.append((H0, E0, Hinc, Einc))
+    with f.Plan.from_coeffs(L, *coef, g["iBc"], g["cont"], g["addr"], ln, g["iBTIin"], batch=3) as p:
+        for b, (H0, E0, Hinc, Einc) in enumerate(excit):
+            p.set_fields(b, H0, E0)
+            p.set_incident(b, Hinc, Einc)
+        p.set_cw_schedule(n2, tp)
+        p.run(0, nsteps)
+        got = [(*p.get_fields(b), *p.get_monitor(b)) for b in range(3)]
+    for b, (H0, E0, Hinc, Einc) in enumerate(excit):
+        H, E = H0.copy(), E0.copy()
+        mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+        port.time_loop(L, *coef, g["iBc"], H, E, g["iBTIin"], Hinc, Einc, n2, tp, 0, nsteps, *mons, g["cont"],
+                       g["addr"])
+        for a, r in zip(got[b], (H, E, *mons)):
+            assert np.array_equal(a, r)
+
+
+def test_general_dft_matches_oracle_fields(built, port):
+    """Multi-frequency DFT on three planes, one cutting the x/y PML, against a
+    DFT of the oracle's fields (total field on split cells)."""
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    L = (10, 9, 12, 2)
+    s = W.random_structure(L, seed=5, pml=(2, 2, 2))
+    pr = W.prepare(s)
+    coef = pr.coefficients()
+    n3, pl = s.n3, L[0] * L[1]
+    tp = (1, 1, 3)
+    src, _ = f.cw_schedule(pr.n2pi, tp)
+    nsteps = 20
+    src = src[:nsteps]
+    rng = np.random.default_rng(3)
+    nf = 3
+    wdt = rng.uniform(0.05, 0.4, nf)
+    k = np.arange(nsteps)[:, None]
+    ph = np.stack([np.cos(wdt * (k + 1)), np.sin(wdt * (k + 1)), np.cos(wdt * (k + 1.5)), np.sin(wdt * (k + 1.5))],
+                  axis=-1)
+    planes = (3, 6, 0)  # plane 0 lies in the z-PML; all cut the x/y PML
+    H0, E0 = W.random_fields(n3, pr.lnotn, seed=9, scale=1e-2)
+    Hinc, Einc = W.random_incident(pl, seed=8)
+    iBTIin = (3, 6, 5, 1)
+    with f.Plan.create(L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma) as p:
+        p.set_fields(0, H0, E0)
+        p.set_incident(0, Hinc, Einc)
+        p.set_schedule(src, planes=planes, phase=ph)
+        p.run(0, nsteps)
+        got = [[p.get_dft(0, fi, q) for q in range(3)] for fi in range(nf)]
+        Hg, Eg = p.get_fields(0)
+    H, E = H0.copy(), E0.copy()
+    acc = np.zeros((nf, 3, 4, pl, 2))
+    mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+    cont, addr = pr.cont, pr.addr
+    for kk in range(nsteps):
+        port.time_loop(L, *coef, s.iBc, H, E, iBTIin, Hinc, Einc, pr.n2pi, tp, kk, kk + 1, *mons, cont, addr)
+        for q, z in enumerate(planes):
+            cells = np.arange(pl) + pl * z
+            x = []
+            for F in (H, E):
+                for v in range(2):
+                    val = F[v + 3 * cells].copy()
+                    split = cont[cells] == ord("a")
+                    val[split] = val[split] + F[v + 3 * (n3 + addr[cells[split]])]
+                    x.append(val)
+            for fi in range(nf):
+                for v in range(4):
+                    pr_, pi_ = (ph[kk, fi, 0], ph[kk, fi, 1]) if v < 2 else (ph[kk, fi, 2], ph[kk, fi, 3])
+                    acc[fi, q, v, :, 0] = acc[fi, q, v, :, 0] + pr_ * x[v]
+                    acc[fi, q, v, :, 1] = acc[fi, q, v, :, 1] + pi_ * x[v]
+    assert np.array_equal(Hg, H) and np.array_equal(Eg, E)
+    for fi in range(nf):
+        for q in range(3):
+            ref = acc[fi, q, :, :, 0] + 1j * acc[fi, q, :, :, 1]
+            assert np.array_equal(got[fi][q], ref)
+
+
+# ---- FP32 -----------------------------------------------------------------
+
+FP32_TOL_FIELDS = 2e-5  # relative, after <= 45 steps of a bounded case
+
+
+@pytest.mark.parametrize("name", ["zpml_plain", "periodic_bc"])
+def test_fp32_run_within_tolerance_of_fp64(built, name):
+    g = load_golden(name)
+    f = _fdtd()
+    with _plan_from_golden(g, f.FP32) as p:
+        p.set_fields(0, g["H0"], g["E0"])
+        p.set_incident(0, g["Hinc"], g["Einc"])
+        p.set_cw_schedule(int(g["n2pi"]), g["time_period"])
+        p.run(0, int(g["nsteps"]))
+        H, E = p.get_fields(0)
+        mons = p.get_monitor(0)
+    assert _relerr(H, g["H"]) < FP32_TOL_FIELDS
+    assert _relerr(E, g["E"]) < FP32_TOL_FIELDS
+    for m, key in zip(mons, ("HB", "EB", "HT", "ET")):
+        assert _relerr(m, g[key]) < FP32_TOL_FIELDS, key
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_fp32_general_cells_within_tolerance(built, port, seed):
+    """Lossy, PEC, metallic ('h','e','b') and split cells, x/y/z PML, FP32 vs FP64."""
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    L = (14, 12, 13, 2)
+    s = W.random_structure(L, seed=seed, pml=(3, 3, 3), metals=0.04, lossy=0.08, pec=0.05, iBc=(1, -1, 0))
+    pr = W.prepare(s)
+    n3, pl = s.n3, L[0] * L[1]
+    H0, E0 = W.random_fields(n3, pr.lnotn, seed=seed, scale=1e-2)
+    Hinc, Einc = W.random_incident(pl, seed=seed)
+    src, ph = f.cw_schedule(pr.n2pi, (1, 1, 3))
+    iBTIin = (4, 9, 6, 1)
+    res = {}
+    for prec in (f.FP64, f.FP32):
+        with f.Plan.create(L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=prec,
+                           pec=s.pec) as p:
+            p.set_fields(0, H0, E0)
+            p.set_incident(0, Hinc, Einc)
+            p.set_schedule(src, planes=(4, 9), phase=ph)
+            p.run(0, 6)
+            res[prec] = (*p.get_fields(0), p.get_dft(0, 0, 0), p.get_dft(0, 0, 1))
+    # the FP64 plan is the oracle's bit pattern (PEC applied to the coefficients)
+    Ah, Bh, Ae, Be = pr.coefficients()
+    pec = np.flatnonzero(s.pec)
+    for c in range(3):
+        Ae[c + 3 * pec] = 0.0
+        Be[c + 3 * pec] = 0.0
+    H, E = H0.copy(), E0.copy()
+    mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+    port.time_loop(L, Ah, Bh, Ae, Be, s.iBc, H, E, iBTIin, Hinc, Einc, pr.n2pi, (1, 1, 3), 0, 6, *mons, pr.cont,
+                   pr.addr)
+    assert np.array_equal(res[f.FP64][0], H) and np.array_equal(res[f.FP64][1], E)
+    for a, b in zip(res[f.FP32], res[f.FP64]):
+        assert _relerr(a, b) < 1e-5
+
+
+def test_fp32_batch_members_are_independent(built):
+    g = load_golden("zpml_plain")
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    L = g["L"]
+    n3, pl, ln = int(np.prod(L[:3])), int(L[0] * L[1]), int(g["lnotn"])
+    ex = [(*W.random_fields(n3, ln, seed=60 + b, scale=1e-3), *W.random_incident(pl, seed=70 + b)) for b in range(4)]
+    outs = []
+    with _plan_from_golden(g, f.FP32, batch=4) as p:
+        for b, (H0, E0, Hi, Ei) in enumerate(ex):
+            p.set_fields(b, H0, E0)
+            p.set_incident(b, Hi, Ei)
+        p.set_cw_schedule(int(g["n2pi"]), g["time_period"])
+        p.run(0, 40)
+        batch = [p.get_fields(b) for b in range(4)]
+    for b, (H0, E0, Hi, Ei) in enumerate(ex):
+        with _plan_from_golden(g, f.FP32) as p:
+            p.set_fields(0, H0, E0)
+            p.set_incident(0, Hi, Ei)
+            p.set_cw_schedule(int(g["n2pi"]), g["time_period"])
+            p.run(0, 40)
+            single = p.get_fields(0)
+        assert np.array_equal(batch[b][0], single[0]) and np.array_equal(batch[b][1], single[1])
+
+
+def test_finite_check_and_errors(built):
+    g = load_golden("zpml_plain")
+    f = _fdtd()
+    with _plan_from_golden(g, f.FP32) as p:
+        ok, m = p.check_finite()
+        assert ok and m == 0.0
+        with pytest.raises(f.FdtdError):
+            p.run(0, 10)  # no schedule yet
+        p.set_cw_schedule(int(g["n2pi"]), g["time_period"])
+        with pytest.raises(f.FdtdError):
+            p.run(0, 10 ** 6)  # beyond the schedule
+        H = g["H0"].copy()
+        H[5] = np.inf
+        p.set_fields(0, H, g["E0"])
+        ok, m = p.check_finite()
+        assert not ok
