@@ -136,12 +136,16 @@ def excitations(bend, modes):
     return out
 
 
-def make_plan(bend, pr, modes, precision, batch, nsteps, stream=None):
+def make_plan(bend, pr, modes, precision, batch, nsteps, stream=None, tuning="auto"):
     from smatranem_gb300 import fdtd as F
     from smatranem_gb300 import workloads as W
     s = bend.s
     p = F.Plan.create(s.L, s.iBc, (bend.iB, bend.iT, bend.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
                       pr.sigma, precision=precision, batch=batch, stream=stream)
+    if tuning == "auto":
+        p.autotune(4)
+    elif tuning is not None:
+        p.set_tuning(*tuning)
     ex = excitations(bend, modes)
     for b in range(batch):
         plane, sign, Hinc, Einc = ex[b % len(ex)]
@@ -295,14 +299,16 @@ def run_ours(args):
     ms_step = t_ms / args.steps
     # per-kernel launch times for the roofline (same stream, CUDA events)
     kt = p32.time_kernels(args.warmup + args.steps, 64)
+    tuning = p32.get_tuning()
+    per_step = 1 if tuning[0] else 2
     bytes_step = algorithmic_bytes_per_step(n3, n_split, batch)
-    sweep_ms = 0.5 * (kt[0] + kt[1])
-    achieved = (bytes_step / 2) / (sweep_ms * 1e-3) / 1e9
+    launch_ms = (kt[0] + kt[1]) / per_step
+    achieved = (bytes_step / per_step) / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
-    launches = 2 * args.steps + 2 * math.ceil(args.steps / 32) + 1
+    launches = per_step * args.steps + 2 * math.ceil(args.steps / 32) + 1
     # ---- full runs: S-matrix columns/s and the FP32-vs-FP64 S error -----
     full = args.full_steps
-    p32b = make_plan(bend, pr, modes, F.FP32, batch, full, stream=stream.cuda_stream)
+    p32b = make_plan(bend, pr, modes, F.FP32, batch, full, stream=stream.cuda_stream, tuning=tuning)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     p32b.run(0, full)
@@ -334,7 +340,7 @@ def run_ours(args):
     s_abs = float(np.max(np.abs(S32 - S64)) / np.abs(S64).max())
     # ---- e2e through the C ABI from host buffers --------------------------
     t0 = time.perf_counter()
-    pe = make_plan(bend, pr, modes, F.FP32, batch, full)
+    pe = make_plan(bend, pr, modes, F.FP32, batch, full, tuning=tuning)
     pe.run(0, full)
     Se = [s_parameters(pe, bend, modes, b) for b in range(batch)]
     pe.close()
@@ -364,8 +370,11 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h / full, "what": f"create+incident+schedule+{full} steps+DFT read-back, "
                                                           f"{t_e2e:.2f} s"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": None, "kernel": "k_sweep32 (H and E sweeps)",
-                     "bytes_per_launch": bytes_step / 2, "ms_per_launch": [kt[0], kt[1]],
+                     "peak_kind": peak_kind, "traffic": None,
+                     "kernel": "k_fused32 (one fused H+E launch per step)" if tuning[0] else "k_sweep32 (H, E)",
+                     "tuning": {"fused": tuning[0], "tile_y": tuning[1], "z_chunk": tuning[2],
+                                "ctas_per_sm": tuning[3], "slots": tuning[4]},
+                     "bytes_per_launch": bytes_step / per_step, "ms_per_launch": launch_ms,
                      "ms_dft_flush_per_step": kt[2]},
         "fp64_plain": {"value": fp64_rate, "unit": "Gcell-updates/s", "steps": args.steps64,
                        "s_cols_per_s": 1.0 / t_full64, "full_run_s": t_full64},
@@ -381,6 +390,23 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def run_profile(args):
+    """A small case for ncu: the bend cross-section with fewer z-layers (inputs
+    still larger than L2), `--warmup` + `--steps` steps of the chosen precision."""
+    import torch
+    from smatranem_gb300 import fdtd as F
+    shape = tuple(int(x) for x in args.shape.split(","))
+    bend, pr, modes = make_workload(shape)
+    prec = F.FP32 if args.profile == "fp32" else F.FP64
+    p = make_plan(bend, pr, modes, prec, args.batch if prec == F.FP32 else 1, args.warmup + args.steps)
+    p.run(0, args.warmup)
+    p.run(args.warmup, args.warmup + args.steps)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "shape": shape, "batch": p.batch, "steps": args.steps,
+                      "device_bytes": p.device_bytes}))
+    p.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -393,10 +419,14 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--ref-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", choices=["fp32", "fp64"], help="small case for ncu captures")
+    ap.add_argument("--shape", default="256,192,48")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

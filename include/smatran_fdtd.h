@@ -202,8 +202,22 @@ int smat_fdtd_check_finite(smat_fdtd_plan *plan, int *finite, double *max_abs);
  * [k_begin, k_begin+nsteps) of the schedule.  The steps are really taken. */
 int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double ms[3]);
 
-/* Launch shape of the FP32 sweeps: threads per block = 32 x block_y (1..8). */
-int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int block_y);
+/* FP32 launch configuration.  fused = 1: one z-marching launch per step with
+ * tiles of 32 x tile_y cells (2..8), z chunks of z_chunk planes, ctas_per_sm
+ * resident CTAs (0: as many as fit) and `slots` shared-memory plane slots
+ * (4..6: planes staged 1..3 ahead); fused = 0: two sweeps with 32 x tile_y
+ * thread blocks (1..8).  Results are bit-identical across configurations. */
+int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int fused, int tile_y, int z_chunk, int ctas_per_sm,
+                         int slots);
+/* {fused, tile_y, z_chunk, ctas_per_sm, slots} of the plan. */
+int smat_fdtd_get_tuning(const smat_fdtd_plan *plan, int out[5]);
+/* Autotuner: times the candidate FP32 configurations (tile rows, staged
+ * slots, z chunk; fused and two-sweep) for nsteps steps each on this plan's
+ * structure and batch, and keeps the fastest (returned in best, its time per
+ * step in *best_ms; either may be NULL).  Needs the zero state (call it before
+ * set_fields / run); sources and DFT sampling are off while it runs, so the
+ * plan is left unchanged apart from its configuration.  FP64: no-op. */
+int smat_fdtd_autotune(smat_fdtd_plan *plan, int nsteps, int best[5], double *best_ms);
 
 /* Device bytes the plan holds. */
 long long smat_fdtd_device_bytes(const smat_fdtd_plan *plan);

@@ -247,12 +247,19 @@ constexpr int RING_MAX = 32;
 
 __global__ void k_flush32(const P32 p, const int rel_end, const int count)
 {
+    extern __shared__ float sph[]; /* [count][nfreq][4] phases of the window */
+    const Dft &d = p.d;
+    const int k0 = *p.s.base + rel_end - count;
+    const int nph = count * d.nfreq * 4;
+    for (int i = threadIdx.x; i < nph; i += blockDim.x) {
+        const int s = i / (d.nfreq * 4), r = i % (d.nfreq * 4);
+        sph[i] = d.xphase32 ? d.xphase32[r & 3] : d.phase32[4 * (long long)(k0 + s) * d.nfreq + r];
+    }
+    __syncthreads();
     const int px = blockIdx.x * blockDim.x + threadIdx.x;
     const int qv = blockIdx.y, b = blockIdx.z;
     const int q = qv >> 2, v = qv & 3;
-    const Dft &d = p.d;
     if (px >= p.g.pl) return;
-    const int k0 = *p.s.base + rel_end - count;
     float x[RING_MAX];
 #pragma unroll
     for (int s = 0; s < RING_MAX; s++)
@@ -263,8 +270,7 @@ __global__ void k_flush32(const P32 p, const int rel_end, const int count)
 #pragma unroll
         for (int s = 0; s < RING_MAX; s++) {
             if (s < count) {
-                const float *ph = d.xphase32 ? d.xphase32 + po
-                                             : d.phase32 + 4 * ((long long)(k0 + s) * d.nfreq + f) + po;
+                const float *ph = sph + (s * d.nfreq + f) * 4 + po;
                 sr = fmaf(ph[0], x[s], sr);
                 si = fmaf(ph[1], x[s], si);
             }
@@ -290,8 +296,10 @@ void launch_e32(const P32 &p, int rel, int by, cudaStream_t st)
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st)
 {
     if (p.d.nfreq <= 0 || p.d.nq <= 0 || count <= 0) return;
-    dim3 blk(128), grd((p.g.pl + 127) / 128, p.d.nq * 4, p.batch);
-    k_flush32<<<grd, blk, 0, st>>>(p, rel_end, count);
+    dim3 blk(256), grd((p.g.pl + 255) / 256, p.d.nq * 4, p.batch);
+    const size_t sm = sizeof(float) * 4 * (size_t)count * p.d.nfreq;
+    if (sm > 48 * 1024) cudaFuncSetAttribute(k_flush32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_flush32<<<grd, blk, sm, st>>>(p, rel_end, count);
 }
 
 } // namespace smat

@@ -100,6 +100,16 @@ struct P32 {
     Dft d;
 };
 
+/* the fused FP32 step: reads the field set in p, writes the other set */
+struct Fused32 {
+    P32 p;
+    float *Hn, *En, *Han, *Ean; /* new set */
+    int ty, zc, ns;             /* tile rows, z-chunk length, staged plane slots (4..6) */
+    int ntx, nty, nzc, nitems;  /* work items: batch x tiles x z-chunks */
+    const int *stable;          /* cells whose E update is the stable form */
+    int nstable;
+};
+
 /* launchers (one translation unit per precision) */
 void launch_h64(const P64 &p, int rel, cudaStream_t st);
 void launch_e64(const P64 &p, int rel, cudaStream_t st);
@@ -107,6 +117,9 @@ void launch_dft64(const P64 &p, int rel, cudaStream_t st);
 void launch_h32(const P32 &p, int rel, int by, cudaStream_t st);
 void launch_e32(const P32 &p, int rel, int by, cudaStream_t st);
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
+void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);
+size_t fused32_smem(int ty, int ns);
+int fused32_max_ctas_per_sm(int ty, int ns);
 void launch_bump(int *base, int by, cudaStream_t st);
 void launch_set(int *base, int value, cudaStream_t st);
 void launch_maxabs(const void *x, long long n, int is_double, double *out, cudaStream_t st);

@@ -84,6 +84,7 @@ struct smat_fdtd_plan {
     bool ref_planes_ok = false; /* no PML cell on iB, iT (else the reference exits, :320) */
     double *d_scratch = nullptr;
     int *d_iI = nullptr;      /* [batch] source plane per excitation */
+    std::vector<int> h_iI;    /* host copy */
     double *d_isgn = nullptr; /* [batch] its sign */
 
     /* FP64 */
@@ -97,6 +98,13 @@ struct smat_fdtd_plan {
     uint8_t *d_pmask = nullptr;
     Rec32 *d_hrec = nullptr, *d_erec = nullptr;
     float *d_H32 = nullptr, *d_E32 = nullptr, *d_Ha32 = nullptr, *d_Ea32 = nullptr;
+    float *d_H32b = nullptr, *d_E32b = nullptr, *d_Ha32b = nullptr, *d_Ea32b = nullptr; /* second set */
+    int cur = 0;          /* FP32: which field set holds the current state */
+    int *d_stable = nullptr;
+    int nstable = 0;
+    /* FP32 launch configuration (autotuned): fused z-march or two sweeps */
+    int fused = 1, ty = 8, zc = 40, ns = 5, ctas_per_sm = 0;
+    int max_ctas = -1; /* cached occupancy of the current configuration */
     int by32 = 8;
 
     /* graphs: a chunk of GRAPH_STEPS steps, position independent via d_base */
@@ -191,13 +199,52 @@ P32 make_p32(const smat_fdtd_plan *p, bool xp)
     q.erec = p->d_erec;
     q.tab = p->d_tab;
     q.pmask = p->d_pmask;
-    q.H = p->d_H32;
-    q.E = p->d_E32;
-    q.Ha = p->d_Ha32;
-    q.Ea = p->d_Ea32;
+    q.H = p->cur ? p->d_H32b : p->d_H32;
+    q.E = p->cur ? p->d_E32b : p->d_E32;
+    q.Ha = p->cur ? p->d_Ha32b : p->d_Ha32;
+    q.Ea = p->cur ? p->d_Ea32b : p->d_Ea32;
     q.s = make_src(p, xp);
     q.d = make_dft(p, xp);
     return q;
+}
+
+Fused32 make_fused(const smat_fdtd_plan *p, bool xp)
+{
+    Fused32 f;
+    f.p = make_p32(p, xp);
+    f.Hn = p->cur ? p->d_H32 : p->d_H32b;
+    f.En = p->cur ? p->d_E32 : p->d_E32b;
+    f.Han = p->cur ? p->d_Ha32 : p->d_Ha32b;
+    f.Ean = p->cur ? p->d_Ea32 : p->d_Ea32b;
+    f.ty = p->ty;
+    f.zc = p->zc;
+    f.ns = p->ns;
+    f.ntx = (p->L[0] + 31) / 32;
+    f.nty = (p->L[1] + p->ty - 1) / p->ty;
+    f.nzc = (p->L[2] + p->zc - 1) / p->zc;
+    f.nitems = p->batch * f.ntx * f.nty * f.nzc;
+    f.stable = p->d_stable;
+    f.nstable = p->nstable;
+    return f;
+}
+
+int sm_count()
+{
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n;
+}
+
+int fused_grid(smat_fdtd_plan *p, const Fused32 &f)
+{
+    if (p->max_ctas < 0) p->max_ctas = fused32_max_ctas_per_sm(p->ty, p->ns);
+    const int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm : (p->max_ctas > 0 ? p->max_ctas : 1);
+    const long long g = (long long)per_sm * sm_count();
+    return (int)(g < f.nitems ? g : f.nitems);
 }
 
 /* the launches of steps rel0 .. rel0+n-1 relative to *d_base (no bump) */
@@ -210,6 +257,13 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
             launch_e64(q, rel0 + i, p->stream);
             launch_dft64(q, rel0 + i, p->stream);
         }
+    } else if (p->fused) {
+        for (int i = 0; i < n; i++) {
+            const Fused32 f = make_fused(p, xp);
+            launch_fused32(f, rel0 + i, fused_grid(p, f), p->stream);
+            p->cur ^= 1;
+        }
+        launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
     } else {
         const P32 q = make_p32(p, xp);
         for (int i = 0; i < n; i++) {
@@ -236,8 +290,10 @@ int build_graph(smat_fdtd_plan *p)
         p->graph_failed = true;
         return SMAT_OK;
     }
+    const int cur0 = p->cur;
     enqueue_steps(p, 0, GRAPH_STEPS, false);
     launch_bump(p->d_base, GRAPH_STEPS, p->stream);
+    p->cur = cur0;
     cudaError_t e = cudaStreamEndCapture(p->stream, &g);
     if (e != cudaSuccess || !g) {
         cudaGetLastError();
@@ -346,6 +402,7 @@ int common_alloc(smat_fdtd_plan *p)
     {
         const int m = p->iBTIin[3];
         std::vector<int> ii(p->batch, p->iBTIin[2]);
+        p->h_iI = ii;
         std::vector<double> sg(p->batch, (double)(m / (m < 0 ? -m : m)));
         CK(cudaMemcpyAsync(p->d_iI, ii.data(), ii.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
         CK(cudaMemcpyAsync(p->d_isgn, sg.data(), sg.size() * 8, cudaMemcpyHostToDevice, p->stream));
@@ -516,6 +573,22 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
     const size_t fs = (size_t)p->batch * 3 * n3;
     if ((rc = p->alloc(&p->d_H32, fs)) || (rc = p->alloc(&p->d_E32, fs))) return rc;
     if ((rc = p->alloc(&p->d_Ha32, fs)) || (rc = p->alloc(&p->d_Ea32, fs))) return rc;
+    if ((rc = p->alloc(&p->d_H32b, fs)) || (rc = p->alloc(&p->d_E32b, fs))) return rc;
+    if ((rc = p->alloc(&p->d_Ha32b, fs)) || (rc = p->alloc(&p->d_Ea32b, fs))) return rc;
+    std::vector<int> stable;
+    for (long long l = 0; l < n3; l++) {
+        float c0 = be[l];
+        if (std::isnan(c0)) {
+            int idx;
+            memcpy(&idx, &be[n3 + l], 4);
+            if (erec[idx].kind == RK_STABLE) stable.push_back((int)l);
+        }
+    }
+    p->nstable = (int)stable.size();
+    if ((rc = p->alloc(&p->d_stable, stable.size() + 1))) return rc;
+    if (!stable.empty())
+        CK(cudaMemcpyAsync(p->d_stable, stable.data(), stable.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           p->stream));
     CK(cudaMemcpyAsync(p->d_bh, bh.data(), bh.size() * 4, cudaMemcpyHostToDevice, p->stream));
     CK(cudaMemcpyAsync(p->d_be, be.data(), be.size() * 4, cudaMemcpyHostToDevice, p->stream));
     CK(cudaMemcpyAsync(p->d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, p->stream));
@@ -688,8 +761,9 @@ extern "C" int smat_fdtd_set_fields(smat_fdtd_plan *p, int b, const double *H_t,
                     t[c * n3 + l] = (float)(main + ax);
                     a[c * n3 + l] = (float)ax;
                 }
-            float *dt = (w ? p->d_E32 : p->d_H32) + (size_t)b * 3 * n3;
-            float *da = (w ? p->d_Ea32 : p->d_Ha32) + (size_t)b * 3 * n3;
+            const P32 q = make_p32(p, false);
+            float *dt = (w ? q.E : q.H) + (size_t)b * 3 * n3;
+            float *da = (w ? q.Ea : q.Ha) + (size_t)b * 3 * n3;
             CK(cudaMemcpyAsync(dt, t.data(), t.size() * 4, cudaMemcpyHostToDevice, p->stream));
             CK(cudaMemcpyAsync(da, a.data(), a.size() * 4, cudaMemcpyHostToDevice, p->stream));
             CK(cudaStreamSynchronize(p->stream));
@@ -720,8 +794,9 @@ extern "C" int smat_fdtd_get_fields(smat_fdtd_plan *p, int b, double *H_t, doubl
             }
         } else {
             std::vector<float> t(3 * n3), a(3 * n3);
-            const float *dt = (w ? p->d_E32 : p->d_H32) + (size_t)b * 3 * n3;
-            const float *da = (w ? p->d_Ea32 : p->d_Ha32) + (size_t)b * 3 * n3;
+            const P32 q = make_p32(p, false);
+            const float *dt = (w ? q.E : q.H) + (size_t)b * 3 * n3;
+            const float *da = (w ? q.Ea : q.Ha) + (size_t)b * 3 * n3;
             CK(cudaMemcpyAsync(t.data(), dt, t.size() * 4, cudaMemcpyDeviceToHost, p->stream));
             CK(cudaMemcpyAsync(a.data(), da, a.size() * 4, cudaMemcpyDeviceToHost, p->stream));
             CK(cudaStreamSynchronize(p->stream));
@@ -758,6 +833,7 @@ extern "C" int smat_fdtd_set_source_plane(smat_fdtd_plan *p, int b, int iI, int 
     if (!p || b < 0 || b >= p->batch || iI < 0 || iI >= p->L[2] || inci_mode == 0)
         return smat_fail(SMAT_EINVAL, "set_source_plane: bad arguments");
     const double sg = (double)(inci_mode / (inci_mode < 0 ? -inci_mode : inci_mode));
+    p->h_iI[b] = iI;
     CK(cudaMemcpyAsync(p->d_iI + b, &iI, sizeof(int), cudaMemcpyHostToDevice, p->stream));
     CK(cudaMemcpyAsync(p->d_isgn + b, &sg, 8, cudaMemcpyHostToDevice, p->stream));
     CK(cudaStreamSynchronize(p->stream));
@@ -857,10 +933,17 @@ extern "C" int smat_fdtd_run(smat_fdtd_plan *p, int k_begin, int k_end)
     if (k_end > p->nsched) return smat_fail(SMAT_EINVAL, "run: k_end %d beyond the %d-step schedule", k_end, p->nsched);
     launch_set(p->d_base, k_begin, p->stream);
     int n = k_end - k_begin;
+    if (p->precision == SMAT_FP32 && p->fused && p->cur != 0 && n >= GRAPH_STEPS + 1) {
+        /* graphs are captured from field set 0: take one step to get there */
+        enqueue_steps(p, 0, 1, false);
+        launch_bump(p->d_base, 1, p->stream);
+        n -= 1;
+    }
     if (n >= GRAPH_STEPS) build_graph(p);
     while (n >= GRAPH_STEPS) {
         if (p->graph) {
             CK(cudaGraphLaunch(p->graph, p->stream));
+            /* the captured chunk toggled cur an even number of times */
         } else {
             enqueue_steps(p, 0, GRAPH_STEPS, false);
             launch_bump(p->d_base, GRAPH_STEPS, p->stream);
@@ -887,19 +970,23 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
     float t;
     launch_set(p->d_base, k_begin, p->stream);
     const P64 q64 = make_p64(p, false);
-    const P32 q32 = make_p32(p, false);
     for (int i = 0; i < nsteps; i++) {
+        const P32 q32 = make_p32(p, false);
         CK(cudaEventRecord(ev[0], p->stream));
         if (p->precision == SMAT_FP64) launch_h64(q64, i, p->stream);
-        else launch_h32(q32, i, p->by32, p->stream);
+        else if (p->fused) {
+            const Fused32 f = make_fused(p, false);
+            launch_fused32(f, i, fused_grid(p, f), p->stream);
+            p->cur ^= 1;
+        } else launch_h32(q32, i, p->by32, p->stream);
         CK(cudaEventRecord(ev[1], p->stream));
         if (p->precision == SMAT_FP64) launch_e64(q64, i, p->stream);
-        else launch_e32(q32, i, p->by32, p->stream);
+        else if (!p->fused) launch_e32(q32, i, p->by32, p->stream);
         CK(cudaEventRecord(ev[2], p->stream));
         if (p->precision == SMAT_FP64) launch_dft64(q64, i, p->stream);
         else if ((i + 1) % RING_K == 0 || i + 1 == nsteps) {
             const int cnt = (i + 1) % RING_K == 0 ? RING_K : (i + 1) % RING_K;
-            launch_flush32(q32, i + 1, cnt, p->stream);
+            launch_flush32(make_p32(p, false), i + 1, cnt, p->stream);
         }
         CK(cudaEventRecord(ev[3], p->stream));
         CK(cudaEventSynchronize(ev[3]));
@@ -917,11 +1004,108 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
     return SMAT_OK;
 }
 
-extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int block_y)
+extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, int z_chunk, int ctas_per_sm,
+                                    int slots)
 {
-    if (!p || block_y < 1 || block_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
-    p->by32 = block_y;
+    smat_clear_error();
+    if (!p) return smat_fail(SMAT_EINVAL, "null plan");
+    if (fused) {
+        if (tile_y < 2 || tile_y > 8 || z_chunk < 1 || ctas_per_sm < 0 || slots < 4 || slots > 6)
+            return smat_fail(SMAT_EINVAL,
+                             "set_tuning: tile_y in 2..8, z_chunk >= 1, ctas_per_sm >= 0, slots in 4..6");
+        const int mx = fused32_max_ctas_per_sm(tile_y, slots);
+        if (mx < 1 || ctas_per_sm > mx)
+            return smat_fail(SMAT_EINVAL, "set_tuning: %d CTAs per SM do not fit (max %d)", ctas_per_sm, mx);
+        p->ty = tile_y;
+        p->zc = z_chunk;
+        p->ns = slots;
+        p->ctas_per_sm = ctas_per_sm;
+        p->max_ctas = mx;
+    } else {
+        if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
+        p->by32 = tile_y;
+    }
+    p->fused = fused ? 1 : 0;
     drop_graph(p);
+    return SMAT_OK;
+}
+
+/* Times each candidate launch configuration over nsteps steps and keeps the
+ * fastest.  Runs on the zero state with sources and DFT sampling switched off,
+ * so a plan whose fields are all zero is left exactly as it was. */
+extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], double *best_ms)
+{
+    smat_clear_error();
+    if (!p || nsteps < 1) return smat_fail(SMAT_EINVAL, "autotune: bad arguments");
+    if (p->precision != SMAT_FP32) {
+        if (best) smat_fdtd_get_tuning(p, best);
+        if (best_ms) *best_ms = 0;
+        return SMAT_OK;
+    }
+    int finite = 0;
+    double mx = 0;
+    int rc = smat_fdtd_check_finite(p, &finite, &mx);
+    if (rc) return rc;
+    if (mx != 0.0) return smat_fail(SMAT_ESTATE, "autotune: needs the zero state (call it before set_fields/run)");
+    struct Cand {
+        int fused, ty, zc, ctas, ns;
+    };
+    std::vector<Cand> cands;
+    const int L2 = p->L[2];
+    for (int ty : {4, 8})
+        for (int ns : {4, 5, 6})
+            for (int zc : {16, 32, 64, 1 << 20}) {
+                const int z = zc > L2 ? L2 : zc;
+                bool dup = false;
+                for (auto &c : cands) dup |= c.fused && c.ty == ty && c.ns == ns && c.zc == z;
+                if (!dup && fused32_max_ctas_per_sm(ty, ns) >= 1) cands.push_back({1, ty, z, 0, ns});
+            }
+    cands.push_back({0, 4, 1, 0, 4});
+    cands.push_back({0, 8, 1, 0, 4});
+    const int nq = p->nq;
+    p->nq = 0;
+    CK(cudaMemsetAsync(p->d_iI, 0xff, sizeof(int) * p->batch, p->stream));
+    const int save[5] = {p->fused, p->fused ? p->ty : p->by32, p->zc, p->ctas_per_sm, p->ns};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double bms = 1e30;
+    Cand bc = {save[0], save[1], save[2], save[3], save[4]};
+    for (const Cand &c : cands) {
+        if (smat_fdtd_set_tuning(p, c.fused, c.ty, c.zc, c.ctas, c.ns) != SMAT_OK) continue;
+        launch_set(p->d_base, 0, p->stream);
+        enqueue_steps(p, 0, 1, false);
+        CK(cudaEventRecord(e0, p->stream));
+        enqueue_steps(p, 0, nsteps, false);
+        CK(cudaEventRecord(e1, p->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < bms) {
+            bms = ms;
+            bc = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p->nq = nq;
+    CK(cudaMemcpyAsync(p->d_iI, p->h_iI.data(), sizeof(int) * p->batch, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    rc = smat_fdtd_set_tuning(p, bc.fused, bc.ty, bc.zc, bc.ctas, bc.ns);
+    if (rc) return rc;
+    if (best) smat_fdtd_get_tuning(p, best);
+    if (best_ms) *best_ms = bms / nsteps;
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
+{
+    if (!p || !out) return smat_fail(SMAT_EINVAL, "get_tuning: bad arguments");
+    out[0] = p->fused;
+    out[1] = p->fused ? p->ty : p->by32;
+    out[2] = p->zc;
+    out[3] = p->ctas_per_sm;
+    out[4] = p->ns;
     return SMAT_OK;
 }
 
@@ -1008,8 +1192,9 @@ extern "C" int smat_fdtd_check_finite(smat_fdtd_plan *p, int *finite, double *ma
     const bool d = p->precision == SMAT_FP64;
     const long long nf = (long long)p->batch * 3 * p->n3;
     const long long na = d ? (long long)p->batch * 3 * (p->lnotn + 1) : nf;
-    const void *arr[4] = {d ? (void *)p->d_H64 : (void *)p->d_H32, d ? (void *)p->d_E64 : (void *)p->d_E32,
-                          d ? (void *)p->d_Ha64 : (void *)p->d_Ha32, d ? (void *)p->d_Ea64 : (void *)p->d_Ea32};
+    const P32 q = make_p32(p, false);
+    const void *arr[4] = {d ? (void *)p->d_H64 : (void *)q.H, d ? (void *)p->d_E64 : (void *)q.E,
+                          d ? (void *)p->d_Ha64 : (void *)q.Ha, d ? (void *)p->d_Ea64 : (void *)q.Ea};
     for (int i = 0; i < 4; i++) launch_maxabs(arr[i], i < 2 ? nf : na, d, p->d_scratch, p->stream);
     unsigned long long bits = 0;
     CK(cudaMemcpyAsync(&bits, p->d_scratch, 8, cudaMemcpyDeviceToHost, p->stream));

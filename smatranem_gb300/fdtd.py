@@ -71,7 +71,9 @@ def lib():
         L.smat_fdtd_sync.argtypes = [_P]
         L.smat_fdtd_info.argtypes = [_P, _P, _P, _P, _P]
         L.smat_fdtd_time_kernels.argtypes = [_P, C.c_int, C.c_int, _P]
-        L.smat_fdtd_set_tuning.argtypes = [_P, C.c_int]
+        L.smat_fdtd_set_tuning.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.smat_fdtd_get_tuning.argtypes = [_P, _P]
+        L.smat_fdtd_autotune.argtypes = [_P, C.c_int, _P, _P]
         _lib = L
     return _lib
 
@@ -284,8 +286,19 @@ class Plan:
         _check(lib().smat_fdtd_time_kernels(self._h, k_begin, nsteps, _ptr(ms)))
         return ms
 
-    def set_tuning(self, block_y):
-        _check(lib().smat_fdtd_set_tuning(self._h, block_y))
+    def set_tuning(self, fused=1, tile_y=8, z_chunk=40, ctas_per_sm=0, slots=5):
+        _check(lib().smat_fdtd_set_tuning(self._h, fused, tile_y, z_chunk, ctas_per_sm, slots))
+
+    def autotune(self, nsteps=4):
+        best = (C.c_int * 5)()
+        ms = C.c_double(0)
+        _check(lib().smat_fdtd_autotune(self._h, nsteps, best, C.byref(ms)))
+        return tuple(best), ms.value
+
+    def get_tuning(self):
+        out = (C.c_int * 5)()
+        _check(lib().smat_fdtd_get_tuning(self._h, out))
+        return tuple(out)
 
     def check_finite(self):
         ok, m = C.c_int(0), C.c_double(0)

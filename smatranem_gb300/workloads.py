@@ -256,6 +256,7 @@ def bend_structure(shape=(256, 192, 160), pml=12, L3=16, radius_um=2.0, core=(0.
     core sits near the inner side of the bend (cell core_cell0 of L0) so that
     1 + kappa*u0 stays above 0.5.  12-cell split PML on all six faces."""
     L0, L1, L2 = shape
+    L3 = min(L3, max(pml + 3, L2 // 4))
     fine, coarse = (c / INV_K0_UM for c in cell_um)
     du0 = graded_spacing(L0, core_cell0, fine, coarse, 40.0)
     du1 = graded_spacing(L1, L1 / 2, fine, coarse, 30.0)

@@ -306,3 +306,97 @@ def test_finite_check_and_errors(built):
         p.set_fields(0, H, g["E0"])
         ok, m = p.check_finite()
         assert not ok
+
+
+# ---- the fused FP32 kernel ----------------------------------------------------
+
+FUSED_CASES = [
+    # (L, seed, structure kwargs, iBTIin)
+    ((37, 13, 15, 2), 21, dict(pml=(3, 2, 3), metals=0.03, lossy=0.05, pec=0.04, iBc=(-1, 0, 1)), (4, 10, 6, 1)),
+    ((40, 17, 19, 3), 22, dict(pml=(4, 4, 4), lossy=0.05, iBc=(1, 1, -1)), (5, 13, 7, -1)),
+    ((33, 9, 12, 2), 23, dict(pml=(0, 0, 2), pml_z_only=True, iBc=(0, -1, 0)), (3, 8, 5, 1)),
+    ((64, 24, 20, 3), 24, dict(pml=(5, 5, 4), metals=0.02, iBc=(0, 0, 0)), (5, 14, 7, 1)),
+]
+TUNINGS = [(1, 8, 40, 0, 5), (1, 4, 5, 0, 4), (1, 2, 3, 1, 6), (1, 8, 7, 1, 6), (1, 3, 1, 0, 5), (1, 2, 2, 0, 4)]
+
+
+def _run_fp32(s, pr, iBTIin, tuning, nsteps, batch=2, seed=0):
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    n3, pl = s.n3, s.L[0] * s.L[1]
+    src, ph = f.cw_schedule(pr.n2pi, (1, 1, 3))
+    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=f.FP32,
+                       batch=batch, pec=s.pec) as p:
+        p.set_tuning(*tuning)
+        for b in range(batch):
+            H0, E0 = W.random_fields(n3, pr.lnotn, seed=seed + b, scale=1e-2)
+            Hinc, Einc = W.random_incident(pl, seed=seed + 10 + b)
+            p.set_fields(b, H0, E0)
+            p.set_incident(b, Hinc, Einc)
+            p.set_source_plane(b, iBTIin[2] + b, 1 - 2 * b)
+        p.set_schedule(src, planes=(iBTIin[0], iBTIin[1], 0), phase=ph)
+        p.run(0, nsteps // 2)
+        p.run(nsteps // 2, nsteps)  # an odd split exercises both field sets
+        return [(*p.get_fields(b), *[p.get_dft(b, 0, q) for q in range(3)]) for b in range(batch)]
+
+
+@pytest.mark.parametrize("case", range(len(FUSED_CASES)))
+def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
+    """The fused z-marching launch reproduces the two-sweep FP32 kernels bit for
+    bit, for every tile shape, z chunk and grid size, across field-set swaps,
+    iBc = -1/0/1 wraps, PML on all faces, lossy/PEC/metal cells and per-excitation
+    source planes."""
+    from smatranem_gb300 import workloads as W
+    L, seed, kw, iBTIin = FUSED_CASES[case]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    nsteps = 9 if kw.get("metals") else 37
+    ref = _run_fp32(s, pr, iBTIin, (0, 4, 1, 0, 4), nsteps)
+    for tuning in TUNINGS:
+        got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
+        for rb, gb in zip(ref, got):
+            for a, b_ in zip(rb, gb):
+                assert np.array_equal(a, b_), tuning
+
+
+def test_fused_fp32_within_tolerance_of_fp64_long_run(built):
+    """A 300-step run with PML on all faces: FP32 (fused) vs the FP64 plan."""
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    L = (48, 40, 36, 4)
+    s = W.random_structure(L, seed=31, pml=(6, 6, 6), lossy=0.02)
+    pr = W.prepare(s)
+    n3, pl = s.n3, L[0] * L[1]
+    src, ph = f.cw_schedule(pr.n2pi, (2, 2, 6))
+    Hinc, Einc = W.random_incident(pl, seed=3)
+    out = {}
+    for prec in (f.FP64, f.FP32):
+        with f.Plan.create(L, s.iBc, (8, 27, 10, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                           precision=prec) as p:
+            p.set_incident(0, Hinc, Einc)
+            p.set_schedule(src, planes=(8, 27), phase=ph)
+            p.run(0, 300)
+            out[prec] = (*p.get_fields(0), p.get_dft(0, 0, 0), p.get_dft(0, 0, 1))
+    for a, b in zip(out[f.FP32], out[f.FP64]):
+        assert _relerr(a, b) < 2e-5
+
+
+def test_autotune_keeps_state_and_results(built):
+    """The autotuner leaves a zero-state plan unchanged; the tuned plan gives the
+    same bits as the two-sweep configuration."""
+    from smatranem_gb300 import workloads as W
+    f = _fdtd()
+    L, seed, kw, iBTIin = FUSED_CASES[1]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                       precision=f.FP32) as p:
+        best, ms = p.autotune(2)
+        assert ms > 0 and p.get_tuning() == best
+        ok, mx = p.check_finite()
+        assert ok and mx == 0.0
+    ref = _run_fp32(s, pr, iBTIin, (0, 4, 1, 0, 4), 21)
+    got = _run_fp32(s, pr, iBTIin, tuple(best[:4]) + (best[4],), 21)
+    for rb, gb in zip(ref, got):
+        for a, b_ in zip(rb, gb):
+            assert np.array_equal(a, b_)
