@@ -156,16 +156,18 @@ def make_plan(bend, pr, modes, precision, batch, nsteps, stream=None, tuning="au
     return p
 
 
+def mode_columns(modes):
+    """tilde-Xi style columns (4*npix rows: Hx, Hy, -Ey, Ex) of the mode sheets."""
+    cols = []
+    for Hinc, Einc in modes:
+        cols.append(np.concatenate([Hinc[0::2], Hinc[1::2], -Einc[1::2], Einc[0::2]]))
+    return np.array(cols)
+
+
 def s_parameters(p, bend, modes, b):
-    """|S|^2-style complex overlaps: [port plane][lambda][mode]."""
-    from smatranem_gb300 import workloads as W
-    S = np.zeros((2, len(LAMS), len(modes)), np.complex128)
-    for q in range(2):
-        for f in range(len(LAMS)):
-            d = p.get_dft(b, f, q)
-            for m, (Hinc, Einc) in enumerate(modes):
-                S[q, f, m] = W.overlap(d, Hinc, Einc)
-    return S
+    """Mode overlaps on the GPU (FP64): [port plane][lambda][mode]."""
+    cols = mode_columns(modes)
+    return np.stack([p.overlap(b, q, cols) for q in range(2)])
 
 
 # ---------------------------------------------------------------------------
@@ -300,7 +302,7 @@ def run_ours(args):
     # per-kernel launch times for the roofline (same stream, CUDA events)
     kt = p32.time_kernels(args.warmup + args.steps, 64)
     tuning = p32.get_tuning()
-    per_step = 1 if tuning[0] else 2
+    per_step = 1 if tuning[0] == 1 else 2
     bytes_step = algorithmic_bytes_per_step(n3, n_split, batch)
     launch_ms = (kt[0] + kt[1]) / per_step
     achieved = (bytes_step / per_step) / (launch_ms * 1e-3) / 1e9
@@ -371,8 +373,9 @@ def run_ours(args):
                                                           f"{t_e2e:.2f} s"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None,
-                     "kernel": "k_fused32 (one fused H+E launch per step)" if tuning[0] else "k_sweep32 (H, E)",
-                     "tuning": {"fused": tuning[0], "tile_y": tuning[1], "z_chunk": tuning[2],
+                     "kernel": {1: "k_fused32 (one fused H+E launch per step)", 2: "k_sweep32v (H, E; float4)",
+                                0: "k_sweep32 (H, E)"}[tuning[0]],
+                     "tuning": {"kernel": tuning[0], "tile_y": tuning[1], "z_chunk": tuning[2],
                                 "ctas_per_sm": tuning[3], "slots": tuning[4]},
                      "bytes_per_launch": bytes_step / per_step, "ms_per_launch": launch_ms,
                      "ms_dft_flush_per_step": kt[2]},
@@ -398,12 +401,14 @@ def run_profile(args):
     shape = tuple(int(x) for x in args.shape.split(","))
     bend, pr, modes = make_workload(shape)
     prec = F.FP32 if args.profile == "fp32" else F.FP64
-    p = make_plan(bend, pr, modes, prec, args.batch if prec == F.FP32 else 1, args.warmup + args.steps)
+    tuning = tuple(int(x) for x in args.tuning.split(",")) if args.tuning else "auto"
+    p = make_plan(bend, pr, modes, prec, args.batch if prec == F.FP32 else 1, args.warmup + args.steps,
+                  tuning=tuning)
     p.run(0, args.warmup)
     p.run(args.warmup, args.warmup + args.steps)
     torch.cuda.synchronize()
     print(json.dumps({"profile": args.profile, "shape": shape, "batch": p.batch, "steps": args.steps,
-                      "device_bytes": p.device_bytes}))
+                      "tuning": p.get_tuning(), "device_bytes": p.device_bytes}))
     p.close()
 
 
@@ -421,6 +426,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", choices=["fp32", "fp64"], help="small case for ncu captures")
     ap.add_argument("--shape", default="256,192,48")
+    ap.add_argument("--tuning", default="", help="fused,tile_y,z_chunk,ctas_per_sm,slots (profile mode)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

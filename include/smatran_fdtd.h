@@ -192,6 +192,32 @@ int smat_fdtd_get_monitor(smat_fdtd_plan *plan, int b, double *HB, double *EB,
  * out = 4*L0*L1 complex, components (Hx, Hy, Ex, Ey) each over L0*L1 pixels. */
 int smat_fdtd_get_dft(smat_fdtd_plan *plan, int b, int f, int q, double *out);
 
+/* Number of DFT frequencies and monitor planes of the current schedule. */
+int smat_fdtd_dft_count(const smat_fdtd_plan *plan, int *nfreq, int *nplanes);
+
+/* Device address of the DFT accumulator of excitation b, frequency f, plane q
+ * (4*L0*L1 complex: Hx, Hy, Ex, Ey) and the distance in complex elements
+ * between consecutive frequencies.  Valid until the next set_schedule. */
+int smat_fdtd_dft_device(smat_fdtd_plan *plan, int b, int f, int q, const double **ptr,
+                         long long *fstride);
+
+/* Mode-overlap projection on the GPU, the S-parameter extraction of S_calc
+ * (FDTDsplitfieldMetal.c:419-448): for nvec DFT planes (plane v at
+ * dft + v*vec_stride complex elements, components Hx, Hy, Ex, Ey over npix
+ * pixels) and ncols columns of tilde-Xi (column-major, 4*npix complex rows in
+ * the reference's row order), S[v*ncols + c] = sum_r conj(tilXi[r, c]) *
+ * (HB_x, HB_y, -EB_y, EB_x)[r].  All pointers are device memory; FP64; the
+ * result is the same bits on every call.  Block partial sums go to scratch
+ * memory the call allocates stream-ordered on `stream` (NULL: the legacy
+ * default stream) and frees again. */
+int smat_overlap(int npix, int ncols, int nvec, long long vec_stride, const double *tilXi,
+                 const double *dft, double *S, void *stream);
+
+/* The same for every frequency of plane q of excitation b of a plan, with
+ * tilde-Xi columns and the result (nfreq*ncols complex) in host memory. */
+int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const double *tilXi_host,
+                      double *S_host);
+
 /* Largest |field| over every excitation (a NaN/Inf check); *finite = 0 when a
  * non-finite value is present. */
 int smat_fdtd_check_finite(smat_fdtd_plan *plan, int *finite, double *max_abs);
@@ -202,14 +228,16 @@ int smat_fdtd_check_finite(smat_fdtd_plan *plan, int *finite, double *max_abs);
  * [k_begin, k_begin+nsteps) of the schedule.  The steps are really taken. */
 int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double ms[3]);
 
-/* FP32 launch configuration.  fused = 1: one z-marching launch per step with
- * tiles of 32 x tile_y cells (2..8), z chunks of z_chunk planes, ctas_per_sm
- * resident CTAs (0: as many as fit) and `slots` shared-memory plane slots
- * (4..6: planes staged 1..3 ahead); fused = 0: two sweeps with 32 x tile_y
- * thread blocks (1..8).  Results are bit-identical across configurations. */
-int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int fused, int tile_y, int z_chunk, int ctas_per_sm,
+/* FP32 launch configuration.  kernel = 1: one fused z-marching launch per step
+ * with tiles of 32 x tile_y cells (2..8), z chunks of z_chunk planes,
+ * ctas_per_sm resident CTAs (0: as many as fit) and `slots` shared-memory
+ * plane slots (4..6: planes staged 1..3 ahead); kernel = 0: two sweeps with
+ * 32 x tile_y thread blocks (1..8); kernel = 2: two sweeps of four cells per
+ * thread (float4, L0 % 4 == 0, tile_y 1..4; the default where it applies).  Results are
+ * bit-identical across configurations. */
+int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int kernel, int tile_y, int z_chunk, int ctas_per_sm,
                          int slots);
-/* {fused, tile_y, z_chunk, ctas_per_sm, slots} of the plan. */
+/* {kernel, tile_y, z_chunk, ctas_per_sm, slots} of the plan. */
 int smat_fdtd_get_tuning(const smat_fdtd_plan *plan, int out[5]);
 /* Autotuner: times the candidate FP32 configurations (tile rows, staged
  * slots, z chunk; fused and two-sweep) for nsteps steps each on this plan's

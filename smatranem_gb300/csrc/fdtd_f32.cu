@@ -100,7 +100,11 @@ __device__ __forceinline__ float *ring_at(const Dft &d, int pl, int b, int k, in
 template <bool EF>
 __global__ void __launch_bounds__(256) k_sweep32(const P32 p, const int rel)
 {
-    const int j0 = blockIdx.x * 32 + threadIdx.x, j1 = blockIdx.y * blockDim.y + threadIdx.y, j2 = blockIdx.z;
+    /* blockIdx.y = row block * batch + excitation: the blocks of one tile for
+     * all excitations launch together and share the coefficient lines in L2 */
+    const int b = blockIdx.y % p.batch;
+    const int j0 = blockIdx.x * 32 + threadIdx.x, j1 = (blockIdx.y / p.batch) * blockDim.y + threadIdx.y;
+    const int j2 = blockIdx.z;
     const Geo &g = p.g;
     if (j0 >= g.L0 || j1 >= g.L1) return;
     const long long n3 = g.n3, l = j0 + (long long)g.L0 * (j1 + (long long)g.L1 * j2);
@@ -113,77 +117,68 @@ __global__ void __launch_bounds__(256) k_sweep32(const P32 p, const int rel)
     const int k = *p.s.base + rel;
     const int q = monitor_index(p.d, j2);
     const int px = j0 + g.L0 * j1;
-    const float c0 = cf[l];
     const long long bs = 3 * n3;
+    /* issue every load of the common paths before any branch, so a thread
+     * waits for DRAM once: its coefficients, its own field, the six curl
+     * neighbours and the PML masks */
+    const float c0 = cf[l], c1 = cf[n3 + l], c2 = cf[2 * n3 + l];
+    const int S = g.L0 + g.L1 + g.L2, s1 = g.L0, s2 = g.L0 + g.L1;
+    const bool split = p.pmask[j0] | p.pmask[s1 + j1] | p.pmask[s2 + j2];
+    const Stn32 st = make_stn32(g, j0, j1, j2, EF);
+    float *F = F0 + b * bs, *Fa = Fa0 + b * bs;
+    const float *G = G0 + b * bs;
+    float pl[3], mi[3], fo[3];
+    {
+        auto get = [&](int c, long long o) { return G[c * n3 + l + o]; };
+        curl32<EF>(get, st, pl, mi);
+#pragma unroll
+        for (int c = 0; c < 3; c++) fo[c] = F[c * n3 + l];
+    }
 
     if (!isnan(c0)) {
-        const float bn[3] = {c0, cf[n3 + l], cf[2 * n3 + l]};
-        const int S = g.L0 + g.L1 + g.L2, s1 = g.L0, s2 = g.L0 + g.L1;
-        const Stn32 st = make_stn32(g, j0, j1, j2, EF);
-        const bool split = p.pmask[j0] | p.pmask[s1 + j1] | p.pmask[s2 + j2];
+        const float bn[3] = {c0, c1, c2};
         if (!split) {
-            for (int b = 0; b < p.batch; b++) {
-                float *F = F0 + b * bs;
-                const float *G = G0 + b * bs;
-                auto get = [&](int c, long long o) { return G[c * n3 + l + o]; };
-                float pl[3], mi[3];
-                curl32<EF>(get, st, pl, mi);
-                float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
-                if (j2 == p.s.iI[b]) {
-                    W[0] += (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 1, px));
-                    W[1] -= (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 0, px));
-                }
-                float f[3];
+            float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+            if (j2 == p.s.iI[b]) {
+                W[0] += (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 1, px));
+                W[1] -= (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 0, px));
+            }
+            float f[3];
 #pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    f[c] = fmaf(sg * bn[c], W[c], F[c * n3 + l]);
-                    F[c * n3 + l] = f[c];
-                }
-                if (q >= 0) {
-                    ring_at(p.d, g.pl, b, k, q, EF ? 2 : 0)[px] = f[0];
-                    ring_at(p.d, g.pl, b, k, q, EF ? 3 : 1)[px] = f[1];
-                }
+            for (int c = 0; c < 3; c++) {
+                f[c] = fmaf(sg * bn[c], W[c], fo[c]);
+                F[c * n3 + l] = f[c];
+            }
+            if (q >= 0) {
+                ring_at(p.d, g.pl, b, k, q, EF ? 2 : 0)[px] = f[0];
+                ring_at(p.d, g.pl, b, k, q, EF ? 3 : 1)[px] = f[1];
             }
         } else {
             const int jx[3] = {j0, s1 + j1, s2 + j2};
             const float *tA = p.tab + (EF ? 2 : 0) * S, *tG = p.tab + (EF ? 3 : 1) * S;
-            float Ap[3], Bp[3], Am[3], Bm[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 const int i1 = jx[(c + 1) % 3], i2 = jx[(c + 2) % 3];
-                Ap[c] = tA[i1];
-                Bp[c] = sg * bn[c] * tG[i1];
-                Am[c] = tA[i2];
-                Bm[c] = sg * bn[c] * tG[i2];
-            }
-            for (int b = 0; b < p.batch; b++) {
-                float *F = F0 + b * bs, *Fa = Fa0 + b * bs;
-                const float *G = G0 + b * bs;
-                auto get = [&](int c, long long o) { return G[c * n3 + l + o]; };
-                float pl[3], mi[3];
-                curl32<EF>(get, st, pl, mi);
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    const float m = Fa[c * n3 + l];
-                    const float pp = F[c * n3 + l] - m;
-                    const float np = fmaf(Bp[c], pl[c], Ap[c] * pp);
-                    const float nm = fmaf(Bm[c], mi[c], Am[c] * m);
-                    F[c * n3 + l] = np + nm;
-                    Fa[c * n3 + l] = nm;
-                    if (q >= 0 && c < 2) ring_at(p.d, g.pl, b, k, q, (EF ? 2 : 0) + c)[px] = np + nm;
-                }
+                const float Ap = tA[i1], Bp = sg * bn[c] * tG[i1];
+                const float Am = tA[i2], Bm = sg * bn[c] * tG[i2];
+                const float m = Fa[c * n3 + l];
+                const float pp = fo[c] - m;
+                const float np = fmaf(Bp, pl[c], Ap * pp);
+                const float nm = fmaf(Bm, mi[c], Am * m);
+                F[c * n3 + l] = np + nm;
+                Fa[c * n3 + l] = nm;
+                if (q >= 0 && c < 2) ring_at(p.d, g.pl, b, k, q, (EF ? 2 : 0) + c)[px] = np + nm;
             }
         }
         return;
     }
 
     /* general cells */
-    const Rec32 r = (EF ? p.erec : p.hrec)[__float_as_int(cf[n3 + l])];
+    const Rec32 r = (EF ? p.erec : p.hrec)[__float_as_int(c1)];
     const bool stable = r.kind == RK_STABLE;
-    const Stn32 st = make_stn32(g, j0, j1, j2, EF && !stable);
-    for (int b = 0; b < p.batch; b++) {
-        float *F = F0 + b * bs, *Fa = Fa0 + b * bs;
-        const float *G = G0 + b * bs, *Ga = Ga0 + b * bs;
+    {
+        const Stn32 sts = make_stn32(g, j0, j1, j2, EF && !stable);
+        const float *Ga = Ga0 + b * bs;
         float main_out[3];
         if (r.kind == RK_FROZEN) {
 #pragma unroll
@@ -191,8 +186,7 @@ __global__ void __launch_bounds__(256) k_sweep32(const P32 p, const int rel)
         } else if (stable) {
             /* the stable form differentiates the MAIN slot of the other field */
             auto get = [&](int c, long long o) { return G[c * n3 + l + o] - Ga[c * n3 + l + o]; };
-            float pl[3], mi[3];
-            curl32<false>(get, st, pl, mi);
+            curl32<false>(get, sts, pl, mi);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 const float W = pl[c] + mi[c];
@@ -206,9 +200,6 @@ __global__ void __launch_bounds__(256) k_sweep32(const P32 p, const int rel)
                 Fa[c * n3 + l] = x;
             }
         } else {
-            auto get = [&](int c, long long o) { return G[c * n3 + l + o]; };
-            float pl[3], mi[3];
-            curl32<EF>(get, st, pl, mi);
             if (r.kind == RK_N) {
                 float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
                 if (j2 == p.s.iI[b]) {
@@ -238,6 +229,282 @@ __global__ void __launch_bounds__(256) k_sweep32(const P32 p, const int rel)
             ring_at(p.d, g.pl, b, k, q, EF ? 2 : 0)[px] = main_out[0];
             ring_at(p.d, g.pl, b, k, q, EF ? 3 : 1)[px] = main_out[1];
         }
+    }
+}
+
+/* ---------------------------------------------------------------------------
+ * Vectorised sweep: four consecutive x-cells per thread (float4 loads and
+ * stores), for L0 % 4 == 0.  Every element is updated with exactly the
+ * expressions of k_sweep32, so the two kernels give the same bits; what changes
+ * is that a thread keeps four cells' worth of loads in flight, which is what
+ * the HBM needs (the six curl neighbours of a cell are mostly cache hits, so a
+ * one-cell thread has only ~25 B of DRAM reads outstanding).  The x
+ * neighbours come from the adjacent lane by warp shuffle.
+ * ------------------------------------------------------------------------- */
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float el(const float4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+__device__ __forceinline__ void set_el(float4 &v, int i, float x)
+{
+    if (i == 0) v.x = x;
+    else if (i == 1) v.y = x;
+    else if (i == 2) v.z = x;
+    else v.w = x;
+}
+__device__ __forceinline__ float4 scale4(float4 v, float f) { return make_float4(f * v.x, f * v.y, f * v.z, f * v.w); }
+
+template <bool EF>
+__global__ void __launch_bounds__(128, 5) k_sweep32v(const P32 p, const int rel)
+{
+    const int b = blockIdx.y % p.batch;
+    const Geo &g = p.g;
+    const int xr = (blockIdx.x * 32 + threadIdx.x) * 4;
+    const int j1 = (blockIdx.y / p.batch) * blockDim.y + threadIdx.y;
+    const int j2 = blockIdx.z;
+    if (j1 >= g.L1) return; /* uniform per warp */
+    const bool live = xr < g.L0;
+    const int x0 = live ? xr : g.L0 - 4; /* idle lanes load valid data, store nothing */
+    const long long n3 = g.n3, bs = 3 * n3;
+    const long long l = x0 + (long long)g.L0 * (j1 + (long long)g.L1 * j2);
+    const float *__restrict__ cf = EF ? p.be : p.bh;
+    float *__restrict__ F = (EF ? p.E : p.H) + b * bs;
+    float *__restrict__ Fa = (EF ? p.Ea : p.Ha) + b * bs;
+    const float *__restrict__ G = (EF ? p.H : p.E) + b * bs;
+    const float sg = EF ? 1.0f : -1.0f;
+    const int k = *p.s.base + rel;
+    const int px0 = x0 + g.L0 * j1;
+    const int S = g.L0 + g.L1 + g.L2, s1 = g.L0, s2 = g.L0 + g.L1;
+    /* neighbours along y and z (whole quads) with the boundary factor */
+    const bool ey = EF ? (j1 + 1 == g.L1) : (j1 == 0);
+    const bool ez = EF ? (j2 + 1 == g.L2) : (j2 == 0);
+    const long long oy = (long long)g.L0 * (EF ? (ey ? -(g.L1 - 1) : 1) : (ey ? g.L1 - 1 : -1));
+    const long long oz = (long long)g.pl * (EF ? (ez ? -(g.L2 - 1) : 1) : (ez ? g.L2 - 1 : -1));
+    const float fy = ey ? (float)g.bc[1] : 1.0f, fz = ez ? (float)g.bc[2] : 1.0f;
+
+    float4 c[3], out[3], gh[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        c[i] = ld4(cf + i * n3 + l);
+        out[i] = ld4(F + i * n3 + l);
+        gh[i] = ld4(G + i * n3 + l);
+    }
+    /* H sweep: Ex, Ez at y-1; Ex, Ey at z-1.  E sweep: Hx, Hz at y+1; Hx, Hy at z+1. */
+    const float4 gy0 = scale4(ld4(G + 0 * n3 + l + oy), fy), gy2 = scale4(ld4(G + 2 * n3 + l + oy), fy);
+    const float4 gz0 = scale4(ld4(G + 0 * n3 + l + oz), fz), gz1 = scale4(ld4(G + 1 * n3 + l + oz), fz);
+    /* x neighbours: H sweep needs Ey, Ez at x-1; E sweep Hy, Hz at x+1 */
+    const unsigned full = 0xffffffffu;
+    float xn1, xn2; /* component 1, 2 of the outer neighbour of the quad */
+    if (!EF) {
+        xn1 = __shfl_up_sync(full, gh[1].w, 1);
+        xn2 = __shfl_up_sync(full, gh[2].w, 1);
+        if (threadIdx.x == 0 || x0 == 0) {
+            const bool edge = x0 == 0;
+            const long long o = edge ? g.L0 - 1 : -1;
+            const float f = edge ? (float)g.bc[0] : 1.0f;
+            xn1 = f * G[1 * n3 + l + o];
+            xn2 = f * G[2 * n3 + l + o];
+        }
+    } else {
+        xn1 = __shfl_down_sync(full, gh[1].x, 1);
+        xn2 = __shfl_down_sync(full, gh[2].x, 1);
+        if (threadIdx.x == 31 || x0 + 4 == g.L0) {
+            const bool edge = x0 + 4 == g.L0;
+            const long long o = edge ? -(g.L0 - 4) : 4;
+            const float f = edge ? (float)g.bc[0] : 1.0f;
+            xn1 = f * G[1 * n3 + l + o];
+            xn2 = f * G[2 * n3 + l + o];
+        }
+    }
+    if (!live) return;
+    const bool pyz = p.pmask[s1 + j1] | p.pmask[s2 + j2];
+    const bool on_src = j2 == p.s.iI[b];
+    const int q = monitor_index(p.d, j2);
+    float4 aux[3];
+    bool any_aux = false;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int xx = x0 + i;
+        const float h0 = el(gh[0], i), h1 = el(gh[1], i), h2 = el(gh[2], i);
+        /* neighbour along x of element i */
+        float n1x, n2x;
+        if (!EF) {
+            n1x = i == 0 ? xn1 : el(gh[1], i - 1);
+            n2x = i == 0 ? xn2 : el(gh[2], i - 1);
+        } else {
+            n1x = i == 3 ? xn1 : el(gh[1], i + 1);
+            n2x = i == 3 ? xn2 : el(gh[2], i + 1);
+        }
+        float pl[3], mi[3];
+        if (!EF) { /* backward, as curl32<false> */
+            pl[0] = h2 - el(gy2, i);
+            mi[0] = el(gz1, i) - h1;
+            pl[1] = h0 - el(gz0, i);
+            mi[1] = n2x - h2;
+            pl[2] = h1 - n1x;
+            mi[2] = el(gy0, i) - h0;
+        } else { /* forward, as curl32<true> */
+            pl[0] = el(gy2, i) - h2;
+            mi[0] = h1 - el(gz1, i);
+            pl[1] = el(gz0, i) - h0;
+            mi[1] = h2 - n2x;
+            pl[2] = n1x - h1;
+            mi[2] = h0 - el(gy0, i);
+        }
+        const float c0 = el(c[0], i);
+        if (isnan(c0)) { /* general cell: rewritten by k_general32 after this launch */
+            any_aux = true;
+            continue;
+        }
+        const bool split = p.pmask[xx] | pyz;
+        const float bn[3] = {c0, el(c[1], i), el(c[2], i)};
+        if (!split) {
+            float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+            if (on_src) {
+                W[0] += (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 1, px0 + i));
+                W[1] -= (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 0, px0 + i));
+            }
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) set_el(out[cc], i, fmaf(sg * bn[cc], W[cc], el(out[cc], i)));
+        } else {
+            any_aux = true;
+        }
+    }
+    /* elements that need their aux slot (split) or a record (general) */
+    if (any_aux) {
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) aux[cc] = ld4(Fa + cc * n3 + l);
+        const int jy = s1 + j1, jz = s2 + j2;
+        const float *tA = p.tab + (EF ? 2 : 0) * S, *tG = p.tab + (EF ? 3 : 1) * S;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int xx = x0 + i;
+            const float c0 = el(c[0], i);
+            if (isnan(c0)) continue;
+            if (!(p.pmask[xx] | pyz)) continue;
+            const float h0 = el(gh[0], i), h1 = el(gh[1], i), h2 = el(gh[2], i);
+            float n1x, n2x;
+            if (!EF) {
+                n1x = i == 0 ? xn1 : el(gh[1], i - 1);
+                n2x = i == 0 ? xn2 : el(gh[2], i - 1);
+            } else {
+                n1x = i == 3 ? xn1 : el(gh[1], i + 1);
+                n2x = i == 3 ? xn2 : el(gh[2], i + 1);
+            }
+            float pl[3], mi[3];
+            if (!EF) {
+                pl[0] = h2 - el(gy2, i);
+                mi[0] = el(gz1, i) - h1;
+                pl[1] = h0 - el(gz0, i);
+                mi[1] = n2x - h2;
+                pl[2] = h1 - n1x;
+                mi[2] = el(gy0, i) - h0;
+            } else {
+                pl[0] = el(gy2, i) - h2;
+                mi[0] = h1 - el(gz1, i);
+                pl[1] = el(gz0, i) - h0;
+                mi[1] = h2 - n2x;
+                pl[2] = n1x - h1;
+                mi[2] = h0 - el(gy0, i);
+            }
+            const int jx[3] = {xx, jy, jz};
+            const float bn[3] = {c0, el(c[1], i), el(c[2], i)};
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+                const int i1 = jx[(cc + 1) % 3], i2 = jx[(cc + 2) % 3];
+                const float Ap = tA[i1], Bp = sg * bn[cc] * tG[i1];
+                const float Am = tA[i2], Bm = sg * bn[cc] * tG[i2];
+                const float m = el(aux[cc], i);
+                const float pp = el(out[cc], i) - m; /* out still holds the old field here */
+                const float np = fmaf(Bp, pl[cc], Ap * pp);
+                const float nm = fmaf(Bm, mi[cc], Am * m);
+                set_el(out[cc], i, np + nm);
+                set_el(aux[cc], i, nm);
+            }
+        }
+    }
+#pragma unroll
+    for (int cc = 0; cc < 3; cc++) st4(F + cc * n3 + l, out[cc]);
+    if (any_aux) {
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) st4(Fa + cc * n3 + l, aux[cc]);
+    }
+    if (q >= 0) {
+        /* split elements sample the total field, ordinary ones their field */
+        st4(ring_at(p.d, g.pl, b, k, q, EF ? 2 : 0) + px0, out[0]);
+        st4(ring_at(p.d, g.pl, b, k, q, EF ? 3 : 1) + px0, out[1]);
+    }
+}
+
+/* general cells of the vectorised sweeps: one thread per record cell, run
+ * after k_sweep32v of the same field (the quads skipped them) */
+template <bool EF>
+__global__ void k_general32(const P32 p, const int rel, const int *cells, int ncells)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (i >= ncells) return;
+    const Geo &g = p.g;
+    const long long n3 = g.n3, bs = 3 * n3;
+    const long long l = cells[i];
+    const int j0 = (int)(l % g.L0), j1 = (int)((l / g.L0) % g.L1), j2 = (int)(l / g.pl);
+    const float *__restrict__ cf = EF ? p.be : p.bh;
+    float *F = (EF ? p.E : p.H) + b * bs, *Fa = (EF ? p.Ea : p.Ha) + b * bs;
+    const float *G = (EF ? p.H : p.E) + b * bs, *Ga = (EF ? p.Ha : p.Ea) + b * bs;
+    const float sg = EF ? 1.0f : -1.0f;
+    const int k = *p.s.base + rel;
+    const int px = j0 + g.L0 * j1;
+    const int q = monitor_index(p.d, j2);
+    const Rec32 r = (EF ? p.erec : p.hrec)[__float_as_int(cf[n3 + l])];
+    const bool stable = r.kind == RK_STABLE;
+    const Stn32 st = make_stn32(g, j0, j1, j2, EF && !stable);
+    float main_out[3];
+    if (r.kind == RK_FROZEN) {
+        for (int c = 0; c < 3; c++) main_out[c] = F[c * n3 + l] - Fa[c * n3 + l];
+    } else if (stable) {
+        auto get = [&](int c, long long o) { return G[c * n3 + l + o] - Ga[c * n3 + l + o]; };
+        float pl[3], mi[3];
+        curl32<false>(get, st, pl, mi);
+        for (int c = 0; c < 3; c++) {
+            const float W = pl[c] + mi[c];
+            float x = Fa[c * n3 + l];
+            float f = F[c * n3 + l] - x;
+            f += 0.5f * x;
+            x = fmaf(sg * r.B1[c], W, r.A1[c] * x);
+            f += 0.5f * x;
+            main_out[c] = f;
+            F[c * n3 + l] = f + x;
+            Fa[c * n3 + l] = x;
+        }
+    } else {
+        auto get = [&](int c, long long o) { return G[c * n3 + l + o]; };
+        float pl[3], mi[3];
+        curl32<EF>(get, st, pl, mi);
+        if (r.kind == RK_N) {
+            float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+            if (j2 == p.s.iI[b]) {
+                W[0] += (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 1, px));
+                W[1] -= (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 0, px));
+            }
+            for (int c = 0; c < 3; c++) {
+                const float f = fmaf(sg * r.B0[c], W[c], r.A0[c] * F[c * n3 + l]);
+                F[c * n3 + l] = f;
+                main_out[c] = f;
+            }
+        } else {
+            for (int c = 0; c < 3; c++) {
+                const float m = Fa[c * n3 + l];
+                const float pp = F[c * n3 + l] - m;
+                const float np = fmaf(sg * r.B0[c], pl[c], r.A0[c] * pp);
+                const float nm = fmaf(sg * r.B1[c], mi[c], r.A1[c] * m);
+                F[c * n3 + l] = np + nm;
+                Fa[c * n3 + l] = nm;
+                main_out[c] = np + nm;
+            }
+        }
+    }
+    if (q >= 0) {
+        ring_at(p.d, g.pl, b, k, q, EF ? 2 : 0)[px] = main_out[0];
+        ring_at(p.d, g.pl, b, k, q, EF ? 3 : 1)[px] = main_out[1];
     }
 }
 
@@ -283,14 +550,28 @@ __global__ void k_flush32(const P32 p, const int rel_end, const int count)
 
 void launch_h32(const P32 &p, int rel, int by, cudaStream_t st)
 {
-    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, (p.g.L1 + by - 1) / by, p.g.L2);
+    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
     k_sweep32<false><<<grd, blk, 0, st>>>(p, rel);
 }
 
 void launch_e32(const P32 &p, int rel, int by, cudaStream_t st)
 {
-    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, (p.g.L1 + by - 1) / by, p.g.L2);
+    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
     k_sweep32<true><<<grd, blk, 0, st>>>(p, rel);
+}
+
+void launch_h32v(const P32 &p, int rel, int by, const int *gcells, int ngh, cudaStream_t st)
+{
+    dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
+    k_sweep32v<false><<<grd, blk, 0, st>>>(p, rel);
+    if (ngh > 0) k_general32<false><<<dim3((ngh + 127) / 128, p.batch), 128, 0, st>>>(p, rel, gcells, ngh);
+}
+
+void launch_e32v(const P32 &p, int rel, int by, const int *gcells, int nge, cudaStream_t st)
+{
+    dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
+    k_sweep32v<true><<<grd, blk, 0, st>>>(p, rel);
+    if (nge > 0) k_general32<true><<<dim3((nge + 127) / 128, p.batch), 128, 0, st>>>(p, rel, gcells, nge);
 }
 
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st)

@@ -389,12 +389,15 @@ __global__ void __launch_bounds__(256) k_fused32(const Fused32 f, const int rel)
             }
             const float c0 = SQ(sc, 1, 0, ly, lx);
             if (isnan(c0)) {
-                h_general(f, b, k, xx, yy, gz, __float_as_int(SQ(sc, 1, 1, ly, lx)), o, om, omain);
+                /* out-of-line results go through a local buffer touched only here,
+                 * so the hot path's values stay in registers */
+                float tmp[9];
+                h_general(f, b, k, xx, yy, gz, __float_as_int(SQ(sc, 1, 1, ly, lx)), tmp, tmp + 3, tmp + 6);
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    o[c] *= fac;
-                    om[c] *= fac;
-                    omain[c] *= fac;
+                    o[c] = tmp[c] * fac;
+                    om[c] = tmp[3 + c] * fac;
+                    omain[c] = tmp[6 + c] * fac;
                 }
                 wa = true;
                 return;
@@ -533,7 +536,20 @@ __global__ void __launch_bounds__(256) k_fused32(const Fused32 f, const int rel)
                     if (p.erec[ridx].kind == RK_STABLE) {
                         done = false; /* finished by k_fix_stable32 */
                     } else {
-                        e_general(f, b, k, gx, gy, zp, ridx, pl_, mi_, e0, eo, eom, emain);
+                        float tmp[18];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            tmp[c] = pl_[c];
+                            tmp[3 + c] = mi_[c];
+                            tmp[6 + c] = e0[c];
+                        }
+                        e_general(f, b, k, gx, gy, zp, ridx, tmp, tmp + 3, tmp + 6, tmp + 9, tmp + 12, tmp + 15);
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            eo[c] = tmp[9 + c];
+                            eom[c] = tmp[12 + c];
+                            emain[c] = tmp[15 + c];
+                        }
                         wa = true;
                     }
                 }

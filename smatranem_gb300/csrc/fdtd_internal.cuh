@@ -117,6 +117,8 @@ void launch_dft64(const P64 &p, int rel, cudaStream_t st);
 void launch_h32(const P32 &p, int rel, int by, cudaStream_t st);
 void launch_e32(const P32 &p, int rel, int by, cudaStream_t st);
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
+void launch_h32v(const P32 &p, int rel, int by, const int *gcells, int ngh, cudaStream_t st);
+void launch_e32v(const P32 &p, int rel, int by, const int *gcells, int nge, cudaStream_t st);
 void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);
 size_t fused32_smem(int ty, int ns);
 int fused32_max_ctas_per_sm(int ty, int ns);

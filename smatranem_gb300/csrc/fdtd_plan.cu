@@ -102,7 +102,10 @@ struct smat_fdtd_plan {
     int cur = 0;          /* FP32: which field set holds the current state */
     int *d_stable = nullptr;
     int nstable = 0;
-    /* FP32 launch configuration (autotuned): fused z-march or two sweeps */
+    int *d_hgen = nullptr, *d_egen = nullptr; /* record (general) cells of each sweep */
+    int nhgen = 0, negen = 0;
+    /* FP32 launch configuration (autotuned): fused z-march (1), two sweeps (0),
+     * two vectorised sweeps (2, needs L0 % 4 == 0) */
     int fused = 1, ty = 8, zc = 40, ns = 5, ctas_per_sm = 0;
     int max_ctas = -1; /* cached occupancy of the current configuration */
     int by32 = 8;
@@ -257,13 +260,20 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
             launch_e64(q, rel0 + i, p->stream);
             launch_dft64(q, rel0 + i, p->stream);
         }
-    } else if (p->fused) {
+    } else if (p->fused == 1) {
         for (int i = 0; i < n; i++) {
             const Fused32 f = make_fused(p, xp);
             launch_fused32(f, rel0 + i, fused_grid(p, f), p->stream);
             p->cur ^= 1;
         }
         launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
+    } else if (p->fused == 2) {
+        const P32 q = make_p32(p, xp);
+        for (int i = 0; i < n; i++) {
+            launch_h32v(q, rel0 + i, p->by32, p->d_hgen, p->nhgen, p->stream);
+            launch_e32v(q, rel0 + i, p->by32, p->d_egen, p->negen, p->stream);
+        }
+        launch_flush32(q, rel0 + n, n, p->stream);
     } else {
         const P32 q = make_p32(p, xp);
         for (int i = 0; i < n; i++) {
@@ -585,6 +595,22 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
         }
     }
     p->nstable = (int)stable.size();
+    std::vector<int> hgen, egen;
+    for (long long l = 0; l < n3; l++) {
+        if (std::isnan(bh[l])) hgen.push_back((int)l);
+        if (std::isnan(be[l])) egen.push_back((int)l);
+    }
+    p->nhgen = (int)hgen.size();
+    p->negen = (int)egen.size();
+    if ((rc = p->alloc(&p->d_hgen, hgen.size() + 1)) || (rc = p->alloc(&p->d_egen, egen.size() + 1))) return rc;
+    if (!hgen.empty())
+        CK(cudaMemcpyAsync(p->d_hgen, hgen.data(), hgen.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    if (!egen.empty())
+        CK(cudaMemcpyAsync(p->d_egen, egen.data(), egen.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    if (p->L[0] % 4 == 0) {
+        p->fused = 2; /* default: vectorised sweeps where they apply */
+        p->by32 = 2;
+    }
     if ((rc = p->alloc(&p->d_stable, stable.size() + 1))) return rc;
     if (!stable.empty())
         CK(cudaMemcpyAsync(p->d_stable, stable.data(), stable.size() * sizeof(int), cudaMemcpyHostToDevice,
@@ -974,14 +1000,16 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
         const P32 q32 = make_p32(p, false);
         CK(cudaEventRecord(ev[0], p->stream));
         if (p->precision == SMAT_FP64) launch_h64(q64, i, p->stream);
-        else if (p->fused) {
+        else if (p->fused == 1) {
             const Fused32 f = make_fused(p, false);
             launch_fused32(f, i, fused_grid(p, f), p->stream);
             p->cur ^= 1;
-        } else launch_h32(q32, i, p->by32, p->stream);
+        } else if (p->fused == 2) launch_h32v(q32, i, p->by32, p->d_hgen, p->nhgen, p->stream);
+        else launch_h32(q32, i, p->by32, p->stream);
         CK(cudaEventRecord(ev[1], p->stream));
         if (p->precision == SMAT_FP64) launch_e64(q64, i, p->stream);
-        else if (!p->fused) launch_e32(q32, i, p->by32, p->stream);
+        else if (p->fused == 2) launch_e32v(q32, i, p->by32, p->d_egen, p->negen, p->stream);
+        else if (p->fused == 0) launch_e32(q32, i, p->by32, p->stream);
         CK(cudaEventRecord(ev[2], p->stream));
         if (p->precision == SMAT_FP64) launch_dft64(q64, i, p->stream);
         else if ((i + 1) % RING_K == 0 || i + 1 == nsteps) {
@@ -1009,7 +1037,10 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
 {
     smat_clear_error();
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
-    if (fused) {
+    if (fused < 0 || fused > 2) return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps)");
+    if (fused == 2 && (p->L[0] % 4 != 0 || tile_y < 1 || tile_y > 4))
+        return smat_fail(SMAT_EINVAL, "set_tuning: vector sweeps need L0 %% 4 == 0 and tile_y in 1..4");
+    if (fused == 1) {
         if (tile_y < 2 || tile_y > 8 || z_chunk < 1 || ctas_per_sm < 0 || slots < 4 || slots > 6)
             return smat_fail(SMAT_EINVAL,
                              "set_tuning: tile_y in 2..8, z_chunk >= 1, ctas_per_sm >= 0, slots in 4..6");
@@ -1025,7 +1056,7 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
         p->by32 = tile_y;
     }
-    p->fused = fused ? 1 : 0;
+    p->fused = fused;
     drop_graph(p);
     return SMAT_OK;
 }
@@ -1062,10 +1093,12 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
             }
     cands.push_back({0, 4, 1, 0, 4});
     cands.push_back({0, 8, 1, 0, 4});
+    if (p->L[0] % 4 == 0)
+        for (int by : {1, 2, 4}) cands.push_back({2, by, 1, 0, 4});
     const int nq = p->nq;
     p->nq = 0;
     CK(cudaMemsetAsync(p->d_iI, 0xff, sizeof(int) * p->batch, p->stream));
-    const int save[5] = {p->fused, p->fused ? p->ty : p->by32, p->zc, p->ctas_per_sm, p->ns};
+    const int save[5] = {p->fused, p->fused == 1 ? p->ty : p->by32, p->zc, p->ctas_per_sm, p->ns};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -1102,7 +1135,7 @@ extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
 {
     if (!p || !out) return smat_fail(SMAT_EINVAL, "get_tuning: bad arguments");
     out[0] = p->fused;
-    out[1] = p->fused ? p->ty : p->by32;
+    out[1] = p->fused == 1 ? p->ty : p->by32;
     out[2] = p->zc;
     out[3] = p->ctas_per_sm;
     out[4] = p->ns;
@@ -1181,6 +1214,23 @@ extern "C" int smat_fdtd_get_dft(smat_fdtd_plan *p, int b, int f, int q, double 
     int rc = read_acc(p, b, f, q, a);
     if (rc) return rc;
     memcpy(out, a.data(), a.size() * 8);
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_dft_count(const smat_fdtd_plan *p, int *nfreq, int *nplanes)
+{
+    if (!p) return smat_fail(SMAT_EINVAL, "null plan");
+    if (nfreq) *nfreq = p->nfreq;
+    if (nplanes) *nplanes = p->nq;
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_dft_device(smat_fdtd_plan *p, int b, int f, int q, const double **ptr, long long *fstride)
+{
+    if (!p || !ptr || b < 0 || b >= p->batch || f < 0 || f >= p->nfreq || q < 0 || q >= p->nq)
+        return smat_fail(SMAT_EINVAL, "dft_device: bad arguments");
+    *ptr = p->d_acc + 2 * ((((size_t)b * p->nfreq + f) * p->nq + q) * 4 * (size_t)p->pl);
+    if (fstride) *fstride = (long long)p->nq * 4 * p->pl;
     return SMAT_OK;
 }
 

@@ -16,6 +16,9 @@ int host_expn(int N, double *out);
  * per step, stop-period*N steps (main :153-167). */
 int host_cw_schedule(int N, const int time_period[3], double *src, double *phase);
 
+struct smat_fdtd_plan;
+int smat_fdtd_dft_count(const struct smat_fdtd_plan *plan, int *nfreq, int *nplanes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -74,6 +74,10 @@ def lib():
         L.smat_fdtd_set_tuning.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.smat_fdtd_get_tuning.argtypes = [_P, _P]
         L.smat_fdtd_autotune.argtypes = [_P, C.c_int, _P, _P]
+        L.smat_fdtd_overlap.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P]
+        L.smat_fdtd_dft_count.argtypes = [_P, _P, _P]
+        L.smat_fdtd_dft_device.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P]
+        L.smat_overlap.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, _P, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -299,6 +303,16 @@ class Plan:
         out = (C.c_int * 5)()
         _check(lib().smat_fdtd_get_tuning(self._h, out))
         return tuple(out)
+
+    def overlap(self, b, q, tilxi_cols):
+        """S for every DFT frequency of plane q: (nfreq, ncols) complex (GPU, FP64)."""
+        t = _c128(tilxi_cols)
+        ncols = t.shape[0]
+        nf = C.c_int(0)
+        _check(lib().smat_fdtd_dft_count(self._h, C.byref(nf), None))
+        S = np.zeros((nf.value, ncols), np.complex128)
+        _check(lib().smat_fdtd_overlap(self._h, b, q, ncols, _ptr(t), _ptr(S)))
+        return S
 
     def check_finite(self):
         ok, m = C.c_int(0), C.c_double(0)

@@ -352,7 +352,8 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     pr = W.prepare(s)
     nsteps = 9 if kw.get("metals") else 37
     ref = _run_fp32(s, pr, iBTIin, (0, 4, 1, 0, 4), nsteps)
-    for tuning in TUNINGS:
+    tunings = TUNINGS + ([(2, 1, 1, 0, 4), (2, 2, 1, 0, 4), (2, 4, 1, 0, 4)] if L[0] % 4 == 0 else [])
+    for tuning in tunings:
         got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
         for rb, gb in zip(ref, got):
             for a, b_ in zip(rb, gb):
@@ -400,3 +401,38 @@ def test_autotune_keeps_state_and_results(built):
     for rb, gb in zip(ref, got):
         for a, b_ in zip(rb, gb):
             assert np.array_equal(a, b_)
+
+
+def test_gpu_overlap_matches_oracle_s_calc(built, port):
+    """GPU mode-overlap projection vs the oracle's S_calc (reference order), FP64,
+    relative tolerance 1e-12 (the GPU sums rows in blocks)."""
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    L = (20, 14, 16, 3)
+    s = W.random_structure(L, seed=8, pml=(3, 3, 3))
+    pr = W.prepare(s)
+    pl = L[0] * L[1]
+    src, _ = f.cw_schedule(pr.n2pi, (1, 1, 3))
+    nsteps = 30
+    k = np.arange(nsteps)[:, None]
+    wdt = np.array([0.11, 0.23, 0.31])
+    ph = np.stack([np.cos(wdt * (k + 1)), np.sin(wdt * (k + 1)), np.cos(wdt * (k + 1.5)), np.sin(wdt * (k + 1.5))],
+                  axis=-1)
+    rng = np.random.default_rng(2)
+    ncols = 5
+    tilxi = rng.standard_normal((ncols, 4 * pl)) + 1j * rng.standard_normal((ncols, 4 * pl))
+    Hinc, Einc = W.random_incident(pl, seed=4)
+    with f.Plan.create(L, s.iBc, (4, 11, 6, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma) as p:
+        p.set_incident(0, Hinc, Einc)
+        p.set_schedule(src[:nsteps], planes=(4, 11), phase=ph)
+        p.run(0, nsteps)
+        for q in range(2):
+            S = p.overlap(0, q, tilxi)
+            for fi in range(3):
+                d = p.get_dft(0, fi, q)
+                HB = np.empty(2 * pl, np.complex128)
+                EB = np.empty(2 * pl, np.complex128)
+                HB[0::2], HB[1::2] = d[0], d[1]
+                EB[0::2], EB[1::2] = d[2], d[3]
+                ref = port.overlap(L, tilxi, HB, EB)
+                assert np.max(np.abs(S[fi] - ref)) <= 1e-12 * np.max(np.abs(ref))
