@@ -213,6 +213,23 @@ int smat_fdtd_dft_device(smat_fdtd_plan *plan, int b, int f, int q, const double
 int smat_overlap(int npix, int ncols, int nvec, long long vec_stride, const double *tilXi,
                  const double *dft, double *S, void *stream);
 
+/* No counterpart in the reference.  smat_overlap without any device
+ * allocation, for callers that must not allocate at this point: inside a
+ * stream capture that may not contain allocation nodes, under a framework that
+ * owns the device's memory pool, or in a loop that must not fail on memory
+ * after start-up.  The block partial sums go to a static device array of
+ * SMAT_OVERLAP_NOALLOC_MAX complex doubles (1 MiB, held on every device that
+ * loads the library until exit); a call needing more (ncols * nvec * blocks,
+ * blocks <= 64 and about 4*npix/1024) fails with SMAT_EINVAL before launching.
+ * The first call on a device looks up the array's device address (no
+ * allocation); make that first call outside any stream capture.  All calls on
+ * a device share the array: calls that overlap on the GPU (different streams,
+ * no ordering) race and corrupt each other's results; calls ordered on one
+ * stream are safe.  Results equal smat_overlap's bit for bit. */
+#define SMAT_OVERLAP_NOALLOC_MAX 65536
+int smat_overlap_noalloc(int npix, int ncols, int nvec, long long vec_stride, const double *tilXi,
+                         const double *dft, double *S, void *stream);
+
 /* The same for every frequency of plane q of excitation b of a plan, with
  * tilde-Xi columns and the result (nfreq*ncols complex) in host memory. */
 int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const double *tilXi_host,

@@ -165,3 +165,59 @@ extern "C" int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, 
     cudaFree(dS);
     return rc;
 }
+
+/* ---------------------------------------------------------------------------
+ * Allocation-free variant of smat_overlap.
+ *
+ * Some callers cannot allocate device memory while they extract S parameters:
+ * code that runs inside a stream capture that must not contain allocation
+ * nodes, a host process whose memory pool is reserved by a framework that
+ * owns the device (and forbids others to call cudaMalloc/cudaMallocAsync), or
+ * a real-time loop that must not risk an allocation failure after start-up.
+ * smat_overlap_noalloc does the same projection with its block partial sums in
+ * a fixed device array that lives in this library's module, so it never
+ * allocates.  The array holds SMAT_OVERLAP_NOALLOC_MAX complex partial sums
+ * (1 MiB) on every device that loads the library, until the process exits.
+ * ------------------------------------------------------------------------- */
+static __device__ __align__(256) double2 g_overlap_scratch[SMAT_OVERLAP_NOALLOC_MAX];
+
+namespace {
+constexpr int MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+double2 *g_noalloc_addr[MAX_DEVICES];
+}
+
+extern "C" int smat_overlap_noalloc(int npix, int ncols, int nvec, long long vec_stride, const double *tilXi,
+                                    const double *dft, double *S, void *stream)
+{
+    smat_clear_error();
+    int rc = overlap_args_ok(npix, ncols, nvec, vec_stride, tilXi, dft, S);
+    if (rc) return rc;
+    const long long need = (long long)overlap_blocks(npix) * ncols * nvec;
+    if (need > SMAT_OVERLAP_NOALLOC_MAX)
+        return smat_fail(SMAT_EINVAL,
+                         "overlap_noalloc: %lld partial sums needed (ncols*nvec*%d blocks), the static scratch "
+                         "holds %d; use smat_overlap or fewer columns/planes per call",
+                         need, overlap_blocks(npix), SMAT_OVERLAP_NOALLOC_MAX);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return smat_fail(SMAT_ECUDA, "overlap_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= MAX_DEVICES) return smat_fail(SMAT_EINVAL, "overlap_noalloc: device %d out of range", dev);
+    double2 *scratch = nullptr;
+    {
+        /* once per device, with that device current: the device address of the
+         * static array (the host-side symbol is not a device address) */
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_overlap_scratch);
+            if (e != cudaSuccess || !ptr)
+                return smat_fail(SMAT_ECUDA, "overlap_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            g_noalloc_addr[dev] = (double2 *)ptr;
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    /* every partial the second pass reads is written by the first pass of the
+     * same call, so the array needs no clearing between calls */
+    return overlap_launch(npix, ncols, nvec, vec_stride, tilXi, dft, S, scratch, (cudaStream_t)stream);
+}
