@@ -95,6 +95,8 @@ int smat_coefficients(const int L[4], int Lnotn, const double *sigma, const doub
                       double *Ah, double *Bh, double *Ae, double *Be);
 /* set_tau :515-524. */
 int smat_set_tau(double omega, double min_Dt, int *N_2pi, double *invtau_R, double *invtau_I);
+/* omega = 2*pi/(wavelength*k0) exactly as input_Lf evaluates it (:740). */
+double smat_omega(double wavelength, double k0);
 /* set_env :452-475; returns NaN where the reference exits ("f_env error!"). */
 double smat_set_env(int N_2pi, const int time_period[3], int j_half, int j_time, int j_period);
 
@@ -234,6 +236,32 @@ int smat_overlap_noalloc(int npix, int ncols, int nvec, long long vec_stride, co
  * tilde-Xi columns and the result (nfreq*ncols complex) in host memory. */
 int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const double *tilXi_host,
                       double *S_host);
+
+/* The FDTD input deck and the drop-in program. ------------------------------
+ * A deck is what the reference FDTD reads (main :44-99): input.txt (keys
+ * Prefix, BoundaryCondition, ModeP, FDTD; input_file0 :759-781, plus the
+ * optional "FDTD_GPU: precision = FP32" line the reference ignores), the
+ * per-layer Med files (input_data :665-699), the Mode files (get_RealNum
+ * :632-661) and the Xi files (set_Xi/set_tilXi :557-628).  Only the tilde-Xi
+ * columns S_calc reports and the incident column are kept. */
+typedef struct smat_deck smat_deck;
+int smat_deck_load(const char *input_txt, smat_deck **deck);
+void smat_deck_free(smat_deck *deck);
+/* L, {iB, iT, iI, inci_mode}, iBc, time_period, omega (2*pi/(lambda*k0)),
+ * min_Dt (sqrt of the smallest "min Dt^2" header), Dt_factor, N_real of the
+ * bottom and top mode files; any pointer may be NULL. */
+int smat_deck_info(const smat_deck *deck, int L[4], int iBTIin[4], int iBc[3], int time_period[3],
+                   double *omega, double *min_dt, double *dt_factor, int nreal[2]);
+/* mu, epsi (3*L3D complex, as stored: stretched), Hinc, Einc (2*L0*L1 complex). */
+int smat_deck_arrays(const smat_deck *deck, double *mu, double *epsi, double *Hinc, double *Einc);
+/* S_calc of the bottom (which = 0, HB/EB) or top (1, HT/ET) monitor plane:
+ * 2*N_real complex values, forward modes then backward modes (S_calc :437-445
+ * in the reference's summation order). */
+int smat_deck_smatrix(const smat_deck *deck, int which, const double *HB, const double *EB, double *S);
+/* The whole drop-in `FDTD input.txt` program (main :32-187): reads the deck,
+ * runs on the GPU, prints the reference's report (including the |S|^2 table
+ * of :182-185) to stderr; returns the process exit status. */
+int smat_fdtd_main(int argc, char **argv);
 
 /* Largest |field| over every excitation (a NaN/Inf check); *finite = 0 when a
  * non-finite value is present. */

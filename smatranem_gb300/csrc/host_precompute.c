@@ -325,3 +325,6 @@ int host_cw_schedule(int N, const int tp[3], double *src, double *phase)
     free(e);
     return rc;
 }
+
+/* omega = 2 pi / (lambda k0) as input_Lf evaluates it (:740, long double 2 pi) */
+double smat_omega(double wavelength, double k0) { return TWO_PI_LD / (wavelength * k0); }

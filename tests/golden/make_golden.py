@@ -9,6 +9,10 @@ oracle port (the reference builds them inside main(), which is not callable);
 they are pinned separately by the deck-level fixture below, where the stock
 reference binary runs end to end.
 
+The deck fixtures (tests/golden/decks/) are written by smatranem_gb300.decks
+and run through the stock reference binary oracle/_ref/FDTD_ref; its stderr
+(the |S|^2 report) is kept beside each deck.
+
 Usage (needs the reference sources, i.e. runs only where they are mounted):
     python tests/golden/make_golden.py
 """
@@ -69,11 +73,45 @@ def run_case(ref, port, name, L, seed, kw, iBTIin, tp, nsteps):
           f"N_2pi={n2pi} steps={nsteps} exits={exits} max|H|={np.abs(H).max():.3e}")
 
 
+# decks for the drop-in program: (name, L, seed, structure kwargs, deck kwargs)
+DECKS = [
+    ("deck_periodic", (3, 3, 12, 3), 41, dict(pml=(0, 0, 1), pml_z_only=True, iBc=(1, 1, 1)),
+     dict(time_period=(1, 1, 3), inci_point="B2", inci_mode=1, targets=("B1", "T1"), nreal=(3, 2))),
+    ("deck_lossy", (4, 3, 12, 3), 42, dict(pml=(0, 0, 1), pml_z_only=True, lossy=0.2, iBc=(-1, 0, 1)),
+     dict(time_period=(1, 2, 4), inci_point="T0", inci_mode=-2, targets=("B1", "T1"), nreal=(2, 3))),
+    # the top monitor plane lies in the z-PML: the reference aborts (:320)
+    ("deck_pml_monitor", (3, 3, 12, 3), 43, dict(pml=(0, 0, 1), pml_z_only=True),
+     dict(time_period=(1, 1, 2), inci_point="B2", inci_mode=1, targets=("B1", "T2"), nreal=(2, 2))),
+]
+
+
+def make_deck(name, L, seed, kw, dkw):
+    """Write a deck with the repository's writer, run the stock reference FDTD
+    binary on it, keep the deck and the reference's stderr."""
+    import shutil
+    import subprocess
+    from smatranem_gb300 import decks
+    root = os.path.join(HERE, "decks", name)
+    shutil.rmtree(root, ignore_errors=True)
+    s = W.random_structure(L, seed=seed, omega=decks.omega_of(1.55e-6, 1.0e7), **kw)
+    decks.write_deck(root, s, seed=seed, **dkw)
+    r = subprocess.run([oracle.REF_BIN, "input.txt"], cwd=root, capture_output=True, text=True)
+    with open(os.path.join(root, "reference_stderr.txt"), "w") as f:
+        f.write(r.stderr)
+    with open(os.path.join(root, "reference_status.txt"), "w") as f:
+        f.write(f"{r.returncode}\n")
+    np.savez_compressed(os.path.join(root, "media.npz"), mu=s.mu.reshape(-1), epsi=s.epsi.reshape(-1),
+                        min_dt=s.min_dt)
+    print(f"{name}: " + r.stderr.strip().splitlines()[-1])
+
+
 def main():
     oracle.build(with_reference=True)
     ref, port = oracle.Oracle("reference"), oracle.Oracle("port")
     for case in CASES:
         run_case(ref, port, *case)
+    for deck in DECKS:
+        make_deck(*deck)
 
 
 if __name__ == "__main__":

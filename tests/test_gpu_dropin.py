@@ -1,0 +1,67 @@
+"""The drop-in `FDTD` executable on the golden decks, against the reference
+FDTD's report of the same decks.  FP64 is bit-identical, so every line of the
+|S|^2 table (printed with %.20e) must match exactly.  The lines that differ by
+design: the start-time stamp, and the check_Xi diagnostic (||tilXi^H Xi - I||)
+which needs the whole Xi matrix the drop-in does not read."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+pytestmark = pytest.mark.gpu
+
+EXE = os.path.join(ROOT, "smatranem_gb300", "_build", "FDTD")
+DECKS = sorted(os.listdir(os.path.join(GOLDEN, "decks")))
+
+
+def _comparable(text):
+    return [l for l in text.splitlines() if l and not l.startswith("# Start time") and not l.startswith("tilXi^+ Xi")]
+
+
+@pytest.mark.parametrize("name", DECKS)
+def test_dropin_report_matches_reference(built, tmp_path, name):
+    src = os.path.join(GOLDEN, "decks", name)
+    work = tmp_path / name
+    shutil.copytree(src, work)
+    r = subprocess.run([EXE, "input.txt"], cwd=work, capture_output=True, text=True, timeout=600)
+    ref = open(os.path.join(src, "reference_stderr.txt")).read()
+    ref_status = int(open(os.path.join(src, "reference_status.txt")).read())
+    if ref_status != 0:
+        # the reference aborts (a PML cell on a monitor plane); so does the drop-in, without running
+        assert r.returncode != 0
+        assert "monitor plane" in r.stderr
+        return
+    assert r.returncode == 0, r.stderr
+    mine, theirs = _comparable(r.stderr), _comparable(ref)
+    table = theirs.index(next(l for l in theirs if l.startswith("Bottom |S_")))
+    assert mine[mine.index(theirs[table]):] == theirs[table:]  # the |S|^2 tables, byte for byte
+    assert mine == theirs  # and every other line of the report
+
+
+def test_dropin_fp32_within_tolerance(built, tmp_path):
+    """The optional FP32 mode ("FDTD_GPU: precision = FP32" in input.txt, a key the
+    reference ignores): |S|^2 within 1e-4 relative of the reference."""
+    name = "deck_periodic"
+    src = os.path.join(GOLDEN, "decks", name)
+    work = tmp_path / name
+    shutil.copytree(src, work)
+    with open(work / "input.txt", "a") as f:
+        f.write("\tFDTD_GPU: precision = FP32\n")
+    r = subprocess.run([EXE, "input.txt"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+
+    def table(text):
+        vals = []
+        for l in text.splitlines():
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) == 4 and parts[0][:1] in "+-":
+                vals += [float(parts[1]), float(parts[3])]
+        return vals
+    a, b = table(r.stderr), table(open(os.path.join(src, "reference_stderr.txt")).read())
+    assert len(a) == len(b) > 0
+    big = max(b)
+    for x, y in zip(a, b):
+        assert abs(x - y) <= 1e-4 * big
