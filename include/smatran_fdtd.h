@@ -278,7 +278,9 @@ int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double
  * ctas_per_sm resident CTAs (0: as many as fit) and `slots` shared-memory
  * plane slots (4..6: planes staged 1..3 ahead); kernel = 0: two sweeps with
  * 32 x tile_y thread blocks (1..8); kernel = 2: two sweeps of four cells per
- * thread (float4, L0 % 4 == 0, tile_y 1..4; the default where it applies).  Results are
+ * thread (float4, L0 % 4 == 0, tile_y 1..4; the default where it applies);
+ * kernel = 3: the fused launch with TMA plane staging (L0 % 4 == 0, same
+ * parameters as kernel 1).  Results are
  * bit-identical across configurations. */
 int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int kernel, int tile_y, int z_chunk, int ctas_per_sm,
                          int slots);
@@ -291,6 +293,9 @@ int smat_fdtd_get_tuning(const smat_fdtd_plan *plan, int out[5]);
  * set_fields / run); sources and DFT sampling are off while it runs, so the
  * plan is left unchanged apart from its configuration.  FP64: no-op. */
 int smat_fdtd_autotune(smat_fdtd_plan *plan, int nsteps, int best[5], double *best_ms);
+
+/* Name, SM count and compute capability (major*10+minor) of the current device. */
+int smat_device_info(char *name, int name_len, int *sm_count, int *cc);
 
 /* Device bytes the plan holds. */
 long long smat_fdtd_device_bytes(const smat_fdtd_plan *plan);

@@ -31,6 +31,7 @@
  *     belong to another tile; they are finished by a small fix-up kernel after
  *     the fused launch (k_fix_stable32).
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.cuh"
@@ -665,6 +666,469 @@ void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st)
     if (f.nstable > 0) {
         dim3 g2((f.nstable + 127) / 128, f.p.batch);
         k_fix_stable32<<<g2, 128, 0, st>>>(f, rel);
+    }
+}
+
+
+/* ===========================================================================
+ * k_fused32t: the fused step with TMA plane staging (sm_90+ bulk tensor copies)
+ *
+ * Same computation and bit-identical results as k_fused32; the difference is
+ * how a plane reaches shared memory: one elected thread issues a handful of
+ * cp.async.bulk.tensor copies per plane (E tile + 1-cell halo, H / coefficient
+ * / aux tiles with the +1 halo, E-side tiles) that complete on the slot's
+ * mbarrier, instead of every thread issuing ~20 four-byte copies.  Needs
+ * L0 % 4 == 0 (16-byte global strides).  Halo entries outside the domain come
+ * back zero-filled; where the boundary factor iBc is +-1 they are patched with
+ * iBc * (the wrapped value) after the copy lands, on boundary tiles only; a
+ * plane wrapped along z is fetched at its wrapped index and scaled.
+ * ========================================================================= */
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+/* bounded wait on the phase `parity` of bar; false on timeout */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+{
+    const unsigned a = smem_u32(bar);
+    for (int it = 0; it < (1 << 24); it++) {
+        unsigned done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load4(float *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                          uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_u32(dst)),
+                 "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+                 "r"(smem_u32(bar))
+                 : "memory");
+}
+
+constexpr int TEX = TX + 8; /* E box width: x from X0-4 (16-byte aligned start) */
+constexpr int TQX = TX + 4; /* H-side box width: x from X0 to X0+35 (covers the +1 halo) */
+
+struct TSlot { /* float offsets inside one slot, each segment 128-byte aligned */
+    int e, qt, qb, qm, be, bm, size;
+};
+
+__host__ __device__ inline int align32f(int n) { return (n + 31) & ~31; }
+
+__host__ __device__ inline TSlot tslot(int ty)
+{
+    TSlot s;
+    int o = 0;
+    s.e = o;
+    o += align32f(3 * (ty + 2) * TEX);
+    s.qt = o;
+    o += align32f(3 * (ty + 1) * TQX);
+    s.qb = o;
+    o += align32f(3 * (ty + 1) * TQX);
+    s.qm = o;
+    o += align32f(3 * (ty + 1) * TQX);
+    s.be = o;
+    o += align32f(3 * ty * TX);
+    s.bm = o;
+    o += align32f(3 * ty * TX);
+    s.size = o;
+    return s;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(256) k_fused32t(const __grid_constant__ Fused32T ft, const int rel)
+{
+    extern __shared__ __align__(128) float smem[];
+    constexpr int DEPTH = NS - 3;
+    const Fused32 &f = ft.f;
+    const P32 &p = f.p;
+    const Geo &g = p.g;
+    const int TY = blockDim.y;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx, nthr = TX * TY;
+    const TSlot sl = tslot(TY);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);       /* NS mbarriers (first 128 bytes) */
+    float *slots = smem + 32;                                  /* NS slots */
+    float *sH = slots + NS * sl.size;                          /* NSH planes of H_new */
+    const int SHY = TY + 1;
+    const long long n3 = g.n3, bs = 3 * n3;
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+    const int S = L0 + L1 + L2, s1 = L0, s2 = L0 + L1;
+    const long long pl = g.pl;
+    const int k = *p.s.base + rel;
+#define TE(s, c, ly, lx) slots[(s) * sl.size + sl.e + ((c) * (TY + 2) + (ly)) * TEX + (lx)]
+#define TQ(s, seg, c, ly, lx) slots[(s) * sl.size + (seg) + ((c) * (TY + 1) + (ly)) * TQX + (lx)]
+#define TB(s, seg, c) slots[(s) * sl.size + (seg) + ((c) * TY + ty) * TX + tx]
+#define HN(s, c, ly, lx) sH[(((s) * 3 + (c)) * SHY + (ly)) * SHX + (lx)]
+
+    for (int item = blockIdx.x; item < f.nitems; item += gridDim.x) {
+        const int b = item % p.batch;
+        int t = item / p.batch;
+        const int tix = t % f.ntx;
+        t /= f.ntx;
+        const int tiy = t % f.nty;
+        const int zci = t / f.nty;
+        const int X0 = tix * TX, Y0 = tiy * TY;
+        const int w = min(TX, L0 - X0), h = min(TY, L1 - Y0);
+        const int z0 = zci * f.zc, z1 = min(z0 + f.zc, L2);
+        const float *Eo = p.E + b * bs, *Ho = p.H + b * bs, *Hao = p.Ha + b * bs, *Eao = p.Ea + b * bs;
+        float *En = f.En + b * bs, *Hn = f.Hn + b * bs, *Han = f.Han + b * bs, *Ean = f.Ean + b * bs;
+        const bool own = tx < w && ty < h;
+        const int gx = X0 + tx, gy = Y0 + ty;
+        const int own2d = gx + L0 * gy;
+        const bool own_split2d = own && (p.pmask[gx] | p.pmask[s1 + gy]);
+        const bool edge_tile = X0 == 0 || X0 + w == L0 || Y0 == 0 || Y0 + h == L1;
+        /* does the tile (with its halo) hold any split cell in x or y? */
+        bool tile_split2d = false;
+        for (int x = X0 - 1; x <= X0 + w; x++) tile_split2d |= p.pmask[(x + L0) % L0] != 0;
+        for (int y = Y0 - 1; y <= Y0 + h; y++) tile_split2d |= p.pmask[s1 + (y + L1) % L1] != 0;
+        int hlx = -1, hly = -1, hxx = 0, hyy = 0;
+        float hfac = 0.0f;
+        bool hsplit2d = false;
+        if (tid < h) {
+            hlx = w;
+            hly = tid;
+        } else if (tid < h + w) {
+            hlx = tid - h;
+            hly = h;
+        }
+        if (hlx >= 0) {
+            float fc = 1.0f;
+            hxx = wrapc(X0 + hlx, L0, g.bc[0], fc);
+            hyy = wrapc(Y0 + hly, L1, g.bc[1], fc);
+            hfac = fc;
+            hsplit2d = p.pmask[hxx] | p.pmask[s1 + hyy];
+        }
+        if (tid == 0)
+            for (int s = 0; s < NS; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        __syncthreads();
+
+        /* producer (thread 0): all copies of logical plane zl into its slot */
+        auto issue = [&](int zl) {
+            const int s = (zl + NS) % NS;
+            float fz = 1.0f;
+            int gz = wrapc(zl, L2, g.bc[2], fz);
+            if (fz == 0.0f) gz = zl; /* out of range: the copy zero-fills, = iBc * value */
+            const bool pre = zl < z0, extra = zl >= z1;
+            float unused = 1.0f;
+            const bool split = tile_split2d || p.pmask[s2 + wrapc(zl, L2, g.bc[2], unused)];
+            unsigned bytes = 4u * 3 * (TY + 2) * TEX;
+            if (!pre) bytes += 4u * 3 * (TY + 1) * TQX * (split ? 3 : 2);
+            if (!pre && !extra) bytes += 4u * 3 * TY * TX * (split ? 2 : 1);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect(&bars[s], bytes);
+            float *base = slots + s * sl.size;
+            tma_load4(base + sl.e, &ft.mE, X0 - 4, Y0 - 1, gz, 3 * b, &bars[s]);
+            if (pre) return;
+            tma_load4(base + sl.qt, &ft.mH, X0, Y0, gz, 3 * b, &bars[s]);
+            tma_load4(base + sl.qb, &ft.mBh, X0, Y0, gz, 0, &bars[s]);
+            if (split) tma_load4(base + sl.qm, &ft.mHa, X0, Y0, gz, 3 * b, &bars[s]);
+            if (extra) return;
+            tma_load4(base + sl.be, &ft.mBe, X0, Y0, gz, 0, &bars[s]);
+            if (split) tma_load4(base + sl.bm, &ft.mEa, X0, Y0, gz, 3 * b, &bars[s]);
+        };
+
+        /* after plane zl landed: the wrapped halo entries scaled by iBc = +-1 */
+        auto patch = [&](int zl) {
+            const int s = (zl + NS) % NS;
+            float fz = 1.0f;
+            const int gz = wrapc(zl, L2, g.bc[2], fz);
+            const bool zw = (zl < 0 || zl >= L2) && fz != 0.0f && fz != 1.0f;
+            if (!edge_tile && !zw) return;
+            const long long base = pl * gz;
+            const int nex = w + 2;
+            for (int i = tid; i < nex * (h + 2); i += nthr) {
+                const int lx = i % nex, ly = i / nex;
+                float fc = fz;
+                const int xx = wrapc(X0 - 1 + lx, L0, g.bc[0], fc);
+                const int yy = wrapc(Y0 - 1 + ly, L1, g.bc[1], fc);
+                const bool oob = xx != X0 - 1 + lx || yy != Y0 - 1 + ly;
+                if (fc == 0.0f || !(oob || zw)) continue;
+                const long long gi = base + xx + (long long)L0 * yy;
+#pragma unroll
+                for (int c = 0; c < 3; c++) TE(s, c, ly, lx + 3) = fc * Eo[c * n3 + gi];
+            }
+            if (zl < z0) return;
+            const bool zsplit = p.pmask[s2 + gz];
+            for (int i = tid; i < (w + 1) * (h + 1); i += nthr) {
+                const int lx = i % (w + 1), ly = i / (w + 1);
+                if (lx == w && ly == h) continue;
+                float fc = fz;
+                const int xx = wrapc(X0 + lx, L0, g.bc[0], fc);
+                const int yy = wrapc(Y0 + ly, L1, g.bc[1], fc);
+                const bool oob = xx != X0 + lx || yy != Y0 + ly;
+                if (!(oob || zw)) continue;
+                const long long gi = base + xx + (long long)L0 * yy;
+                const bool split = zsplit || p.pmask[xx] || p.pmask[s1 + yy];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    TQ(s, sl.qt, c, ly, lx) = fc * Ho[c * n3 + gi];
+                    if (oob) TQ(s, sl.qb, c, ly, lx) = p.bh[c * n3 + gi];
+                    if (split) TQ(s, sl.qm, c, ly, lx) = fc * Hao[c * n3 + gi];
+                }
+            }
+        };
+
+        auto h_update = [&](int z, int lx, int ly, int xx, int yy, float fxy, bool split2d, float o[3], float om[3],
+                            float omain[3], bool &wa) {
+            wa = false;
+            const int sc = (z + NS) % NS, sp = (z + NS - 1) % NS;
+            float fac = fxy;
+            const int gz = wrapc(z, L2, g.bc[2], fac);
+            if (fac == 0.0f) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) o[c] = om[c] = omain[c] = 0.0f;
+                return;
+            }
+            const float c0 = TQ(sc, sl.qb, 0, ly, lx);
+            if (isnan(c0)) {
+                float tmp[9];
+                h_general(f, b, k, xx, yy, gz, __float_as_int(TQ(sc, sl.qb, 1, ly, lx)), tmp, tmp + 3, tmp + 6);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    o[c] = tmp[c] * fac;
+                    om[c] = tmp[3 + c] * fac;
+                    omain[c] = tmp[6 + c] * fac;
+                }
+                wa = true;
+                return;
+            }
+            const int ex = lx + 4, ey = ly + 1;
+            const float Ex = TE(sc, 0, ey, ex), Ey = TE(sc, 1, ey, ex), Ez = TE(sc, 2, ey, ex);
+            const float pl_[3] = {Ez - TE(sc, 2, ey - 1, ex), Ex - TE(sp, 0, ey, ex), Ey - TE(sc, 1, ey, ex - 1)};
+            const float mi_[3] = {TE(sp, 1, ey, ex) - Ey, TE(sc, 2, ey, ex - 1) - Ez, TE(sc, 0, ey - 1, ex) - Ex};
+            const bool split = split2d | p.pmask[s2 + gz];
+            if (!split) {
+                float W[3] = {pl_[0] + mi_[0], pl_[1] + mi_[1], pl_[2] + mi_[2]};
+                if (gz == p.s.iI[b]) {
+                    const int px = xx + L0 * yy;
+                    W[0] += fac * (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, true, 1, px));
+                    W[1] -= fac * (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, true, 0, px));
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    o[c] = fmaf(-1.0f * TQ(sc, sl.qb, c, ly, lx), W[c], TQ(sc, sl.qt, c, ly, lx));
+                    om[c] = 0.0f;
+                    omain[c] = o[c];
+                }
+            } else {
+                const int jx[3] = {xx, s1 + yy, s2 + gz};
+                const float *tA = p.tab, *tG = p.tab + S;
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const int i1 = jx[(c + 1) % 3], i2 = jx[(c + 2) % 3];
+                    const float bn = TQ(sc, sl.qb, c, ly, lx);
+                    const float Ap = tA[i1], Bp = -1.0f * bn * tG[i1];
+                    const float Am = tA[i2], Bm = -1.0f * bn * tG[i2];
+                    const float m = TQ(sc, sl.qm, c, ly, lx);
+                    const float pp = TQ(sc, sl.qt, c, ly, lx) - m;
+                    const float np = fmaf(Bp, pl_[c], Ap * pp);
+                    const float nm = fmaf(Bm, mi_[c], Am * m);
+                    o[c] = np + nm;
+                    om[c] = nm;
+                    omain[c] = np + nm;
+                }
+                wa = true;
+            }
+        };
+
+        bool ok = true;
+        if (tid == 0) {
+            issue(z0 - 1);
+            for (int d = 0; d < DEPTH; d++)
+                if (z0 + d <= z1) issue(z0 + d);
+        }
+        for (int z = z0; z <= z1; z++) {
+            if (tid == 0 && z + DEPTH <= z1) issue(z + DEPTH);
+            /* wait for plane z (and, on the first plane, the pre-plane z0-1) */
+            const int sc = (z + NS) % NS;
+            bool arrived = true;
+            if (z == z0) {
+                arrived = mbar_wait(&bars[(z0 - 1 + NS) % NS], 0);
+                if (arrived) patch(z0 - 1);
+            }
+            if (arrived) arrived = mbar_wait(&bars[sc], (unsigned)(((z - (z0 - 1)) / NS) & 1));
+            if (arrived) patch(z);
+            ok = __syncthreads_and(arrived) != 0; /* one decision for the whole CTA */
+            if (!ok) {
+                if (tid == 0) atomicExch(ft.err, 1);
+                /* let the copies still in flight land (bounded) before leaving */
+                for (int zz = z + 1; zz <= min(z + DEPTH, z1); zz++)
+                    mbar_wait(&bars[(zz + NS) % NS], (unsigned)(((zz - (z0 - 1)) / NS) & 1));
+                break;
+            }
+
+            const int hs = (z - z0) % NSH;
+            if (own) {
+                float o[3], om[3], omain[3];
+                bool wa;
+                h_update(z, tx, ty, gx, gy, 1.0f, own_split2d, o, om, omain, wa);
+#pragma unroll
+                for (int c = 0; c < 3; c++) HN(hs, c, ty, tx) = o[c];
+                if (z < z1) {
+                    const long long gi = own2d + pl * z;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) Hn[c * n3 + gi] = o[c];
+                    if (wa) {
+#pragma unroll
+                        for (int c = 0; c < 3; c++) Han[c * n3 + gi] = om[c];
+                    }
+                    const int q = mon_index(p.d, z);
+                    if (q >= 0) {
+                        ring_ptr(p.d, g.pl, b, k, q, 0)[own2d] = omain[0];
+                        ring_ptr(p.d, g.pl, b, k, q, 1)[own2d] = omain[1];
+                    }
+                }
+            }
+            if (hlx >= 0 && z < z1) {
+                float o[3], om[3], omain[3];
+                bool wa;
+                h_update(z, hlx, hly, hxx, hyy, hfac, hsplit2d, o, om, omain, wa);
+#pragma unroll
+                for (int c = 0; c < 3; c++) HN(hs, c, hly, hlx) = o[c];
+            }
+            __syncthreads();
+
+            if (z > z0 && own) {
+                const int zp = z - 1;
+                const int hp = (zp - z0) % NSH;
+                const int se = (zp + NS) % NS;
+                const float Hx = HN(hp, 0, ty, tx), Hy = HN(hp, 1, ty, tx), Hz = HN(hp, 2, ty, tx);
+                const float pl_[3] = {HN(hp, 2, ty + 1, tx) - Hz, HN(hs, 0, ty, tx) - Hx, HN(hp, 1, ty, tx + 1) - Hy};
+                const float mi_[3] = {Hy - HN(hs, 1, ty, tx), Hz - HN(hp, 2, ty, tx + 1), Hx - HN(hp, 0, ty + 1, tx)};
+                const float e0[3] = {TE(se, 0, ty + 1, tx + 4), TE(se, 1, ty + 1, tx + 4), TE(se, 2, ty + 1, tx + 4)};
+                const long long gi = own2d + pl * zp;
+                const float c0 = TB(se, sl.be, 0);
+                float eo[3], eom[3], emain[3];
+                bool done = true, wa = false;
+                if (!isnan(c0)) {
+                    const bool split = own_split2d | p.pmask[s2 + zp];
+                    if (!split) {
+                        float W[3] = {pl_[0] + mi_[0], pl_[1] + mi_[1], pl_[2] + mi_[2]};
+                        if (zp == p.s.iI[b]) {
+                            W[0] += (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, false, 1, own2d));
+                            W[1] -= (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, false, 0, own2d));
+                        }
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            eo[c] = fmaf(1.0f * TB(se, sl.be, c), W[c], e0[c]);
+                            emain[c] = eo[c];
+                        }
+                    } else {
+                        const int jx[3] = {gx, s1 + gy, s2 + zp};
+                        const float *tA = p.tab + 2 * S, *tG = p.tab + 3 * S;
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            const int i1 = jx[(c + 1) % 3], i2 = jx[(c + 2) % 3];
+                            const float bn = TB(se, sl.be, c);
+                            const float Ap = tA[i1], Bp = 1.0f * bn * tG[i1];
+                            const float Am = tA[i2], Bm = 1.0f * bn * tG[i2];
+                            const float m = TB(se, sl.bm, c);
+                            const float pp = e0[c] - m;
+                            const float np = fmaf(Bp, pl_[c], Ap * pp);
+                            const float nm = fmaf(Bm, mi_[c], Am * m);
+                            eo[c] = np + nm;
+                            eom[c] = nm;
+                            emain[c] = np + nm;
+                        }
+                        wa = true;
+                    }
+                } else {
+                    const int ridx = __float_as_int(TB(se, sl.be, 1));
+                    if (p.erec[ridx].kind == RK_STABLE) {
+                        done = false;
+                    } else {
+                        float tmp[18];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            tmp[c] = pl_[c];
+                            tmp[3 + c] = mi_[c];
+                            tmp[6 + c] = e0[c];
+                        }
+                        e_general(f, b, k, gx, gy, zp, ridx, tmp, tmp + 3, tmp + 6, tmp + 9, tmp + 12, tmp + 15);
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            eo[c] = tmp[9 + c];
+                            eom[c] = tmp[12 + c];
+                            emain[c] = tmp[15 + c];
+                        }
+                        wa = true;
+                    }
+                }
+                if (done) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) En[c * n3 + gi] = eo[c];
+                    if (wa) {
+#pragma unroll
+                        for (int c = 0; c < 3; c++) Ean[c * n3 + gi] = eom[c];
+                    }
+                    const int q = mon_index(p.d, zp);
+                    if (q >= 0) {
+                        ring_ptr(p.d, g.pl, b, k, q, 2)[own2d] = emain[0];
+                        ring_ptr(p.d, g.pl, b, k, q, 3)[own2d] = emain[1];
+                    }
+                }
+            }
+        }
+        if (!ok) return; /* every thread of the CTA saw the same timeout */
+        __syncthreads();
+    }
+#undef TE
+#undef TQ
+#undef TB
+#undef HN
+}
+
+size_t fused32t_smem(int ty, int ns) { return sizeof(float) * (32 + (size_t)ns * tslot(ty).size + (size_t)NSH * 3 * (ty + 1) * SHX); }
+
+static void *fused_t_kernel(int ns)
+{
+    switch (ns) {
+    case 4: return (void *)k_fused32t<4>;
+    case 5: return (void *)k_fused32t<5>;
+    default: return (void *)k_fused32t<6>;
+    }
+}
+
+int fused32t_max_ctas_per_sm(int ty, int ns)
+{
+    int n = 0;
+    const size_t sm = fused32t_smem(ty, ns);
+    cudaFuncSetAttribute(fused_t_kernel(ns), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fused_t_kernel(ns), TX * ty, sm) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+void launch_fused32t(const Fused32T &ft, int rel, int grid, cudaStream_t st)
+{
+    dim3 blk(TX, ft.f.ty, 1);
+    const size_t sm = fused32t_smem(ft.f.ty, ft.f.ns);
+    if (ft.f.ns == 4) k_fused32t<4><<<grid, blk, sm, st>>>(ft, rel);
+    else if (ft.f.ns == 5) k_fused32t<5><<<grid, blk, sm, st>>>(ft, rel);
+    else k_fused32t<6><<<grid, blk, sm, st>>>(ft, rel);
+    if (ft.f.nstable > 0) {
+        dim3 g2((ft.f.nstable + 127) / 128, ft.f.p.batch);
+        k_fix_stable32<<<g2, 128, 0, st>>>(ft.f, rel);
     }
 }
 

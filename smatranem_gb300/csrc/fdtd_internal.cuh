@@ -27,6 +27,7 @@
 #define SMATRAN_FDTD_INTERNAL_CUH
 
 #include <cstdint>
+#include <cuda.h>
 
 namespace smat {
 
@@ -110,6 +111,14 @@ struct Fused32 {
     int nstable;
 };
 
+/* the fused step with TMA staging: tensor maps of the current ("old") field set
+ * and of the coefficient streams, and the pipeline error flag */
+struct Fused32T {
+    Fused32 f;
+    CUtensorMap mE, mH, mEa, mHa, mBh, mBe;
+    int *err;
+};
+
 /* launchers (one translation unit per precision) */
 void launch_h64(const P64 &p, int rel, cudaStream_t st);
 void launch_e64(const P64 &p, int rel, cudaStream_t st);
@@ -121,6 +130,9 @@ void launch_h32v(const P32 &p, int rel, int by, const int *gcells, int ngh, cuda
 void launch_e32v(const P32 &p, int rel, int by, const int *gcells, int nge, cudaStream_t st);
 void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);
 size_t fused32_smem(int ty, int ns);
+void launch_fused32t(const Fused32T &f, int rel, int grid, cudaStream_t st);
+size_t fused32t_smem(int ty, int ns);
+int fused32t_max_ctas_per_sm(int ty, int ns);
 int fused32_max_ctas_per_sm(int ty, int ns);
 void launch_bump(int *base, int by, cudaStream_t st);
 void launch_set(int *base, int value, cudaStream_t st);

@@ -7,6 +7,8 @@
  * main :146-167) and its per-step main_calc (:242-329); the host precompute
  * in host_precompute.c replaces main :62-143.
  */
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -108,6 +110,10 @@ struct smat_fdtd_plan {
      * two vectorised sweeps (2, needs L0 % 4 == 0) */
     int fused = 1, ty = 8, zc = 40, ns = 5, ctas_per_sm = 0;
     int max_ctas = -1; /* cached occupancy of the current configuration */
+    /* TMA tensor maps (kernel 3), built for tile rows tma_ty: [set][E, H, Ea, Ha], bh, be */
+    CUtensorMap tmap[2][4], tmap_bh, tmap_be;
+    int tma_ty = -1;
+    int *d_err = nullptr; /* device pipeline error flag */
     int by32 = 8;
 
     /* graphs: a chunk of GRAPH_STEPS steps, position independent via d_base */
@@ -242,9 +248,76 @@ int sm_count()
     return n;
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+/* a 4-D map (x, y, z, component-block) of one [w][L2][L1][L0] float array */
+int encode_map(CUtensorMap *m, const float *base, const int L[4], int nw, int bx, int by)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
+    if (!enc) return smat_fail(SMAT_ECUDA, "cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[4] = {(cuuint64_t)L[0], (cuuint64_t)L[1], (cuuint64_t)L[2], (cuuint64_t)nw};
+    const cuuint64_t strides[3] = {(cuuint64_t)L[0] * 4, (cuuint64_t)L[0] * L[1] * 4,
+                                   (cuuint64_t)L[0] * L[1] * L[2] * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)bx, (cuuint32_t)by, 1, 3};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void *)base, dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return smat_fail(SMAT_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return SMAT_OK;
+}
+
+int build_tmaps(smat_fdtd_plan *p)
+{
+    if (p->tma_ty == p->ty) return SMAT_OK;
+    const int ty = p->ty, nw = 3 * p->batch;
+    float *sets[2][4] = {{p->d_E32, p->d_H32, p->d_Ea32, p->d_Ha32}, {p->d_E32b, p->d_H32b, p->d_Ea32b, p->d_Ha32b}};
+    int rc = SMAT_OK;
+    for (int st = 0; st < 2 && !rc; st++) {
+        rc = encode_map(&p->tmap[st][0], sets[st][0], p->L, nw, 40, ty + 2);          /* E tile + halo */
+        if (!rc) rc = encode_map(&p->tmap[st][1], sets[st][1], p->L, nw, 36, ty + 1); /* H + halo col/row */
+        if (!rc) rc = encode_map(&p->tmap[st][2], sets[st][2], p->L, nw, 32, ty);     /* E aux, tile */
+        if (!rc) rc = encode_map(&p->tmap[st][3], sets[st][3], p->L, nw, 36, ty + 1); /* H aux + halo */
+    }
+    if (!rc) rc = encode_map(&p->tmap_bh, p->d_bh, p->L, 3, 36, ty + 1);
+    if (!rc) rc = encode_map(&p->tmap_be, p->d_be, p->L, 3, 32, ty);
+    if (!rc) p->tma_ty = ty;
+    return rc;
+}
+
+Fused32T make_fused_t(const smat_fdtd_plan *p, bool xp)
+{
+    Fused32T ft;
+    ft.f = make_fused(p, xp);
+    const int st = p->cur;
+    ft.mE = p->tmap[st][0];
+    ft.mH = p->tmap[st][1];
+    ft.mEa = p->tmap[st][2];
+    ft.mHa = p->tmap[st][3];
+    ft.mBh = p->tmap_bh;
+    ft.mBe = p->tmap_be;
+    ft.err = p->d_err;
+    return ft;
+}
+
 int fused_grid(smat_fdtd_plan *p, const Fused32 &f)
 {
-    if (p->max_ctas < 0) p->max_ctas = fused32_max_ctas_per_sm(p->ty, p->ns);
+    if (p->max_ctas < 0)
+        p->max_ctas = p->fused == 3 ? fused32t_max_ctas_per_sm(p->ty, p->ns) : fused32_max_ctas_per_sm(p->ty, p->ns);
     const int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm : (p->max_ctas > 0 ? p->max_ctas : 1);
     const long long g = (long long)per_sm * sm_count();
     return (int)(g < f.nitems ? g : f.nitems);
@@ -264,6 +337,13 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
         for (int i = 0; i < n; i++) {
             const Fused32 f = make_fused(p, xp);
             launch_fused32(f, rel0 + i, fused_grid(p, f), p->stream);
+            p->cur ^= 1;
+        }
+        launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
+    } else if (p->fused == 3) {
+        for (int i = 0; i < n; i++) {
+            const Fused32T ft = make_fused_t(p, xp);
+            launch_fused32t(ft, rel0 + i, fused_grid(p, ft.f), p->stream);
             p->cur ^= 1;
         }
         launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
@@ -409,6 +489,7 @@ int common_alloc(smat_fdtd_plan *p)
     if ((rc = p->alloc(&p->d_xphase32, 4))) return rc;
     if ((rc = p->alloc(&p->d_scratch, 4))) return rc;
     if ((rc = p->alloc(&p->d_iI, p->batch)) || (rc = p->alloc(&p->d_isgn, p->batch))) return rc;
+    if ((rc = p->alloc(&p->d_err, 1))) return rc;
     {
         const int m = p->iBTIin[3];
         std::vector<int> ii(p->batch, p->iBTIin[2]);
@@ -959,7 +1040,7 @@ extern "C" int smat_fdtd_run(smat_fdtd_plan *p, int k_begin, int k_end)
     if (k_end > p->nsched) return smat_fail(SMAT_EINVAL, "run: k_end %d beyond the %d-step schedule", k_end, p->nsched);
     launch_set(p->d_base, k_begin, p->stream);
     int n = k_end - k_begin;
-    if (p->precision == SMAT_FP32 && p->fused && p->cur != 0 && n >= GRAPH_STEPS + 1) {
+    if (p->precision == SMAT_FP32 && (p->fused == 1 || p->fused == 3) && p->cur != 0 && n >= GRAPH_STEPS + 1) {
         /* graphs are captured from field set 0: take one step to get there */
         enqueue_steps(p, 0, 1, false);
         launch_bump(p->d_base, 1, p->stream);
@@ -1004,6 +1085,10 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
             const Fused32 f = make_fused(p, false);
             launch_fused32(f, i, fused_grid(p, f), p->stream);
             p->cur ^= 1;
+        } else if (p->fused == 3) {
+            const Fused32T ft = make_fused_t(p, false);
+            launch_fused32t(ft, i, fused_grid(p, ft.f), p->stream);
+            p->cur ^= 1;
         } else if (p->fused == 2) launch_h32v(q32, i, p->by32, p->d_hgen, p->nhgen, p->stream);
         else launch_h32(q32, i, p->by32, p->stream);
         CK(cudaEventRecord(ev[1], p->stream));
@@ -1037,14 +1122,16 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
 {
     smat_clear_error();
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
-    if (fused < 0 || fused > 2) return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps)");
+    if (fused < 0 || fused > 3)
+        return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps), 3 (fused, TMA)");
+    if (fused == 3 && p->L[0] % 4 != 0) return smat_fail(SMAT_EINVAL, "set_tuning: the TMA kernel needs L0 %% 4 == 0");
     if (fused == 2 && (p->L[0] % 4 != 0 || tile_y < 1 || tile_y > 4))
         return smat_fail(SMAT_EINVAL, "set_tuning: vector sweeps need L0 %% 4 == 0 and tile_y in 1..4");
-    if (fused == 1) {
+    if (fused == 1 || fused == 3) {
         if (tile_y < 2 || tile_y > 8 || z_chunk < 1 || ctas_per_sm < 0 || slots < 4 || slots > 6)
             return smat_fail(SMAT_EINVAL,
                              "set_tuning: tile_y in 2..8, z_chunk >= 1, ctas_per_sm >= 0, slots in 4..6");
-        const int mx = fused32_max_ctas_per_sm(tile_y, slots);
+        const int mx = fused == 3 ? fused32t_max_ctas_per_sm(tile_y, slots) : fused32_max_ctas_per_sm(tile_y, slots);
         if (mx < 1 || ctas_per_sm > mx)
             return smat_fail(SMAT_EINVAL, "set_tuning: %d CTAs per SM do not fit (max %d)", ctas_per_sm, mx);
         p->ty = tile_y;
@@ -1052,6 +1139,11 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         p->ns = slots;
         p->ctas_per_sm = ctas_per_sm;
         p->max_ctas = mx;
+        if (fused == 3) {
+            p->fused = 3;
+            int rc = build_tmaps(p);
+            if (rc) return rc;
+        }
     } else {
         if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
         p->by32 = tile_y;
@@ -1093,16 +1185,28 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
             }
     cands.push_back({0, 4, 1, 0, 4});
     cands.push_back({0, 8, 1, 0, 4});
-    if (p->L[0] % 4 == 0)
+    if (p->L[0] % 4 == 0) {
         for (int by : {1, 2, 4}) cands.push_back({2, by, 1, 0, 4});
+        for (int ty : {2, 4, 8})
+            for (int ns : {4, 5, 6})
+                for (int zc : {16, 32, 64, 1 << 20}) {
+                    const int z = zc > L2 ? L2 : zc;
+                    bool dup = false;
+                    for (auto &c : cands) dup |= c.fused == 3 && c.ty == ty && c.ns == ns && c.zc == z;
+                    if (!dup && fused32t_max_ctas_per_sm(ty, ns) >= 1) cands.push_back({3, ty, z, 0, ns});
+                }
+    }
     const int nq = p->nq;
     p->nq = 0;
     CK(cudaMemsetAsync(p->d_iI, 0xff, sizeof(int) * p->batch, p->stream));
-    const int save[5] = {p->fused, p->fused == 1 ? p->ty : p->by32, p->zc, p->ctas_per_sm, p->ns};
+    const int save[5] = {p->fused, (p->fused == 1 || p->fused == 3) ? p->ty : p->by32, p->zc, p->ctas_per_sm, p->ns};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     double bms = 1e30;
+    /* SMATRAN_AUTOTUNE_VERBOSE=1 prints every candidate's time to stderr */
+    const char *vs = getenv("SMATRAN_AUTOTUNE_VERBOSE");
+    const bool verbose = vs && vs[0] && vs[0] != '0';
     Cand bc = {save[0], save[1], save[2], save[3], save[4]};
     for (const Cand &c : cands) {
         if (smat_fdtd_set_tuning(p, c.fused, c.ty, c.zc, c.ctas, c.ns) != SMAT_OK) continue;
@@ -1114,6 +1218,9 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
         CK(cudaEventSynchronize(e1));
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (verbose)
+            fprintf(stderr, "autotune: kernel %d tile_y %d z_chunk %d slots %d: %.4f ms/step\n", c.fused, c.ty, c.zc,
+                    c.ns, ms / nsteps);
         if (ms < bms) {
             bms = ms;
             bc = c;
@@ -1131,11 +1238,26 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
     return SMAT_OK;
 }
 
+extern "C" int smat_device_info(char *name, int name_len, int *sm_count, int *cc)
+{
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    cudaDeviceProp pr;
+    CK(cudaGetDeviceProperties(&pr, dev));
+    if (name && name_len > 0) {
+        strncpy(name, pr.name, name_len - 1);
+        name[name_len - 1] = '\0';
+    }
+    if (sm_count) *sm_count = pr.multiProcessorCount;
+    if (cc) *cc = pr.major * 10 + pr.minor;
+    return SMAT_OK;
+}
+
 extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
 {
     if (!p || !out) return smat_fail(SMAT_EINVAL, "get_tuning: bad arguments");
     out[0] = p->fused;
-    out[1] = p->fused == 1 ? p->ty : p->by32;
+    out[1] = (p->fused == 1 || p->fused == 3) ? p->ty : p->by32;
     out[2] = p->zc;
     out[3] = p->ctas_per_sm;
     out[4] = p->ns;
@@ -1146,6 +1268,14 @@ extern "C" int smat_fdtd_sync(smat_fdtd_plan *p)
 {
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
     CK(cudaStreamSynchronize(p->stream));
+    if (p->d_err) {
+        int err = 0;
+        CK(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) {
+            CK(cudaMemset(p->d_err, 0, sizeof(int)));
+            return smat_fail(SMAT_ECUDA, "fused pipeline: a staged plane did not arrive (timed out)");
+        }
+    }
     return SMAT_OK;
 }
 

@@ -13,6 +13,7 @@ cannot be loaded; there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 
 import numpy as np
@@ -73,6 +74,7 @@ def lib():
         L.smat_fdtd_time_kernels.argtypes = [_P, C.c_int, C.c_int, _P]
         L.smat_fdtd_set_tuning.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.smat_fdtd_get_tuning.argtypes = [_P, _P]
+        L.smat_device_info.argtypes = [_P, C.c_int, _P, _P]
         L.smat_fdtd_autotune.argtypes = [_P, C.c_int, _P, _P]
         L.smat_fdtd_overlap.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P]
         L.smat_fdtd_dft_count.argtypes = [_P, _P, _P]
@@ -166,6 +168,25 @@ def main_calc(L, Ah, Bh, Ae, Be, iBc, H_t, E_t, iBTIin, Hi, Ei, ExpN2, HB, EB, H
 
 
 # -- plans ------------------------------------------------------------------
+
+TUNING_CACHE = os.environ.get("SMATRAN_TUNING_CACHE", os.path.join(_HERE, "_build", "tuning_cache.json"))
+
+
+def _load_cache():
+    try:
+        with open(TUNING_CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def device_info():
+    """(name, SM count, compute capability) of the current CUDA device."""
+    name = C.create_string_buffer(128)
+    sms, cc = C.c_int(0), C.c_int(0)
+    _check(lib().smat_device_info(name, 128, C.byref(sms), C.byref(cc)))
+    return name.value.decode(), sms.value, cc.value
+
 
 class Plan:
     """A structure and its excitations resident on the GPU (smat_fdtd_* API)."""
@@ -293,10 +314,31 @@ class Plan:
     def set_tuning(self, fused=1, tile_y=8, z_chunk=40, ctas_per_sm=0, slots=5):
         _check(lib().smat_fdtd_set_tuning(self._h, fused, tile_y, z_chunk, ctas_per_sm, slots))
 
-    def autotune(self, nsteps=4):
+    def autotune(self, nsteps=4, cache=True):
+        """Pick the fastest FP32 configuration (smat_fdtd_autotune).  With cache,
+        the choice is remembered per (grid, batch, precision, GPU model, SM
+        count) in TUNING_CACHE and reused without timing."""
+        key = None
+        if cache:
+            key = json.dumps([list(self.L), self.batch, self.precision, *device_info()])
+            entry = _load_cache().get(key)
+            if entry:
+                try:
+                    self.set_tuning(*entry["tuning"])
+                    return tuple(entry["tuning"]), entry["ms"]
+                except FdtdError:
+                    pass
         best = (C.c_int * 5)()
         ms = C.c_double(0)
         _check(lib().smat_fdtd_autotune(self._h, nsteps, best, C.byref(ms)))
+        if key is not None:
+            c = _load_cache()
+            c[key] = {"tuning": list(best), "ms": ms.value}
+            try:
+                with open(TUNING_CACHE, "w") as f:
+                    json.dump(c, f, indent=1)
+            except OSError:
+                pass
         return tuple(best), ms.value
 
     def get_tuning(self):

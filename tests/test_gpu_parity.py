@@ -352,7 +352,8 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     pr = W.prepare(s)
     nsteps = 9 if kw.get("metals") else 37
     ref = _run_fp32(s, pr, iBTIin, (0, 4, 1, 0, 4), nsteps)
-    tunings = TUNINGS + ([(2, 1, 1, 0, 4), (2, 2, 1, 0, 4), (2, 4, 1, 0, 4)] if L[0] % 4 == 0 else [])
+    tunings = TUNINGS + ([(2, 1, 1, 0, 4), (2, 2, 1, 0, 4), (2, 4, 1, 0, 4), (3, 8, 40, 0, 5), (3, 4, 5, 0, 4),
+                          (3, 2, 3, 1, 6), (3, 4, 1, 0, 5), (3, 8, 7, 1, 6)] if L[0] % 4 == 0 else [])
     for tuning in tunings:
         got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
         for rb, gb in zip(ref, got):
@@ -392,7 +393,7 @@ def test_autotune_keeps_state_and_results(built):
     pr = W.prepare(s)
     with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
                        precision=f.FP32) as p:
-        best, ms = p.autotune(2)
+        best, ms = p.autotune(2, cache=False)
         assert ms > 0 and p.get_tuning() == best
         ok, mx = p.check_finite()
         assert ok and mx == 0.0
