@@ -52,6 +52,15 @@ WORKLOAD = ("bend 256x192x160 curvilinear (R=2um, Si strip in SiO2), 12-cell spl
             "batch 8 = 2 ports x 4 modes, Gaussian pulse, FP64 DFT at 21 wavelengths on 2 port planes")
 
 
+def launches_per_step(tuning, L2):
+    """Update-kernel launches of one step: one fused launch (kernels 1, 3), or
+    an H and an E sweep per z-chunk (kernels 0, 2; z_chunk 0 = one chunk)."""
+    if tuning[0] in (1, 3):
+        return 1
+    zc = tuning[2]
+    return 2 * (1 if zc <= 0 or zc >= L2 else math.ceil(L2 / zc))
+
+
 def algorithmic_bytes_per_step(n3, n_split, batch, s_f=4, coef_bytes=24):
     """Compulsory HBM traffic of one step: every field component read and
     written once per excitation (12*s_f per cell), the per-cell coefficients
@@ -303,10 +312,11 @@ def run_ours(args):
     # per-kernel launch times for the roofline (same stream, CUDA events)
     kt = p32.time_kernels(args.warmup + args.steps, 64)
     tuning = p32.get_tuning()
-    per_step = 1 if tuning[0] in (1, 3) else 2
+    per_step = launches_per_step(tuning, bend.s.L[2])
     bytes_step = algorithmic_bytes_per_step(n3, n_split, batch)
-    launch_ms = (kt[0] + kt[1]) / per_step
-    achieved = (bytes_step / per_step) / (launch_ms * 1e-3) / 1e9
+    step_kernel_ms = kt[0] + kt[1]  # the update kernels of one step (DFT flush apart)
+    launch_ms = step_kernel_ms / per_step
+    achieved = bytes_step / (step_kernel_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     launches = per_step * args.steps + 2 * math.ceil(args.steps / 32) + 1
     # ---- full runs: S-matrix columns/s and the FP32-vs-FP64 S error -----
@@ -374,12 +384,15 @@ def run_ours(args):
                                                           f"{t_e2e:.2f} s"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None,
-                     "kernel": {1: "k_fused32 (one fused H+E launch per step)", 2: "k_sweep32v (H, E; float4)",
+                     "kernel": {1: "k_fused32 (one fused H+E launch per step)",
+                                2: "k_sweep32v (H, E; float4)" + (f", z-chunks of {tuning[2]} planes"
+                                                                   if 0 < tuning[2] < bend.s.L[2] else ""),
                                 3: "k_fused32t (one fused H+E launch per step, TMA-staged planes)",
                                 0: "k_sweep32 (H, E)"}[tuning[0]],
                      "tuning": {"kernel": tuning[0], "tile_y": tuning[1], "z_chunk": tuning[2],
                                 "ctas_per_sm": tuning[3], "slots": tuning[4]},
                      "bytes_per_launch": bytes_step / per_step, "ms_per_launch": launch_ms,
+                     "launches_per_step": per_step, "ms_per_step_kernels": step_kernel_ms,
                      "ms_dft_flush_per_step": kt[2]},
         "fp64_plain": {"value": fp64_rate, "unit": "Gcell-updates/s", "steps": args.steps64,
                        "s_cols_per_s": 1.0 / t_full64, "full_run_s": t_full64},

@@ -237,6 +237,27 @@ int smat_overlap_noalloc(int npix, int ncols, int nvec, long long vec_stride, co
 int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const double *tilXi_host,
                       double *S_host);
 
+/* Adjoint gradient. ----------------------------------------------------------
+ * No counterpart in the reference (it has no gradient).  The objective is
+ *   J = sum_b |S_b|^2,  S_b = sum_r conj(t_r) x_r,  x = (HB_x, HB_y, -EB_y, EB_x)
+ * of excitation b's DFT at frequency f on DFT plane slot q (the S_calc
+ * projection, S_calc :437-445, of one mode column t = tilXi_col, 4*L0*L1
+ * complex, rows in that order).  The call runs the plan's schedule from rest
+ * (fields and DFT zeroed) for nsteps steps with a checkpoint every K steps,
+ * then runs the discrete adjoint backwards, recomputing each K-step segment
+ * from its checkpoint.  Returns J and, for each cell i of the box
+ * [box[0],box[1]) x [box[2],box[3]) x [box[4],box[5]) (x fastest),
+ *   grad[i]      = dJ/ds_i, where s_i scales the cell's permittivity,
+ *                  epsi -> epsi * (1 + s_i) on all three components
+ *                  (so dJ/d eps_r = grad / eps_r for epsi = eps_r * metric),
+ *   grad_c[c][i] = the same per E component (optional, may be NULL).
+ * Design cells must be ordinary ('n') cells and the plan must hold no
+ * stable-form (metal) cells.  Afterwards the DFT holds the forward result and
+ * the fields are those of the first checkpoint segment.  Device memory: one
+ * state copy per checkpoint (ceil(nsteps/K) copies) plus four field arrays. */
+int smat_fdtd_adjoint_grad(smat_fdtd_plan *plan, int nsteps, int K, int f, int q, const double *tilXi_col,
+                           const int box[6], double *grad, double *grad_c, double *J);
+
 /* The FDTD input deck and the drop-in program. ------------------------------
  * A deck is what the reference FDTD reads (main :44-99): input.txt (keys
  * Prefix, BoundaryCondition, ModeP, FDTD; input_file0 :759-781, plus the

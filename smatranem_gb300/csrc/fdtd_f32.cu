@@ -98,13 +98,13 @@ __device__ __forceinline__ float *ring_at(const Dft &d, int pl, int b, int k, in
 /* One sweep.  EF = false: H from E (backward curls, sign -); EF = true: E from
  * H (forward curls, sign +; the stable form uses backward curls, :310). */
 template <bool EF>
-__global__ void __launch_bounds__(256) k_sweep32(const P32 p, const int rel)
+__global__ void __launch_bounds__(256) k_sweep32(const P32 p, const int rel, const int z0)
 {
     /* blockIdx.y = row block * batch + excitation: the blocks of one tile for
      * all excitations launch together and share the coefficient lines in L2 */
     const int b = blockIdx.y % p.batch;
     const int j0 = blockIdx.x * 32 + threadIdx.x, j1 = (blockIdx.y / p.batch) * blockDim.y + threadIdx.y;
-    const int j2 = blockIdx.z;
+    const int j2 = z0 + blockIdx.z;
     const Geo &g = p.g;
     if (j0 >= g.L0 || j1 >= g.L1) return;
     const long long n3 = g.n3, l = j0 + (long long)g.L0 * (j1 + (long long)g.L1 * j2);
@@ -253,14 +253,21 @@ __device__ __forceinline__ void set_el(float4 &v, int i, float x)
 }
 __device__ __forceinline__ float4 scale4(float4 v, float f) { return make_float4(f * v.x, f * v.y, f * v.z, f * v.w); }
 
-template <bool EF>
-__global__ void __launch_bounds__(128, 5) k_sweep32v(const P32 p, const int rel)
+/* loads of the other field: CG = true reads through L2 only (ld.global.cg),
+ * for data another CTA of the same launch may have written */
+template <bool CG> __device__ __forceinline__ float4 ldG4(const float *p)
 {
-    const int b = blockIdx.y % p.batch;
+    return CG ? __ldcg(reinterpret_cast<const float4 *>(p)) : *reinterpret_cast<const float4 *>(p);
+}
+template <bool CG> __device__ __forceinline__ float ldG(const float *p) { return CG ? __ldcg(p) : *p; }
+
+/* one quad row segment: cells x = xr..xr+3 of row j1, plane j2, excitation b;
+ * a warp covers 128 consecutive x-cells (lane = threadIdx.x) */
+template <bool EF, bool CG>
+__device__ __forceinline__ void sweep32v_quad(const P32 &p, const int rel, const int b, const int j1, const int j2,
+                                              const int xr)
+{
     const Geo &g = p.g;
-    const int xr = (blockIdx.x * 32 + threadIdx.x) * 4;
-    const int j1 = (blockIdx.y / p.batch) * blockDim.y + threadIdx.y;
-    const int j2 = blockIdx.z;
     if (j1 >= g.L1) return; /* uniform per warp */
     const bool live = xr < g.L0;
     const int x0 = live ? xr : g.L0 - 4; /* idle lanes load valid data, store nothing */
@@ -286,33 +293,33 @@ __global__ void __launch_bounds__(128, 5) k_sweep32v(const P32 p, const int rel)
     for (int i = 0; i < 3; i++) {
         c[i] = ld4(cf + i * n3 + l);
         out[i] = ld4(F + i * n3 + l);
-        gh[i] = ld4(G + i * n3 + l);
+        gh[i] = ldG4<CG>(G + i * n3 + l);
     }
     /* H sweep: Ex, Ez at y-1; Ex, Ey at z-1.  E sweep: Hx, Hz at y+1; Hx, Hy at z+1. */
-    const float4 gy0 = scale4(ld4(G + 0 * n3 + l + oy), fy), gy2 = scale4(ld4(G + 2 * n3 + l + oy), fy);
-    const float4 gz0 = scale4(ld4(G + 0 * n3 + l + oz), fz), gz1 = scale4(ld4(G + 1 * n3 + l + oz), fz);
+    const float4 gy0 = scale4(ldG4<CG>(G + 0 * n3 + l + oy), fy), gy2 = scale4(ldG4<CG>(G + 2 * n3 + l + oy), fy);
+    const float4 gz0 = scale4(ldG4<CG>(G + 0 * n3 + l + oz), fz), gz1 = scale4(ldG4<CG>(G + 1 * n3 + l + oz), fz);
     /* x neighbours: H sweep needs Ey, Ez at x-1; E sweep Hy, Hz at x+1 */
     const unsigned full = 0xffffffffu;
     float xn1, xn2; /* component 1, 2 of the outer neighbour of the quad */
     if (!EF) {
         xn1 = __shfl_up_sync(full, gh[1].w, 1);
         xn2 = __shfl_up_sync(full, gh[2].w, 1);
-        if (threadIdx.x == 0 || x0 == 0) {
+        if ((threadIdx.x & 31) == 0 || x0 == 0) {
             const bool edge = x0 == 0;
             const long long o = edge ? g.L0 - 1 : -1;
             const float f = edge ? (float)g.bc[0] : 1.0f;
-            xn1 = f * G[1 * n3 + l + o];
-            xn2 = f * G[2 * n3 + l + o];
+            xn1 = f * ldG<CG>(G + 1 * n3 + l + o);
+            xn2 = f * ldG<CG>(G + 2 * n3 + l + o);
         }
     } else {
         xn1 = __shfl_down_sync(full, gh[1].x, 1);
         xn2 = __shfl_down_sync(full, gh[2].x, 1);
-        if (threadIdx.x == 31 || x0 + 4 == g.L0) {
+        if ((threadIdx.x & 31) == 31 || x0 + 4 == g.L0) {
             const bool edge = x0 + 4 == g.L0;
             const long long o = edge ? -(g.L0 - 4) : 4;
             const float f = edge ? (float)g.bc[0] : 1.0f;
-            xn1 = f * G[1 * n3 + l + o];
-            xn2 = f * G[2 * n3 + l + o];
+            xn1 = f * ldG<CG>(G + 1 * n3 + l + o);
+            xn2 = f * ldG<CG>(G + 2 * n3 + l + o);
         }
     }
     if (!live) return;
@@ -435,17 +442,22 @@ __global__ void __launch_bounds__(128, 5) k_sweep32v(const P32 p, const int rel)
     }
 }
 
+template <bool EF>
+__global__ void __launch_bounds__(128, 5) k_sweep32v(const P32 p, const int rel, const int z0)
+{
+    const int b = blockIdx.y % p.batch;
+    const int xr = (blockIdx.x * 32 + threadIdx.x) * 4;
+    const int j1 = (blockIdx.y / p.batch) * blockDim.y + threadIdx.y;
+    sweep32v_quad<EF, false>(p, rel, b, j1, z0 + blockIdx.z, xr);
+}
+
 /* general cells of the vectorised sweeps: one thread per record cell, run
  * after k_sweep32v of the same field (the quads skipped them) */
-template <bool EF>
-__global__ void k_general32(const P32 p, const int rel, const int *cells, int ncells)
+template <bool EF, bool CG>
+__device__ void general32_cell(const P32 &p, const int rel, const int b, const long long l)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int b = blockIdx.y;
-    if (i >= ncells) return;
     const Geo &g = p.g;
     const long long n3 = g.n3, bs = 3 * n3;
-    const long long l = cells[i];
     const int j0 = (int)(l % g.L0), j1 = (int)((l / g.L0) % g.L1), j2 = (int)(l / g.pl);
     const float *__restrict__ cf = EF ? p.be : p.bh;
     float *F = (EF ? p.E : p.H) + b * bs, *Fa = (EF ? p.Ea : p.Ha) + b * bs;
@@ -461,7 +473,7 @@ __global__ void k_general32(const P32 p, const int rel, const int *cells, int nc
     if (r.kind == RK_FROZEN) {
         for (int c = 0; c < 3; c++) main_out[c] = F[c * n3 + l] - Fa[c * n3 + l];
     } else if (stable) {
-        auto get = [&](int c, long long o) { return G[c * n3 + l + o] - Ga[c * n3 + l + o]; };
+        auto get = [&](int c, long long o) { return ldG<CG>(G + c * n3 + l + o) - ldG<CG>(Ga + c * n3 + l + o); };
         float pl[3], mi[3];
         curl32<false>(get, st, pl, mi);
         for (int c = 0; c < 3; c++) {
@@ -476,7 +488,7 @@ __global__ void k_general32(const P32 p, const int rel, const int *cells, int nc
             Fa[c * n3 + l] = x;
         }
     } else {
-        auto get = [&](int c, long long o) { return G[c * n3 + l + o]; };
+        auto get = [&](int c, long long o) { return ldG<CG>(G + c * n3 + l + o); };
         float pl[3], mi[3];
         curl32<EF>(get, st, pl, mi);
         if (r.kind == RK_N) {
@@ -506,6 +518,158 @@ __global__ void k_general32(const P32 p, const int rel, const int *cells, int nc
         ring_at(p.d, g.pl, b, k, q, EF ? 2 : 0)[px] = main_out[0];
         ring_at(p.d, g.pl, b, k, q, EF ? 3 : 1)[px] = main_out[1];
     }
+}
+
+template <bool EF>
+__global__ void k_general32(const P32 p, const int rel, const int *cells, int ncells)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncells) return;
+    general32_cell<EF, false>(p, rel, blockIdx.y, cells[i]);
+}
+
+/* ---------------------------------------------------------------------------
+ * Pipelined sweeps (kernel 4).  The same quad and general-cell updates as
+ * k_sweep32v / k_general32 (so the same bits), but H and E of one step run in
+ * one launch, ordered plane by plane: the E sweep of plane z runs right after
+ * the H sweep of plane z+1, while the old E of plane z (read by both H sweeps
+ * around it) and the new H of planes z, z+1 are still in L2.  HBM then sees
+ * each field read once and written once per step, as in a fused kernel, with
+ * the sweeps' access pattern and occupancy.
+ *
+ * The E sweep of plane z runs D planes behind the H sweep (after H(z+D)), so
+ * that what it waits for was issued a group or more earlier.
+ *
+ * Items are assigned statically (item i to CTA i mod grid, in increasing i)
+ * and every wait is on an H item of an earlier group, so with all CTAs
+ * resident (a cooperative launch) the earliest unfinished item can always
+ * proceed.  Waits are bounded: after ~2^22 polls the CTA records error 2 and
+ * goes on (results are then invalid, the launch still ends).
+ * ------------------------------------------------------------------------- */
+__device__ __forceinline__ int ld_acquire_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool wait_epoch(const int *flag, int ep)
+{
+    for (int it = 0; it < (1 << 22); it++) {
+        if (ld_acquire_gpu(flag) - ep >= 0) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
+/* out of line: general cells are rare and must not cost the quads registers */
+__device__ __noinline__ void pipe_general(const P32 &p, int rel, int b, long long l, bool efield)
+{
+    if (efield) general32_cell<true, true>(p, rel, b, l);
+    else general32_cell<false, false>(p, rel, b, l);
+}
+
+__global__ void __launch_bounds__(128, 4) k_pipe32v(const P32 p, const int rel, const Pipe32 pp)
+{
+    const Geo &g = p.g;
+    const int ep = ld_acquire_gpu(&pp.ctl[0]) + 1;
+    const int per_group = pp.nyb * p.batch;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    const int D = pp.lag;
+    const int L2 = g.L2;
+    auto hflag = [&](int z, int yb, int b) { return pp.hflag + ((long long)z * pp.nyb + yb) * p.batch + b; };
+    for (int item = blockIdx.x; item < pp.nitems; item += gridDim.x) {
+        const int grp = item / per_group, r = item % per_group;
+        const int b = r % p.batch, yb = r / p.batch;
+        /* groups: H(0..D-1), then H(t), E(t-D) for t = D..L2-1, then E(L2-D..L2-1) */
+        bool efield;
+        int z;
+        if (grp < D) {
+            efield = false;
+            z = grp;
+        } else if (grp < 2 * L2 - D) {
+            const int u = grp - D, t = D + u / 2;
+            efield = u & 1;
+            z = efield ? t - D : t;
+        } else {
+            efield = true;
+            z = grp - L2;
+        }
+        if (efield) {
+            if (tid == 0) {
+                const int zn = z + 1 == L2 ? 0 : z + 1, yn = yb + 1 == pp.nyb ? 0 : yb + 1;
+                bool ok = wait_epoch(hflag(z, yb, b), ep) && wait_epoch(hflag(z, yn, b), ep) &&
+                          wait_epoch(hflag(zn, yb, b), ep);
+                if (ok && pp.wait_back) {
+                    /* stable-form E cells read the new H of their backward
+                     * neighbours; plans that wrap z with such cells are not
+                     * pipelined, so plane 0 has no z-1 dependence */
+                    const int yp = yb == 0 ? pp.nyb - 1 : yb - 1;
+                    ok = (z == 0 || wait_epoch(hflag(z - 1, yb, b), ep)) && wait_epoch(hflag(z, yp, b), ep);
+                }
+                if (!ok) atomicExch(pp.err, 2);
+            }
+            __syncthreads();
+        }
+        const int j1 = yb * pp.by + threadIdx.y;
+        for (int xb = 0; xb * 4 * (int)blockDim.x < g.L0; xb++) {
+            const int xr = (xb * blockDim.x + threadIdx.x) * 4;
+            if (efield) sweep32v_quad<true, true>(p, rel, b, j1, z, xr);
+            else sweep32v_quad<false, false>(p, rel, b, j1, z, xr);
+        }
+        const int *grow = efield ? pp.egen_row : pp.hgen_row;
+        const int g0 = grow[z * pp.nyb + yb], g1 = grow[z * pp.nyb + yb + 1];
+        if (g1 > g0) {
+            __syncthreads(); /* the quads stored placeholders for these cells */
+            const int *gl = efield ? pp.egen : pp.hgen;
+            for (int i = g0 + tid; i < g1; i += nthr) pipe_general(p, rel, b, gl[i], efield);
+        }
+        __syncthreads();
+        if (!efield && tid == 0) {
+            __threadfence();
+            st_release_gpu(hflag(z, yb, b), ep);
+        }
+    }
+    /* the last CTA out publishes the epoch for the next launch */
+    if (tid == 0) {
+        __threadfence();
+        const int n = atomicAdd(&pp.ctl[1], 1);
+        if (n == (int)gridDim.x - 1) {
+            pp.ctl[1] = 0;
+            __threadfence();
+            atomicAdd(&pp.ctl[0], 1);
+        }
+    }
+}
+
+int pipe32v_max_ctas_per_sm(int threads)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pipe32v, threads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(pp.nxw, pp.by);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_pipe32v, p, rel, pp);
 }
 
 /* Fold `count` ring slots ending at step *base + rel_end into the FP64 DFT
@@ -548,29 +712,31 @@ __global__ void k_flush32(const P32 p, const int rel_end, const int count)
     }
 }
 
-void launch_h32(const P32 &p, int rel, int by, cudaStream_t st)
+/* Sweeps over the planes z0 <= z < z1 (the whole grid: 0, L2). */
+void launch_h32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st)
 {
-    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
-    k_sweep32<false><<<grd, blk, 0, st>>>(p, rel);
+    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, z1 - z0);
+    k_sweep32<false><<<grd, blk, 0, st>>>(p, rel, z0);
 }
 
-void launch_e32(const P32 &p, int rel, int by, cudaStream_t st)
+void launch_e32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st)
 {
-    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
-    k_sweep32<true><<<grd, blk, 0, st>>>(p, rel);
+    dim3 blk(32, by, 1), grd((p.g.L0 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, z1 - z0);
+    k_sweep32<true><<<grd, blk, 0, st>>>(p, rel, z0);
 }
 
-void launch_h32v(const P32 &p, int rel, int by, const int *gcells, int ngh, cudaStream_t st)
+/* gcells / ngh: the general cells of those planes */
+void launch_h32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int ngh, cudaStream_t st)
 {
-    dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
-    k_sweep32v<false><<<grd, blk, 0, st>>>(p, rel);
+    dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, z1 - z0);
+    k_sweep32v<false><<<grd, blk, 0, st>>>(p, rel, z0);
     if (ngh > 0) k_general32<false><<<dim3((ngh + 127) / 128, p.batch), 128, 0, st>>>(p, rel, gcells, ngh);
 }
 
-void launch_e32v(const P32 &p, int rel, int by, const int *gcells, int nge, cudaStream_t st)
+void launch_e32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int nge, cudaStream_t st)
 {
-    dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, p.g.L2);
-    k_sweep32v<true><<<grd, blk, 0, st>>>(p, rel);
+    dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, z1 - z0);
+    k_sweep32v<true><<<grd, blk, 0, st>>>(p, rel, z0);
     if (nge > 0) k_general32<true><<<dim3((nge + 127) / 128, p.batch), 128, 0, st>>>(p, rel, gcells, nge);
 }
 

@@ -101,6 +101,23 @@ struct P32 {
     Dft d;
 };
 
+/* Pipelined sweeps (kernel 4): one cooperative launch per step.  Items are
+ * (plane z, block of `by` rows, excitation b) of the H sweep or the E sweep in
+ * the order H(0..D-1), H(D), E(0), H(D+1), E(1), ..., E(L2-1); an E
+ * item waits until the H items it reads (and whose E inputs it overwrites)
+ * have finished, through per-item flags stamped with a launch epoch. */
+struct Pipe32 {
+    int by, nyb, nitems;
+    int nxw;                        /* threads along x (a multiple of 32): four cells each */
+    int lag;                        /* D: E(z) runs after H(z+D), 1 <= D <= L2 */
+    int *hflag;                     /* [L2][nyb][batch]: epoch of the finished H item */
+    int *ctl;                       /* [0] epoch of the last finished launch, [1] exit count */
+    int *err;                       /* set to 2 when a wait gives up */
+    const int *hgen, *egen;         /* general (record) cells, cell order */
+    const int *hgen_row, *egen_row; /* [L2*nyb + 1]: first general cell of item (z, yb) */
+    int wait_back;                  /* E items also wait for H(z-1), H(z, yb-1) (stable-form E cells) */
+};
+
 /* the fused FP32 step: reads the field set in p, writes the other set */
 struct Fused32 {
     P32 p;
@@ -123,11 +140,13 @@ struct Fused32T {
 void launch_h64(const P64 &p, int rel, cudaStream_t st);
 void launch_e64(const P64 &p, int rel, cudaStream_t st);
 void launch_dft64(const P64 &p, int rel, cudaStream_t st);
-void launch_h32(const P32 &p, int rel, int by, cudaStream_t st);
-void launch_e32(const P32 &p, int rel, int by, cudaStream_t st);
+void launch_h32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st);
+void launch_e32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st);
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
-void launch_h32v(const P32 &p, int rel, int by, const int *gcells, int ngh, cudaStream_t st);
-void launch_e32v(const P32 &p, int rel, int by, const int *gcells, int nge, cudaStream_t st);
+void launch_h32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int ngh, cudaStream_t st);
+void launch_e32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int nge, cudaStream_t st);
+void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStream_t st);
+int pipe32v_max_ctas_per_sm(int threads);
 void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);
 size_t fused32_smem(int ty, int ns);
 void launch_fused32t(const Fused32T &f, int rel, int grid, cudaStream_t st);

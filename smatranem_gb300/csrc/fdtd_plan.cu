@@ -14,126 +14,17 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
-#include "fdtd_internal.cuh"
-#include "host_internal.h"
-#include "smatran_fdtd.h"
+#include "plan_internal.cuh"
 
 using namespace smat;
+using namespace smat::plan;
 
-namespace {
-
-constexpr int GRAPH_STEPS = 32; /* steps per captured graph (= FP32 ring length) */
-constexpr int RING_K = 32;
-
-int cuda_fail(cudaError_t e, const char *what)
-{
-    return smat_fail(SMAT_ECUDA, "%s: %s", what, cudaGetErrorString(e));
-}
-
-#define CK(call)                                                                                                       \
-    do {                                                                                                               \
-        cudaError_t e_ = (call);                                                                                       \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call);                                                            \
-    } while (0)
-
-/* zero-filled device allocation, ordered on stream st */
-template <class T> int dalloc(T **p, size_t n, cudaStream_t st)
-{
-    *p = nullptr;
-    if (n == 0) return SMAT_OK;
-    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
-    if (e != cudaSuccess) {
-        *p = nullptr;
-        cudaGetLastError();
-        return smat_fail(SMAT_ENOMEM, "cudaMalloc of %zu bytes: %s", n * sizeof(T), cudaGetErrorString(e));
-    }
-    e = cudaMemsetAsync(*p, 0, n * sizeof(T), st);
-    if (e != cudaSuccess) return smat_fail(SMAT_ECUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
-    return SMAT_OK;
-}
-
-} // namespace
-
-struct smat_fdtd_plan {
-    int L[4], iBc[3], iBTIin[4];
-    int precision, batch, lnotn;
-    long long n3;
-    int pl;
-    double invtau_R = 0, invtau_I = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    long long dev_bytes = 0;
-    std::vector<char> cont;    /* host copy of the cell classes */
-    std::vector<int> addr;     /* host copy of address_notn */
-
-    /* common device state */
-    int *d_base = nullptr;
-    double *d_inc = nullptr;   /* [batch][8*pl] */
-    double *d_xsrc = nullptr;  /* explicit sheet planes */
-    double *d_xphase = nullptr;
-    float *d_xphase32 = nullptr;
-    double *d_sched = nullptr; /* [nsched][6] */
-    int nsched = 0;
-    double *d_phase = nullptr; /* [nsched][nfreq][4] */
-    float *d_phase32 = nullptr;
-    double *d_acc = nullptr;   /* [batch][nfreq][nq][4][pl] complex */
-    float *d_ring = nullptr;
-    int nfreq = 0, nq = 0, planes[MAX_PLANES] = {0};
-    bool ref_dft = false;      /* DFT slot 0 on planes (iB, iT) is the reference one */
-    bool ref_planes_ok = false; /* no PML cell on iB, iT (else the reference exits, :320) */
-    double *d_scratch = nullptr;
-    int *d_iI = nullptr;      /* [batch] source plane per excitation */
-    std::vector<int> h_iI;    /* host copy */
-    double *d_isgn = nullptr; /* [batch] its sign */
-
-    /* FP64 */
-    uint8_t *d_flags = nullptr;
-    int *d_addr = nullptr;
-    double *d_cm = nullptr, *d_ca = nullptr;
-    double *d_H64 = nullptr, *d_E64 = nullptr, *d_Ha64 = nullptr, *d_Ea64 = nullptr;
-
-    /* FP32 */
-    float *d_bh = nullptr, *d_be = nullptr, *d_tab = nullptr;
-    uint8_t *d_pmask = nullptr;
-    Rec32 *d_hrec = nullptr, *d_erec = nullptr;
-    float *d_H32 = nullptr, *d_E32 = nullptr, *d_Ha32 = nullptr, *d_Ea32 = nullptr;
-    float *d_H32b = nullptr, *d_E32b = nullptr, *d_Ha32b = nullptr, *d_Ea32b = nullptr; /* second set */
-    int cur = 0;          /* FP32: which field set holds the current state */
-    int *d_stable = nullptr;
-    int nstable = 0;
-    int *d_hgen = nullptr, *d_egen = nullptr; /* record (general) cells of each sweep */
-    int nhgen = 0, negen = 0;
-    /* FP32 launch configuration (autotuned): fused z-march (1), two sweeps (0),
-     * two vectorised sweeps (2, needs L0 % 4 == 0) */
-    int fused = 1, ty = 8, zc = 40, ns = 5, ctas_per_sm = 0;
-    int max_ctas = -1; /* cached occupancy of the current configuration */
-    /* TMA tensor maps (kernel 3), built for tile rows tma_ty: [set][E, H, Ea, Ha], bh, be */
-    CUtensorMap tmap[2][4], tmap_bh, tmap_be;
-    int tma_ty = -1;
-    int *d_err = nullptr; /* device pipeline error flag */
-    int by32 = 8;
-
-    /* graphs: a chunk of GRAPH_STEPS steps, position independent via d_base */
-    cudaGraphExec_t graph = nullptr;
-    bool graph_failed = false;
-
-    std::vector<void *> allocations;
-
-    template <class T> int alloc(T **p, size_t n)
-    {
-        int rc = dalloc(p, n, stream);
-        if (rc == SMAT_OK && *p) {
-            allocations.push_back((void *)*p);
-            dev_bytes += (long long)(n * sizeof(T));
-        }
-        return rc;
-    }
-};
-
-namespace {
+namespace smat {
+namespace plan {
 
 Geo make_geo(const smat_fdtd_plan *p)
 {
@@ -347,20 +238,106 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
             p->cur ^= 1;
         }
         launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
-    } else if (p->fused == 2) {
+    } else if (p->fused == 4) {
         const P32 q = make_p32(p, xp);
-        for (int i = 0; i < n; i++) {
-            launch_h32v(q, rel0 + i, p->by32, p->d_hgen, p->nhgen, p->stream);
-            launch_e32v(q, rel0 + i, p->by32, p->d_egen, p->negen, p->stream);
-        }
+        const Pipe32 pp = make_pipe(p);
+        for (int i = 0; i < n; i++) launch_pipe32v(q, rel0 + i, pp, p->pipe_grid, p->stream);
         launch_flush32(q, rel0 + n, n, p->stream);
     } else {
         const P32 q = make_p32(p, xp);
-        for (int i = 0; i < n; i++) {
-            launch_h32(q, rel0 + i, p->by32, p->stream);
-            launch_e32(q, rel0 + i, p->by32, p->stream);
-        }
+        for (int i = 0; i < n; i++) sweep_step(p, q, rel0 + i);
         launch_flush32(q, rel0 + n, n, p->stream);
+    }
+}
+
+Pipe32 make_pipe(const smat_fdtd_plan *p)
+{
+    Pipe32 pp;
+    pp.by = p->pipe_by;
+    pp.nyb = (p->L[1] + p->pipe_by - 1) / p->pipe_by;
+    pp.nitems = 2 * p->L[2] * pp.nyb * p->batch;
+    pp.hflag = p->d_hflag;
+    pp.ctl = p->d_pipe_ctl;
+    pp.err = p->d_err;
+    pp.hgen = p->d_hgen;
+    pp.egen = p->d_egen;
+    pp.hgen_row = p->d_hgen_row;
+    pp.egen_row = p->d_egen_row;
+    pp.wait_back = p->nstable > 0;
+    pp.nxw = p->pipe_nxw;
+    pp.lag = p->pipe_lag;
+    return pp;
+}
+
+/* x-threads of a pipelined item: the whole row at four cells a thread, up to 128 */
+int pipe_nxw(int L0)
+{
+    const int t = ((L0 / 4 + 31) / 32) * 32;
+    return t < 128 ? t : 128;
+}
+
+/* kernel 4 for `by` rows per item: flags, per-item general-cell offsets, grid */
+int setup_pipe(smat_fdtd_plan *p, int by, int lag)
+{
+    int rc;
+    const int L1 = p->L[1], L2 = p->L[2];
+    if (!p->d_hflag) {
+        if ((rc = p->alloc(&p->d_hflag, (size_t)L2 * L1 * p->batch))) return rc;
+        if ((rc = p->alloc(&p->d_pipe_ctl, 2))) return rc;
+        if ((rc = p->alloc(&p->d_hgen_row, (size_t)L2 * L1 + 1))) return rc;
+        if ((rc = p->alloc(&p->d_egen_row, (size_t)L2 * L1 + 1))) return rc;
+    }
+    const int nyb = (L1 + by - 1) / by;
+    for (int side = 0; side < 2; side++) {
+        const std::vector<int> &gl = side ? p->egen_host : p->hgen_host;
+        std::vector<int> rows((size_t)L2 * nyb + 1);
+        for (int z = 0; z < L2; z++)
+            for (int yb = 0; yb < nyb; yb++) {
+                const long long first = (long long)z * p->pl + (long long)yb * by * p->L[0];
+                rows[(size_t)z * nyb + yb] = (int)(std::lower_bound(gl.begin(), gl.end(), first) - gl.begin());
+            }
+        rows[(size_t)L2 * nyb] = (int)gl.size();
+        CK(cudaMemcpyAsync(side ? p->d_egen_row : p->d_hgen_row, rows.data(), rows.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, p->stream));
+    }
+    CK(cudaStreamSynchronize(p->stream));
+    const int nxw = pipe_nxw(p->L[0]);
+    const int per_sm = pipe32v_max_ctas_per_sm(nxw * by);
+    if (per_sm < 1) return smat_fail(SMAT_ECUDA, "pipelined sweeps: no resident CTA of %d x %d threads", nxw, by);
+    const int want = p->ctas_per_sm > 0 && p->ctas_per_sm < per_sm ? p->ctas_per_sm : per_sm;
+    const long long nitems = 2LL * L2 * nyb * p->batch;
+    const long long grid = (long long)want * sm_count();
+    p->pipe_grid = (int)(grid < nitems ? grid : nitems);
+    p->pipe_by = by;
+    p->pipe_lag = lag;
+    p->pipe_nxw = nxw;
+    return SMAT_OK;
+}
+
+/* One FP32 step as two sweeps (kernels 0 and 2), in z-chunks of szc planes:
+ * H on planes [z0, z1), then E on [z0-1, z1-1) -- E of a plane needs H_new of
+ * the plane above, H of a plane needs E_old of the plane below, and both
+ * still hold at every chunk boundary.  A chunk small enough to stay in L2
+ * lets the E sweep read E_old and H_new from L2 rather than HBM. */
+void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel)
+{
+    const int L2 = p->L[2];
+    /* a stable-form E cell at z = 0 reads the new H of plane L2-1 through a
+     * wrapped z boundary: such plans sweep the whole grid at once */
+    const bool whole = p->szc <= 0 || p->szc >= L2 || (p->nstable > 0 && p->iBc[2] != 0);
+    const int zc = whole ? L2 : p->szc;
+    for (int z0 = 0; z0 < L2; z0 += zc) {
+        const int z1 = z0 + zc < L2 ? z0 + zc : L2;
+        const int e0 = z0 == 0 ? 0 : z0 - 1, e1 = z1 == L2 ? L2 : z1 - 1;
+        if (p->fused == 2) {
+            launch_h32v(q, rel, p->by32, z0, z1, p->d_hgen + p->hgen_z[z0], p->hgen_z[z1] - p->hgen_z[z0], p->stream);
+            if (e1 > e0)
+                launch_e32v(q, rel, p->by32, e0, e1, p->d_egen + p->egen_z[e0], p->egen_z[e1] - p->egen_z[e0],
+                            p->stream);
+        } else {
+            launch_h32(q, rel, p->by32, z0, z1, p->stream);
+            if (e1 > e0) launch_e32(q, rel, p->by32, e0, e1, p->stream);
+        }
     }
 }
 
@@ -683,6 +660,15 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
     }
     p->nhgen = (int)hgen.size();
     p->negen = (int)egen.size();
+    p->hgen_host = hgen;
+    p->egen_host = egen;
+    p->hgen_z.assign(p->L[2] + 1, 0);
+    p->egen_z.assign(p->L[2] + 1, 0);
+    for (int z = 0; z <= p->L[2]; z++) {
+        const long long first = (long long)z * p->pl;
+        p->hgen_z[z] = (int)(std::lower_bound(hgen.begin(), hgen.end(), first) - hgen.begin());
+        p->egen_z[z] = (int)(std::lower_bound(egen.begin(), egen.end(), first) - egen.begin());
+    }
     if ((rc = p->alloc(&p->d_hgen, hgen.size() + 1)) || (rc = p->alloc(&p->d_egen, egen.size() + 1))) return rc;
     if (!hgen.empty())
         CK(cudaMemcpyAsync(p->d_hgen, hgen.data(), hgen.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
@@ -723,7 +709,8 @@ int finish_create(smat_fdtd_plan *p, int rc, smat_fdtd_plan **out)
     return SMAT_OK;
 }
 
-} // namespace
+} // namespace plan
+} // namespace smat
 
 /* ===================================================================== */
 
@@ -1089,12 +1076,20 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
             const Fused32T ft = make_fused_t(p, false);
             launch_fused32t(ft, i, fused_grid(p, ft.f), p->stream);
             p->cur ^= 1;
-        } else if (p->fused == 2) launch_h32v(q32, i, p->by32, p->d_hgen, p->nhgen, p->stream);
-        else launch_h32(q32, i, p->by32, p->stream);
+        } else if (p->fused == 4) {
+            launch_pipe32v(q32, i, make_pipe(p), p->pipe_grid, p->stream);
+        } else if (p->szc > 0 && p->szc < p->L[2]) {
+            sweep_step(p, q32, i); /* chunked sweeps: the whole step in ms[0] */
+        } else if (p->fused == 2) {
+            launch_h32v(q32, i, p->by32, 0, p->L[2], p->d_hgen, p->nhgen, p->stream);
+        } else {
+            launch_h32(q32, i, p->by32, 0, p->L[2], p->stream);
+        }
         CK(cudaEventRecord(ev[1], p->stream));
         if (p->precision == SMAT_FP64) launch_e64(q64, i, p->stream);
-        else if (p->fused == 2) launch_e32v(q32, i, p->by32, p->d_egen, p->negen, p->stream);
-        else if (p->fused == 0) launch_e32(q32, i, p->by32, p->stream);
+        else if (p->fused == 4 || (p->szc > 0 && p->szc < p->L[2])) {
+        } else if (p->fused == 2) launch_e32v(q32, i, p->by32, 0, p->L[2], p->d_egen, p->negen, p->stream);
+        else if (p->fused == 0) launch_e32(q32, i, p->by32, 0, p->L[2], p->stream);
         CK(cudaEventRecord(ev[2], p->stream));
         if (p->precision == SMAT_FP64) launch_dft64(q64, i, p->stream);
         else if ((i + 1) % RING_K == 0 || i + 1 == nsteps) {
@@ -1122,8 +1117,26 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
 {
     smat_clear_error();
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
-    if (fused < 0 || fused > 3)
-        return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps), 3 (fused, TMA)");
+    if (fused < 0 || fused > 4)
+        return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps), 3 (fused, TMA), "
+                                      "4 (pipelined vector sweeps)");
+    if (fused == 4) {
+        const int lag = z_chunk < 1 ? 1 : z_chunk;
+        if (p->L[0] % 4 != 0 || tile_y < 1 || pipe_nxw(p->L[0]) * tile_y > 128 || ctas_per_sm < 0 ||
+            lag > p->L[2])
+            return smat_fail(SMAT_EINVAL, "set_tuning: pipelined sweeps need L0 %% 4 == 0, tile_y rows of at most "
+                                          "128 threads (%d per row) and a lag (z_chunk) of 1..L2",
+                             pipe_nxw(p->L[0]));
+        if (p->nstable > 0 && p->iBc[2] != 0)
+            return smat_fail(SMAT_EINVAL, "set_tuning: pipelined sweeps cannot order stable-form E cells across a "
+                                          "wrapped z boundary");
+        p->ctas_per_sm = ctas_per_sm;
+        int rc = setup_pipe(p, tile_y, lag);
+        if (rc) return rc;
+        p->fused = 4;
+        drop_graph(p);
+        return SMAT_OK;
+    }
     if (fused == 3 && p->L[0] % 4 != 0) return smat_fail(SMAT_EINVAL, "set_tuning: the TMA kernel needs L0 %% 4 == 0");
     if (fused == 2 && (p->L[0] % 4 != 0 || tile_y < 1 || tile_y > 4))
         return smat_fail(SMAT_EINVAL, "set_tuning: vector sweeps need L0 %% 4 == 0 and tile_y in 1..4");
@@ -1146,7 +1159,9 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         }
     } else {
         if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
+        if (z_chunk < 0) return smat_fail(SMAT_EINVAL, "set_tuning: z_chunk >= 0 (0: whole grid per sweep)");
         p->by32 = tile_y;
+        p->szc = z_chunk >= p->L[2] ? 0 : z_chunk;
     }
     p->fused = fused;
     drop_graph(p);
@@ -1175,31 +1190,32 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
     };
     std::vector<Cand> cands;
     const int L2 = p->L[2];
-    for (int ty : {4, 8})
-        for (int ns : {4, 5, 6})
-            for (int zc : {16, 32, 64, 1 << 20}) {
-                const int z = zc > L2 ? L2 : zc;
-                bool dup = false;
-                for (auto &c : cands) dup |= c.fused && c.ty == ty && c.ns == ns && c.zc == z;
-                if (!dup && fused32_max_ctas_per_sm(ty, ns) >= 1) cands.push_back({1, ty, z, 0, ns});
-            }
-    cands.push_back({0, 4, 1, 0, 4});
-    cands.push_back({0, 8, 1, 0, 4});
+    /* sweeps, whole grid or z-chunked (chunk sizes that leave L2 a useful share) */
+    const int chunks[] = {0, 2, 4, 8, 16};
     if (p->L[0] % 4 == 0) {
-        for (int by : {1, 2, 4}) cands.push_back({2, by, 1, 0, 4});
-        for (int ty : {2, 4, 8})
-            for (int ns : {4, 5, 6})
-                for (int zc : {16, 32, 64, 1 << 20}) {
-                    const int z = zc > L2 ? L2 : zc;
-                    bool dup = false;
-                    for (auto &c : cands) dup |= c.fused == 3 && c.ty == ty && c.ns == ns && c.zc == z;
-                    if (!dup && fused32t_max_ctas_per_sm(ty, ns) >= 1) cands.push_back({3, ty, z, 0, ns});
-                }
+        for (int by : {1, 2})
+            for (int zc : chunks)
+                if (zc < L2) cands.push_back({2, by, zc, 0, 4});
+        cands.push_back({2, 4, 0, 0, 4});
+    }
+    if (p->L[0] % 4 == 0 && !(p->nstable > 0 && p->iBc[2] != 0))
+        for (int by : {1, 2, 4})
+            for (int lag : {1, 2, 4})
+                if (pipe_nxw(p->L[0]) * by <= 128 && lag <= L2) cands.push_back({4, by, lag, 0, 0});
+    cands.push_back({0, 4, 0, 0, 4});
+    cands.push_back({0, 8, 0, 0, 4});
+    cands.push_back({0, 4, 4 < L2 ? 4 : 0, 0, 4});
+    /* fused z-march: a few representative shapes */
+    for (int ns : {4, 5}) {
+        const int z = 32 > L2 ? L2 : 32;
+        if (fused32_max_ctas_per_sm(8, ns) >= 1) cands.push_back({1, 8, z, 0, ns});
+        if (p->L[0] % 4 == 0 && fused32t_max_ctas_per_sm(8, ns) >= 1) cands.push_back({3, 8, z, 0, ns});
     }
     const int nq = p->nq;
     p->nq = 0;
     CK(cudaMemsetAsync(p->d_iI, 0xff, sizeof(int) * p->batch, p->stream));
-    const int save[5] = {p->fused, (p->fused == 1 || p->fused == 3) ? p->ty : p->by32, p->zc, p->ctas_per_sm, p->ns};
+    int save[5];
+    smat_fdtd_get_tuning(p, save);
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -1257,8 +1273,8 @@ extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
 {
     if (!p || !out) return smat_fail(SMAT_EINVAL, "get_tuning: bad arguments");
     out[0] = p->fused;
-    out[1] = (p->fused == 1 || p->fused == 3) ? p->ty : p->by32;
-    out[2] = p->zc;
+    out[1] = (p->fused == 1 || p->fused == 3) ? p->ty : p->fused == 4 ? p->pipe_by : p->by32;
+    out[2] = (p->fused == 1 || p->fused == 3) ? p->zc : p->fused == 4 ? p->pipe_lag : p->szc;
     out[3] = p->ctas_per_sm;
     out[4] = p->ns;
     return SMAT_OK;
@@ -1273,7 +1289,8 @@ extern "C" int smat_fdtd_sync(smat_fdtd_plan *p)
         CK(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) {
             CK(cudaMemset(p->d_err, 0, sizeof(int)));
-            return smat_fail(SMAT_ECUDA, "fused pipeline: a staged plane did not arrive (timed out)");
+            return smat_fail(SMAT_ECUDA, err == 2 ? "pipelined sweeps: a wait for an H item timed out"
+                                                  : "fused pipeline: a staged plane did not arrive (timed out)");
         }
     }
     return SMAT_OK;

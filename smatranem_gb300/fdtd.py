@@ -80,6 +80,7 @@ def lib():
         L.smat_fdtd_dft_count.argtypes = [_P, _P, _P]
         L.smat_fdtd_dft_device.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P]
         L.smat_overlap.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, _P, _P, _P, _P]
+        L.smat_fdtd_adjoint_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -355,6 +356,22 @@ class Plan:
         S = np.zeros((nf.value, ncols), np.complex128)
         _check(lib().smat_fdtd_overlap(self._h, b, q, ncols, _ptr(t), _ptr(S)))
         return S
+
+    def adjoint_grad(self, nsteps, K, f, q, tilxi_col, box):
+        """J = sum_b |S_b|^2 of mode column tilxi_col (4*L0*L1 complex) on DFT
+        plane slot q at frequency f, and dJ/ds for every cell of box
+        (x0, x1, y0, y1, z0, z1), s scaling the cell's permittivity by (1 + s)
+        (smat_fdtd_adjoint_grad).  Returns (J, grad [nz, ny, nx], grad_c
+        [3, nz, ny, nx])."""
+        t = _c128(tilxi_col).reshape(-1)
+        bx = _i32(box)
+        shape = (int(bx[5] - bx[4]), int(bx[3] - bx[2]), int(bx[1] - bx[0]))
+        g = np.zeros(shape)
+        gc = np.zeros((3,) + shape)
+        J = C.c_double(0)
+        _check(lib().smat_fdtd_adjoint_grad(self._h, nsteps, K, f, q, _ptr(t), _ptr(bx), _ptr(g), _ptr(gc),
+                                            C.byref(J)))
+        return J.value, g, gc
 
     def check_finite(self):
         ok, m = C.c_int(0), C.c_double(0)

@@ -361,3 +361,118 @@ def overlap(dft_plane, Hinc, Einc):
     v = np.stack([dft_plane[0], dft_plane[1], -dft_plane[3], dft_plane[2]])
     m = np.concatenate([mh, me])
     return complex(np.sum(np.conj(m) * v))
+
+
+# ---------------------------------------------------------------------------
+# Inverse-design structure (the adjoint-gradient workload)
+# ---------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class Design(Bend):
+    box: tuple = (0, 0, 0, 0, 0, 0)   # design cells [x0, x1) x [y0, y1) x [z0, z1)
+    eps: np.ndarray | None = None     # their eps_r, (nz, ny, nx)
+    eps_base: np.ndarray | None = None  # stretched epsi of the whole grid, design cells at eps_r = 1
+
+    def with_eps(self, eps) -> Structure:
+        """The structure with design permittivities eps (nz, ny, nx); the
+        design box lies outside the PML, so a cell's stored epsi is eps_r times
+        the metric factor dx (held in eps_base)."""
+        x0, x1, y0, y1, z0, z1 = self.box
+        L0, L1 = self.s.L[0], self.s.L[1]
+        ep = self.eps_base.copy()
+        j = np.indices((z1 - z0, y1 - y0, x1 - x0)).reshape(3, -1)
+        cells = (x0 + j[2]) + L0 * ((y0 + j[1]) + L1 * (z0 + j[0]))
+        ep[cells, :] = self.eps_base[cells, :] * np.asarray(eps, dtype=np.float64).reshape(-1)[:, None]
+        return dataclasses.replace(self.s, epsi=ep)
+
+
+def design_structure(shape=(160, 160, 120), design=(60, 60, 20), pml=12, seed=0, core=(0.45, 0.22),
+                     eps_core=12.11, eps_clad=2.085, eps_range=(2.085, 12.11), dx_um=0.02, lam0_um=1.55,
+                     sq_ref=1e-12, power=3, pml_xy=True) -> Design:
+    """A straight silicon strip along z (two single-mode ports) through a
+    design region of seeded random permittivity, on a uniform grid of dx_um
+    cells (metric factor dx), split PML on all six faces (pml_xy=False: on the
+    z faces only, x/y walls with iBc = 0, so that the monitor planes hold no
+    PML cell and the reference's own DFT applies).  Source plane iI and
+    monitor planes iB (below the source) and iT (the output port, above the
+    design region)."""
+    L0, L1, L2 = shape
+    nx, ny, nz = design
+    dx = dx_um / INV_K0_UM
+    n3 = L0 * L1 * L2
+    u0 = (np.arange(L0) + 0.5 - 0.5 * L0) * dx_um
+    u1 = (np.arange(L1) + 0.5 - 0.5 * L1) * dx_um
+    j = np.indices((L2, L1, L0)).reshape(3, -1)[::-1]
+    in_core = (np.abs(u0[j[0]]) <= 0.5 * core[0]) & (np.abs(u1[j[1]]) <= 0.5 * core[1])
+    eps_r = np.where(in_core, eps_core, eps_clad)
+    x0, y0, z0 = (L0 - nx) // 2, (L1 - ny) // 2, (L2 - nz) // 2
+    box = (x0, x0 + nx, y0, y0 + ny, z0, z0 + nz)
+    in_box = (j[0] >= x0) & (j[0] < x0 + nx) & (j[1] >= y0) & (j[1] < y0 + ny) & (j[2] >= z0) & (j[2] < z0 + nz)
+    rng = np.random.default_rng(seed)
+    eps_d = rng.uniform(eps_range[0], eps_range[1], size=(nz, ny, nx))
+    eps_r = np.where(in_box, 1.0, eps_r)
+    # metric factor fx_c = H_{c+1} H_{c+2} / H_c = dx on a uniform grid
+    mu_r = np.full((n3, 3), dx)
+    eps3 = np.repeat(eps_r[:, None] * dx, 3, axis=1)
+    omega = 2 * math.pi * INV_K0_UM / lam0_um
+    sig = [pml_sigma(n, pml, pml, omega, pml * dx, pml * dx, sq_ref, power) if (a == 2 or pml_xy)
+           else np.zeros((2, n)) for a, n in enumerate((L0, L1, L2))]
+    mu_s, ep_s = stretch_media((L0, L1, L2), mu_r, eps3, sig)
+    eps_min = np.full((n3, 3), min(eps_clad, eps_range[0]) * dx)
+    min_dt = cfl_min_dt(mu_r, eps_min)
+    s = Structure(L=(L0, L1, L2, pml + 2), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=(0, 0, 0),
+                  name=f"design{L0}x{L1}x{L2}")
+    d = Design(s=s, iB=pml + 1, iT=L2 - pml - 2, iI=pml + 3, pml=pml, u0=u0, u1=u1, box=box, eps=eps_d,
+               eps_base=ep_s)
+    d.s = d.with_eps(eps_d)
+    return d
+
+
+def slab_structure(shape, seed=0, pml=12, slab_um=0.22, eps_slab=12.11, eps_clad=2.085,
+                   eps_range=(2.085, 12.11), n_incl=(1, 6), dx_um=0.02, lam0_um=1.55, sq_ref=1e-12,
+                   power=3) -> Bend:
+    """A silicon slab (normal to y) in SiO2 with 1-6 seeded cuboid inclusions of
+    random permittivity, on a uniform grid of dx_um cells, split PML on all six
+    faces.  Returned as a Bend-like record (source plane iI, monitor planes iB,
+    iT) so that mode_profiles() gives its port sheets."""
+    L0, L1, L2 = shape
+    dx = dx_um / INV_K0_UM
+    n3 = L0 * L1 * L2
+    rng = np.random.default_rng(seed)
+    u0 = (np.arange(L0) + 0.5 - 0.5 * L0) * dx_um
+    u1 = (np.arange(L1) + 0.5 - 0.5 * L1) * dx_um
+    j = np.indices((L2, L1, L0)).reshape(3, -1)[::-1]
+    eps_r = np.where(np.abs(u1[j[1]]) <= 0.5 * slab_um, eps_slab, eps_clad).astype(np.float64)
+    lo, hi = pml + 2, [n - pml - 2 for n in (L0, L1, L2)]
+    for _ in range(int(rng.integers(n_incl[0], n_incl[1] + 1))):
+        a = [int(rng.integers(lo, max(lo + 1, hi[d] - 8))) for d in range(3)]
+        b = [min(hi[d], a[d] + int(rng.integers(4, max(5, (hi[d] - lo) // 3)))) for d in range(3)]
+        inside = np.ones(n3, bool)
+        for d in range(3):
+            inside &= (j[d] >= a[d]) & (j[d] < b[d])
+        eps_r[inside] = rng.uniform(*eps_range)
+    mu_r = np.full((n3, 3), dx)
+    eps3 = np.repeat(eps_r[:, None] * dx, 3, axis=1)
+    omega = 2 * math.pi * INV_K0_UM / lam0_um
+    sig = [pml_sigma(n, pml, pml, omega, pml * dx, pml * dx, sq_ref, power) for n in (L0, L1, L2)]
+    mu_s, ep_s = stretch_media((L0, L1, L2), mu_r, eps3, sig)
+    min_dt = cfl_min_dt(mu_r, np.full((n3, 3), min(eps_clad, eps_range[0]) * dx))
+    s = Structure(L=(L0, L1, L2, pml + 2), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=(0, 0, 0),
+                  name=f"slab{L0}x{L1}x{L2}")
+    return Bend(s=s, iB=pml + 1, iT=L2 - pml - 2, iI=pml + 3, pml=pml, u0=u0, u1=u1)
+
+
+def slab_shapes(n=16, seed=0, lo=(128, 128, 128), hi=(256, 256, 192)):
+    """n seeded grid shapes from lo to hi (multiples of 8 in x, for the float4
+    sweeps): the uneven structures of the batched S-matrix workload."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        t = i / max(1, n - 1)
+        shp = []
+        for d in range(3):
+            v = lo[d] + t * (hi[d] - lo[d]) + rng.integers(-8, 9)
+            v = int(min(hi[d], max(lo[d], v)))
+            shp.append(v - v % 8)
+        out.append(tuple(shp))
+    return out

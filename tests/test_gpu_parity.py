@@ -342,8 +342,9 @@ def _run_fp32(s, pr, iBTIin, tuning, nsteps, batch=2, seed=0):
 
 @pytest.mark.parametrize("case", range(len(FUSED_CASES)))
 def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
-    """The fused z-marching launch reproduces the two-sweep FP32 kernels bit for
-    bit, for every tile shape, z chunk and grid size, across field-set swaps,
+    """The fused z-marching launches and the z-chunked sweeps reproduce the
+    two-sweep FP32 kernels bit for bit, for every tile shape, z chunk and grid
+    size, across field-set swaps,
     iBc = -1/0/1 wraps, PML on all faces, lossy/PEC/metal cells and per-excitation
     source planes."""
     from smatranem_gb300 import workloads as W
@@ -351,9 +352,15 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     s = W.random_structure(L, seed=seed, **kw)
     pr = W.prepare(s)
     nsteps = 9 if kw.get("metals") else 37
-    ref = _run_fp32(s, pr, iBTIin, (0, 4, 1, 0, 4), nsteps)
-    tunings = TUNINGS + ([(2, 1, 1, 0, 4), (2, 2, 1, 0, 4), (2, 4, 1, 0, 4), (3, 8, 40, 0, 5), (3, 4, 5, 0, 4),
-                          (3, 2, 3, 1, 6), (3, 4, 1, 0, 5), (3, 8, 7, 1, 6)] if L[0] % 4 == 0 else [])
+    ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
+    # z_chunk of the sweeps (kernels 0, 2): planes per H/E chunk, 0 = whole grid
+    tunings = TUNINGS + [(0, 4, 1, 0, 4), (0, 2, 3, 0, 4)]
+    if L[0] % 4 == 0:
+        tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (2, 4, 3, 0, 4), (2, 1, 5, 0, 4), (2, 2, 16, 0, 4),
+                    (3, 8, 40, 0, 5), (3, 4, 5, 0, 4), (3, 2, 3, 1, 6), (3, 4, 1, 0, 5), (3, 8, 7, 1, 6)]
+        if not (kw.get("metals") and kw["iBc"][2] != 0):  # pipelined sweeps (kernel 4)
+            # (4, rows per item, lag D, ctas_per_sm, -)
+            tunings += [(4, 1, 1, 0, 0), (4, 2, 2, 0, 0), (4, 1, 3, 1, 0), (4, 1, L[2], 0, 0)]
     for tuning in tunings:
         got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
         for rb, gb in zip(ref, got):
