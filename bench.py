@@ -427,8 +427,166 @@ def run_profile(args):
     p.close()
 
 
+# ---------------------------------------------------------------------------
+# the other configurations, one JSON summary line each (not the contract line)
+# ---------------------------------------------------------------------------
+
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def run_adjoint(args):
+    """Adjoint gradient workload: 160x160x120 cells, a 60x60x20 design region of
+    seeded eps_r in [2.085, 12.11] between two strip-waveguide ports, objective
+    |overlap of the output-port DFT at 1.55 um with TE0|^2, FP32 with a
+    checkpoint every 64 steps.  Checked against central differences (delta
+    eps_r = 1e-3) of the FP64 forward -- bit-identical to the reference loop --
+    on seeded cells, and against the FP64 adjoint."""
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    from smatranem_gb300.autograd import objective_and_grad
+    d = W.design_structure(shape=(160, 160, 120), design=(60, 60, 20), pml=12, seed=0)
+    pr = W.prepare(d.s, dt_factor=1.0 / 0.99)
+    nsteps, K = args.adj_steps, 64
+    src, ph = W.pulse_schedule(nsteps, pr.dt, lams_um=[1.55])
+    mode = W.mode_profiles(d, n_modes=1)[0]
+    kw = dict(nsteps=nsteps, K=K, mode=mode, src=src, phase=ph)
+    (J32, g32), t32 = _timed(lambda: objective_and_grad(d, d.eps, precision=F.FP32, **kw))
+    (J64, g64), t64 = _timed(lambda: objective_and_grad(d, d.eps, precision=F.FP64, **kw))
+    rng = np.random.default_rng(7)
+    flat = rng.choice(d.eps.size, size=args.fd_cells, replace=False)
+    cells = [np.unravel_index(i, d.eps.shape) for i in flat]
+
+    def objective(eps):
+        s = d.with_eps(eps)
+        prx = W.prepare(s, dt_factor=1.0 / 0.99)
+        p = F.Plan.create(s.L, s.iBc, (d.iB, d.iT, d.iI, 1), prx.invtau_R, prx.invtau_I, prx.mu, prx.epsi,
+                          prx.sigma, precision=F.FP64, batch=1)
+        with p:
+            p.set_incident(0, *mode)
+            p.set_schedule(src, planes=(d.iB, d.iT), phase=ph)
+            p.run(0, nsteps)
+            return abs(W.overlap(p.get_dft(0, 0, 1), *mode)) ** 2
+
+    t0 = time.perf_counter()
+    fd = []
+    for c in cells:
+        e = d.eps.copy()
+        e[c] += 1e-3
+        jp = objective(e)
+        e[c] -= 2e-3
+        fd.append((jp - objective(e)) / 2e-3)
+    t_fd = time.perf_counter() - t0
+    fd = np.array(fd)
+    a32 = np.array([g32[c] for c in cells])
+    a64 = np.array([g64[c] for c in cells])
+    fs = float(np.max(np.abs(fd)))
+    cells_total = d.s.n3 * nsteps
+    print(json.dumps({
+        "mode": "adjoint", "config": "design 160x160x120, 60x60x20 design cells, 12-cell PML on 6 faces, TE0 "
+                                     "output-port overlap at 1.55 um, Gaussian pulse",
+        "steps": nsteps, "checkpoint_every": K, "J_fp32": J32, "J_fp64": J64,
+        "adjoint_fp32_s": t32, "adjoint_fp64_s": t64,
+        "adjoint_fp32_gcell_per_s": 3 * cells_total / t32 / 1e9,
+        "fd_cells": int(args.fd_cells), "fd_s": t_fd,
+        "err_fp32_adjoint_vs_fd": float(np.max(np.abs(a32 - fd)) / fs),
+        "err_fp64_adjoint_vs_fd": float(np.max(np.abs(a64 - fd)) / fs),
+        "median_rel_err_fp32_vs_fd": float(np.median(np.abs(a32 - fd) / np.maximum(np.abs(fd), 1e-300))),
+        "err_fp32_vs_fp64_adjoint_whole_box": float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64))),
+        "errors_are": "max |g - g_fd| / max |g_fd| over the checked cells (and over the whole box for fp32 vs fp64)",
+    }))
+
+
+def run_group(args):
+    """Batched S-matrix workload: the bend with its 8 excitations plus 16 slabs of
+    uneven size (128^3 .. 256x256x192, 1-6 random cuboid inclusions each, one
+    excitation each), all FP32, advanced together by one group (one launch per
+    sweep for all structures); compared with the same plans stepped one by one."""
+    import torch
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    bend, pr, modes = make_workload()
+    nsteps = args.warmup + args.steps
+    plans = [make_plan(bend, pr, modes, F.FP32, BATCH, nsteps, tuning=(2, 1, 0, 0, 4))]
+    cells = bend.s.n3 * BATCH
+    for i, shp in enumerate(W.slab_shapes(16, seed=args.group_seed)):
+        sl = W.slab_structure(shp, seed=100 + i)
+        prs = W.prepare(sl.s, dt_factor=1.0 / 0.99)
+        p = F.Plan.create(sl.s.L, sl.s.iBc, (sl.iB, sl.iT, sl.iI, 1), prs.invtau_R, prs.invtau_I, prs.mu,
+                          prs.epsi, prs.sigma, precision=F.FP32, batch=1)
+        p.set_tuning(2, 1, 0, 0, 4)
+        p.set_incident(0, *W.mode_profiles(sl, n_modes=1)[0])
+        src, ph = W.pulse_schedule(nsteps, prs.dt, lams_um=LAMS)
+        p.set_schedule(src, planes=(sl.iB, sl.iT), phase=ph)
+        plans.append(p)
+        cells += sl.s.n3
+    g = F.Group(plans)
+    by, _ = g.autotune(4)
+    g.run(0, args.warmup)
+    _, t_group = _timed(lambda: g.run(args.warmup, nsteps))
+    g.close()
+    for p in plans:  # the same steps again as separate plans, each on its own stream
+        p.set_tuning(2, by, 0, 0, 4)
+
+    def one_by_one():
+        for p in plans:
+            p.run(args.warmup, nsteps, sync=False)
+        for p in plans:
+            p.sync()
+    _, t_sep = _timed(one_by_one)
+    print(json.dumps({
+        "mode": "group", "config": "bend 256x192x160 x 8 excitations + 16 slabs 128^3..256x256x192, FP32, "
+                                   "21-wavelength FP64 DFT on 2 planes each",
+        "structures": len(plans), "cell_excitations": cells, "steps": args.steps, "block_y": by,
+        "group_gcell_per_s": cells * args.steps / t_group / 1e9, "group_ms_per_step": 1e3 * t_group / args.steps,
+        "separate_plans_gcell_per_s": cells * args.steps / t_sep / 1e9,
+        "device_gb": sum(p.device_bytes for p in plans) / 1e9,
+    }))
+    for p in plans:
+        p.close()
+
+
+def run_large(args):
+    """Large-domain throughput: 640x640x512 cells (~210M) in FP32, split PML,
+    gently curved substrate (radius 50 um), PEC patch-array grating."""
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    t0 = time.perf_counter()
+    st = W.large_structure()
+    pr = W.prepare(st.s, dt_factor=1.0 / 0.99)
+    p = F.Plan.create(st.s.L, st.s.iBc, (st.iB, st.iT, st.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
+                      pr.sigma, precision=F.FP32, batch=1, pec=st.s.pec)
+    nsteps = args.warmup + args.steps
+    p.set_incident(0, *W.mode_profiles(st, n_modes=1)[0])
+    src, ph = W.pulse_schedule(nsteps, pr.dt, lams_um=[1.55])
+    p.set_schedule(src, planes=(st.iB, st.iT), phase=ph)
+    t_setup = time.perf_counter() - t0
+    best, _ = p.autotune(2)
+    p.run(0, args.warmup)
+    _, t = _timed(lambda: p.run(args.warmup, nsteps))
+    ok, mx = p.check_finite()
+    print(json.dumps({
+        "mode": "large", "config": "640x640x512 FP32, 12-cell split PML, curved substrate R=50um, PEC patch array",
+        "cells": st.s.n3, "split_cells": pr.lnotn, "steps": args.steps, "tuning": list(best),
+        "gcell_per_s": st.s.n3 * args.steps / t / 1e9, "ms_per_step": 1e3 * t / args.steps,
+        "device_gb": p.device_bytes / 1e9, "setup_s": t_setup, "finite": ok,
+    }))
+    p.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--mode", default="main", choices=["main", "adjoint", "group", "large"],
+                    help="main: the contract line; the others: the adjoint, batched-structures and large-domain "
+                         "workloads (one summary line each)")
+    ap.add_argument("--adj-steps", type=int, default=6000)
+    ap.add_argument("--fd-cells", type=int, default=32)
+    ap.add_argument("--group-seed", type=int, default=0)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
@@ -447,6 +605,8 @@ def main():
         args.warmup = 3
     if args.profile:
         run_profile(args)
+    elif args.mode != "main":
+        {"adjoint": run_adjoint, "group": run_group, "large": run_large}[args.mode](args)
     elif args.impl == "reference":
         run_reference(args)
     else:

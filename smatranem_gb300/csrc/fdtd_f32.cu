@@ -558,6 +558,23 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v)
     asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ void red_add_release_gpu(int *p, int v)
+{
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+/* E-plane progress counters count finished items and are never reset: launch
+ * `ep` has finished plane z when the counter reaches ep * per_plane */
+__device__ __forceinline__ bool wait_epoch_count(const int *ctr, int ep, int per_plane)
+{
+    const int want = ep * per_plane;
+    for (int it = 0; it < (1 << 22); it++) {
+        if (ld_acquire_gpu(ctr) - want >= 0) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
 __device__ __forceinline__ bool wait_epoch(const int *flag, int ep)
 {
     for (int it = 0; it < (1 << 22); it++) {
@@ -574,69 +591,76 @@ __device__ __noinline__ void pipe_general(const P32 &p, int rel, int b, long lon
     else general32_cell<false, false>(p, rel, b, l);
 }
 
-__global__ void __launch_bounds__(128, 4) k_pipe32v(const P32 p, const int rel, const Pipe32 pp)
+/* the items of one sweep (H: EF = false, E: EF = true) taken by `ncta` CTAs,
+ * this one being number `cta`: plane-major order, (row block, excitation)
+ * inside a plane */
+template <bool EF>
+__device__ __forceinline__ void pipe_loop(const P32 &p, const int rel, const Pipe32 &pp, const int ep, const int cta,
+                                          const int ncta)
 {
     const Geo &g = p.g;
-    const int ep = ld_acquire_gpu(&pp.ctl[0]) + 1;
-    const int per_group = pp.nyb * p.batch;
+    const int per_plane = pp.nyb * p.batch;
+    const int nitems = g.L2 * per_plane;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-    const int D = pp.lag;
     const int L2 = g.L2;
     auto hflag = [&](int z, int yb, int b) { return pp.hflag + ((long long)z * pp.nyb + yb) * p.batch + b; };
-    for (int item = blockIdx.x; item < pp.nitems; item += gridDim.x) {
-        const int grp = item / per_group, r = item % per_group;
+    for (int item = cta; item < nitems; item += ncta) {
+        const int z = item / per_plane, r = item % per_plane;
         const int b = r % p.batch, yb = r / p.batch;
-        /* groups: H(0..D-1), then H(t), E(t-D) for t = D..L2-1, then E(L2-D..L2-1) */
-        bool efield;
-        int z;
-        if (grp < D) {
-            efield = false;
-            z = grp;
-        } else if (grp < 2 * L2 - D) {
-            const int u = grp - D, t = D + u / 2;
-            efield = u & 1;
-            z = efield ? t - D : t;
-        } else {
-            efield = true;
-            z = grp - L2;
-        }
-        if (efield) {
-            if (tid == 0) {
+        if (EF) {
+            /* lanes 0..4 of warp 0 each wait on one H item, in parallel */
+            if (tid < 5) {
                 const int zn = z + 1 == L2 ? 0 : z + 1, yn = yb + 1 == pp.nyb ? 0 : yb + 1;
-                bool ok = wait_epoch(hflag(z, yb, b), ep) && wait_epoch(hflag(z, yn, b), ep) &&
-                          wait_epoch(hflag(zn, yb, b), ep);
-                if (ok && pp.wait_back) {
-                    /* stable-form E cells read the new H of their backward
-                     * neighbours; plans that wrap z with such cells are not
-                     * pipelined, so plane 0 has no z-1 dependence */
-                    const int yp = yb == 0 ? pp.nyb - 1 : yb - 1;
-                    ok = (z == 0 || wait_epoch(hflag(z - 1, yb, b), ep)) && wait_epoch(hflag(z, yp, b), ep);
-                }
-                if (!ok) atomicExch(pp.err, 2);
+                const int yp = yb == 0 ? pp.nyb - 1 : yb - 1;
+                /* stable-form E cells read the new H of their backward
+                 * neighbours (waits 3, 4); plans that wrap z with such cells
+                 * are not pipelined, so plane 0 has no z-1 dependence */
+                const int *f = tid == 0 ? hflag(z, yb, b) : tid == 1 ? hflag(z, yn, b) : tid == 2 ? hflag(zn, yb, b)
+                             : tid == 3 ? (pp.wait_back && z > 0 ? hflag(z - 1, yb, b) : nullptr)
+                                        : (pp.wait_back ? hflag(z, yp, b) : nullptr);
+                if (f && !wait_epoch(f, ep)) atomicExch(pp.err, 2);
             }
             __syncthreads();
+        } else if (pp.lag > 0 && z >= pp.lag) {
+            /* keep the H sweep at most `lag` planes ahead of the E sweep, so
+             * that what E re-reads is still in L2 */
+            if (tid == 0 && !wait_epoch_count(pp.eplane + (z - pp.lag), ep, per_plane)) atomicExch(pp.err, 2);
+            __syncthreads();
         }
-        const int j1 = yb * pp.by + threadIdx.y;
-        for (int xb = 0; xb * 4 * (int)blockDim.x < g.L0; xb++) {
-            const int xr = (xb * blockDim.x + threadIdx.x) * 4;
-            if (efield) sweep32v_quad<true, true>(p, rel, b, j1, z, xr);
-            else sweep32v_quad<false, false>(p, rel, b, j1, z, xr);
+        /* rows [yb*R, yb*R + R) of plane z, blockDim.y rows at a time */
+        const int R = pp.by, yend = min(g.L1, yb * R + R);
+        for (int j1 = yb * R + threadIdx.y; j1 < yend; j1 += blockDim.y) { /* uniform per warp: one row each */
+            for (int xb = 0; xb * 4 * (int)blockDim.x < g.L0; xb++)
+                sweep32v_quad<EF, EF>(p, rel, b, j1, z, (xb * blockDim.x + threadIdx.x) * 4);
         }
-        const int *grow = efield ? pp.egen_row : pp.hgen_row;
+        const int *grow = EF ? pp.egen_row : pp.hgen_row;
         const int g0 = grow[z * pp.nyb + yb], g1 = grow[z * pp.nyb + yb + 1];
         if (g1 > g0) {
             __syncthreads(); /* the quads stored placeholders for these cells */
-            const int *gl = efield ? pp.egen : pp.hgen;
-            for (int i = g0 + tid; i < g1; i += nthr) pipe_general(p, rel, b, gl[i], efield);
+            const int *gl = EF ? pp.egen : pp.hgen;
+            for (int i = g0 + tid; i < g1; i += nthr) pipe_general(p, rel, b, gl[i], EF);
         }
         __syncthreads();
-        if (!efield && tid == 0) {
-            __threadfence();
-            st_release_gpu(hflag(z, yb, b), ep);
+        /* release at gpu scope after the barrier: cumulative over the CTA's writes */
+        if (tid == 0) {
+            if (!EF) st_release_gpu(hflag(z, yb, b), ep);
+            else if (pp.lag > 0) red_add_release_gpu(pp.eplane + z, 1);
         }
     }
+}
+
+__global__ void __launch_bounds__(128, 5) k_pipe32v(const P32 p, const int rel, const Pipe32 pp)
+{
+    const int ep = ld_acquire_gpu(&pp.ctl[0]) + 1;
+    /* CTAs [0, nh) run the H sweep, the rest the E sweep: H CTAs wait only on
+     * finished E planes `lag` behind, E CTAs on H items of their own and the
+     * next plane; with every CTA resident (a cooperative launch) both ends
+     * always have a runnable item */
+    const int nh = gridDim.x / 2;
+    if ((int)blockIdx.x < nh) pipe_loop<false>(p, rel, pp, ep, blockIdx.x, nh);
+    else pipe_loop<true>(p, rel, pp, ep, blockIdx.x - nh, gridDim.x - nh);
     /* the last CTA out publishes the epoch for the next launch */
-    if (tid == 0) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
         __threadfence();
         const int n = atomicAdd(&pp.ctl[1], 1);
         if (n == (int)gridDim.x - 1) {
@@ -661,7 +685,7 @@ void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStrea
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(pp.nxw, pp.by);
+    cfg.blockDim = dim3(pp.nxw, 128 / pp.nxw); /* rows of an item are walked blockDim.y at a time */
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
@@ -670,6 +694,51 @@ void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStrea
     cfg.attrs = at;
     cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, k_pipe32v, p, rel, pp);
+}
+
+/* ---------------------------------------------------------------------------
+ * Groups: the vectorised H (E) sweep of every member plan in one launch.
+ * Block i belongs to the member m with blk[m] <= i < blk[m+1]; inside it the
+ * block decodes exactly as a k_sweep32v block (x block fastest, then row
+ * block x excitation, then plane), so each member gets the same bits as
+ * when it is stepped alone.
+ * ------------------------------------------------------------------------- */
+template <bool EF>
+__global__ void __launch_bounds__(128, 5) k_group32v(const __grid_constant__ Group32 gr, const int rel)
+{
+    int m = 0;
+    while (m + 1 < gr.n && (int)blockIdx.x >= gr.blk[m + 1]) m++;
+    const P32 &p = gr.p[m];
+    const int local = blockIdx.x - gr.blk[m];
+    const int nxb = (p.g.L0 / 4 + 31) / 32;
+    const int nyb = ((p.g.L1 + gr.by - 1) / gr.by) * p.batch;
+    const int xb = local % nxb, t = local / nxb;
+    const int yb = t % nyb, z = t / nyb;
+    const int b = yb % p.batch;
+    const int j1 = (yb / p.batch) * blockDim.y + threadIdx.y;
+    sweep32v_quad<EF, false>(p, rel, b, j1, z, (xb * 32 + threadIdx.x) * 4);
+}
+
+template <bool EF>
+__global__ void k_group_general32(const __grid_constant__ Group32 gr, const int rel)
+{
+    const int *gb = EF ? gr.gen_e : gr.gen_h;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= gb[gr.n]) return;
+    int m = 0;
+    while (m + 1 < gr.n && i >= gb[m + 1]) m++;
+    const int ng = EF ? gr.negen[m] : gr.nhgen[m];
+    const int local = i - gb[m];
+    general32_cell<EF, false>(gr.p[m], rel, local / ng, (EF ? gr.egen[m] : gr.hgen[m])[local % ng]);
+}
+
+void launch_group32v(const Group32 &gr, int rel, cudaStream_t st)
+{
+    const dim3 blk(32, gr.by, 1);
+    k_group32v<false><<<gr.blk[gr.n], blk, 0, st>>>(gr, rel);
+    if (gr.gen_h[gr.n] > 0) k_group_general32<false><<<(gr.gen_h[gr.n] + 127) / 128, 128, 0, st>>>(gr, rel);
+    k_group32v<true><<<gr.blk[gr.n], blk, 0, st>>>(gr, rel);
+    if (gr.gen_e[gr.n] > 0) k_group_general32<true><<<(gr.gen_e[gr.n] + 127) / 128, 128, 0, st>>>(gr, rel);
 }
 
 /* Fold `count` ring slots ending at step *base + rel_end into the FP64 DFT

@@ -1,0 +1,246 @@
+/*
+ * Groups: many structures of uneven size (each an FP32 plan with its own batch
+ * of excitations) advanced together, one launch per sweep for all of them.
+ *
+ * The reference runs one structure per process (FDTDcalc/FDTDsplitfieldMetal.c
+ * main); an S-matrix sweep over a family of structures is a loop of such
+ * runs.  Here the member plans keep their own device state, schedule, sources
+ * and DFT; the group only replaces their per-step launches by grouped ones
+ * (k_group32v) and flushes each member's DFT ring.  Member results are
+ * bit-identical to stepping each plan alone with the vectorised sweeps.
+ */
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "plan_internal.cuh"
+
+using namespace smat;
+using namespace smat::plan;
+
+struct smat_fdtd_group {
+    std::vector<smat_fdtd_plan *> m;
+    cudaStream_t stream = nullptr;
+    int by = 1;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
+};
+
+namespace {
+
+Group32 make_group(const smat_fdtd_group *g)
+{
+    Group32 gr;
+    memset(&gr, 0, sizeof gr);
+    gr.n = (int)g->m.size();
+    gr.by = g->by;
+    int blk = 0, gh = 0, ge = 0;
+    for (int i = 0; i < gr.n; i++) {
+        smat_fdtd_plan *p = g->m[i];
+        gr.blk[i] = blk;
+        gr.gen_h[i] = gh;
+        gr.gen_e[i] = ge;
+        gr.p[i] = make_p32(p, false);
+        gr.hgen[i] = p->d_hgen;
+        gr.egen[i] = p->d_egen;
+        gr.nhgen[i] = p->nhgen;
+        gr.negen[i] = p->negen;
+        const int nxb = (p->L[0] / 4 + 31) / 32;
+        blk += nxb * ((p->L[1] + g->by - 1) / g->by) * p->batch * p->L[2];
+        gh += p->nhgen * p->batch;
+        ge += p->negen * p->batch;
+    }
+    gr.blk[gr.n] = blk;
+    gr.gen_h[gr.n] = gh;
+    gr.gen_e[gr.n] = ge;
+    return gr;
+}
+
+/* steps rel0 .. rel0+n-1 of every member (relative to each member's d_base) */
+void enqueue_group(smat_fdtd_group *g, int rel0, int n)
+{
+    const Group32 gr = make_group(g);
+    for (int i = 0; i < n; i++) launch_group32v(gr, rel0 + i, g->stream);
+    for (smat_fdtd_plan *p : g->m) launch_flush32(make_p32(p, false), rel0 + n, n, g->stream);
+}
+
+void drop_group_graph(smat_fdtd_group *g)
+{
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
+    g->graph_failed = false;
+}
+
+void build_group_graph(smat_fdtd_group *g)
+{
+    if (g->graph || g->graph_failed) return;
+    cudaGraph_t gg = nullptr;
+    if (cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        g->graph_failed = true;
+        return;
+    }
+    enqueue_group(g, 0, GRAPH_STEPS);
+    for (smat_fdtd_plan *p : g->m) launch_bump(p->d_base, GRAPH_STEPS, g->stream);
+    if (cudaStreamEndCapture(g->stream, &gg) != cudaSuccess || !gg) {
+        cudaGetLastError();
+        g->graph_failed = true;
+        return;
+    }
+    if (cudaGraphInstantiate(&g->graph, gg, 0) != cudaSuccess) {
+        cudaGetLastError();
+        g->graph = nullptr;
+        g->graph_failed = true;
+    }
+    cudaGraphDestroy(gg);
+}
+
+int sync_members(smat_fdtd_group *g)
+{
+    for (smat_fdtd_plan *p : g->m) CK(cudaStreamSynchronize(p->stream));
+    return SMAT_OK;
+}
+
+} // namespace
+
+extern "C" int smat_fdtd_group_create(smat_fdtd_plan *const *plans, int nplans, smat_fdtd_group **out)
+{
+    smat_clear_error();
+    if (!plans || !out || nplans < 1) return smat_fail(SMAT_EINVAL, "group_create: bad arguments");
+    if (nplans > MAX_GROUP) return smat_fail(SMAT_EINVAL, "group_create: at most %d plans per group", MAX_GROUP);
+    *out = nullptr;
+    for (int i = 0; i < nplans; i++) {
+        const smat_fdtd_plan *p = plans[i];
+        if (!p) return smat_fail(SMAT_EINVAL, "group_create: plan %d is null", i);
+        if (p->precision != SMAT_FP32 || p->L[0] % 4 != 0)
+            return smat_fail(SMAT_EINVAL, "group_create: plan %d is not an FP32 plan with L0 %% 4 == 0", i);
+        for (int j = 0; j < i; j++)
+            if (plans[j] == p) return smat_fail(SMAT_EINVAL, "group_create: plan %d appears twice", i);
+    }
+    smat_fdtd_group *g = new (std::nothrow) smat_fdtd_group();
+    if (!g) return smat_fail(SMAT_ENOMEM, "group_create: out of host memory");
+    g->m.assign(plans, plans + nplans);
+    g->stream = plans[0]->stream;
+    *out = g;
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_group_destroy(smat_fdtd_group *g)
+{
+    if (!g) return SMAT_OK;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    drop_group_graph(g);
+    delete g;
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_group_set_tuning(smat_fdtd_group *g, int block_y)
+{
+    smat_clear_error();
+    if (!g || block_y < 1 || block_y > 4) return smat_fail(SMAT_EINVAL, "group_set_tuning: block_y in 1..4");
+    g->by = block_y;
+    drop_group_graph(g);
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_group_run(smat_fdtd_group *g, int k_begin, int k_end)
+{
+    smat_clear_error();
+    if (!g || k_begin < 0 || k_end < k_begin) return smat_fail(SMAT_EINVAL, "group_run: bad step range");
+    for (size_t i = 0; i < g->m.size(); i++) {
+        const smat_fdtd_plan *p = g->m[i];
+        if (!p->d_sched) return smat_fail(SMAT_ESTATE, "group_run: member %zu has no schedule", i);
+        if (k_end > p->nsched)
+            return smat_fail(SMAT_EINVAL, "group_run: k_end %d beyond member %zu's %d-step schedule", k_end, i,
+                             p->nsched);
+    }
+    int rc = sync_members(g); /* members' own streams may still hold work */
+    if (rc) return rc;
+    for (smat_fdtd_plan *p : g->m) launch_set(p->d_base, k_begin, g->stream);
+    int n = k_end - k_begin;
+    if (n >= GRAPH_STEPS) build_group_graph(g);
+    while (n >= GRAPH_STEPS) {
+        if (g->graph) {
+            CK(cudaGraphLaunch(g->graph, g->stream));
+        } else {
+            enqueue_group(g, 0, GRAPH_STEPS);
+            for (smat_fdtd_plan *p : g->m) launch_bump(p->d_base, GRAPH_STEPS, g->stream);
+        }
+        n -= GRAPH_STEPS;
+    }
+    if (n > 0) {
+        enqueue_group(g, 0, n);
+        for (smat_fdtd_plan *p : g->m) launch_bump(p->d_base, n, g->stream);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "group_run: launch");
+    return SMAT_OK;
+}
+
+extern "C" int smat_fdtd_group_sync(smat_fdtd_group *g)
+{
+    if (!g) return smat_fail(SMAT_EINVAL, "null group");
+    CK(cudaStreamSynchronize(g->stream));
+    for (smat_fdtd_plan *p : g->m) {
+        int rc = smat_fdtd_sync(p);
+        if (rc) return rc;
+    }
+    return SMAT_OK;
+}
+
+/* Times each block_y over nsteps steps and keeps the fastest.  Like the plan
+ * autotuner it needs every member at the zero state and runs with sources and
+ * DFT sampling off, so the members are left as they were. */
+extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int *best_by, double *best_ms)
+{
+    smat_clear_error();
+    if (!g || nsteps < 1) return smat_fail(SMAT_EINVAL, "group_autotune: bad arguments");
+    for (smat_fdtd_plan *p : g->m) {
+        int finite = 0;
+        double mx = 0;
+        int rc = smat_fdtd_check_finite(p, &finite, &mx);
+        if (rc) return rc;
+        if (mx != 0.0) return smat_fail(SMAT_ESTATE, "group_autotune: needs every member at the zero state");
+    }
+    std::vector<int> nq(g->m.size());
+    for (size_t i = 0; i < g->m.size(); i++) {
+        smat_fdtd_plan *p = g->m[i];
+        nq[i] = p->nq;
+        p->nq = 0;
+        CK(cudaMemsetAsync(p->d_iI, 0xff, sizeof(int) * p->batch, g->stream));
+        launch_set(p->d_base, 0, g->stream);
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double bms = 1e30;
+    int bby = g->by;
+    for (int by : {1, 2, 4}) {
+        g->by = by;
+        enqueue_group(g, 0, 1);
+        CK(cudaEventRecord(e0, g->stream));
+        enqueue_group(g, 0, nsteps);
+        CK(cudaEventRecord(e1, g->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < bms) {
+            bms = ms;
+            bby = by;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (size_t i = 0; i < g->m.size(); i++) {
+        smat_fdtd_plan *p = g->m[i];
+        p->nq = nq[i];
+        CK(cudaMemcpyAsync(p->d_iI, p->h_iI.data(), sizeof(int) * p->batch, cudaMemcpyHostToDevice, g->stream));
+    }
+    CK(cudaStreamSynchronize(g->stream));
+    g->by = bby;
+    drop_group_graph(g);
+    if (best_by) *best_by = bby;
+    if (best_ms) *best_ms = bms / nsteps;
+    return SMAT_OK;
+}

@@ -102,20 +102,35 @@ struct P32 {
 };
 
 /* Pipelined sweeps (kernel 4): one cooperative launch per step.  Items are
- * (plane z, block of `by` rows, excitation b) of the H sweep or the E sweep in
- * the order H(0..D-1), H(D), E(0), H(D+1), E(1), ..., E(L2-1); an E
- * item waits until the H items it reads (and whose E inputs it overwrites)
- * have finished, through per-item flags stamped with a launch epoch. */
+ * (plane z, block of `by` rows, excitation b); half of the CTAs take the H
+ * items, half the E items, each in plane order.  An E item waits until the H
+ * items it reads (and whose E inputs it overwrites) have finished, through
+ * per-item flags stamped with a launch epoch; an H item waits until the E
+ * sweep is at most `lag` planes behind. */
 struct Pipe32 {
-    int by, nyb, nitems;
+    int by, nyb, nitems;            /* rows per item, row blocks per plane, items per step */
     int nxw;                        /* threads along x (a multiple of 32): four cells each */
-    int lag;                        /* D: E(z) runs after H(z+D), 1 <= D <= L2 */
+    int lag;                        /* H may run at most `lag` planes ahead of E (0: no limit, else >= 2) */
+    int *eplane;                    /* [L2]: finished E items per plane, cumulative over launches */
     int *hflag;                     /* [L2][nyb][batch]: epoch of the finished H item */
     int *ctl;                       /* [0] epoch of the last finished launch, [1] exit count */
     int *err;                       /* set to 2 when a wait gives up */
     const int *hgen, *egen;         /* general (record) cells, cell order */
     const int *hgen_row, *egen_row; /* [L2*nyb + 1]: first general cell of item (z, yb) */
     int wait_back;                  /* E items also wait for H(z-1), H(z, yb-1) (stable-form E cells) */
+};
+
+/* Several FP32 plans stepped together (a group): one vectorised-sweep launch
+ * covers the cells of every member; block ranges and general-cell ranges per
+ * member are prefix sums.  Passed by value as a __grid_constant__ parameter. */
+constexpr int MAX_GROUP = 32;
+struct Group32 {
+    int n, by;
+    int blk[MAX_GROUP + 1];                  /* first block of member m */
+    int gen_h[MAX_GROUP + 1], gen_e[MAX_GROUP + 1]; /* first general (cell, excitation) of member m */
+    const int *hgen[MAX_GROUP], *egen[MAX_GROUP];
+    int nhgen[MAX_GROUP], negen[MAX_GROUP];
+    P32 p[MAX_GROUP];
 };
 
 /* the fused FP32 step: reads the field set in p, writes the other set */
@@ -146,6 +161,7 @@ void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
 void launch_h32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int ngh, cudaStream_t st);
 void launch_e32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int nge, cudaStream_t st);
 void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStream_t st);
+void launch_group32v(const Group32 &gr, int rel, cudaStream_t st);
 int pipe32v_max_ctas_per_sm(int threads);
 void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);
 size_t fused32_smem(int ty, int ns);

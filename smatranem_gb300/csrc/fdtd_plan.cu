@@ -266,6 +266,7 @@ Pipe32 make_pipe(const smat_fdtd_plan *p)
     pp.wait_back = p->nstable > 0;
     pp.nxw = p->pipe_nxw;
     pp.lag = p->pipe_lag;
+    pp.eplane = p->d_eplane;
     return pp;
 }
 
@@ -286,7 +287,13 @@ int setup_pipe(smat_fdtd_plan *p, int by, int lag)
         if ((rc = p->alloc(&p->d_pipe_ctl, 2))) return rc;
         if ((rc = p->alloc(&p->d_hgen_row, (size_t)L2 * L1 + 1))) return rc;
         if ((rc = p->alloc(&p->d_egen_row, (size_t)L2 * L1 + 1))) return rc;
+        if ((rc = p->alloc(&p->d_eplane, (size_t)L2))) return rc;
     }
+    /* flags and counters are relative to the epoch: restart both */
+    drop_graph(p);
+    CK(cudaMemsetAsync(p->d_hflag, 0, sizeof(int) * (size_t)L2 * L1 * p->batch, p->stream));
+    CK(cudaMemsetAsync(p->d_eplane, 0, sizeof(int) * (size_t)L2, p->stream));
+    CK(cudaMemsetAsync(p->d_pipe_ctl, 0, sizeof(int) * 2, p->stream));
     const int nyb = (L1 + by - 1) / by;
     for (int side = 0; side < 2; side++) {
         const std::vector<int> &gl = side ? p->egen_host : p->hgen_host;
@@ -302,7 +309,7 @@ int setup_pipe(smat_fdtd_plan *p, int by, int lag)
     }
     CK(cudaStreamSynchronize(p->stream));
     const int nxw = pipe_nxw(p->L[0]);
-    const int per_sm = pipe32v_max_ctas_per_sm(nxw * by);
+    const int per_sm = pipe32v_max_ctas_per_sm(128);
     if (per_sm < 1) return smat_fail(SMAT_ECUDA, "pipelined sweeps: no resident CTA of %d x %d threads", nxw, by);
     const int want = p->ctas_per_sm > 0 && p->ctas_per_sm < per_sm ? p->ctas_per_sm : per_sm;
     const long long nitems = 2LL * L2 * nyb * p->batch;
@@ -1121,12 +1128,11 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps), 3 (fused, TMA), "
                                       "4 (pipelined vector sweeps)");
     if (fused == 4) {
-        const int lag = z_chunk < 1 ? 1 : z_chunk;
-        if (p->L[0] % 4 != 0 || tile_y < 1 || pipe_nxw(p->L[0]) * tile_y > 128 || ctas_per_sm < 0 ||
+        const int lag = z_chunk;
+        if (p->L[0] % 4 != 0 || tile_y < 1 || tile_y > p->L[1] || ctas_per_sm < 0 || lag < 0 || lag == 1 ||
             lag > p->L[2])
-            return smat_fail(SMAT_EINVAL, "set_tuning: pipelined sweeps need L0 %% 4 == 0, tile_y rows of at most "
-                                          "128 threads (%d per row) and a lag (z_chunk) of 1..L2",
-                             pipe_nxw(p->L[0]));
+            return smat_fail(SMAT_EINVAL, "set_tuning: pipelined sweeps need L0 %% 4 == 0, tile_y (rows per item) "
+                                          "in 1..L1 and a lag (z_chunk) of 0 (none) or 2..L2");
         if (p->nstable > 0 && p->iBc[2] != 0)
             return smat_fail(SMAT_EINVAL, "set_tuning: pipelined sweeps cannot order stable-form E cells across a "
                                           "wrapped z boundary");
@@ -1199,9 +1205,9 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
         cands.push_back({2, 4, 0, 0, 4});
     }
     if (p->L[0] % 4 == 0 && !(p->nstable > 0 && p->iBc[2] != 0))
-        for (int by : {1, 2, 4})
-            for (int lag : {1, 2, 4})
-                if (pipe_nxw(p->L[0]) * by <= 128 && lag <= L2) cands.push_back({4, by, lag, 0, 0});
+        for (int rows : {2, 4, 8})
+            for (int lag : {0, 4, 8})
+                if (rows <= p->L[1] && lag <= L2) cands.push_back({4, rows, lag, 0, 0});
     cands.push_back({0, 4, 0, 0, 4});
     cands.push_back({0, 8, 0, 0, 4});
     cands.push_back({0, 4, 4 < L2 ? 4 : 0, 0, 4});

@@ -108,6 +108,7 @@ struct smat_fdtd_plan {
     /* pipelined sweeps (kernel 4) */
     int pipe_by = 0, pipe_grid = 0, pipe_lag = 1, pipe_nxw = 32;
     int *d_hflag = nullptr, *d_pipe_ctl = nullptr, *d_hgen_row = nullptr, *d_egen_row = nullptr;
+    int *d_eplane = nullptr;
     /* FP32 launch configuration (autotuned): fused z-march (1), two sweeps (0),
      * two vectorised sweeps (2, needs L0 % 4 == 0) */
     int fused = 1, ty = 8, zc = 40, ns = 5, ctas_per_sm = 0;

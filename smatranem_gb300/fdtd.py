@@ -81,6 +81,12 @@ def lib():
         L.smat_fdtd_dft_device.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P]
         L.smat_overlap.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, _P, _P, _P, _P]
         L.smat_fdtd_adjoint_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P]
+        L.smat_fdtd_group_create.argtypes = [_P, C.c_int, _P]
+        L.smat_fdtd_group_destroy.argtypes = [_P]
+        L.smat_fdtd_group_set_tuning.argtypes = [_P, C.c_int]
+        L.smat_fdtd_group_autotune.argtypes = [_P, C.c_int, _P, _P]
+        L.smat_fdtd_group_run.argtypes = [_P, C.c_int, C.c_int]
+        L.smat_fdtd_group_sync.argtypes = [_P]
         _lib = L
     return _lib
 
@@ -377,6 +383,46 @@ class Plan:
         ok, m = C.c_int(0), C.c_double(0)
         _check(lib().smat_fdtd_check_finite(self._h, C.byref(ok), C.byref(m)))
         return bool(ok.value), m.value
+
+
+class Group:
+    """Several FP32 plans stepped together, one launch per sweep for all
+    (smat_fdtd_group_*).  The plans stay owned by the caller and must outlive
+    the group."""
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        arr = (_P * len(self.plans))(*[p._h for p in self.plans])
+        h = _P()
+        _check(lib().smat_fdtd_group_create(arr, len(self.plans), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().smat_fdtd_group_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_tuning(self, block_y):
+        _check(lib().smat_fdtd_group_set_tuning(self._h, block_y))
+
+    def autotune(self, nsteps=4):
+        by, ms = C.c_int(0), C.c_double(0)
+        _check(lib().smat_fdtd_group_autotune(self._h, nsteps, C.byref(by), C.byref(ms)))
+        return by.value, ms.value
+
+    def run(self, k_begin, k_end, sync=True):
+        _check(lib().smat_fdtd_group_run(self._h, k_begin, k_end))
+        if sync:
+            self.sync()
+
+    def sync(self):
+        _check(lib().smat_fdtd_group_sync(self._h))
 
 
 def cw_schedule(n2pi, time_period):

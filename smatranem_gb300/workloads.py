@@ -476,3 +476,65 @@ def slab_shapes(n=16, seed=0, lo=(128, 128, 128), hi=(256, 256, 192)):
             shp.append(v - v % 8)
         out.append(tuple(shp))
     return out
+
+
+def large_structure(shape=(640, 640, 512), pml=12, radius_um=50.0, dx_um=0.02, eps_sub=2.085, sub=(0.30, 0.50),
+                    period=40, patch=20, thick=2, lam0_um=1.55, beam_um=4.0, sq_ref=1e-12, power=3) -> Bend:
+    """Large-domain workload: an eps_sub slab (z fraction `sub` of the grid) in
+    vacuum carrying a PEC patch array (patch x patch x thick cells, period
+    cells, clipped to the non-PML cells) on its top face, on a gently curved
+    substrate: cylindrical coordinates with the x arc at radius R + u2, so
+    H0 = dx (1 + (u2 - u2_mid) / R), H1 = H2 = dx.  Split PML on all six
+    faces.  Built plane by plane (the grid has ~210M cells); only the
+    stretched mu and epsi (complex, n3 x 3) are held in full."""
+    L0, L1, L2 = shape
+    dx = dx_um / INV_K0_UM
+    pl = L0 * L1
+    n3 = pl * L2
+    omega = 2 * math.pi * INV_K0_UM / lam0_um
+    sig = [pml_sigma(n, pml, pml, omega, pml * dx, pml * dx, sq_ref, power) for n in (L0, L1, L2)]
+    u2 = (np.arange(L2) + 0.5) * dx_um
+    h0 = 1.0 + (u2 - u2.mean()) / radius_um
+    z0, z1 = int(sub[0] * L2), int(sub[1] * L2)
+    # patch mask of one plane
+    jx = np.arange(L0)
+    jy = np.arange(L1)
+    off = (period - patch) // 2
+    px_in = ((jx % period) >= off) & ((jx % period) < off + patch) & (jx >= pml + 1) & (jx < L0 - pml - 1)
+    py_in = ((jy % period) >= off) & ((jy % period) < off + patch) & (jy >= pml + 1) & (jy < L1 - pml - 1)
+    patch2d = (py_in[:, None] & px_in[None, :]).reshape(-1)
+    mu = np.empty((n3, 3), np.complex128)
+    ep = np.empty((n3, 3), np.complex128)
+    pec = np.zeros(n3, np.uint8)
+    # in-plane stretch factors s_h, s_e for x and y (z: per plane)
+    sx = [1 + 1j * sig[0][h] for h in range(2)]
+    sy = [1 + 1j * sig[1][h] for h in range(2)]
+    sxy = [[np.tile(sx[h], L1), np.repeat(sy[h], L0)] for h in range(2)]
+    r_min = np.inf
+    for z in range(L2):
+        fx = np.array([dx / h0[z], dx * h0[z], dx * h0[z]])  # H1 H2 / H0, H2 H0 / H1, H0 H1 / H2
+        eps_z = eps_sub if z0 <= z < z1 else 1.0
+        m = np.broadcast_to(fx, (pl, 3)).astype(np.complex128)
+        e = (eps_z * m).copy()
+        sz = [1 + 1j * sig[2][h][z] for h in range(2)]
+        s = [[sxy[h][0], sxy[h][1], np.full(pl, sz[h])] for h in range(2)]
+        for c in range(3):
+            a1, a2 = (c + 1) % 3, (c + 2) % 3
+            m[:, c] = m[:, c] * s[0][a1] * s[0][a2] / s[1][c]
+            e[:, c] = e[:, c] * s[1][a1] * s[1][a2] / s[0][c]
+        mu[z * pl:(z + 1) * pl] = m
+        ep[z * pl:(z + 1) * pl] = e
+        if z1 <= z < z1 + thick:
+            pec[z * pl:(z + 1) * pl] = patch2d
+        er, mr = eps_z * fx, fx
+        r_min = min(r_min, float(np.prod(er) * np.prod(mr) / (er.sum() * mr.sum())))
+    min_dt = math.sqrt(math.sqrt(r_min))
+    s = Structure(L=(L0, L1, L2, pml + 2), mu=mu, epsi=ep, omega=omega, min_dt=min_dt, iBc=(0, 0, 0), pec=pec,
+                  name=f"large{L0}x{L1}x{L2}")
+    u0 = (np.arange(L0) + 0.5 - 0.5 * L0) * dx_um
+    u1 = (np.arange(L1) + 0.5 - 0.5 * L1) * dx_um
+    # source below the slab, launched towards +z through slab and grating;
+    # coordinates scaled so that mode_profiles' Gaussian is beam_um wide
+    b = Bend(s=s, iB=pml + 1, iT=L2 - pml - 2, iI=pml + 3, pml=pml, u0=u0 * (2.0 / beam_um),
+             u1=u1 * (2.0 / beam_um), n_eff=1.0)
+    return b

@@ -1,0 +1,93 @@
+"""Groups: structures of uneven size stepped together (smat_fdtd_group_*).
+
+Every member of a group must end bit-identical -- fields and DFT -- to the same
+plan stepped alone with the vectorised sweeps."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# (L, seed, structure kwargs, iBTIin, batch)
+MEMBERS = [
+    ((40, 17, 19, 3), 31, dict(pml=(4, 4, 4), lossy=0.05, iBc=(1, 1, -1)), (5, 13, 7, 1), 2),
+    ((64, 24, 20, 3), 32, dict(pml=(5, 5, 4), pec=0.03, lossy=0.04, iBc=(0, 0, 0)), (5, 14, 7, 1), 1),
+    ((32, 12, 16, 2), 33, dict(pml=(0, 0, 3), pml_z_only=True, iBc=(-1, 0, 0)), (4, 11, 6, -1), 3),
+    ((136, 9, 12, 2), 34, dict(pml=(3, 2, 3)), (3, 8, 5, 1), 1),
+]
+
+
+def _setup(f, W, s, pr, iBTIin, batch, seed, nsteps):
+    n3, pl = s.n3, s.L[0] * s.L[1]
+    src, ph = f.cw_schedule(pr.n2pi, (1, 1, 3))
+    p = f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=f.FP32,
+                      batch=batch, pec=s.pec)
+    for b in range(batch):
+        H0, E0 = W.random_fields(n3, pr.lnotn, seed=seed + b, scale=1e-2)
+        Hinc, Einc = W.random_incident(pl, seed=seed + 10 + b)
+        p.set_fields(b, H0, E0)
+        p.set_incident(b, Hinc, Einc)
+        p.set_source_plane(b, iBTIin[2] + b % 2, 1 - 2 * (b % 2))
+    p.set_schedule(src[:nsteps], planes=(iBTIin[0], iBTIin[1], 0), phase=ph[:nsteps])
+    return p
+
+
+def _result(p, batch):
+    return [(*p.get_fields(b), *[p.get_dft(b, 0, q) for q in range(3)]) for b in range(batch)]
+
+
+@pytest.mark.parametrize("block_y", [1, 2, 4])
+def test_group_members_match_plans_stepped_alone(built, block_y):
+    from smatranem_gb300 import fdtd as f
+    from smatranem_gb300 import workloads as W
+    nsteps = 60  # windows of 20 and 40 steps: the second holds a captured 32-step chunk
+    structs = []
+    for L, seed, kw, iBTIin, batch in MEMBERS:
+        s = W.random_structure(L, seed=seed, **kw)
+        structs.append((s, W.prepare(s), iBTIin, batch, seed))
+    alone = []
+    for s, pr, iBTIin, batch, seed in structs:
+        with _setup(f, W, s, pr, iBTIin, batch, seed, nsteps) as p:
+            p.set_tuning(2, block_y, 0, 0, 4)
+            # the same run() windows as the group: the FP32 DFT ring is folded
+            # into the FP64 sums at the end of each window
+            p.run(0, 20)
+            p.run(20, nsteps)
+            alone.append(_result(p, batch))
+    plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
+    try:
+        with f.Group(plans) as g:
+            g.set_tuning(block_y)
+            g.run(0, 20)
+            g.run(20, nsteps)
+        for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
+            got = _result(p, batch)
+            for rb, gb in zip(ref, got):
+                for a, b_ in zip(rb, gb):
+                    assert np.all(np.isfinite(a)) and np.array_equal(a, b_)
+    finally:
+        for p in plans:
+            p.close()
+
+
+def test_group_autotune_and_errors(built):
+    from smatranem_gb300 import fdtd as f
+    from smatranem_gb300 import workloads as W
+    L, seed, kw, iBTIin, batch = MEMBERS[0]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    src, ph = f.cw_schedule(pr.n2pi, (1, 1, 3))
+    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                       precision=f.FP32, batch=2) as p, \
+            f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                          precision=f.FP64) as p64:
+        p.set_schedule(src, planes=(iBTIin[0], iBTIin[1]), phase=ph)
+        with f.Group([p]) as g:
+            by, ms = g.autotune(2)
+            assert by in (1, 2, 4) and ms > 0
+            assert p.check_finite() == (True, 0.0)  # left at the zero state
+            with pytest.raises(f.FdtdError):
+                g.run(0, src.shape[0] + 1)  # beyond the schedule
+        with pytest.raises(f.FdtdError):
+            f.Group([p, p64])  # FP64 member
+        with pytest.raises(f.FdtdError):
+            f.Group([p, p])  # the same plan twice

@@ -359,8 +359,8 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
         tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (2, 4, 3, 0, 4), (2, 1, 5, 0, 4), (2, 2, 16, 0, 4),
                     (3, 8, 40, 0, 5), (3, 4, 5, 0, 4), (3, 2, 3, 1, 6), (3, 4, 1, 0, 5), (3, 8, 7, 1, 6)]
         if not (kw.get("metals") and kw["iBc"][2] != 0):  # pipelined sweeps (kernel 4)
-            # (4, rows per item, lag D, ctas_per_sm, -)
-            tunings += [(4, 1, 1, 0, 0), (4, 2, 2, 0, 0), (4, 1, 3, 1, 0), (4, 1, L[2], 0, 0)]
+            # (4, rows per item, lag (0: none), ctas_per_sm, -)
+            tunings += [(4, 1, 0, 0, 0), (4, 2, 2, 0, 0), (4, 5, 3, 1, 0), (4, 3, L[2], 0, 0), (4, L[1], 0, 0, 0)]
     for tuning in tunings:
         got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
         for rb, gb in zip(ref, got):
