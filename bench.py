@@ -55,7 +55,7 @@ WORKLOAD = ("bend 256x192x160 curvilinear (R=2um, Si strip in SiO2), 12-cell spl
 def launches_per_step(tuning, L2):
     """Update-kernel launches of one step: one fused launch (kernels 1, 3), or
     an H and an E sweep per z-chunk (kernels 0, 2; z_chunk 0 = one chunk)."""
-    if tuning[0] in (1, 3):
+    if tuning[0] in (1, 3, 5):
         return 1
     zc = tuning[2]
     return 2 * (1 if zc <= 0 or zc >= L2 else math.ceil(L2 / zc))
@@ -388,6 +388,8 @@ def run_ours(args):
                                 2: "k_sweep32v (H, E; float4)" + (f", z-chunks of {tuning[2]} planes"
                                                                    if 0 < tuning[2] < bend.s.L[2] else ""),
                                 3: "k_fused32t (one fused H+E launch per step, TMA-staged planes)",
+                                4: "k_pipe32v (pipelined H/E sweeps in one cooperative launch)",
+                                5: "k_zm32 (one fused H+E launch per step: 128x4 tiles, TMA producer warp)",
                                 0: "k_sweep32 (H, E)"}[tuning[0]],
                      "tuning": {"kernel": tuning[0], "tile_y": tuning[1], "z_chunk": tuning[2],
                                 "ctas_per_sm": tuning[3], "slots": tuning[4]},
@@ -526,7 +528,7 @@ def run_group(args):
         plans.append(p)
         cells += sl.s.n3
     g = F.Group(plans)
-    by, _ = g.autotune(4)
+    (gmode, by), _ = g.autotune(4)
     g.run(0, args.warmup)
     _, t_group = _timed(lambda: g.run(args.warmup, nsteps))
     g.close()
@@ -542,7 +544,9 @@ def run_group(args):
     print(json.dumps({
         "mode": "group", "config": "bend 256x192x160 x 8 excitations + 16 slabs 128^3..256x256x192, FP32, "
                                    "21-wavelength FP64 DFT on 2 planes each",
-        "structures": len(plans), "cell_excitations": cells, "steps": args.steps, "block_y": by,
+        "structures": len(plans), "cell_excitations": cells, "steps": args.steps,
+        "group_tuning": {"mode": ["one grouped launch per sweep", "members' own launches in one graph"][gmode],
+                         "block_y": by},
         "group_gcell_per_s": cells * args.steps / t_group / 1e9, "group_ms_per_step": 1e3 * t_group / args.steps,
         "separate_plans_gcell_per_s": cells * args.steps / t_sep / 1e9,
         "device_gb": sum(p.device_bytes for p in plans) / 1e9,

@@ -240,9 +240,9 @@ int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const doubl
 /* Groups of structures. -----------------------------------------------------
  * No counterpart in the reference (it runs one structure per process, main
  * :32-187).  A group advances several FP32 plans -- structures of any size,
- * each with its own batch of excitations, schedule and DFT -- together: every
- * step is one vectorised-sweep launch per field over the cells of all members
- * (plus the general cells and each member's DFT flush).  Members need
+ * each with its own batch of excitations, schedule and DFT -- together, one
+ * CUDA graph launch per 32 steps (see set_tuning for the two launch forms
+ * inside it, plus the general cells and each member's DFT flush).  Members need
  * L0 % 4 == 0 and stay usable on their own; results are bit-identical to
  * stepping each member alone with the vectorised sweeps.  At most 32 members;
  * the group launches on the first member's stream and waits for the others'
@@ -250,10 +250,14 @@ int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const doubl
 typedef struct smat_fdtd_group smat_fdtd_group;
 int smat_fdtd_group_create(smat_fdtd_plan *const *plans, int nplans, smat_fdtd_group **group);
 int smat_fdtd_group_destroy(smat_fdtd_group *group);
-int smat_fdtd_group_set_tuning(smat_fdtd_group *group, int block_y);
-/* fastest block_y (rows per block, 1..4) over nsteps steps; members must be at
- * the zero state and are left as they were */
-int smat_fdtd_group_autotune(smat_fdtd_group *group, int nsteps, int *best_block_y, double *best_ms);
+/* mode 0: one grouped sweep launch for all members (blocks find their member
+ * by prefix sums); mode 1: every member's own sweep launches back to back on
+ * the group's stream.  Both are captured as one graph per 32 steps.  block_y:
+ * rows per block, 1..4. */
+int smat_fdtd_group_set_tuning(smat_fdtd_group *group, int mode, int block_y);
+/* fastest {mode, block_y} over nsteps steps; members must be at the zero state
+ * and are left as they were */
+int smat_fdtd_group_autotune(smat_fdtd_group *group, int nsteps, int best[2], double *best_ms);
 /* steps [k_begin, k_end) of every member's schedule */
 int smat_fdtd_group_run(smat_fdtd_group *group, int k_begin, int k_end);
 int smat_fdtd_group_sync(smat_fdtd_group *group);

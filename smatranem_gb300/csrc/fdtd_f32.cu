@@ -288,12 +288,20 @@ __device__ __forceinline__ void sweep32v_quad(const P32 &p, const int rel, const
     const long long oz = (long long)g.pl * (EF ? (ez ? -(g.L2 - 1) : 1) : (ez ? g.L2 - 1 : -1));
     const float fy = ey ? (float)g.bc[1] : 1.0f, fz = ez ? (float)g.bc[2] : 1.0f;
 
-    float4 c[3], out[3], gh[3];
+    /* split-PML quads need their aux slots: decided from the 1-D masks before
+     * any load, so that those loads leave with the others (one DRAM round trip) */
+    const bool pyz = p.pmask[s1 + j1] | p.pmask[s2 + j2];
+    const bool qsplit = pyz | p.pmask[x0] | p.pmask[x0 + 1] | p.pmask[x0 + 2] | p.pmask[x0 + 3];
+    float4 c[3], out[3], gh[3], aux[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         c[i] = ld4(cf + i * n3 + l);
         out[i] = ld4(F + i * n3 + l);
         gh[i] = ldG4<CG>(G + i * n3 + l);
+    }
+    if (qsplit) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) aux[i] = ld4(Fa + i * n3 + l);
     }
     /* H sweep: Ex, Ez at y-1; Ex, Ey at z-1.  E sweep: Hx, Hz at y+1; Hx, Hy at z+1. */
     const float4 gy0 = scale4(ldG4<CG>(G + 0 * n3 + l + oy), fy), gy2 = scale4(ldG4<CG>(G + 2 * n3 + l + oy), fy);
@@ -323,10 +331,8 @@ __device__ __forceinline__ void sweep32v_quad(const P32 &p, const int rel, const
         }
     }
     if (!live) return;
-    const bool pyz = p.pmask[s1 + j1] | p.pmask[s2 + j2];
     const bool on_src = j2 == p.s.iI[b];
     const int q = monitor_index(p.d, j2);
-    float4 aux[3];
     bool any_aux = false;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
@@ -378,8 +384,10 @@ __device__ __forceinline__ void sweep32v_quad(const P32 &p, const int rel, const
     }
     /* elements that need their aux slot (split) or a record (general) */
     if (any_aux) {
+        if (!qsplit) { /* a general (record) cell in an unsplit quad: rare */
 #pragma unroll
-        for (int cc = 0; cc < 3; cc++) aux[cc] = ld4(Fa + cc * n3 + l);
+            for (int cc = 0; cc < 3; cc++) aux[cc] = ld4(Fa + cc * n3 + l);
+        }
         const int jy = s1 + j1, jz = s2 + j2;
         const float *tA = p.tab + (EF ? 2 : 0) * S, *tG = p.tab + (EF ? 3 : 1) * S;
 #pragma unroll
@@ -706,9 +714,20 @@ void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStrea
 template <bool EF>
 __global__ void __launch_bounds__(128, 5) k_group32v(const __grid_constant__ Group32 gr, const int rel)
 {
+    /* the member's parameters, copied once per block to shared memory (a
+     * dynamically indexed parameter array would be read element by element) */
+    __shared__ P32 sp;
     int m = 0;
     while (m + 1 < gr.n && (int)blockIdx.x >= gr.blk[m + 1]) m++;
-    const P32 &p = gr.p[m];
+    {
+        static_assert(sizeof(P32) % 4 == 0, "P32 is copied as words");
+        const int *src = reinterpret_cast<const int *>(&gr.p[m]);
+        int *dst = reinterpret_cast<int *>(&sp);
+        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < (int)(sizeof(P32) / 4); i += blockDim.x * blockDim.y)
+            dst[i] = src[i];
+    }
+    __syncthreads();
+    const P32 &p = sp;
     const int local = blockIdx.x - gr.blk[m];
     const int nxb = (p.g.L0 / 4 + 31) / 32;
     const int nyb = ((p.g.L1 + gr.by - 1) / gr.by) * p.batch;

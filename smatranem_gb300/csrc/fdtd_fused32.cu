@@ -1133,3 +1133,552 @@ void launch_fused32t(const Fused32T &ft, int rel, int grid, cudaStream_t st)
 }
 
 } // namespace smat
+
+namespace smat {
+
+/* ===========================================================================
+ * k_zm32: the fused step on 128 x ZNW tiles, a TMA producer warp and ZNW
+ * consumer warps (kernel 5).
+ *
+ * Same computation and bit-identical results as the sweeps (the H and E
+ * expressions of k_sweep32v per element).  Differences from k_fused32t:
+ *   - a lane owns four x-cells (float4 from shared memory), so one barrier
+ *     per plane covers 512 cells, not 32 x TY;
+ *   - a dedicated producer warp keeps ZNS - 2 planes of TMA copies in flight
+ *     ahead of the consumers (full/empty mbarriers), so the prefetch depth
+ *     costs no consumer registers;
+ *   - the +1 halo row and column of H_new are shared out over all consumer
+ *     warps; H_new planes are triple-buffered so one named barrier per plane
+ *     orders the H and E phases.
+ * Plans with iBc = 0 on every axis only: the copies' zero fill outside the
+ * grid is then exactly the reference's boundary factor (the fill is +0 where
+ * the reference has +-0, which changes no value).  The last z chunk's extra
+ * plane (z = L2) and the pre-plane -1 are fetched out of range for the same
+ * reason.  Stable-form E cells are finished by k_fix_stable32.
+ * ======================================================================== */
+constexpr int ZTX = 128;     /* tile width: 32 lanes x 4 cells */
+constexpr int ZNW = 4;       /* consumer warps = tile rows */
+constexpr int ZNS = 4;       /* plane slots */
+constexpr int ZEX = ZTX + 8; /* E box: x from X0-4 to X0+131 */
+constexpr int ZQX = ZTX + 4; /* H, bh, Ha boxes: x from X0 to X0+131 */
+constexpr int ZHX = ZTX + 4; /* H_new plane row pitch (columns 0..128 used) */
+constexpr int ZNH = 3;       /* H_new planes kept */
+
+struct ZSlot {
+    int e, qt, qb, qm, be, bm, size;
+};
+
+__host__ __device__ inline ZSlot zslot()
+{
+    ZSlot s;
+    int o = 0;
+    s.e = o;
+    o += align32f(3 * (ZNW + 2) * ZEX);
+    s.qt = o;
+    o += align32f(3 * (ZNW + 1) * ZQX);
+    s.qb = o;
+    o += align32f(3 * (ZNW + 1) * ZQX);
+    s.qm = o;
+    o += align32f(3 * (ZNW + 1) * ZQX);
+    s.be = o;
+    o += align32f(3 * ZNW * ZTX);
+    s.bm = o;
+    o += align32f(3 * ZNW * ZTX);
+    s.size = o;
+    return s;
+}
+
+size_t zm32_smem() { return sizeof(float) * (32 + (size_t)ZNS * zslot().size + (size_t)ZNH * 3 * (ZNW + 1) * ZHX); }
+
+__device__ __forceinline__ void named_bar(int id, int n) { asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(n) : "memory"); }
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+/* bounded wait on phase `parity` of bar that gives up at once when another
+ * warp of the CTA has already timed out (*abort): after a timeout every warp
+ * still reaches every barrier, quickly, and the launch ends with the error
+ * flag set instead of hanging */
+__device__ __forceinline__ bool zwait(uint64_t *bar, unsigned parity, volatile int *abort, int *err)
+{
+    const unsigned a = smem_u32(bar);
+    for (int it = 0; it < (1 << 24); it++) {
+        unsigned done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done) return true;
+        if (*abort) return false;
+    }
+    *abort = 1;
+    atomicExch(err, 3);
+    return false;
+}
+
+/* work item -> (excitation, tile origin, z chunk) */
+struct ZItem {
+    int b, X0, Y0, z0, z1;
+};
+
+__device__ __forceinline__ ZItem zitem(const Fused32 &f, int item)
+{
+    ZItem it;
+    it.b = item % f.p.batch;
+    int t = item / f.p.batch;
+    const int tix = t % f.ntx;
+    t /= f.ntx;
+    const int tiy = t % f.nty;
+    const int zci = t / f.nty;
+    it.X0 = tix * ZTX;
+    it.Y0 = tiy * ZNW;
+    it.z0 = zci * f.zc;
+    it.z1 = min(it.z0 + f.zc, f.p.g.L2);
+    return it;
+}
+
+/* does the tile (with its +-1 halo) hold a split cell in x or y? */
+__device__ __forceinline__ bool ztile_split(const P32 &p, int X0, int Y0)
+{
+    const Geo &g = p.g;
+    bool s = false;
+    for (int x = max(0, X0 - 1); x <= min(g.L0 - 1, X0 + ZTX); x++) s |= p.pmask[x] != 0;
+    for (int y = max(0, Y0 - 1); y <= min(g.L1 - 1, Y0 + ZNW); y++) s |= p.pmask[g.L0 + y] != 0;
+    return s;
+}
+
+/* H_new of one element (cell gx, gy, gz); inputs as in k_sweep32v: h = own E
+ * (x, y, z components), ey0/ey2 = Ex/Ez at y-1, ez0/ez1 = Ex/Ey at z-1,
+ * nx1/nx2 = Ey/Ez at x-1; old = old total H, m = old aux, bn = coefficients.
+ * Returns the new total in out, the aux in aux, and whether aux was written. */
+__device__ __forceinline__ bool zm_h_elem(const Fused32 &f, int b, int k, int gx, int gy, int gz, const float h[3],
+                                          float ey0, float ey2, float ez0, float ez1, float nx1, float nx2,
+                                          const float bn[3], float out[3], float aux[3])
+{
+    const P32 &p = f.p;
+    const Geo &g = p.g;
+    if (isnan(bn[0])) { /* general cell: out of line, from the old set in global memory */
+        float tmp[9];
+        h_general(f, b, k, gx, gy, gz, __float_as_int(bn[1]), tmp, tmp + 3, tmp + 6);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            out[c] = tmp[c];
+            aux[c] = tmp[3 + c];
+        }
+        return true;
+    }
+    float pl[3], mi[3];
+    pl[0] = h[2] - ey2;
+    mi[0] = ez1 - h[1];
+    pl[1] = h[0] - ez0;
+    mi[1] = nx2 - h[2];
+    pl[2] = h[1] - nx1;
+    mi[2] = ey0 - h[0];
+    const int S = g.L0 + g.L1 + g.L2, s1 = g.L0, s2 = g.L0 + g.L1;
+    const bool split = p.pmask[gx] | p.pmask[s1 + gy] | p.pmask[s2 + gz];
+    if (!split) {
+        float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+        if (gz == p.s.iI[b]) {
+            const int px = gx + g.L0 * gy;
+            W[0] += (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, true, 1, px));
+            W[1] -= (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, true, 0, px));
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) out[c] = fmaf(-1.0f * bn[c], W[c], out[c]);
+        return false;
+    }
+    const int jx[3] = {gx, s1 + gy, s2 + gz};
+    const float *tA = p.tab, *tG = p.tab + S;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int i1 = jx[(c + 1) % 3], i2 = jx[(c + 2) % 3];
+        const float Ap = tA[i1], Bp = -1.0f * bn[c] * tG[i1];
+        const float Am = tA[i2], Bm = -1.0f * bn[c] * tG[i2];
+        const float m = aux[c];
+        const float pp = out[c] - m;
+        const float np = fmaf(Bp, pl[c], Ap * pp);
+        const float nm = fmaf(Bm, mi[c], Am * m);
+        out[c] = np + nm;
+        aux[c] = nm;
+    }
+    return true;
+}
+
+/* E_new of one element on plane gz: h = own H_new (x, y, z), hy0/hy2 = Hx/Hz at
+ * y+1, hz0/hz1 = Hx/Hy at z+1, nx1/nx2 = Hy/Hz at x+1; out = old total E in,
+ * new out.  Returns 0: plain, 1: aux written, 2: stable form (left to the
+ * fix-up kernel, nothing written). */
+__device__ __forceinline__ int zm_e_elem(const Fused32 &f, int b, int k, int gx, int gy, int gz, const float h[3],
+                                         float hy0, float hy2, float hz0, float hz1, float nx1, float nx2,
+                                         const float bn[3], float out[3], float aux[3])
+{
+    const P32 &p = f.p;
+    const Geo &g = p.g;
+    float pl[3], mi[3];
+    pl[0] = hy2 - h[2];
+    mi[0] = h[1] - hz1;
+    pl[1] = hz0 - h[0];
+    mi[1] = h[2] - nx2;
+    pl[2] = nx1 - h[1];
+    mi[2] = h[0] - hy0;
+    if (isnan(bn[0])) {
+        const int ridx = __float_as_int(bn[1]);
+        if (p.erec[ridx].kind == RK_STABLE) return 2;
+        float tmp[18];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            tmp[c] = pl[c];
+            tmp[3 + c] = mi[c];
+            tmp[6 + c] = out[c];
+        }
+        e_general(f, b, k, gx, gy, gz, ridx, tmp, tmp + 3, tmp + 6, tmp + 9, tmp + 12, tmp + 15);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            out[c] = tmp[9 + c];
+            aux[c] = tmp[12 + c];
+        }
+        return 1;
+    }
+    const int S = g.L0 + g.L1 + g.L2, s1 = g.L0, s2 = g.L0 + g.L1;
+    const bool split = p.pmask[gx] | p.pmask[s1 + gy] | p.pmask[s2 + gz];
+    if (!split) {
+        float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+        if (gz == p.s.iI[b]) {
+            const int px = gx + g.L0 * gy;
+            W[0] += (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, false, 1, px));
+            W[1] -= (float)(p.s.sgn[b] * sheet_f(p.s, g.pl, b, k, false, 0, px));
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) out[c] = fmaf(1.0f * bn[c], W[c], out[c]);
+        return 0;
+    }
+    const int jx[3] = {gx, s1 + gy, s2 + gz};
+    const float *tA = p.tab + 2 * S, *tG = p.tab + 3 * S;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int i1 = jx[(c + 1) % 3], i2 = jx[(c + 2) % 3];
+        const float Ap = tA[i1], Bp = 1.0f * bn[c] * tG[i1];
+        const float Am = tA[i2], Bm = 1.0f * bn[c] * tG[i2];
+        const float m = aux[c];
+        const float pp = out[c] - m;
+        const float np = fmaf(Bp, pl[c], Ap * pp);
+        const float nm = fmaf(Bm, mi[c], Am * m);
+        out[c] = np + nm;
+        aux[c] = nm;
+    }
+    return 1;
+}
+
+__global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constant__ Fused32T ft, const int rel)
+{
+    extern __shared__ __align__(128) float smem[];
+    const Fused32 &f = ft.f;
+    const P32 &p = f.p;
+    const Geo &g = p.g;
+    const ZSlot sl = zslot();
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem), *empty = full + ZNS;
+    float *slots = smem + 32;
+    float *hn = slots + ZNS * sl.size; /* [ZNH][3][ZNW+1][ZHX] */
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long n3 = g.n3, bs = 3 * n3, pl = g.pl;
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+    const int s2 = L0 + L1;
+    const int k = *p.s.base + rel;
+#define ZE(s, c, r, x) slots[(s) * sl.size + sl.e + ((c) * (ZNW + 2) + (r)) * ZEX + (x)]
+#define ZQ(s, seg, c, r, x) slots[(s) * sl.size + (seg) + ((c) * (ZNW + 1) + (r)) * ZQX + (x)]
+#define ZB(s, seg, c, r, x) slots[(s) * sl.size + (seg) + ((c) * ZNW + (r)) * ZTX + (x)]
+#define ZH(h, c, r, x) hn[(((h) * 3 + (c)) * (ZNW + 1) + (r)) * ZHX + (x)]
+    __shared__ volatile int zabort;
+    if (threadIdx.x == 0) {
+        zabort = 0;
+        for (int s = 0; s < ZNS; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], ZNW);
+        }
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    __syncthreads();
+
+    if (warp == ZNW) {
+        /* ---------------- producer: one lane issues every copy ---------------- */
+        if (lane != 0) return;
+        unsigned seq = 0, issued_to = 0;
+        for (int item = blockIdx.x; item < f.nitems && !zabort; item += gridDim.x) {
+            const ZItem it = zitem(f, item);
+            const bool tsplit = ztile_split(p, it.X0, it.Y0);
+            for (int zl = it.z0 - 1; zl <= it.z1 && !zabort; zl++, seq++) {
+                const int s = seq % ZNS;
+                if (seq >= ZNS && !zwait(&empty[s], ((seq / ZNS) - 1) & 1, &zabort, ft.err)) break;
+                issued_to = seq + 1;
+                const bool pre = zl < it.z0, first = zl == it.z0;
+                const bool zin = zl >= 0 && zl < L2, zpin = zl - 1 >= 0 && zl - 1 < L2;
+                const bool split = tsplit || (zin && p.pmask[s2 + zl]);
+                const bool bsplit = tsplit || (zpin && p.pmask[s2 + zl - 1]);
+                unsigned bytes = 4u * 3 * (ZNW + 2) * ZEX;
+                if (!pre) bytes += 4u * 3 * (ZNW + 1) * ZQX * (split ? 3 : 2);
+                if (!pre && !first) bytes += 4u * 3 * ZNW * ZTX * (bsplit ? 2 : 1);
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                mbar_expect(&full[s], bytes);
+                float *base = slots + s * sl.size;
+                /* out-of-range planes (-1, L2) read as zero: iBc[2] = 0 */
+                tma_load4(base + sl.e, &ft.mE, it.X0 - 4, it.Y0 - 1, zl, 3 * it.b, &full[s]);
+                if (pre) continue;
+                tma_load4(base + sl.qt, &ft.mH, it.X0, it.Y0, zl, 3 * it.b, &full[s]);
+                tma_load4(base + sl.qb, &ft.mBh, it.X0, it.Y0, zl, 0, &full[s]);
+                if (split) tma_load4(base + sl.qm, &ft.mHa, it.X0, it.Y0, zl, 3 * it.b, &full[s]);
+                if (first) continue;
+                tma_load4(base + sl.be, &ft.mBe, it.X0, it.Y0, zl - 1, 0, &full[s]);
+                if (bsplit) tma_load4(base + sl.bm, &ft.mEa, it.X0, it.Y0, zl - 1, 3 * it.b, &full[s]);
+            }
+        }
+        /* stay until every issued copy has landed (bounded, also after an abort) */
+        for (unsigned q = (issued_to > ZNS ? issued_to - ZNS : 0); q < issued_to; q++)
+            mbar_wait(&full[q % ZNS], (q / ZNS) & 1);
+        return;
+    }
+
+    /* ---------------- consumers: warp = tile row, lane = four x-cells ---------------- */
+    unsigned seq = 0;
+    const int cx = 4 * lane; /* first column of the lane's quad in the tile */
+    for (int item = blockIdx.x; item < f.nitems; item += gridDim.x) {
+        const ZItem it = zitem(f, item);
+        const int b = it.b;
+        const int gy = it.Y0 + warp, gx0 = it.X0 + cx;
+        const bool live = gy < L1 && gx0 < L0;
+        const bool tsplit = ztile_split(p, it.X0, it.Y0);
+        float *Hn = f.Hn + b * bs, *Han = f.Han + b * bs, *En = f.En + b * bs, *Ean = f.Ean + b * bs;
+        float eprev[3][4]; /* old E of the previous plane, own quad */
+        float hprev[3][4]; /* new H of the previous plane, own quad */
+        for (int zl = it.z0 - 1; zl <= it.z1; zl++, seq++) {
+            const int s = seq % ZNS, sp = (seq + ZNS - 1) % ZNS;
+            /* after an abort the data are garbage but control flow stays uniform */
+            zwait(&full[s], (seq / ZNS) & 1, &zabort, ft.err);
+            __syncwarp();
+            if (zl < it.z0) { /* the pre-plane: own old E of plane z0-1 */
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const float4 v = lds4(&ZE(s, c, warp + 1, cx + 4));
+                    eprev[c][0] = v.x, eprev[c][1] = v.y, eprev[c][2] = v.z, eprev[c][3] = v.w;
+                }
+                continue;
+            }
+            const int z = zl, hz = (z - it.z0) % ZNH, hzp = (z - it.z0 + ZNH - 1) % ZNH;
+            const bool zsplit = tsplit || (z < L2 && p.pmask[s2 + z]);
+            /* ---- phase A: H_new(z), own quad ---- */
+            float hnew[3][4], ecur[3][4];
+            {
+                float e[3][4], ey[3][4], hq[3][4], bq[3][4], mq[3][4];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const float4 v = lds4(&ZE(s, c, warp + 1, cx + 4));
+                    e[c][0] = v.x, e[c][1] = v.y, e[c][2] = v.z, e[c][3] = v.w;
+                    const float4 u = lds4(&ZE(s, c, warp, cx + 4));
+                    ey[c][0] = u.x, ey[c][1] = u.y, ey[c][2] = u.z, ey[c][3] = u.w;
+                    const float4 hh = lds4(&ZQ(s, sl.qt, c, warp, cx));
+                    hq[c][0] = hh.x, hq[c][1] = hh.y, hq[c][2] = hh.z, hq[c][3] = hh.w;
+                    const float4 bb = lds4(&ZQ(s, sl.qb, c, warp, cx));
+                    bq[c][0] = bb.x, bq[c][1] = bb.y, bq[c][2] = bb.z, bq[c][3] = bb.w;
+                    if (zsplit) {
+                        const float4 mm = lds4(&ZQ(s, sl.qm, c, warp, cx));
+                        mq[c][0] = mm.x, mq[c][1] = mm.y, mq[c][2] = mm.z, mq[c][3] = mm.w;
+                    } else {
+                        mq[c][0] = mq[c][1] = mq[c][2] = mq[c][3] = 0.0f;
+                    }
+                }
+                const float xm1 = ZE(s, 1, warp + 1, cx + 3), xm2 = ZE(s, 2, warp + 1, cx + 3);
+                bool wa = false;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float h3[3] = {e[0][i], e[1][i], e[2][i]};
+                    const float bn[3] = {bq[0][i], bq[1][i], bq[2][i]};
+                    float out[3] = {hq[0][i], hq[1][i], hq[2][i]}, aux[3] = {mq[0][i], mq[1][i], mq[2][i]};
+                    const float nx1 = i == 0 ? xm1 : e[1][i - 1], nx2 = i == 0 ? xm2 : e[2][i - 1];
+                    if (live && z < L2) /* elsewhere zero: inputs are zero-filled and iBc = 0 */
+                        wa |= zm_h_elem(f, b, k, gx0 + i, gy, z, h3, ey[0][i], ey[2][i], eprev[0][i], eprev[1][i],
+                                        nx1, nx2, bn, out, aux);
+                    else
+                        out[0] = out[1] = out[2] = aux[0] = aux[1] = aux[2] = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        hnew[c][i] = out[c];
+                        mq[c][i] = aux[c];
+                        ecur[c][i] = e[c][i];
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    *reinterpret_cast<float4 *>(&ZH(hz, c, warp, cx)) =
+                        make_float4(hnew[c][0], hnew[c][1], hnew[c][2], hnew[c][3]);
+                if (live && z < it.z1) {
+                    const long long gi = gx0 + (long long)L0 * gy + pl * z;
+#pragma unroll
+                    for (int c = 0; c < 3; c++)
+                        *reinterpret_cast<float4 *>(Hn + c * n3 + gi) =
+                            make_float4(hnew[c][0], hnew[c][1], hnew[c][2], hnew[c][3]);
+                    if (wa) {
+#pragma unroll
+                        for (int c = 0; c < 3; c++)
+                            *reinterpret_cast<float4 *>(Han + c * n3 + gi) =
+                                make_float4(mq[c][0], mq[c][1], mq[c][2], mq[c][3]);
+                    }
+                    const int q = mon_index(p.d, z);
+                    if (q >= 0) {
+                        const int px = gx0 + L0 * gy;
+                        *reinterpret_cast<float4 *>(ring_ptr(p.d, g.pl, b, k, q, 0) + px) =
+                            make_float4(hnew[0][0], hnew[0][1], hnew[0][2], hnew[0][3]);
+                        *reinterpret_cast<float4 *>(ring_ptr(p.d, g.pl, b, k, q, 1) + px) =
+                            make_float4(hnew[1][0], hnew[1][1], hnew[1][2], hnew[1][3]);
+                    }
+                }
+            }
+            /* halo H_new: row ZNW (x = X0 + 4j .. +3 for the warp's 8 lanes) and
+             * column ZTX (rows 0..ZNW, by lanes 8..8+ZNW of the last warp) */
+            if (lane < 8 || (warp == ZNW - 1 && lane < 9 + ZNW)) {
+                const bool row = lane < 8;
+                const int nq = row ? 4 : 1;
+                const int r = row ? ZNW : lane - 8;
+                const int c0 = row ? 32 * warp + 4 * lane : ZTX;
+                for (int i = 0; i < nq; i++) {
+                    const int cxh = c0 + i, hx = it.X0 + cxh, hy = it.Y0 + r;
+                    const float h3[3] = {ZE(s, 0, r + 1, cxh + 4), ZE(s, 1, r + 1, cxh + 4), ZE(s, 2, r + 1, cxh + 4)};
+                    const float bn[3] = {ZQ(s, sl.qb, 0, r, cxh), ZQ(s, sl.qb, 1, r, cxh), ZQ(s, sl.qb, 2, r, cxh)};
+                    float out[3] = {ZQ(s, sl.qt, 0, r, cxh), ZQ(s, sl.qt, 1, r, cxh), ZQ(s, sl.qt, 2, r, cxh)};
+                    float aux[3] = {0.0f, 0.0f, 0.0f};
+                    if (zsplit) {
+                        aux[0] = ZQ(s, sl.qm, 0, r, cxh);
+                        aux[1] = ZQ(s, sl.qm, 1, r, cxh);
+                        aux[2] = ZQ(s, sl.qm, 2, r, cxh);
+                    }
+                    if (hx < L0 && hy < L1 && z < L2) {
+                        zm_h_elem(f, b, k, hx, hy, z, h3, ZE(s, 0, r, cxh + 4), ZE(s, 2, r, cxh + 4),
+                                  ZE(sp, 0, r + 1, cxh + 4), ZE(sp, 1, r + 1, cxh + 4), ZE(s, 1, r + 1, cxh + 3),
+                                  ZE(s, 2, r + 1, cxh + 3), bn, out, aux);
+                    } else { /* outside the grid: iBc = 0 makes the neighbour zero */
+                        out[0] = out[1] = out[2] = 0.0f;
+                    }
+                    ZH(hz, 0, r, cxh) = out[0];
+                    ZH(hz, 1, r, cxh) = out[1];
+                    ZH(hz, 2, r, cxh) = out[2];
+                }
+            }
+            named_bar(1, 32 * ZNW);
+            /* the previous plane's slot is no longer read */
+            if (lane == 0) mbar_arrive(&empty[sp]);
+            /* ---- phase B: E_new(z-1), own quad ---- */
+            if (z > it.z0) {
+                const int ze = z - 1;
+                float hy[3][4], bq[3][4], mq[3][4];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const float4 u = lds4(&ZH(hzp, c, warp + 1, cx));
+                    hy[c][0] = u.x, hy[c][1] = u.y, hy[c][2] = u.z, hy[c][3] = u.w;
+                    const float4 bb = lds4(&ZB(s, sl.be, c, warp, cx));
+                    bq[c][0] = bb.x, bq[c][1] = bb.y, bq[c][2] = bb.z, bq[c][3] = bb.w;
+                    const bool bsplit = tsplit || p.pmask[s2 + ze];
+                    if (bsplit) {
+                        const float4 mm = lds4(&ZB(s, sl.bm, c, warp, cx));
+                        mq[c][0] = mm.x, mq[c][1] = mm.y, mq[c][2] = mm.z, mq[c][3] = mm.w;
+                    } else {
+                        mq[c][0] = mq[c][1] = mq[c][2] = mq[c][3] = 0.0f;
+                    }
+                }
+                const float xp1 = ZH(hzp, 1, warp, cx + 4), xp2 = ZH(hzp, 2, warp, cx + 4);
+                float eo[3][4];
+                int wa = 0, stable = 0;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float h3[3] = {hprev[0][i], hprev[1][i], hprev[2][i]};
+                    const float bn[3] = {bq[0][i], bq[1][i], bq[2][i]};
+                    float out[3] = {eprev[0][i], eprev[1][i], eprev[2][i]}, aux[3] = {mq[0][i], mq[1][i], mq[2][i]};
+                    const float nx1 = i == 3 ? xp1 : hprev[1][i + 1], nx2 = i == 3 ? xp2 : hprev[2][i + 1];
+                    const int r = live ? zm_e_elem(f, b, k, gx0 + i, gy, ze, h3, hy[0][i], hy[2][i], hnew[0][i],
+                                                   hnew[1][i], nx1, nx2, bn, out, aux)
+                                       : 0;
+                    wa |= r == 1;
+                    stable |= (r == 2) << i;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        eo[c][i] = out[c];
+                        mq[c][i] = aux[c];
+                    }
+                }
+                if (live) {
+                    const long long gi = gx0 + (long long)L0 * gy + pl * ze;
+                    if (!stable) {
+#pragma unroll
+                        for (int c = 0; c < 3; c++)
+                            *reinterpret_cast<float4 *>(En + c * n3 + gi) =
+                                make_float4(eo[c][0], eo[c][1], eo[c][2], eo[c][3]);
+                        if (wa) {
+#pragma unroll
+                            for (int c = 0; c < 3; c++)
+                                *reinterpret_cast<float4 *>(Ean + c * n3 + gi) =
+                                    make_float4(mq[c][0], mq[c][1], mq[c][2], mq[c][3]);
+                        }
+                    } else { /* element-wise: stable-form cells are left to k_fix_stable32 */
+                        for (int i = 0; i < 4; i++) {
+                            if ((stable >> i) & 1) continue;
+                            for (int c = 0; c < 3; c++) {
+                                En[c * n3 + gi + i] = eo[c][i];
+                                if (wa) Ean[c * n3 + gi + i] = mq[c][i];
+                            }
+                        }
+                    }
+                    const int q = mon_index(p.d, ze);
+                    if (q >= 0) {
+                        const int px = gx0 + L0 * gy;
+                        for (int i = 0; i < 4; i++) {
+                            if ((stable >> i) & 1) continue;
+                            ring_ptr(p.d, g.pl, b, k, q, 2)[px + i] = eo[0][i];
+                            ring_ptr(p.d, g.pl, b, k, q, 3)[px + i] = eo[1][i];
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    eprev[c][i] = ecur[c][i];
+                    hprev[c][i] = hnew[c][i];
+                }
+        }
+        /* every warp is done with this item's H_new planes before the next item
+         * writes them; then the item's last slot is free */
+        named_bar(1, 32 * ZNW);
+        if (lane == 0) mbar_arrive(&empty[(seq + ZNS - 1) % ZNS]);
+    }
+#undef ZE
+#undef ZQ
+#undef ZB
+#undef ZH
+}
+
+int zm32_max_ctas_per_sm()
+{
+    int n = 0;
+    const size_t sm = zm32_smem();
+    cudaFuncSetAttribute(k_zm32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_zm32, 32 * (ZNW + 1), sm) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+void launch_zm32(const Fused32T &ft, int rel, int grid, cudaStream_t st)
+{
+    const size_t sm = zm32_smem();
+    k_zm32<<<grid, 32 * (ZNW + 1), sm, st>>>(ft, rel);
+    if (ft.f.nstable > 0) {
+        dim3 g2((ft.f.nstable + 127) / 128, ft.f.p.batch);
+        k_fix_stable32<<<g2, 128, 0, st>>>(ft.f, rel);
+    }
+}
+
+} // namespace smat

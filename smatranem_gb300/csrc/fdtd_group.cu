@@ -1,13 +1,18 @@
 /*
  * Groups: many structures of uneven size (each an FP32 plan with its own batch
- * of excitations) advanced together, one launch per sweep for all of them.
+ * of excitations) advanced together, one CUDA graph launch per 32 steps.
  *
  * The reference runs one structure per process (FDTDcalc/FDTDsplitfieldMetal.c
  * main); an S-matrix sweep over a family of structures is a loop of such
  * runs.  Here the member plans keep their own device state, schedule, sources
- * and DFT; the group only replaces their per-step launches by grouped ones
- * (k_group32v) and flushes each member's DFT ring.  Member results are
- * bit-identical to stepping each plan alone with the vectorised sweeps.
+ * and DFT; the group replaces their per-step launches, in one of two modes:
+ *   0: one grouped launch per sweep over the cells of every member
+ *      (k_group32v: a block finds its member by prefix sums);
+ *   1: each member's own vectorised-sweep launches, back to back on the
+ *      group's stream;
+ * either way captured as one CUDA graph per 32 steps, with each member's DFT
+ * ring flushed in it.  Member results are bit-identical to stepping each
+ * plan alone with the vectorised sweeps.
  */
 #include <cuda_runtime.h>
 
@@ -22,6 +27,7 @@ using namespace smat::plan;
 struct smat_fdtd_group {
     std::vector<smat_fdtd_plan *> m;
     cudaStream_t stream = nullptr;
+    int mode = 0; /* 0: one grouped launch per sweep; 1: each member's own sweep launches */
     int by = 1;
     cudaGraphExec_t graph = nullptr;
     bool graph_failed = false;
@@ -60,8 +66,24 @@ Group32 make_group(const smat_fdtd_group *g)
 /* steps rel0 .. rel0+n-1 of every member (relative to each member's d_base) */
 void enqueue_group(smat_fdtd_group *g, int rel0, int n)
 {
-    const Group32 gr = make_group(g);
-    for (int i = 0; i < n; i++) launch_group32v(gr, rel0 + i, g->stream);
+    if (g->mode == 0) {
+        const Group32 gr = make_group(g);
+        for (int i = 0; i < n; i++) launch_group32v(gr, rel0 + i, g->stream);
+    } else {
+        /* each member's own vectorised sweeps (rows g->by, whole grid), in
+         * order on the group's stream: one graph launch per chunk of steps */
+        for (int i = 0; i < n; i++)
+            for (smat_fdtd_plan *p : g->m) {
+                const int by = p->by32, szc = p->szc, fu = p->fused;
+                p->by32 = g->by;
+                p->szc = 0;
+                p->fused = 2;
+                sweep_step(p, make_p32(p, false), rel0 + i, g->stream);
+                p->by32 = by;
+                p->szc = szc;
+                p->fused = fu;
+            }
+    }
     for (smat_fdtd_plan *p : g->m) launch_flush32(make_p32(p, false), rel0 + n, n, g->stream);
 }
 
@@ -135,10 +157,13 @@ extern "C" int smat_fdtd_group_destroy(smat_fdtd_group *g)
     return SMAT_OK;
 }
 
-extern "C" int smat_fdtd_group_set_tuning(smat_fdtd_group *g, int block_y)
+extern "C" int smat_fdtd_group_set_tuning(smat_fdtd_group *g, int mode, int block_y)
 {
     smat_clear_error();
-    if (!g || block_y < 1 || block_y > 4) return smat_fail(SMAT_EINVAL, "group_set_tuning: block_y in 1..4");
+    if (!g || mode < 0 || mode > 1 || block_y < 1 || block_y > 4)
+        return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 0 (one launch per sweep) or 1 (members' own "
+                                      "launches), block_y in 1..4");
+    g->mode = mode;
     g->by = block_y;
     drop_group_graph(g);
     return SMAT_OK;
@@ -189,10 +214,10 @@ extern "C" int smat_fdtd_group_sync(smat_fdtd_group *g)
     return SMAT_OK;
 }
 
-/* Times each block_y over nsteps steps and keeps the fastest.  Like the plan
+/* Times each mode and block_y over nsteps steps and keeps the fastest.  Like the plan
  * autotuner it needs every member at the zero state and runs with sources and
  * DFT sampling off, so the members are left as they were. */
-extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int *best_by, double *best_ms)
+extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best[2], double *best_ms)
 {
     smat_clear_error();
     if (!g || nsteps < 1) return smat_fail(SMAT_EINVAL, "group_autotune: bad arguments");
@@ -215,21 +240,24 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int *bes
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     double bms = 1e30;
-    int bby = g->by;
-    for (int by : {1, 2, 4}) {
-        g->by = by;
-        enqueue_group(g, 0, 1);
-        CK(cudaEventRecord(e0, g->stream));
-        enqueue_group(g, 0, nsteps);
-        CK(cudaEventRecord(e1, g->stream));
-        CK(cudaEventSynchronize(e1));
-        float ms = 0;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < bms) {
-            bms = ms;
-            bby = by;
+    int bmode = g->mode, bby = g->by;
+    for (int mode : {0, 1})
+        for (int by : {1, 2, 4}) {
+            g->mode = mode;
+            g->by = by;
+            enqueue_group(g, 0, 1);
+            CK(cudaEventRecord(e0, g->stream));
+            enqueue_group(g, 0, nsteps);
+            CK(cudaEventRecord(e1, g->stream));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < bms) {
+                bms = ms;
+                bmode = mode;
+                bby = by;
+            }
         }
-    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     for (size_t i = 0; i < g->m.size(); i++) {
@@ -238,9 +266,13 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int *bes
         CK(cudaMemcpyAsync(p->d_iI, p->h_iI.data(), sizeof(int) * p->batch, cudaMemcpyHostToDevice, g->stream));
     }
     CK(cudaStreamSynchronize(g->stream));
+    g->mode = bmode;
     g->by = bby;
     drop_group_graph(g);
-    if (best_by) *best_by = bby;
+    if (best) {
+        best[0] = bmode;
+        best[1] = bby;
+    }
     if (best_ms) *best_ms = bms / nsteps;
     return SMAT_OK;
 }

@@ -166,6 +166,10 @@ int pipe32v_max_ctas_per_sm(int threads);
 void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);
 size_t fused32_smem(int ty, int ns);
 void launch_fused32t(const Fused32T &f, int rel, int grid, cudaStream_t st);
+/* kernel 5: 128 x 4 tiles, TMA producer warp (plans with iBc = 0 only) */
+void launch_zm32(const Fused32T &f, int rel, int grid, cudaStream_t st);
+size_t zm32_smem();
+int zm32_max_ctas_per_sm();
 size_t fused32t_smem(int ty, int ns);
 int fused32t_max_ctas_per_sm(int ty, int ns);
 int fused32_max_ctas_per_sm(int ty, int ns);

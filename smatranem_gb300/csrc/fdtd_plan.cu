@@ -205,10 +205,50 @@ Fused32T make_fused_t(const smat_fdtd_plan *p, bool xp)
     return ft;
 }
 
+/* kernel 5: tile 128 x 4, tensor maps with its box sizes */
+int build_zmaps(smat_fdtd_plan *p)
+{
+    if (p->zmaps) return SMAT_OK;
+    const int nw = 3 * p->batch;
+    float *sets[2][4] = {{p->d_E32, p->d_H32, p->d_Ea32, p->d_Ha32}, {p->d_E32b, p->d_H32b, p->d_Ea32b, p->d_Ha32b}};
+    int rc = SMAT_OK;
+    for (int st = 0; st < 2 && !rc; st++) {
+        rc = encode_map(&p->zmap[st][0], sets[st][0], p->L, nw, 136, 6);
+        if (!rc) rc = encode_map(&p->zmap[st][1], sets[st][1], p->L, nw, 132, 5);
+        if (!rc) rc = encode_map(&p->zmap[st][2], sets[st][2], p->L, nw, 128, 4);
+        if (!rc) rc = encode_map(&p->zmap[st][3], sets[st][3], p->L, nw, 132, 5);
+    }
+    if (!rc) rc = encode_map(&p->zmap_bh, p->d_bh, p->L, 3, 132, 5);
+    if (!rc) rc = encode_map(&p->zmap_be, p->d_be, p->L, 3, 128, 4);
+    if (!rc) p->zmaps = true;
+    return rc;
+}
+
+Fused32T make_zm(const smat_fdtd_plan *p, bool xp)
+{
+    Fused32T ft;
+    ft.f = make_fused(p, xp);
+    ft.f.ty = 4;
+    ft.f.ntx = (p->L[0] + 127) / 128;
+    ft.f.nty = (p->L[1] + 3) / 4;
+    ft.f.nitems = p->batch * ft.f.ntx * ft.f.nty * ft.f.nzc;
+    const int st = p->cur;
+    ft.mE = p->zmap[st][0];
+    ft.mH = p->zmap[st][1];
+    ft.mEa = p->zmap[st][2];
+    ft.mHa = p->zmap[st][3];
+    ft.mBh = p->zmap_bh;
+    ft.mBe = p->zmap_be;
+    ft.err = p->d_err;
+    return ft;
+}
+
 int fused_grid(smat_fdtd_plan *p, const Fused32 &f)
 {
     if (p->max_ctas < 0)
-        p->max_ctas = p->fused == 3 ? fused32t_max_ctas_per_sm(p->ty, p->ns) : fused32_max_ctas_per_sm(p->ty, p->ns);
+        p->max_ctas = p->fused == 5   ? zm32_max_ctas_per_sm()
+                      : p->fused == 3 ? fused32t_max_ctas_per_sm(p->ty, p->ns)
+                                      : fused32_max_ctas_per_sm(p->ty, p->ns);
     const int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm : (p->max_ctas > 0 ? p->max_ctas : 1);
     const long long g = (long long)per_sm * sm_count();
     return (int)(g < f.nitems ? g : f.nitems);
@@ -238,6 +278,13 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
             p->cur ^= 1;
         }
         launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
+    } else if (p->fused == 5) {
+        for (int i = 0; i < n; i++) {
+            const Fused32T ft = make_zm(p, xp);
+            launch_zm32(ft, rel0 + i, fused_grid(p, ft.f), p->stream);
+            p->cur ^= 1;
+        }
+        launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
     } else if (p->fused == 4) {
         const P32 q = make_p32(p, xp);
         const Pipe32 pp = make_pipe(p);
@@ -245,7 +292,7 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
         launch_flush32(q, rel0 + n, n, p->stream);
     } else {
         const P32 q = make_p32(p, xp);
-        for (int i = 0; i < n; i++) sweep_step(p, q, rel0 + i);
+        for (int i = 0; i < n; i++) sweep_step(p, q, rel0 + i, p->stream);
         launch_flush32(q, rel0 + n, n, p->stream);
     }
 }
@@ -326,7 +373,7 @@ int setup_pipe(smat_fdtd_plan *p, int by, int lag)
  * the plane above, H of a plane needs E_old of the plane below, and both
  * still hold at every chunk boundary.  A chunk small enough to stay in L2
  * lets the E sweep read E_old and H_new from L2 rather than HBM. */
-void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel)
+void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel, cudaStream_t st)
 {
     const int L2 = p->L[2];
     /* a stable-form E cell at z = 0 reads the new H of plane L2-1 through a
@@ -337,13 +384,13 @@ void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel)
         const int z1 = z0 + zc < L2 ? z0 + zc : L2;
         const int e0 = z0 == 0 ? 0 : z0 - 1, e1 = z1 == L2 ? L2 : z1 - 1;
         if (p->fused == 2) {
-            launch_h32v(q, rel, p->by32, z0, z1, p->d_hgen + p->hgen_z[z0], p->hgen_z[z1] - p->hgen_z[z0], p->stream);
+            launch_h32v(q, rel, p->by32, z0, z1, p->d_hgen + p->hgen_z[z0], p->hgen_z[z1] - p->hgen_z[z0], st);
             if (e1 > e0)
                 launch_e32v(q, rel, p->by32, e0, e1, p->d_egen + p->egen_z[e0], p->egen_z[e1] - p->egen_z[e0],
-                            p->stream);
+                            st);
         } else {
-            launch_h32(q, rel, p->by32, z0, z1, p->stream);
-            if (e1 > e0) launch_e32(q, rel, p->by32, e0, e1, p->stream);
+            launch_h32(q, rel, p->by32, z0, z1, st);
+            if (e1 > e0) launch_e32(q, rel, p->by32, e0, e1, st);
         }
     }
 }
@@ -1034,7 +1081,8 @@ extern "C" int smat_fdtd_run(smat_fdtd_plan *p, int k_begin, int k_end)
     if (k_end > p->nsched) return smat_fail(SMAT_EINVAL, "run: k_end %d beyond the %d-step schedule", k_end, p->nsched);
     launch_set(p->d_base, k_begin, p->stream);
     int n = k_end - k_begin;
-    if (p->precision == SMAT_FP32 && (p->fused == 1 || p->fused == 3) && p->cur != 0 && n >= GRAPH_STEPS + 1) {
+    if (p->precision == SMAT_FP32 && (p->fused == 1 || p->fused == 3 || p->fused == 5) && p->cur != 0 &&
+        n >= GRAPH_STEPS + 1) {
         /* graphs are captured from field set 0: take one step to get there */
         enqueue_steps(p, 0, 1, false);
         launch_bump(p->d_base, 1, p->stream);
@@ -1083,10 +1131,14 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
             const Fused32T ft = make_fused_t(p, false);
             launch_fused32t(ft, i, fused_grid(p, ft.f), p->stream);
             p->cur ^= 1;
+        } else if (p->fused == 5) {
+            const Fused32T ft = make_zm(p, false);
+            launch_zm32(ft, i, fused_grid(p, ft.f), p->stream);
+            p->cur ^= 1;
         } else if (p->fused == 4) {
             launch_pipe32v(q32, i, make_pipe(p), p->pipe_grid, p->stream);
         } else if (p->szc > 0 && p->szc < p->L[2]) {
-            sweep_step(p, q32, i); /* chunked sweeps: the whole step in ms[0] */
+            sweep_step(p, q32, i, p->stream); /* chunked sweeps: the whole step in ms[0] */
         } else if (p->fused == 2) {
             launch_h32v(q32, i, p->by32, 0, p->L[2], p->d_hgen, p->nhgen, p->stream);
         } else {
@@ -1124,9 +1176,22 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
 {
     smat_clear_error();
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
-    if (fused < 0 || fused > 4)
+    if (fused < 0 || fused > 5)
         return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps), 3 (fused, TMA), "
-                                      "4 (pipelined vector sweeps)");
+                                      "4 (pipelined vector sweeps), 5 (fused, 128x4 tiles, TMA producer warp)");
+    if (fused == 5) {
+        if (p->L[0] % 4 != 0 || p->iBc[0] != 0 || p->iBc[1] != 0 || p->iBc[2] != 0 || z_chunk < 1)
+            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 5 needs L0 %% 4 == 0, iBc = (0,0,0) and z_chunk >= 1");
+        if (zm32_max_ctas_per_sm() < 1) return smat_fail(SMAT_ECUDA, "set_tuning: kernel 5 does not fit an SM");
+        int rc = build_zmaps(p);
+        if (rc) return rc;
+        p->zc = z_chunk;
+        p->ctas_per_sm = 1;
+        p->max_ctas = 1;
+        p->fused = 5;
+        drop_graph(p);
+        return SMAT_OK;
+    }
     if (fused == 4) {
         const int lag = z_chunk;
         if (p->L[0] % 4 != 0 || tile_y < 1 || tile_y > p->L[1] || ctas_per_sm < 0 || lag < 0 || lag == 1 ||
@@ -1204,6 +1269,13 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
                 if (zc < L2) cands.push_back({2, by, zc, 0, 4});
         cands.push_back({2, 4, 0, 0, 4});
     }
+    if (p->L[0] % 4 == 0 && p->iBc[0] == 0 && p->iBc[1] == 0 && p->iBc[2] == 0)
+        for (int zc : {20, 40, 80, 1 << 20}) {
+            const int z = zc > L2 ? L2 : zc;
+            bool dup = false;
+            for (auto &c : cands) dup |= c.fused == 5 && c.zc == z;
+            if (!dup) cands.push_back({5, 4, z, 1, 4});
+        }
     if (p->L[0] % 4 == 0 && !(p->nstable > 0 && p->iBc[2] != 0))
         for (int rows : {2, 4, 8})
             for (int lag : {0, 4, 8})
@@ -1279,8 +1351,8 @@ extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
 {
     if (!p || !out) return smat_fail(SMAT_EINVAL, "get_tuning: bad arguments");
     out[0] = p->fused;
-    out[1] = (p->fused == 1 || p->fused == 3) ? p->ty : p->fused == 4 ? p->pipe_by : p->by32;
-    out[2] = (p->fused == 1 || p->fused == 3) ? p->zc : p->fused == 4 ? p->pipe_lag : p->szc;
+    out[1] = (p->fused == 1 || p->fused == 3) ? p->ty : p->fused == 4 ? p->pipe_by : p->fused == 5 ? 4 : p->by32;
+    out[2] = (p->fused == 1 || p->fused == 3 || p->fused == 5) ? p->zc : p->fused == 4 ? p->pipe_lag : p->szc;
     out[3] = p->ctas_per_sm;
     out[4] = p->ns;
     return SMAT_OK;

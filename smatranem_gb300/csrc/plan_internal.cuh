@@ -115,6 +115,8 @@ struct smat_fdtd_plan {
     int max_ctas = -1; /* cached occupancy of the current configuration */
     /* TMA tensor maps (kernel 3), built for tile rows tma_ty: [set][E, H, Ea, Ha], bh, be */
     CUtensorMap tmap[2][4], tmap_bh, tmap_be;
+    CUtensorMap zmap[2][4], zmap_bh, zmap_be; /* kernel 5: boxes 136x6 (E), 132x5 (H side), 128x4 (E side) */
+    bool zmaps = false;
     int tma_ty = -1;
     int *d_err = nullptr; /* device pipeline error flag */
     int by32 = 8;
@@ -143,7 +145,7 @@ P64 make_p64(const smat_fdtd_plan *p, bool xp);
 P32 make_p32(const smat_fdtd_plan *p, bool xp);
 /* the launches of steps rel0 .. rel0+n-1 relative to *d_base (no bump) */
 void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp);
-void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel);
+void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel, cudaStream_t st);
 Pipe32 make_pipe(const smat_fdtd_plan *p);
 int setup_pipe(smat_fdtd_plan *p, int by, int lag);
 int pipe_nxw(int L0);

@@ -83,7 +83,7 @@ def lib():
         L.smat_fdtd_adjoint_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P]
         L.smat_fdtd_group_create.argtypes = [_P, C.c_int, _P]
         L.smat_fdtd_group_destroy.argtypes = [_P]
-        L.smat_fdtd_group_set_tuning.argtypes = [_P, C.c_int]
+        L.smat_fdtd_group_set_tuning.argtypes = [_P, C.c_int, C.c_int]
         L.smat_fdtd_group_autotune.argtypes = [_P, C.c_int, _P, _P]
         L.smat_fdtd_group_run.argtypes = [_P, C.c_int, C.c_int]
         L.smat_fdtd_group_sync.argtypes = [_P]
@@ -408,13 +408,15 @@ class Group:
     def __exit__(self, *a):
         self.close()
 
-    def set_tuning(self, block_y):
-        _check(lib().smat_fdtd_group_set_tuning(self._h, block_y))
+    def set_tuning(self, mode, block_y):
+        """mode 0: one grouped launch per sweep; 1: members' own launches."""
+        _check(lib().smat_fdtd_group_set_tuning(self._h, mode, block_y))
 
     def autotune(self, nsteps=4):
-        by, ms = C.c_int(0), C.c_double(0)
-        _check(lib().smat_fdtd_group_autotune(self._h, nsteps, C.byref(by), C.byref(ms)))
-        return by.value, ms.value
+        """((mode, block_y), ms per step) of the fastest form."""
+        best, ms = (C.c_int * 2)(), C.c_double(0)
+        _check(lib().smat_fdtd_group_autotune(self._h, nsteps, best, C.byref(ms)))
+        return (best[0], best[1]), ms.value
 
     def run(self, k_begin, k_end, sync=True):
         _check(lib().smat_fdtd_group_run(self._h, k_begin, k_end))

@@ -35,8 +35,8 @@ def _result(p, batch):
     return [(*p.get_fields(b), *[p.get_dft(b, 0, q) for q in range(3)]) for b in range(batch)]
 
 
-@pytest.mark.parametrize("block_y", [1, 2, 4])
-def test_group_members_match_plans_stepped_alone(built, block_y):
+@pytest.mark.parametrize("mode,block_y", [(0, 1), (0, 2), (0, 4), (1, 1), (1, 2)])
+def test_group_members_match_plans_stepped_alone(built, mode, block_y):
     from smatranem_gb300 import fdtd as f
     from smatranem_gb300 import workloads as W
     nsteps = 60  # windows of 20 and 40 steps: the second holds a captured 32-step chunk
@@ -56,7 +56,7 @@ def test_group_members_match_plans_stepped_alone(built, block_y):
     plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
     try:
         with f.Group(plans) as g:
-            g.set_tuning(block_y)
+            g.set_tuning(mode, block_y)
             g.run(0, 20)
             g.run(20, nsteps)
         for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
@@ -82,8 +82,8 @@ def test_group_autotune_and_errors(built):
                           precision=f.FP64) as p64:
         p.set_schedule(src, planes=(iBTIin[0], iBTIin[1]), phase=ph)
         with f.Group([p]) as g:
-            by, ms = g.autotune(2)
-            assert by in (1, 2, 4) and ms > 0
+            (mode, by), ms = g.autotune(2)
+            assert mode in (0, 1) and by in (1, 2, 4) and ms > 0
             assert p.check_finite() == (True, 0.0)  # left at the zero state
             with pytest.raises(f.FdtdError):
                 g.run(0, src.shape[0] + 1)  # beyond the schedule

@@ -316,6 +316,8 @@ FUSED_CASES = [
     ((40, 17, 19, 3), 22, dict(pml=(4, 4, 4), lossy=0.05, iBc=(1, 1, -1)), (5, 13, 7, -1)),
     ((33, 9, 12, 2), 23, dict(pml=(0, 0, 2), pml_z_only=True, iBc=(0, -1, 0)), (3, 8, 5, 1)),
     ((64, 24, 20, 3), 24, dict(pml=(5, 5, 4), metals=0.02, iBc=(0, 0, 0)), (5, 14, 7, 1)),
+    # partial 128 x 4 tiles in x and y (kernel 5), lossy and PEC records
+    ((136, 13, 17, 2), 25, dict(pml=(4, 3, 3), lossy=0.05, pec=0.03, iBc=(0, 0, 0)), (4, 12, 6, 1)),
 ]
 TUNINGS = [(1, 8, 40, 0, 5), (1, 4, 5, 0, 4), (1, 2, 3, 1, 6), (1, 8, 7, 1, 6), (1, 3, 1, 0, 5), (1, 2, 2, 0, 4)]
 
@@ -358,6 +360,8 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     if L[0] % 4 == 0:
         tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (2, 4, 3, 0, 4), (2, 1, 5, 0, 4), (2, 2, 16, 0, 4),
                     (3, 8, 40, 0, 5), (3, 4, 5, 0, 4), (3, 2, 3, 1, 6), (3, 4, 1, 0, 5), (3, 8, 7, 1, 6)]
+        if tuple(kw["iBc"]) == (0, 0, 0):  # 128 x 4 tiles with a TMA producer warp (kernel 5)
+            tunings += [(5, 4, 40, 1, 4), (5, 4, 5, 1, 4), (5, 4, 1, 1, 4), (5, 4, 7, 1, 4)]
         if not (kw.get("metals") and kw["iBc"][2] != 0):  # pipelined sweeps (kernel 4)
             # (4, rows per item, lag (0: none), ctas_per_sm, -)
             tunings += [(4, 1, 0, 0, 0), (4, 2, 2, 0, 0), (4, 5, 3, 1, 0), (4, 3, L[2], 0, 0), (4, L[1], 0, 0, 0)]
