@@ -450,8 +450,11 @@ __device__ __forceinline__ void sweep32v_quad(const P32 &p, const int rel, const
     }
 }
 
-template <bool EF>
-__global__ void __launch_bounds__(128, 5) k_sweep32v(const P32 p, const int rel, const int z0)
+/* MB: the register bound, as a minimum of resident 128-thread blocks per SM
+ * (5: 96 registers, no spill; 6, 8: 80, 64 registers, more warps in flight
+ * against a few spilled values) -- chosen by the autotuner */
+template <bool EF, int MB>
+__global__ void __launch_bounds__(128, MB) k_sweep32v(const P32 p, const int rel, const int z0)
 {
     const int b = blockIdx.y % p.batch;
     const int xr = (blockIdx.x * 32 + threadIdx.x) * 4;
@@ -814,17 +817,26 @@ void launch_e32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st)
 }
 
 /* gcells / ngh: the general cells of those planes */
-void launch_h32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int ngh, cudaStream_t st)
+template <bool EF>
+static void launch_sweep32v(const P32 &p, int rel, int by, int mb, int z0, int z1, cudaStream_t st)
 {
     dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, z1 - z0);
-    k_sweep32v<false><<<grd, blk, 0, st>>>(p, rel, z0);
+    if (mb >= 8) k_sweep32v<EF, 8><<<grd, blk, 0, st>>>(p, rel, z0);
+    else if (mb == 6) k_sweep32v<EF, 6><<<grd, blk, 0, st>>>(p, rel, z0);
+    else k_sweep32v<EF, 5><<<grd, blk, 0, st>>>(p, rel, z0);
+}
+
+void launch_h32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int ngh,
+                 cudaStream_t st)
+{
+    launch_sweep32v<false>(p, rel, by, mb, z0, z1, st);
     if (ngh > 0) k_general32<false><<<dim3((ngh + 127) / 128, p.batch), 128, 0, st>>>(p, rel, gcells, ngh);
 }
 
-void launch_e32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int nge, cudaStream_t st)
+void launch_e32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int nge,
+                 cudaStream_t st)
 {
-    dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, z1 - z0);
-    k_sweep32v<true><<<grd, blk, 0, st>>>(p, rel, z0);
+    launch_sweep32v<true>(p, rel, by, mb, z0, z1, st);
     if (nge > 0) k_general32<true><<<dim3((nge + 127) / 128, p.batch), 128, 0, st>>>(p, rel, gcells, nge);
 }
 

@@ -1258,7 +1258,7 @@ __device__ __forceinline__ bool ztile_split(const P32 &p, int X0, int Y0)
  * Returns the new total in out, the aux in aux, and whether aux was written. */
 __device__ __forceinline__ bool zm_h_elem(const Fused32 &f, int b, int k, int gx, int gy, int gz, const float h[3],
                                           float ey0, float ey2, float ez0, float ez1, float nx1, float nx2,
-                                          const float bn[3], float out[3], float aux[3])
+                                          const float bn[3], float out[3], float aux[3], float smp[2])
 {
     const P32 &p = f.p;
     const Geo &g = p.g;
@@ -1270,6 +1270,8 @@ __device__ __forceinline__ bool zm_h_elem(const Fused32 &f, int b, int k, int gx
             out[c] = tmp[c];
             aux[c] = tmp[3 + c];
         }
+        smp[0] = tmp[6]; /* the DFT samples the main slot of a stable-form cell */
+        smp[1] = tmp[7];
         return true;
     }
     float pl[3], mi[3];
@@ -1290,6 +1292,8 @@ __device__ __forceinline__ bool zm_h_elem(const Fused32 &f, int b, int k, int gx
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) out[c] = fmaf(-1.0f * bn[c], W[c], out[c]);
+        smp[0] = out[0];
+        smp[1] = out[1];
         return false;
     }
     const int jx[3] = {gx, s1 + gy, s2 + gz};
@@ -1306,6 +1310,8 @@ __device__ __forceinline__ bool zm_h_elem(const Fused32 &f, int b, int k, int gx
         out[c] = np + nm;
         aux[c] = nm;
     }
+    smp[0] = out[0];
+    smp[1] = out[1];
     return true;
 }
 
@@ -1315,7 +1321,7 @@ __device__ __forceinline__ bool zm_h_elem(const Fused32 &f, int b, int k, int gx
  * fix-up kernel, nothing written). */
 __device__ __forceinline__ int zm_e_elem(const Fused32 &f, int b, int k, int gx, int gy, int gz, const float h[3],
                                          float hy0, float hy2, float hz0, float hz1, float nx1, float nx2,
-                                         const float bn[3], float out[3], float aux[3])
+                                         const float bn[3], float out[3], float aux[3], float smp[2])
 {
     const P32 &p = f.p;
     const Geo &g = p.g;
@@ -1342,6 +1348,8 @@ __device__ __forceinline__ int zm_e_elem(const Fused32 &f, int b, int k, int gx,
             out[c] = tmp[9 + c];
             aux[c] = tmp[12 + c];
         }
+        smp[0] = tmp[15];
+        smp[1] = tmp[16];
         return 1;
     }
     const int S = g.L0 + g.L1 + g.L2, s1 = g.L0, s2 = g.L0 + g.L1;
@@ -1355,6 +1363,8 @@ __device__ __forceinline__ int zm_e_elem(const Fused32 &f, int b, int k, int gx,
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) out[c] = fmaf(1.0f * bn[c], W[c], out[c]);
+        smp[0] = out[0];
+        smp[1] = out[1];
         return 0;
     }
     const int jx[3] = {gx, s1 + gy, s2 + gz};
@@ -1371,6 +1381,8 @@ __device__ __forceinline__ int zm_e_elem(const Fused32 &f, int b, int k, int gx,
         out[c] = np + nm;
         aux[c] = nm;
     }
+    smp[0] = out[0];
+    smp[1] = out[1];
     return 1;
 }
 
@@ -1492,17 +1504,21 @@ __global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constan
                 }
                 const float xm1 = ZE(s, 1, warp + 1, cx + 3), xm2 = ZE(s, 2, warp + 1, cx + 3);
                 bool wa = false;
+                float smp[2][4];
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
                     const float h3[3] = {e[0][i], e[1][i], e[2][i]};
                     const float bn[3] = {bq[0][i], bq[1][i], bq[2][i]};
                     float out[3] = {hq[0][i], hq[1][i], hq[2][i]}, aux[3] = {mq[0][i], mq[1][i], mq[2][i]};
+                    float sm[2] = {0.0f, 0.0f};
                     const float nx1 = i == 0 ? xm1 : e[1][i - 1], nx2 = i == 0 ? xm2 : e[2][i - 1];
                     if (live && z < L2) /* elsewhere zero: inputs are zero-filled and iBc = 0 */
                         wa |= zm_h_elem(f, b, k, gx0 + i, gy, z, h3, ey[0][i], ey[2][i], eprev[0][i], eprev[1][i],
-                                        nx1, nx2, bn, out, aux);
+                                        nx1, nx2, bn, out, aux, sm);
                     else
                         out[0] = out[1] = out[2] = aux[0] = aux[1] = aux[2] = 0.0f;
+                    smp[0][i] = sm[0];
+                    smp[1][i] = sm[1];
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         hnew[c][i] = out[c];
@@ -1530,9 +1546,9 @@ __global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constan
                     if (q >= 0) {
                         const int px = gx0 + L0 * gy;
                         *reinterpret_cast<float4 *>(ring_ptr(p.d, g.pl, b, k, q, 0) + px) =
-                            make_float4(hnew[0][0], hnew[0][1], hnew[0][2], hnew[0][3]);
+                            make_float4(smp[0][0], smp[0][1], smp[0][2], smp[0][3]);
                         *reinterpret_cast<float4 *>(ring_ptr(p.d, g.pl, b, k, q, 1) + px) =
-                            make_float4(hnew[1][0], hnew[1][1], hnew[1][2], hnew[1][3]);
+                            make_float4(smp[1][0], smp[1][1], smp[1][2], smp[1][3]);
                     }
                 }
             }
@@ -1548,7 +1564,7 @@ __global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constan
                     const float h3[3] = {ZE(s, 0, r + 1, cxh + 4), ZE(s, 1, r + 1, cxh + 4), ZE(s, 2, r + 1, cxh + 4)};
                     const float bn[3] = {ZQ(s, sl.qb, 0, r, cxh), ZQ(s, sl.qb, 1, r, cxh), ZQ(s, sl.qb, 2, r, cxh)};
                     float out[3] = {ZQ(s, sl.qt, 0, r, cxh), ZQ(s, sl.qt, 1, r, cxh), ZQ(s, sl.qt, 2, r, cxh)};
-                    float aux[3] = {0.0f, 0.0f, 0.0f};
+                    float aux[3] = {0.0f, 0.0f, 0.0f}, hsm[2];
                     if (zsplit) {
                         aux[0] = ZQ(s, sl.qm, 0, r, cxh);
                         aux[1] = ZQ(s, sl.qm, 1, r, cxh);
@@ -1557,7 +1573,7 @@ __global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constan
                     if (hx < L0 && hy < L1 && z < L2) {
                         zm_h_elem(f, b, k, hx, hy, z, h3, ZE(s, 0, r, cxh + 4), ZE(s, 2, r, cxh + 4),
                                   ZE(sp, 0, r + 1, cxh + 4), ZE(sp, 1, r + 1, cxh + 4), ZE(s, 1, r + 1, cxh + 3),
-                                  ZE(s, 2, r + 1, cxh + 3), bn, out, aux);
+                                  ZE(s, 2, r + 1, cxh + 3), bn, out, aux, hsm);
                     } else { /* outside the grid: iBc = 0 makes the neighbour zero */
                         out[0] = out[1] = out[2] = 0.0f;
                     }
@@ -1588,7 +1604,7 @@ __global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constan
                     }
                 }
                 const float xp1 = ZH(hzp, 1, warp, cx + 4), xp2 = ZH(hzp, 2, warp, cx + 4);
-                float eo[3][4];
+                float eo[3][4], esm[2][4];
                 int wa = 0, stable = 0;
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
@@ -1596,9 +1612,12 @@ __global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constan
                     const float bn[3] = {bq[0][i], bq[1][i], bq[2][i]};
                     float out[3] = {eprev[0][i], eprev[1][i], eprev[2][i]}, aux[3] = {mq[0][i], mq[1][i], mq[2][i]};
                     const float nx1 = i == 3 ? xp1 : hprev[1][i + 1], nx2 = i == 3 ? xp2 : hprev[2][i + 1];
+                    float sm[2] = {0.0f, 0.0f};
                     const int r = live ? zm_e_elem(f, b, k, gx0 + i, gy, ze, h3, hy[0][i], hy[2][i], hnew[0][i],
-                                                   hnew[1][i], nx1, nx2, bn, out, aux)
+                                                   hnew[1][i], nx1, nx2, bn, out, aux, sm)
                                        : 0;
+                    esm[0][i] = sm[0];
+                    esm[1][i] = sm[1];
                     wa |= r == 1;
                     stable |= (r == 2) << i;
 #pragma unroll
@@ -1634,8 +1653,8 @@ __global__ void __launch_bounds__(32 * (ZNW + 1), 1) k_zm32(const __grid_constan
                         const int px = gx0 + L0 * gy;
                         for (int i = 0; i < 4; i++) {
                             if ((stable >> i) & 1) continue;
-                            ring_ptr(p.d, g.pl, b, k, q, 2)[px + i] = eo[0][i];
-                            ring_ptr(p.d, g.pl, b, k, q, 3)[px + i] = eo[1][i];
+                            ring_ptr(p.d, g.pl, b, k, q, 2)[px + i] = esm[0][i];
+                            ring_ptr(p.d, g.pl, b, k, q, 3)[px + i] = esm[1][i];
                         }
                     }
                 }

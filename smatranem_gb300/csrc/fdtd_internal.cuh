@@ -158,8 +158,9 @@ void launch_dft64(const P64 &p, int rel, cudaStream_t st);
 void launch_h32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st);
 void launch_e32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st);
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
-void launch_h32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int ngh, cudaStream_t st);
-void launch_e32v(const P32 &p, int rel, int by, int z0, int z1, const int *gcells, int nge, cudaStream_t st);
+/* mb: register bound of the vectorised sweep (minimum resident blocks: 5, 6 or 8) */
+void launch_h32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int ngh, cudaStream_t st);
+void launch_e32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int nge, cudaStream_t st);
 void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStream_t st);
 void launch_group32v(const Group32 &gr, int rel, cudaStream_t st);
 int pipe32v_max_ctas_per_sm(int threads);

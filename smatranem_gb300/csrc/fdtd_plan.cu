@@ -384,10 +384,11 @@ void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel, cudaStream_t st)
         const int z1 = z0 + zc < L2 ? z0 + zc : L2;
         const int e0 = z0 == 0 ? 0 : z0 - 1, e1 = z1 == L2 ? L2 : z1 - 1;
         if (p->fused == 2) {
-            launch_h32v(q, rel, p->by32, z0, z1, p->d_hgen + p->hgen_z[z0], p->hgen_z[z1] - p->hgen_z[z0], st);
+            launch_h32v(q, rel, p->by32, p->sweep_mb, z0, z1, p->d_hgen + p->hgen_z[z0],
+                        p->hgen_z[z1] - p->hgen_z[z0], st);
             if (e1 > e0)
-                launch_e32v(q, rel, p->by32, e0, e1, p->d_egen + p->egen_z[e0], p->egen_z[e1] - p->egen_z[e0],
-                            st);
+                launch_e32v(q, rel, p->by32, p->sweep_mb, e0, e1, p->d_egen + p->egen_z[e0],
+                            p->egen_z[e1] - p->egen_z[e0], st);
         } else {
             launch_h32(q, rel, p->by32, z0, z1, st);
             if (e1 > e0) launch_e32(q, rel, p->by32, e0, e1, st);
@@ -1140,14 +1141,15 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
         } else if (p->szc > 0 && p->szc < p->L[2]) {
             sweep_step(p, q32, i, p->stream); /* chunked sweeps: the whole step in ms[0] */
         } else if (p->fused == 2) {
-            launch_h32v(q32, i, p->by32, 0, p->L[2], p->d_hgen, p->nhgen, p->stream);
+            launch_h32v(q32, i, p->by32, p->sweep_mb, 0, p->L[2], p->d_hgen, p->nhgen, p->stream);
         } else {
             launch_h32(q32, i, p->by32, 0, p->L[2], p->stream);
         }
         CK(cudaEventRecord(ev[1], p->stream));
         if (p->precision == SMAT_FP64) launch_e64(q64, i, p->stream);
         else if (p->fused == 4 || (p->szc > 0 && p->szc < p->L[2])) {
-        } else if (p->fused == 2) launch_e32v(q32, i, p->by32, 0, p->L[2], p->d_egen, p->negen, p->stream);
+        } else if (p->fused == 2)
+            launch_e32v(q32, i, p->by32, p->sweep_mb, 0, p->L[2], p->d_egen, p->negen, p->stream);
         else if (p->fused == 0) launch_e32(q32, i, p->by32, 0, p->L[2], p->stream);
         CK(cudaEventRecord(ev[2], p->stream));
         if (p->precision == SMAT_FP64) launch_dft64(q64, i, p->stream);
@@ -1231,8 +1233,11 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
     } else {
         if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
         if (z_chunk < 0) return smat_fail(SMAT_EINVAL, "set_tuning: z_chunk >= 0 (0: whole grid per sweep)");
+        if (ctas_per_sm != 0 && ctas_per_sm != 5 && ctas_per_sm != 6 && ctas_per_sm != 8)
+            return smat_fail(SMAT_EINVAL, "set_tuning: sweeps take ctas_per_sm 0 (= 5), 5, 6 or 8 (register bound)");
         p->by32 = tile_y;
         p->szc = z_chunk >= p->L[2] ? 0 : z_chunk;
+        p->sweep_mb = ctas_per_sm == 0 ? 5 : ctas_per_sm;
     }
     p->fused = fused;
     drop_graph(p);
@@ -1265,9 +1270,11 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
     const int chunks[] = {0, 2, 4, 8, 16};
     if (p->L[0] % 4 == 0) {
         for (int by : {1, 2})
+            for (int mb : {5, 6, 8}) cands.push_back({2, by, 0, mb, 4});
+        for (int by : {1, 2})
             for (int zc : chunks)
-                if (zc < L2) cands.push_back({2, by, zc, 0, 4});
-        cands.push_back({2, 4, 0, 0, 4});
+                if (zc > 0 && zc < L2) cands.push_back({2, by, zc, 5, 4});
+        cands.push_back({2, 4, 0, 5, 4});
     }
     if (p->L[0] % 4 == 0 && p->iBc[0] == 0 && p->iBc[1] == 0 && p->iBc[2] == 0)
         for (int zc : {20, 40, 80, 1 << 20}) {
@@ -1313,8 +1320,8 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         if (verbose)
-            fprintf(stderr, "autotune: kernel %d tile_y %d z_chunk %d slots %d: %.4f ms/step\n", c.fused, c.ty, c.zc,
-                    c.ns, ms / nsteps);
+            fprintf(stderr, "autotune: kernel %d tile_y %d z_chunk %d ctas_per_sm %d slots %d: %.4f ms/step\n",
+                    c.fused, c.ty, c.zc, c.ctas, c.ns, ms / nsteps);
         if (ms < bms) {
             bms = ms;
             bc = c;
@@ -1353,7 +1360,7 @@ extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
     out[0] = p->fused;
     out[1] = (p->fused == 1 || p->fused == 3) ? p->ty : p->fused == 4 ? p->pipe_by : p->fused == 5 ? 4 : p->by32;
     out[2] = (p->fused == 1 || p->fused == 3 || p->fused == 5) ? p->zc : p->fused == 4 ? p->pipe_lag : p->szc;
-    out[3] = p->ctas_per_sm;
+    out[3] = (p->fused == 0 || p->fused == 2) ? p->sweep_mb : p->ctas_per_sm;
     out[4] = p->ns;
     return SMAT_OK;
 }
