@@ -293,6 +293,12 @@ int smat_fdtd_adjoint_grad(smat_fdtd_plan *plan, int nsteps, int K, int f, int q
 typedef struct smat_deck smat_deck;
 int smat_deck_load(const char *input_txt, smat_deck **deck);
 void smat_deck_free(smat_deck *deck);
+/* 1 if the deck came from its binary cache.  No counterpart in the reference:
+ * with the extra input.txt line "FDTD_GPU: cache = y" the parsed arrays are
+ * kept in <prefix>.smatdeck, keyed by every data file's size and modification
+ * time and by the input.txt keys that select Xi columns, and reused by later
+ * loads while that key matches. */
+int smat_deck_from_cache(const smat_deck *deck);
 /* L, {iB, iT, iI, inci_mode}, iBc, time_period, omega (2*pi/(lambda*k0)),
  * min_Dt (sqrt of the smallest "min Dt^2" header), Dt_factor, N_real of the
  * bottom and top mode files; any pointer may be NULL. */

@@ -10,10 +10,14 @@
  * first max(N_real, |inci_mode|) column blocks of each Xi file, once, instead
  * of the whole (4*L0*L1)^2 matrix up to four times.
  */
+#define _POSIX_C_SOURCE 200809L /* stat's nanosecond mtime, for the deck cache */
+
 #include "host_internal.h"
 #include "smatran_fdtd.h"
 
 #include <complex.h>
+#include <stdint.h>
+#include <sys/stat.h>
 #include <ctype.h>
 #include <float.h>
 #include <math.h>
@@ -33,6 +37,8 @@ struct smat_deck {
     double dt_factor, omega, wavelength, k0, min_dt;
     char prefix[BUF], target[2][BUF], inci_point[BUF];
     int precision; /* extra key "FDTD_GPU: precision = FP32" (ignored by the reference) */
+    int use_cache;  /* extra key "FDTD_GPU: cache = y": keep a binary copy of the parsed deck */
+    int from_cache; /* this load came from that copy */
     double complex *mu, *epsi;
     double complex *Hinc, *Einc;
     int nreal[2];                /* bottom, top */
@@ -106,6 +112,12 @@ static int read_input(smat_deck *d, const char *path)
             seen |= 4;
         } else if (strncmp(buf, "FDTD_GPU", 8) == 0) {
             if (strstr(buf, "FP32") || strstr(buf, "fp32")) d->precision = SMAT_FP32;
+            const char *c = strstr(buf, "cache");
+            if (c && (c = strchr(c, '=')) != NULL) {
+                while (*++c == ' ')
+                    ;
+                d->use_cache = *c == 'y' || *c == 'Y' || *c == '1';
+            }
         } else if (!(seen & 8) && strncmp(buf, "FDTD", 4) == 0 &&
                    sscanf(buf,
                           "%*[^=] %*[=] %d %*[^=] %*[=] %d %*[^=] %*[=] %d %*[^=] %*[=] %s %*[^=] %*[=] %d "
@@ -284,6 +296,130 @@ static int plane_side(const int L[4], int z)
     return -1;
 }
 
+/* ---- optional binary cache of a parsed deck --------------------------------
+ * Text parsing dominates the reference program's run time on real decks (the
+ * Med files hold 2*L0*L1 lines per layer, the Xi files (4*L0*L1)^2 numbers).
+ * With "FDTD_GPU: cache = y" in input.txt the parsed arrays are kept in
+ * <prefix>.smatdeck, keyed by a signature of every source file's size and
+ * modification time and of the input.txt keys that select what is kept; a
+ * later load with the same signature reads the binary copy instead.  The copy
+ * is written to a temporary name and renamed, so a reader never sees half of
+ * one. */
+#define CACHE_MAGIC "SMATDECK1"
+
+static uint64_t fnv1a(uint64_t h, const void *p, size_t n)
+{
+    const unsigned char *c = (const unsigned char *)p;
+    for (size_t i = 0; i < n; i++) h = (h ^ c[i]) * 1099511628211ULL;
+    return h;
+}
+
+static uint64_t file_sig(uint64_t h, const char *name)
+{
+    struct stat st;
+    long long v[3] = {-1, -1, -1};
+    if (stat(name, &st) == 0) {
+        v[0] = (long long)st.st_size;
+        v[1] = (long long)st.st_mtim.tv_sec;
+        v[2] = (long long)st.st_mtim.tv_nsec;
+    }
+    h = fnv1a(h, name, strlen(name));
+    return fnv1a(h, v, sizeof v);
+}
+
+static uint64_t deck_signature(const smat_deck *d)
+{
+    uint64_t h = 14695981039346656037ULL;
+    h = fnv1a(h, d->prefix, strlen(d->prefix));
+    h = fnv1a(h, d->target[0], strlen(d->target[0]));
+    h = fnv1a(h, d->target[1], strlen(d->target[1]));
+    h = fnv1a(h, d->inci_point, strlen(d->inci_point));
+    h = fnv1a(h, &d->inci_mode, sizeof d->inci_mode);
+    h = fnv1a(h, d->L, sizeof d->L);
+    for (int z = 0; z < d->L[2]; z++) {
+        char name[BUF];
+        layer_file(d->prefix, d->L, z, name);
+        h = file_sig(h, name);
+    }
+    for (int side = 0; side < 2; side++) {
+        char xi[BUF + 32], mode[BUF + 32];
+        xi_names(d, side, xi, mode);
+        h = file_sig(h, xi);
+        h = file_sig(h, mode);
+    }
+    return h;
+}
+
+static void cache_name(const smat_deck *d, char *out) { snprintf(out, BUF + 32, "%s.smatdeck", d->prefix); }
+
+/* everything smat_deck_load derives from the data files */
+static int cache_io(smat_deck *d, FILE *f, int writing)
+{
+    const long n3 = (long)d->L[0] * d->L[1] * d->L[2], pl = (long)d->L[0] * d->L[1], NA = 2 * pl;
+#define IO(ptr, n)                                                                                                     \
+    do {                                                                                                               \
+        const size_t n_ = (size_t)(n);                                                                                 \
+        if ((writing ? fwrite((ptr), sizeof *(ptr), n_, f) : fread((ptr), sizeof *(ptr), n_, f)) != n_) return -1;     \
+    } while (0)
+    IO(d->nreal, 2);
+    IO(d->ncols, 2);
+    IO(&d->iB, 1);
+    IO(&d->iT, 1);
+    IO(&d->iI, 1);
+    IO(&d->changed_iT, 1);
+    IO(&d->min_dt, 1);
+    if (!writing) {
+        if (d->ncols[0] < 0 || d->ncols[1] < 0 || d->ncols[0] > 2 * NA || d->ncols[1] > 2 * NA) return -1;
+        d->mu = calloc(3 * n3, sizeof(double complex));
+        d->epsi = calloc(3 * n3, sizeof(double complex));
+        d->Hinc = calloc(2 * pl, sizeof(double complex));
+        d->Einc = calloc(2 * pl, sizeof(double complex));
+        for (int s = 0; s < 2; s++)
+            if (d->ncols[s]) d->tilxi[s] = calloc((size_t)d->ncols[s] * 2 * NA + 1, sizeof(double complex));
+        if (!d->mu || !d->epsi || !d->Hinc || !d->Einc) return -1;
+        for (int s = 0; s < 2; s++)
+            if (d->ncols[s] && !d->tilxi[s]) return -1;
+    }
+    IO(d->mu, 3 * n3);
+    IO(d->epsi, 3 * n3);
+    IO(d->Hinc, 2 * pl);
+    IO(d->Einc, 2 * pl);
+    for (int s = 0; s < 2; s++)
+        if (d->ncols[s]) IO(d->tilxi[s], (size_t)d->ncols[s] * 2 * NA);
+#undef IO
+    return 0;
+}
+
+static int read_cache(smat_deck *d, uint64_t sig)
+{
+    char name[BUF + 32], magic[sizeof CACHE_MAGIC];
+    cache_name(d, name);
+    FILE *f = fopen(name, "rb");
+    if (!f) return -1;
+    uint64_t s = 0;
+    int L[4];
+    int rc = fread(magic, 1, sizeof magic, f) == sizeof magic && memcmp(magic, CACHE_MAGIC, sizeof magic) == 0 &&
+                     fread(&s, sizeof s, 1, f) == 1 && s == sig && fread(L, sizeof L, 1, f) == 1 &&
+                     memcmp(L, d->L, sizeof L) == 0
+                 ? cache_io(d, f, 0)
+                 : -1;
+    fclose(f);
+    return rc;
+}
+
+static void write_cache(smat_deck *d, uint64_t sig)
+{
+    char name[BUF + 32], tmp[BUF + 64];
+    cache_name(d, name);
+    snprintf(tmp, sizeof tmp, "%s.tmp%ld", name, (long)time(NULL));
+    FILE *f = fopen(tmp, "wb");
+    if (!f) return; /* the cache is optional: no copy, no error */
+    int ok = fwrite(CACHE_MAGIC, 1, sizeof CACHE_MAGIC, f) == sizeof CACHE_MAGIC && fwrite(&sig, sizeof sig, 1, f) == 1 &&
+             fwrite(d->L, sizeof d->L, 1, f) == 1 && cache_io(d, f, 1) == 0;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || rename(tmp, name) != 0) remove(tmp);
+}
+
 void smat_deck_free(smat_deck *d)
 {
     if (!d) return;
@@ -309,6 +445,18 @@ int smat_deck_load(const char *input_txt, smat_deck **out)
     if (rc) {
         smat_deck_free(d);
         return rc;
+    }
+    uint64_t sig = 0;
+    if (d->use_cache) {
+        sig = deck_signature(d);
+        if (read_cache(d, sig) == 0) {
+            d->from_cache = 1;
+            *out = d;
+            return SMAT_OK;
+        }
+        /* no usable copy: forget what a partial read allocated, parse the text */
+        free(d->mu), free(d->epsi), free(d->Hinc), free(d->Einc), free(d->tilxi[0]), free(d->tilxi[1]);
+        d->mu = d->epsi = d->Hinc = d->Einc = d->tilxi[0] = d->tilxi[1] = NULL;
     }
     const int *L = d->L;
     const long n3 = (long)L[0] * L[1] * L[2], pl = (long)L[0] * L[1];
@@ -417,9 +565,12 @@ int smat_deck_load(const char *input_txt, smat_deck **out)
         smat_deck_free(d);
         return rc;
     }
+    if (d->use_cache) write_cache(d, sig);
     *out = d;
     return SMAT_OK;
 }
+
+int smat_deck_from_cache(const smat_deck *d) { return d ? d->from_cache : 0; }
 
 int smat_deck_info(const smat_deck *d, int L[4], int iBTIin[4], int iBc[3], int time_period[3], double *omega,
                    double *min_dt, double *dt_factor, int nreal[2])

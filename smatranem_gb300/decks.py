@@ -103,13 +103,14 @@ def write_deck(root: str, s: Structure, *, prefix="Data/deck", wavelength_m=1.55
     return path
 
 
-def load(input_txt: str):
-    """Read a deck through the library: a dict of its numbers and arrays."""
+def _open(input_txt: str):
     lib = fdtd.lib()
     lib.smat_deck_load.argtypes = [C.c_char_p, C.c_void_p]
     lib.smat_deck_free.argtypes = [C.c_void_p]
     lib.smat_deck_info.argtypes = [C.c_void_p] * 9
     lib.smat_deck_arrays.argtypes = [C.c_void_p] * 5
+    lib.smat_deck_from_cache.argtypes = [C.c_void_p]
+    lib.smat_deck_smatrix.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     h = C.c_void_p()
     # the Prefix of input.txt is relative to the directory the FDTD runs in
     cwd = os.getcwd()
@@ -120,6 +121,31 @@ def load(input_txt: str):
         os.chdir(cwd)
     if rc != 0:
         raise fdtd.FdtdError(rc, lib.smat_last_error().decode())
+    return lib, h
+
+
+def smatrix(input_txt: str, which: int, HB, EB):
+    """S_calc of the deck's bottom (which = 0) or top (1) plane for monitor
+    planes HB, EB (2*L0*L1 complex each): 2*N_real complex values."""
+    lib, h = _open(input_txt)
+    try:
+        nr = (C.c_int * 2)()
+        lib.smat_deck_info(h, None, None, None, None, None, None, None, nr)
+        S = np.zeros(2 * nr[which], np.complex128)
+        HB = np.ascontiguousarray(HB, np.complex128)
+        EB = np.ascontiguousarray(EB, np.complex128)
+        rc = lib.smat_deck_smatrix(h, which, HB.ctypes.data_as(C.c_void_p), EB.ctypes.data_as(C.c_void_p),
+                                   S.ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise fdtd.FdtdError(rc, lib.smat_last_error().decode())
+        return S
+    finally:
+        lib.smat_deck_free(h)
+
+
+def load(input_txt: str):
+    """Read a deck through the library: a dict of its numbers and arrays."""
+    lib, h = _open(input_txt)
     try:
         L = (C.c_int * 4)()
         bti = (C.c_int * 4)()
@@ -136,6 +162,7 @@ def load(input_txt: str):
         lib.smat_deck_arrays(h, mu.ctypes.data_as(C.c_void_p), ep.ctypes.data_as(C.c_void_p),
                              Hi.ctypes.data_as(C.c_void_p), Ei.ctypes.data_as(C.c_void_p))
         return dict(L=tuple(L), iBTIin=tuple(bti), iBc=tuple(bc), time_period=tuple(tp), omega=om.value,
-                    min_dt=mdt.value, dt_factor=dtf.value, nreal=tuple(nr), mu=mu, epsi=ep, Hinc=Hi, Einc=Ei)
+                    min_dt=mdt.value, dt_factor=dtf.value, nreal=tuple(nr), mu=mu, epsi=ep, Hinc=Hi, Einc=Ei,
+                    from_cache=bool(lib.smat_deck_from_cache(h)))
     finally:
         lib.smat_deck_free(h)

@@ -77,3 +77,43 @@ def test_deck_reader_errors(built, tmp_path):
                  "Dt_factor = 1.\n")
     with pytest.raises(fdtd.FdtdError, match="open error"):
         decks.load(str(p))
+
+
+def test_deck_binary_cache(built, tmp_path):
+    """"FDTD_GPU: cache = y" keeps the parsed deck in <prefix>.smatdeck: a second
+    load reads it (same arrays and tilde-Xi columns, bit for bit); touching a
+    data file or dropping the key makes the loader parse the text again."""
+    import shutil
+    from smatranem_gb300 import decks
+    for name in DECKS:
+        dst = tmp_path / name
+        shutil.copytree(os.path.join(GOLDEN, "decks", name), dst)
+        txt = str(dst / "input.txt")
+        with open(txt) as f:
+            plain = f.read()
+        with open(txt, "a") as f:
+            f.write("\tFDTD_GPU: cache = y\n")
+        a = decks.load(txt)
+        b = decks.load(txt)
+        assert not a["from_cache"] and b["from_cache"]
+        for k in ("mu", "epsi", "Hinc", "Einc"):
+            assert np.array_equal(a[k], b[k])
+        for k in ("L", "iBTIin", "min_dt", "nreal", "omega", "time_period"):
+            assert a[k] == b[k]
+        rng = np.random.default_rng(1)
+        pl = a["L"][0] * a["L"][1]
+        HB, EB = (rng.standard_normal(2 * pl) + 1j * rng.standard_normal(2 * pl) for _ in range(2))
+        for which in (0, 1):
+            s_parse = decks.smatrix(txt, which, HB, EB)  # from the cache now
+            with open(txt, "w") as f:
+                f.write(plain)
+            s_text = decks.smatrix(txt, which, HB, EB)
+            assert np.array_equal(s_parse, s_text)
+            with open(txt, "a") as f:
+                f.write("\tFDTD_GPU: cache = y\n")
+        med = sorted((dst / "Data").glob("*_Med*.dat"))[0]
+        st = os.stat(med)
+        os.utime(med, ns=(st.st_atime_ns, st.st_mtime_ns + 1_000_000))
+        c = decks.load(txt)
+        assert not c["from_cache"] and np.array_equal(c["mu"], a["mu"])
+        assert decks.load(txt)["from_cache"]
