@@ -52,6 +52,12 @@ WORKLOAD = ("bend 256x192x160 curvilinear (R=2um, Si strip in SiO2), 12-cell spl
             "batch 8 = 2 ports x 4 modes, Gaussian pulse, FP64 DFT at 21 wavelengths on 2 port planes")
 
 
+# DRAM traffic of one k_sweep32v launch on the bench workload, from one ncu
+# capture of the full-size workload (dram__bytes_read.sum + dram__bytes_write.sum,
+# a one-pass metric set; the summary is kept with the other ncu summaries)
+SWEEP32V_TRAFFIC_PER_LAUNCH = 1.95e9 + 0.977e9
+
+
 def launches_per_step(tuning, L2):
     """Update-kernel launches of one step: one fused launch (kernels 1, 3), or
     an H and an E sweep per z-chunk (kernels 0, 2; z_chunk 0 = one chunk)."""
@@ -383,7 +389,9 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h / full, "what": f"create+incident+schedule+{full} steps+DFT read-back, "
                                                           f"{t_e2e:.2f} s"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "traffic": SWEEP32V_TRAFFIC_PER_LAUNCH if tuning[0] == 2 and batch == BATCH else None,
+                     "traffic_per": "launch (ncu, dram read + write)",
                      "kernel": {1: "k_fused32 (one fused H+E launch per step)",
                                 2: "k_sweep32v (H, E; float4)" + (f", z-chunks of {tuning[2]} planes"
                                                                    if 0 < tuning[2] < bend.s.L[2] else ""),

@@ -325,15 +325,24 @@ int smat_fdtd_check_finite(smat_fdtd_plan *plan, int *finite, double *max_abs);
  * [k_begin, k_begin+nsteps) of the schedule.  The steps are really taken. */
 int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double ms[3]);
 
-/* FP32 launch configuration.  kernel = 1: one fused z-marching launch per step
- * with tiles of 32 x tile_y cells (2..8), z chunks of z_chunk planes,
- * ctas_per_sm resident CTAs (0: as many as fit) and `slots` shared-memory
- * plane slots (4..6: planes staged 1..3 ahead); kernel = 0: two sweeps with
- * 32 x tile_y thread blocks (1..8); kernel = 2: two sweeps of four cells per
- * thread (float4, L0 % 4 == 0, tile_y 1..4; the default where it applies);
- * kernel = 3: the fused launch with TMA plane staging (L0 % 4 == 0, same
- * parameters as kernel 1).  Results are
- * bit-identical across configurations. */
+/* FP32 launch configuration (smat_fdtd_autotune picks one by timing).
+ *   kernel 0: two sweeps with 32 x tile_y thread blocks (1..8); z_chunk > 0
+ *             runs H and E in chunks of that many planes (0: whole grid).
+ *   kernel 2: two sweeps of four cells per thread (float4, L0 % 4 == 0,
+ *             tile_y 1..4; the default where it applies); z_chunk as for 0;
+ *             ctas_per_sm = register bound as minimum resident blocks (0 or 5:
+ *             96 registers, 6, 8), or -3 for two z-planes per thread (168).
+ *   kernel 1: one fused z-marching launch per step with tiles of 32 x tile_y
+ *             cells (2..8), z chunks of z_chunk planes, ctas_per_sm resident
+ *             CTAs (0: as many as fit) and `slots` shared-memory plane slots
+ *             (4..6: planes staged 1..3 ahead).
+ *   kernel 3: kernel 1 with TMA plane staging (L0 % 4 == 0).
+ *   kernel 4: H and E sweeps pipelined in one cooperative launch; tile_y rows
+ *             per item, z_chunk = how many planes H may run ahead of E (0: no
+ *             limit, else >= 2).
+ *   kernel 5: one fused launch per step on 128 x 4 tiles with a TMA producer
+ *             warp (L0 % 4 == 0, iBc = 0 on every axis); z_chunk planes per item.
+ * Results are bit-identical across configurations. */
 int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int kernel, int tile_y, int z_chunk, int ctas_per_sm,
                          int slots);
 /* {kernel, tile_y, z_chunk, ctas_per_sm, slots} of the plan. */

@@ -261,6 +261,230 @@ template <bool CG> __device__ __forceinline__ float4 ldG4(const float *p)
 }
 template <bool CG> __device__ __forceinline__ float ldG(const float *p) { return CG ? __ldcg(p) : *p; }
 
+/* The loads of one quad row segment (cells x = xr..xr+3 of row j1, plane j2,
+ * excitation b; a warp covers 128 consecutive x-cells, lane = threadIdx.x % 32)
+ * into q, including the x neighbours by warp shuffle.  False for a row past
+ * the grid (uniform per warp). */
+struct QIn {
+    float4 c[3], out[3], gh[3], aux[3], gy0, gy2, gz0, gz1;
+    float xn1, xn2;
+    long long l;
+    int x0;
+    bool live, qsplit, pyz;
+};
+
+template <bool EF, bool CG>
+__device__ __forceinline__ bool quad_load(const P32 &p, const int b, const int j1, const int j2, const int xr, QIn &q)
+{
+    const Geo &g = p.g;
+    if (j1 >= g.L1) return false; /* uniform per warp */
+    const bool live = xr < g.L0;
+    const int x0 = live ? xr : g.L0 - 4; /* idle lanes load valid data, store nothing */
+    const long long n3 = g.n3, bs = 3 * n3;
+    const long long l = x0 + (long long)g.L0 * (j1 + (long long)g.L1 * j2);
+    const float *__restrict__ cf = EF ? p.be : p.bh;
+    const float *__restrict__ F = (EF ? p.E : p.H) + b * bs;
+    const float *__restrict__ Fa = (EF ? p.Ea : p.Ha) + b * bs;
+    const float *__restrict__ G = (EF ? p.H : p.E) + b * bs;
+    const int s1 = g.L0, s2 = g.L0 + g.L1;
+    /* neighbours along y and z (whole quads) with the boundary factor */
+    const bool ey = EF ? (j1 + 1 == g.L1) : (j1 == 0);
+    const bool ez = EF ? (j2 + 1 == g.L2) : (j2 == 0);
+    const long long oy = (long long)g.L0 * (EF ? (ey ? -(g.L1 - 1) : 1) : (ey ? g.L1 - 1 : -1));
+    const long long oz = (long long)g.pl * (EF ? (ez ? -(g.L2 - 1) : 1) : (ez ? g.L2 - 1 : -1));
+    const float fy = ey ? (float)g.bc[1] : 1.0f, fz = ez ? (float)g.bc[2] : 1.0f;
+
+    /* split-PML quads need their aux slots: decided from the 1-D masks before
+     * any load, so that those loads leave with the others (one DRAM round trip) */
+    const bool pyz = p.pmask[s1 + j1] | p.pmask[s2 + j2];
+    const bool qsplit = pyz | p.pmask[x0] | p.pmask[x0 + 1] | p.pmask[x0 + 2] | p.pmask[x0 + 3];
+    q.pyz = pyz;
+    q.qsplit = qsplit;
+    q.live = live;
+    q.x0 = x0;
+    q.l = l;
+    float4 *c = q.c, *out = q.out, *gh = q.gh, *aux = q.aux;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        c[i] = ld4(cf + i * n3 + l);
+        out[i] = ld4(F + i * n3 + l);
+        gh[i] = ldG4<CG>(G + i * n3 + l);
+    }
+    if (qsplit) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) aux[i] = ld4(Fa + i * n3 + l);
+    }
+    /* H sweep: Ex, Ez at y-1; Ex, Ey at z-1.  E sweep: Hx, Hz at y+1; Hx, Hy at z+1. */
+    q.gy0 = scale4(ldG4<CG>(G + 0 * n3 + l + oy), fy);
+    q.gy2 = scale4(ldG4<CG>(G + 2 * n3 + l + oy), fy);
+    q.gz0 = scale4(ldG4<CG>(G + 0 * n3 + l + oz), fz);
+    q.gz1 = scale4(ldG4<CG>(G + 1 * n3 + l + oz), fz);
+    /* x neighbours: H sweep needs Ey, Ez at x-1; E sweep Hy, Hz at x+1 */
+    const unsigned full = 0xffffffffu;
+    float &xn1 = q.xn1, &xn2 = q.xn2; /* component 1, 2 of the outer neighbour of the quad */
+    if (!EF) {
+        xn1 = __shfl_up_sync(full, gh[1].w, 1);
+        xn2 = __shfl_up_sync(full, gh[2].w, 1);
+        if ((threadIdx.x & 31) == 0 || x0 == 0) {
+            const bool edge = x0 == 0;
+            const long long o = edge ? g.L0 - 1 : -1;
+            const float f = edge ? (float)g.bc[0] : 1.0f;
+            xn1 = f * ldG<CG>(G + 1 * n3 + l + o);
+            xn2 = f * ldG<CG>(G + 2 * n3 + l + o);
+        }
+    } else {
+        xn1 = __shfl_down_sync(full, gh[1].x, 1);
+        xn2 = __shfl_down_sync(full, gh[2].x, 1);
+        if ((threadIdx.x & 31) == 31 || x0 + 4 == g.L0) {
+            const bool edge = x0 + 4 == g.L0;
+            const long long o = edge ? -(g.L0 - 4) : 4;
+            const float f = edge ? (float)g.bc[0] : 1.0f;
+            xn1 = f * ldG<CG>(G + 1 * n3 + l + o);
+            xn2 = f * ldG<CG>(G + 2 * n3 + l + o);
+        }
+    }
+    return true;
+}
+
+/* The update and stores of a quad loaded by quad_load (same expressions as
+ * k_sweep32: the same bits) */
+template <bool EF>
+__device__ __forceinline__ void quad_compute(const P32 &p, const int rel, const int b, const int j1, const int j2,
+                                             QIn &qi)
+{
+    if (!qi.live) return;
+    const Geo &g = p.g;
+    const long long n3 = g.n3, bs = 3 * n3, l = qi.l;
+    const int x0 = qi.x0;
+    float *__restrict__ F = (EF ? p.E : p.H) + b * bs;
+    float *__restrict__ Fa = (EF ? p.Ea : p.Ha) + b * bs;
+    const float sg = EF ? 1.0f : -1.0f;
+    const int k = *p.s.base + rel;
+    const int px0 = x0 + g.L0 * j1;
+    const int S = g.L0 + g.L1 + g.L2, s1 = g.L0, s2 = g.L0 + g.L1;
+    const bool pyz = qi.pyz, qsplit = qi.qsplit;
+    float4 *c = qi.c, *out = qi.out, *gh = qi.gh, *aux = qi.aux;
+    const float4 gy0 = qi.gy0, gy2 = qi.gy2, gz0 = qi.gz0, gz1 = qi.gz1;
+    const float xn1 = qi.xn1, xn2 = qi.xn2;
+    const bool on_src = j2 == p.s.iI[b];
+    const int q = monitor_index(p.d, j2);
+    bool any_aux = false;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int xx = x0 + i;
+        const float h0 = el(gh[0], i), h1 = el(gh[1], i), h2 = el(gh[2], i);
+        /* neighbour along x of element i */
+        float n1x, n2x;
+        if (!EF) {
+            n1x = i == 0 ? xn1 : el(gh[1], i - 1);
+            n2x = i == 0 ? xn2 : el(gh[2], i - 1);
+        } else {
+            n1x = i == 3 ? xn1 : el(gh[1], i + 1);
+            n2x = i == 3 ? xn2 : el(gh[2], i + 1);
+        }
+        float pl[3], mi[3];
+        if (!EF) { /* backward, as curl32<false> */
+            pl[0] = h2 - el(gy2, i);
+            mi[0] = el(gz1, i) - h1;
+            pl[1] = h0 - el(gz0, i);
+            mi[1] = n2x - h2;
+            pl[2] = h1 - n1x;
+            mi[2] = el(gy0, i) - h0;
+        } else { /* forward, as curl32<true> */
+            pl[0] = el(gy2, i) - h2;
+            mi[0] = h1 - el(gz1, i);
+            pl[1] = el(gz0, i) - h0;
+            mi[1] = h2 - n2x;
+            pl[2] = n1x - h1;
+            mi[2] = h0 - el(gy0, i);
+        }
+        const float c0 = el(c[0], i);
+        if (isnan(c0)) { /* general cell: rewritten by k_general32 after this launch */
+            any_aux = true;
+            continue;
+        }
+        const bool split = p.pmask[xx] | pyz;
+        const float bn[3] = {c0, el(c[1], i), el(c[2], i)};
+        if (!split) {
+            float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+            if (on_src) {
+                W[0] += (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 1, px0 + i));
+                W[1] -= (float)(p.s.sgn[b] * sheet32(p.s, g.pl, b, k, !EF, 0, px0 + i));
+            }
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) set_el(out[cc], i, fmaf(sg * bn[cc], W[cc], el(out[cc], i)));
+        } else {
+            any_aux = true;
+        }
+    }
+    /* elements that need their aux slot (split) or a record (general) */
+    if (any_aux) {
+        if (!qsplit) { /* a general (record) cell in an unsplit quad: rare */
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) aux[cc] = ld4(Fa + cc * n3 + l);
+        }
+        const int jy = s1 + j1, jz = s2 + j2;
+        const float *tA = p.tab + (EF ? 2 : 0) * S, *tG = p.tab + (EF ? 3 : 1) * S;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int xx = x0 + i;
+            const float c0 = el(c[0], i);
+            if (isnan(c0)) continue;
+            if (!(p.pmask[xx] | pyz)) continue;
+            const float h0 = el(gh[0], i), h1 = el(gh[1], i), h2 = el(gh[2], i);
+            float n1x, n2x;
+            if (!EF) {
+                n1x = i == 0 ? xn1 : el(gh[1], i - 1);
+                n2x = i == 0 ? xn2 : el(gh[2], i - 1);
+            } else {
+                n1x = i == 3 ? xn1 : el(gh[1], i + 1);
+                n2x = i == 3 ? xn2 : el(gh[2], i + 1);
+            }
+            float pl[3], mi[3];
+            if (!EF) {
+                pl[0] = h2 - el(gy2, i);
+                mi[0] = el(gz1, i) - h1;
+                pl[1] = h0 - el(gz0, i);
+                mi[1] = n2x - h2;
+                pl[2] = h1 - n1x;
+                mi[2] = el(gy0, i) - h0;
+            } else {
+                pl[0] = el(gy2, i) - h2;
+                mi[0] = h1 - el(gz1, i);
+                pl[1] = el(gz0, i) - h0;
+                mi[1] = h2 - n2x;
+                pl[2] = n1x - h1;
+                mi[2] = h0 - el(gy0, i);
+            }
+            const int jx[3] = {xx, jy, jz};
+            const float bn[3] = {c0, el(c[1], i), el(c[2], i)};
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+                const int i1 = jx[(cc + 1) % 3], i2 = jx[(cc + 2) % 3];
+                const float Ap = tA[i1], Bp = sg * bn[cc] * tG[i1];
+                const float Am = tA[i2], Bm = sg * bn[cc] * tG[i2];
+                const float m = el(aux[cc], i);
+                const float pp = el(out[cc], i) - m; /* out still holds the old field here */
+                const float np = fmaf(Bp, pl[cc], Ap * pp);
+                const float nm = fmaf(Bm, mi[cc], Am * m);
+                set_el(out[cc], i, np + nm);
+                set_el(aux[cc], i, nm);
+            }
+        }
+    }
+#pragma unroll
+    for (int cc = 0; cc < 3; cc++) st4(F + cc * n3 + l, out[cc]);
+    if (any_aux) {
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) st4(Fa + cc * n3 + l, aux[cc]);
+    }
+    if (q >= 0) {
+        /* split elements sample the total field, ordinary ones their field */
+        st4(ring_at(p.d, g.pl, b, k, q, EF ? 2 : 0) + px0, out[0]);
+        st4(ring_at(p.d, g.pl, b, k, q, EF ? 3 : 1) + px0, out[1]);
+    }
+}
+
 /* one quad row segment: cells x = xr..xr+3 of row j1, plane j2, excitation b;
  * a warp covers 128 consecutive x-cells (lane = threadIdx.x) */
 template <bool EF, bool CG>
@@ -817,10 +1041,35 @@ void launch_e32(const P32 &p, int rel, int by, int z0, int z1, cudaStream_t st)
 }
 
 /* gcells / ngh: the general cells of those planes */
+/* Two z-planes per thread: the loads of both quads leave before either is
+ * computed, so a warp keeps twice the bytes in flight at the same occupancy
+ * (the single-plane sweep is latency-bound).  Same updates, same bits.  MB as
+ * for k_sweep32v (4: 128 registers). */
+template <bool EF, int MB>
+__global__ void __launch_bounds__(128, MB) k_sweep32v2(const P32 p, const int rel, const int z0, const int z1)
+{
+    const int b = blockIdx.y % p.batch;
+    const int xr = (blockIdx.x * 32 + threadIdx.x) * 4;
+    const int j1 = (blockIdx.y / p.batch) * blockDim.y + threadIdx.y;
+    const int za = z0 + 2 * blockIdx.z;
+    const bool two = za + 1 < z1;
+    QIn qa, qb;
+    if (!quad_load<EF, false>(p, b, j1, za, xr, qa)) return;
+    if (two) quad_load<EF, false>(p, b, j1, za + 1, xr, qb);
+    quad_compute<EF>(p, rel, b, j1, za, qa);
+    if (two) quad_compute<EF>(p, rel, b, j1, za + 1, qb);
+}
+
 template <bool EF>
 static void launch_sweep32v(const P32 &p, int rel, int by, int mb, int z0, int z1, cudaStream_t st)
 {
     dim3 blk(32, by, 1), grd((p.g.L0 / 4 + 31) / 32, ((p.g.L1 + by - 1) / by) * p.batch, z1 - z0);
+    if (mb < 0) { /* two planes per thread: -mb = register bound */
+        grd.z = (z1 - z0 + 1) / 2;
+        if (mb == -3) k_sweep32v2<EF, 3><<<grd, blk, 0, st>>>(p, rel, z0, z1);
+        else k_sweep32v2<EF, 4><<<grd, blk, 0, st>>>(p, rel, z0, z1);
+        return;
+    }
     if (mb >= 8) k_sweep32v<EF, 8><<<grd, blk, 0, st>>>(p, rel, z0);
     else if (mb == 6) k_sweep32v<EF, 6><<<grd, blk, 0, st>>>(p, rel, z0);
     else k_sweep32v<EF, 5><<<grd, blk, 0, st>>>(p, rel, z0);

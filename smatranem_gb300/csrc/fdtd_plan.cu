@@ -1233,8 +1233,10 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
     } else {
         if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
         if (z_chunk < 0) return smat_fail(SMAT_EINVAL, "set_tuning: z_chunk >= 0 (0: whole grid per sweep)");
-        if (ctas_per_sm != 0 && ctas_per_sm != 5 && ctas_per_sm != 6 && ctas_per_sm != 8)
-            return smat_fail(SMAT_EINVAL, "set_tuning: sweeps take ctas_per_sm 0 (= 5), 5, 6 or 8 (register bound)");
+        if (ctas_per_sm != 0 && ctas_per_sm != 5 && ctas_per_sm != 6 && ctas_per_sm != 8 &&
+            !(fused == 2 && ctas_per_sm == -3))
+            return smat_fail(SMAT_EINVAL, "set_tuning: sweeps take ctas_per_sm 0 (= 5), 5, 6 or 8 (register bound), "
+                                          "or -3 (vector sweeps, two planes per thread)");
         p->by32 = tile_y;
         p->szc = z_chunk >= p->L[2] ? 0 : z_chunk;
         p->sweep_mb = ctas_per_sm == 0 ? 5 : ctas_per_sm;
@@ -1270,7 +1272,7 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
     const int chunks[] = {0, 2, 4, 8, 16};
     if (p->L[0] % 4 == 0) {
         for (int by : {1, 2})
-            for (int mb : {5, 6, 8}) cands.push_back({2, by, 0, mb, 4});
+            for (int mb : {5, 6, -3}) cands.push_back({2, by, 0, mb, 4});
         for (int by : {1, 2})
             for (int zc : chunks)
                 if (zc > 0 && zc < L2) cands.push_back({2, by, zc, 5, 4});

@@ -359,7 +359,7 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     tunings = TUNINGS + [(0, 4, 1, 0, 4), (0, 2, 3, 0, 4)]
     if L[0] % 4 == 0:
         tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (2, 4, 3, 0, 4), (2, 1, 5, 0, 4), (2, 2, 16, 0, 4),
-                    (2, 1, 0, 6, 4), (2, 2, 0, 8, 4),
+                    (2, 1, 0, 6, 4), (2, 2, 0, 8, 4), (2, 1, 0, -3, 4), (2, 2, 3, -3, 4),
                     (3, 8, 40, 0, 5), (3, 4, 5, 0, 4), (3, 2, 3, 1, 6), (3, 4, 1, 0, 5), (3, 8, 7, 1, 6)]
         if tuple(kw["iBc"]) == (0, 0, 0):  # 128 x 4 tiles with a TMA producer warp (kernel 5)
             tunings += [(5, 4, 40, 1, 4), (5, 4, 5, 1, 4), (5, 4, 1, 1, 4), (5, 4, 7, 1, 4)]
