@@ -936,28 +936,22 @@ void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStrea
  * Block i belongs to the member m with blk[m] <= i < blk[m+1]; inside it the
  * block decodes exactly as a k_sweep32v block (x block fastest, then row
  * block x excitation, then plane), so each member gets the same bits as
- * when it is stepped alone.
+ * when it is stepped alone.  The member table lives in constant memory: a
+ * block-uniform index into it is served by the constant cache, as kernel
+ * parameters are, so a member's fields cost the sweep no extra registers.
+ * One table per device: the host side runs one such group at a time.
  * ------------------------------------------------------------------------- */
+__constant__ Group32 c_group;
+
 template <bool EF>
-__global__ void __launch_bounds__(128, 5) k_group32v(const __grid_constant__ Group32 gr, const int rel)
+__global__ void __launch_bounds__(128, 5) k_group32v(const int rel)
 {
-    /* the member's parameters, copied once per block to shared memory (a
-     * dynamically indexed parameter array would be read element by element) */
-    __shared__ P32 sp;
     int m = 0;
-    while (m + 1 < gr.n && (int)blockIdx.x >= gr.blk[m + 1]) m++;
-    {
-        static_assert(sizeof(P32) % 4 == 0, "P32 is copied as words");
-        const int *src = reinterpret_cast<const int *>(&gr.p[m]);
-        int *dst = reinterpret_cast<int *>(&sp);
-        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < (int)(sizeof(P32) / 4); i += blockDim.x * blockDim.y)
-            dst[i] = src[i];
-    }
-    __syncthreads();
-    const P32 &p = sp;
-    const int local = blockIdx.x - gr.blk[m];
+    while (m + 1 < c_group.n && (int)blockIdx.x >= c_group.blk[m + 1]) m++;
+    const P32 &p = c_group.p[m];
+    const int local = blockIdx.x - c_group.blk[m];
     const int nxb = (p.g.L0 / 4 + 31) / 32;
-    const int nyb = ((p.g.L1 + gr.by - 1) / gr.by) * p.batch;
+    const int nyb = ((p.g.L1 + c_group.by - 1) / c_group.by) * p.batch;
     const int xb = local % nxb, t = local / nxb;
     const int yb = t % nyb, z = t / nyb;
     const int b = yb % p.batch;
@@ -966,25 +960,32 @@ __global__ void __launch_bounds__(128, 5) k_group32v(const __grid_constant__ Gro
 }
 
 template <bool EF>
-__global__ void k_group_general32(const __grid_constant__ Group32 gr, const int rel)
+__global__ void k_group_general32(const int rel)
 {
-    const int *gb = EF ? gr.gen_e : gr.gen_h;
+    const int *gb = EF ? c_group.gen_e : c_group.gen_h;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= gb[gr.n]) return;
+    if (i >= gb[c_group.n]) return;
     int m = 0;
-    while (m + 1 < gr.n && i >= gb[m + 1]) m++;
-    const int ng = EF ? gr.negen[m] : gr.nhgen[m];
+    while (m + 1 < c_group.n && i >= gb[m + 1]) m++;
+    const int ng = EF ? c_group.negen[m] : c_group.nhgen[m];
     const int local = i - gb[m];
-    general32_cell<EF, false>(gr.p[m], rel, local / ng, (EF ? gr.egen[m] : gr.hgen[m])[local % ng]);
+    general32_cell<EF, false>(c_group.p[m], rel, local / ng, (EF ? c_group.egen[m] : c_group.hgen[m])[local % ng]);
+}
+
+/* the member table for the steps that follow on stream st (from pinned host
+ * memory, so that a captured graph reads it at each replay) */
+void load_group32(const Group32 *host_pinned, cudaStream_t st)
+{
+    cudaMemcpyToSymbolAsync(c_group, host_pinned, sizeof(Group32), 0, cudaMemcpyHostToDevice, st);
 }
 
 void launch_group32v(const Group32 &gr, int rel, cudaStream_t st)
 {
     const dim3 blk(32, gr.by, 1);
-    k_group32v<false><<<gr.blk[gr.n], blk, 0, st>>>(gr, rel);
-    if (gr.gen_h[gr.n] > 0) k_group_general32<false><<<(gr.gen_h[gr.n] + 127) / 128, 128, 0, st>>>(gr, rel);
-    k_group32v<true><<<gr.blk[gr.n], blk, 0, st>>>(gr, rel);
-    if (gr.gen_e[gr.n] > 0) k_group_general32<true><<<(gr.gen_e[gr.n] + 127) / 128, 128, 0, st>>>(gr, rel);
+    k_group32v<false><<<gr.blk[gr.n], blk, 0, st>>>(rel);
+    if (gr.gen_h[gr.n] > 0) k_group_general32<false><<<(gr.gen_h[gr.n] + 127) / 128, 128, 0, st>>>(rel);
+    k_group32v<true><<<gr.blk[gr.n], blk, 0, st>>>(rel);
+    if (gr.gen_e[gr.n] > 0) k_group_general32<true><<<(gr.gen_e[gr.n] + 127) / 128, 128, 0, st>>>(rel);
 }
 
 /* Fold `count` ring slots ending at step *base + rel_end into the FP64 DFT

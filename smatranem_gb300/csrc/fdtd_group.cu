@@ -7,7 +7,9 @@
  * runs.  Here the member plans keep their own device state, schedule, sources
  * and DFT; the group replaces their per-step launches, in one of two modes:
  *   0: one grouped launch per sweep over the cells of every member
- *      (k_group32v: a block finds its member by prefix sums);
+ *      (k_group32v: a block finds its member by prefix sums in a
+ *      constant-memory table; one such group per device at a time, so
+ *      group_run holds a lock and completes before returning in this mode);
  *   1: each member's own vectorised-sweep launches, back to back on the
  *      group's stream;
  * either way captured as one CUDA graph per 32 steps, with each member's DFT
@@ -17,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "plan_internal.cuh"
@@ -26,6 +29,8 @@ using namespace smat::plan;
 
 struct smat_fdtd_group {
     std::vector<smat_fdtd_plan *> m;
+    std::vector<int> cur; /* members' field sets when the graph was captured */
+    Group32 *h_gr = nullptr; /* pinned copy of the member table (mode 0) */
     cudaStream_t stream = nullptr;
     int mode = 0; /* 0: one grouped launch per sweep; 1: each member's own sweep launches */
     int by = 1;
@@ -34,6 +39,8 @@ struct smat_fdtd_group {
 };
 
 namespace {
+
+std::mutex g_table_mu; /* the constant-memory member table of mode 0 */
 
 Group32 make_group(const smat_fdtd_group *g)
 {
@@ -67,8 +74,9 @@ Group32 make_group(const smat_fdtd_group *g)
 void enqueue_group(smat_fdtd_group *g, int rel0, int n)
 {
     if (g->mode == 0) {
-        const Group32 gr = make_group(g);
-        for (int i = 0; i < n; i++) launch_group32v(gr, rel0 + i, g->stream);
+        *g->h_gr = make_group(g); /* same bytes on every call while the members stand still */
+        load_group32(g->h_gr, g->stream);
+        for (int i = 0; i < n; i++) launch_group32v(*g->h_gr, rel0 + i, g->stream);
     } else {
         /* each member's own vectorised sweeps (rows g->by, whole grid), in
          * order on the group's stream: one graph launch per chunk of steps */
@@ -105,6 +113,8 @@ void build_group_graph(smat_fdtd_group *g)
     }
     enqueue_group(g, 0, GRAPH_STEPS);
     for (smat_fdtd_plan *p : g->m) launch_bump(p->d_base, GRAPH_STEPS, g->stream);
+    g->cur.clear();
+    for (smat_fdtd_plan *p : g->m) g->cur.push_back(p->cur);
     if (cudaStreamEndCapture(g->stream, &gg) != cudaSuccess || !gg) {
         cudaGetLastError();
         g->graph_failed = true;
@@ -142,6 +152,11 @@ extern "C" int smat_fdtd_group_create(smat_fdtd_plan *const *plans, int nplans, 
     }
     smat_fdtd_group *g = new (std::nothrow) smat_fdtd_group();
     if (!g) return smat_fail(SMAT_ENOMEM, "group_create: out of host memory");
+    if (cudaMallocHost((void **)&g->h_gr, sizeof(Group32)) != cudaSuccess) {
+        cudaGetLastError();
+        delete g;
+        return smat_fail(SMAT_ENOMEM, "group_create: pinned host memory");
+    }
     g->m.assign(plans, plans + nplans);
     g->stream = plans[0]->stream;
     *out = g;
@@ -153,6 +168,7 @@ extern "C" int smat_fdtd_group_destroy(smat_fdtd_group *g)
     if (!g) return SMAT_OK;
     if (g->stream) cudaStreamSynchronize(g->stream);
     drop_group_graph(g);
+    if (g->h_gr) cudaFreeHost(g->h_gr);
     delete g;
     return SMAT_OK;
 }
@@ -180,8 +196,18 @@ extern "C" int smat_fdtd_group_run(smat_fdtd_group *g, int k_begin, int k_end)
             return smat_fail(SMAT_EINVAL, "group_run: k_end %d beyond member %zu's %d-step schedule", k_end, i,
                              p->nsched);
     }
+    /* mode 0 uses the device's one constant-memory member table: one such
+     * group runs at a time (the run completes before the lock is released) */
+    std::unique_lock<std::mutex> lock(g_table_mu, std::defer_lock);
+    if (g->mode == 0) lock.lock();
     int rc = sync_members(g); /* members' own streams may still hold work */
     if (rc) return rc;
+    /* a member stepped on its own with a fused kernel may have swapped field sets */
+    for (size_t i = 0; i < g->cur.size() && i < g->m.size(); i++)
+        if (g->cur[i] != g->m[i]->cur) {
+            drop_group_graph(g);
+            break;
+        }
     for (smat_fdtd_plan *p : g->m) launch_set(p->d_base, k_begin, g->stream);
     int n = k_end - k_begin;
     if (n >= GRAPH_STEPS) build_group_graph(g);
@@ -200,6 +226,7 @@ extern "C" int smat_fdtd_group_run(smat_fdtd_group *g, int k_begin, int k_end)
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "group_run: launch");
+    if (g->mode == 0) CK(cudaStreamSynchronize(g->stream));
     return SMAT_OK;
 }
 
@@ -241,6 +268,7 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best
     CK(cudaEventCreate(&e1));
     double bms = 1e30;
     int bmode = g->mode, bby = g->by;
+    std::lock_guard<std::mutex> lock(g_table_mu);
     for (int mode : {0, 1})
         for (int by : {1, 2, 4}) {
             g->mode = mode;

@@ -122,7 +122,8 @@ struct Pipe32 {
 
 /* Several FP32 plans stepped together (a group): one vectorised-sweep launch
  * covers the cells of every member; block ranges and general-cell ranges per
- * member are prefix sums.  Passed by value as a __grid_constant__ parameter. */
+ * member are prefix sums.  Loaded into a constant-memory table before the
+ * group's launches (load_group32). */
 constexpr int MAX_GROUP = 32;
 struct Group32 {
     int n, by;
@@ -162,6 +163,7 @@ void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
 void launch_h32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int ngh, cudaStream_t st);
 void launch_e32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int nge, cudaStream_t st);
 void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStream_t st);
+void load_group32(const Group32 *host_pinned, cudaStream_t st);
 void launch_group32v(const Group32 &gr, int rel, cudaStream_t st);
 int pipe32v_max_ctas_per_sm(int threads);
 void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);

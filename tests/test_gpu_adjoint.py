@@ -187,3 +187,24 @@ def test_adjoint_rejects_bad_requests(built):
             p.adjoint_grad(nsteps, 64, 3, 1, col, d.box)
         with pytest.raises(F.FdtdError):  # more steps than scheduled
             p.adjoint_grad(nsteps + 1, 64, 0, 1, col, d.box)
+
+
+def test_adjoint_sums_over_the_batch(built):
+    """J = sum_b |S_b|^2: a batch of two identical excitations gives exactly
+    twice J and twice the gradient of one (FP64)."""
+    F, W = _mods()
+    d = _design(pml_xy=True, shape=(24, 20, 28), design=(6, 5, 4), pml=6)
+    J1, g1, _ = _adjoint(d, d.eps, F.FP64, "pulse", K=32)
+    s = d.with_eps(d.eps)
+    pr = W.prepare(s, dt_factor=1.0 / 0.99)
+    mode = W.mode_profiles(d, n_modes=1)[0]
+    nsteps = 8 * pr.n2pi
+    src, ph = W.pulse_schedule(nsteps, pr.dt, bandwidth=0.5, lams_um=[1.55])
+    with F.Plan.create(s.L, s.iBc, (d.iB, d.iT, d.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                       precision=F.FP64, batch=2) as p:
+        for b in range(2):
+            p.set_incident(b, *mode)
+        p.set_schedule(src, planes=(d.iB, d.iT), phase=ph)
+        J2, g2, _ = p.adjoint_grad(nsteps, 32, 0, 1, _column(mode), d.box)
+    assert J2 == 2 * J1
+    assert np.array_equal(g2 / d.eps, 2 * g1)
