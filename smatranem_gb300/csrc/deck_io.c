@@ -18,6 +18,7 @@
 #include <complex.h>
 #include <stdint.h>
 #include <sys/stat.h>
+#include <unistd.h>
 #include <ctype.h>
 #include <float.h>
 #include <math.h>
@@ -411,7 +412,7 @@ static void write_cache(smat_deck *d, uint64_t sig)
 {
     char name[BUF + 32], tmp[BUF + 64];
     cache_name(d, name);
-    snprintf(tmp, sizeof tmp, "%s.tmp%ld", name, (long)time(NULL));
+    snprintf(tmp, sizeof tmp, "%s.tmp%ld", name, (long)getpid()); /* one writer per process */
     FILE *f = fopen(tmp, "wb");
     if (!f) return; /* the cache is optional: no copy, no error */
     int ok = fwrite(CACHE_MAGIC, 1, sizeof CACHE_MAGIC, f) == sizeof CACHE_MAGIC && fwrite(&sig, sizeof sig, 1, f) == 1 &&

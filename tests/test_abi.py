@@ -3,6 +3,9 @@ import ctypes
 import os
 import re
 
+import numpy as np
+import pytest
+
 from conftest import ROOT
 
 
@@ -35,3 +38,18 @@ def test_error_message_is_reported(built):
     assert lib.smat_set_tau(ctypes.c_double(0.0), ctypes.c_double(1.0), ctypes.byref(n), ctypes.byref(r),
                             ctypes.byref(i)) == -1
     assert b"positive" in lib.smat_last_error()
+
+
+@pytest.mark.parametrize("L,batch,msg", [
+    ((1000, 1000, 1000, 1), 1, b"too large"),   # 3*L3D past 32-bit reference indices
+    ((0, 4, 4, 1), 1, b"positive"),
+    ((4, 4, -1, 1), 1, b"positive"),
+    ((4, 4, 4, 1), 0, b"batch"),
+])
+def test_create_rejects_bad_shapes(built, L, batch, msg):
+    """Plan creation checks the grid before touching the GPU or the arrays."""
+    from smatranem_gb300 import fdtd
+    dummy = np.zeros(8, np.complex128)
+    with pytest.raises(fdtd.FdtdError) as e:
+        fdtd.Plan.create(L, (0, 0, 0), (0, 1, 0, 1), 1.0, 0.0, dummy, dummy, np.zeros(8), batch=batch)
+    assert e.value.code == -1 and msg in str(e.value).encode()

@@ -449,3 +449,61 @@ def test_gpu_overlap_matches_oracle_s_calc(built, port):
                 EB[0::2], EB[1::2] = d[2], d[3]
                 ref = port.overlap(L, tilxi, HB, EB)
                 assert np.max(np.abs(S[fi] - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+# ---- degenerate grids -------------------------------------------------------
+
+DEGENERATE = [
+    # (L, iBc, iBTIin): a dimension of 1 or 2 wraps onto itself / its neighbour
+    ((1, 1, 6, 1), (1, 1, 1), (0, 5, 2, 1)),
+    ((2, 3, 5, 1), (-1, 0, 1), (0, 4, 1, -1)),
+    ((4, 1, 7, 2), (0, -1, -1), (1, 6, 3, 1)),
+    ((1, 5, 4, 1), (1, -1, 0), (0, 3, 2, 1)),
+    ((8, 2, 2, 0), (1, 1, -1), (0, 1, 1, 1)),
+]
+
+
+@pytest.mark.parametrize("case", range(len(DEGENERATE)))
+def test_degenerate_grids(built, port, case):
+    """Grids with a dimension of 1 or 2 (every curl neighbour wraps onto the
+    cell itself or its only neighbour, with each boundary factor): FP64
+    bit-identical to the oracle's reference loop, every FP32 tuning
+    bit-identical to the scalar sweeps and within 2e-5 of FP64."""
+    f = _fdtd()
+    from smatranem_gb300 import workloads as W
+    L, iBc, iBTIin = DEGENERATE[case]
+    s = W.random_structure(L, seed=40 + case, pml=(0, 0, 0), iBc=iBc)
+    pr = W.prepare(s)
+    coef = pr.coefficients()
+    n3, pl = s.n3, L[0] * L[1]
+    tp = (1, 1, 3)
+    nsteps = 25
+    H0, E0 = W.random_fields(n3, pr.lnotn, seed=7, scale=1e-2)
+    Hinc, Einc = W.random_incident(pl, seed=6)
+    with f.Plan.create(L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma) as p:
+        p.set_fields(0, H0, E0)
+        p.set_incident(0, Hinc, Einc)
+        p.set_cw_schedule(pr.n2pi, tp)
+        p.run(0, nsteps)
+        Hg, Eg = p.get_fields(0)
+        mon = p.get_monitor(0)
+    H, E = H0.copy(), E0.copy()
+    mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+    assert port.time_loop(L, *coef, s.iBc, H, E, iBTIin, Hinc, Einc, pr.n2pi, tp, 0, nsteps, *mons, pr.cont,
+                          pr.addr) == 0
+    assert np.array_equal(Hg, H) and np.array_equal(Eg, E)
+    for a, b_ in zip(mon, mons):
+        assert np.array_equal(a, b_)
+    # FP32: all tunings that apply give the scalar sweeps' bits
+    fp32_planes = (iBTIin[0], iBTIin[1], 0, 1)
+    ref = _run_fp32(s, pr, fp32_planes, (0, 4, 0, 0, 4), 20, batch=1)
+    tunings = [(0, 1, 0, 0, 4), (0, 2, 1, 0, 4), (1, 2, 1, 0, 4), (1, 8, 3, 0, 5)]
+    if L[0] % 4 == 0:
+        tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (3, 2, 2, 0, 4), (4, 1, 0, 0, 0)]
+        if tuple(iBc) == (0, 0, 0):
+            tunings += [(5, 4, 2, 1, 4)]
+    for tuning in tunings:
+        got = _run_fp32(s, pr, fp32_planes, tuning, 20, batch=1)
+        for rb, gb in zip(ref, got):
+            for a, b_ in zip(rb, gb):
+                assert np.array_equal(a, b_), tuning
