@@ -495,8 +495,9 @@ def run_adjoint(args):
     fd = np.array(fd)
     a32 = np.array([g32[c] for c in cells])
     a64 = np.array([g64[c] for c in cells])
-    fs = float(np.max(np.abs(fd)))
+    fs = float(np.max(np.abs(fd))) if len(cells) else float("nan")
     cells_total = d.s.n3 * nsteps
+    nan = float("nan")
     print(json.dumps({
         "mode": "adjoint", "config": "design 160x160x120, 60x60x20 design cells, 12-cell PML on 6 faces, TE0 "
                                      "output-port overlap at 1.55 um, Gaussian pulse",
@@ -504,9 +505,10 @@ def run_adjoint(args):
         "adjoint_fp32_s": t32, "adjoint_fp64_s": t64,
         "adjoint_fp32_gcell_per_s": 3 * cells_total / t32 / 1e9,
         "fd_cells": int(args.fd_cells), "fd_s": t_fd,
-        "err_fp32_adjoint_vs_fd": float(np.max(np.abs(a32 - fd)) / fs),
-        "err_fp64_adjoint_vs_fd": float(np.max(np.abs(a64 - fd)) / fs),
-        "median_rel_err_fp32_vs_fd": float(np.median(np.abs(a32 - fd) / np.maximum(np.abs(fd), 1e-300))),
+        "err_fp32_adjoint_vs_fd": float(np.max(np.abs(a32 - fd)) / fs) if len(cells) else nan,
+        "err_fp64_adjoint_vs_fd": float(np.max(np.abs(a64 - fd)) / fs) if len(cells) else nan,
+        "median_rel_err_fp32_vs_fd": (float(np.median(np.abs(a32 - fd) / np.maximum(np.abs(fd), 1e-300)))
+                                      if len(cells) else nan),
         "err_fp32_vs_fp64_adjoint_whole_box": float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64))),
         "errors_are": "max |g - g_fd| / max |g_fd| over the checked cells (and over the whole box for fp32 vs fp64)",
     }))
