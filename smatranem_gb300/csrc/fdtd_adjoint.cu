@@ -37,6 +37,7 @@
 
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -254,6 +255,179 @@ __global__ void k_adj_record(const Geo g, const int batch, const Box bx, const T
     for (int c = 0; c < 3; c++) dst[((long long)b * 3 + c) * bx.n + i] = E[((long long)b * 3 + c) * g.n3 + l];
 }
 
+/* ---------------------------------------------------------------------------
+ * Vectorised FP32 adjoint steps (L0 % 4 == 0): four x-cells per thread, as
+ * the forward sweep k_sweep32v -- float4 loads of the adjoint fields and the
+ * coefficient stream, x neighbours by warp shuffle -- with the per-element
+ * arithmetic of k_adj_e / k_adj_h.  A block is 32 x by threads; grid as
+ * k_sweep32v's (x blocks, row blocks x excitations, planes).
+ * ------------------------------------------------------------------------- */
+__device__ __forceinline__ float4 ldf4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void stf4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float e4(const float4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+__device__ __forceinline__ void s4(float4 &v, int i, float x)
+{
+    if (i == 0) v.x = x;
+    else if (i == 1) v.y = x;
+    else if (i == 2) v.z = x;
+    else v.w = x;
+}
+
+/* coefficients (A+, B+, A-, B-) of component c of element i of a quad whose
+ * coefficient stream components are cq[3] (same rules as Coef32::get) */
+__device__ __forceinline__ void coef32_elem(const Coef32 &cf, bool efield, const float4 cq[3], int i, int c,
+                                            bool split, int x, int y, int z, float &Ap, float &Bp, float &Am,
+                                            float &Bm)
+{
+    const float c0 = e4(cq[0], i);
+    if (isnan(c0)) {
+        const Rec32 r = (efield ? cf.erec : cf.hrec)[__float_as_int(e4(cq[1], i))];
+        Ap = r.A0[c];
+        Bp = r.B0[c];
+        if (r.kind == RK_A) {
+            Am = r.A1[c];
+            Bm = r.B1[c];
+        } else {
+            Am = Ap;
+            Bm = Bp;
+        }
+        return;
+    }
+    const float bn = e4(cq[c], i);
+    if (!split) {
+        Ap = Am = 1.0f;
+        Bp = Bm = bn;
+        return;
+    }
+    const int jx[3] = {x, cf.s1 + y, cf.s2 + z};
+    const int i1 = jx[(c + 1) % 3], i2 = jx[(c + 2) % 3];
+    const float *tA = cf.tab + (efield ? 2 * cf.S : 0), *tG = cf.tab + (efield ? 3 * cf.S : cf.S);
+    Ap = tA[i1];
+    Bp = bn * tG[i1];
+    Am = tA[i2];
+    Bm = bn * tG[i2];
+}
+
+template <bool EF>
+__global__ void __launch_bounds__(128, 4) k_adj32v(const Geo g, const int batch, const Coef32 cf,
+                                                  const AState<float> s, const Obj o, const int k, const Box bx,
+                                                  const float *__restrict__ rec1, const float *__restrict__ rec0,
+                                                  double *__restrict__ grad)
+{
+    const int b = blockIdx.y % batch;
+    const int xr = (blockIdx.x * 32 + threadIdx.x) * 4;
+    const int y = (blockIdx.y / batch) * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (y >= g.L1) return; /* uniform per warp */
+    const bool live = xr < g.L0;
+    const int x0 = live ? xr : g.L0 - 4;
+    const long long n3 = g.n3, bs = 3 * n3;
+    const long long l = x0 + (long long)g.L0 * (y + (long long)g.L1 * z);
+    /* EF: transpose of the E sweep (reads the H adjoint, forward neighbours);
+     * else of the H sweep (reads the E adjoint, backward neighbours) */
+    const float *PG = (EF ? s.phiH : s.phiE) + b * bs, *QG = (EF ? s.psiH : s.psiE) + b * bs;
+    float *PF = (EF ? s.phiE : s.phiH) + b * bs, *QF = (EF ? s.psiE : s.psiH) + b * bs;
+    const float *cfs = EF ? cf.be : cf.bh;
+    const bool ey = EF ? (y + 1 == g.L1) : (y == 0);
+    const bool ez = EF ? (z + 1 == g.L2) : (z == 0);
+    const long long oy = (long long)g.L0 * (EF ? (ey ? -(g.L1 - 1) : 1) : (ey ? g.L1 - 1 : -1));
+    const long long oz = (long long)g.pl * (EF ? (ez ? -(g.L2 - 1) : 1) : (ez ? g.L2 - 1 : -1));
+    const float fy = ey ? (float)g.bc[1] : 1.0f, fz = ez ? (float)g.bc[2] : 1.0f;
+    float4 cq[3], pf[3], qf[3], pg[3], qg[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        cq[c] = ldf4(cfs + c * n3 + l);
+        pf[c] = ldf4(PF + c * n3 + l);
+        qf[c] = ldf4(QF + c * n3 + l);
+        pg[c] = ldf4(PG + c * n3 + l);
+        qg[c] = ldf4(QG + c * n3 + l);
+    }
+    /* y and z neighbours: EF reads psi_z, phi_x at y+1 and phi_y, psi_x at z+1;
+     * the H transpose reads psi_z, phi_x at y-1 and phi_y, psi_x at z-1 */
+    float4 qyz = ldf4(QG + 2 * n3 + l + oy), pyx = ldf4(PG + 0 * n3 + l + oy);
+    float4 pzy = ldf4(PG + 1 * n3 + l + oz), qzx = ldf4(QG + 0 * n3 + l + oz);
+    /* x neighbours: phi_z and psi_y at x+1 (EF) or x-1 */
+    const unsigned full = 0xffffffffu;
+    float xpz, xqy;
+    if (EF) {
+        xpz = __shfl_down_sync(full, pg[2].x, 1);
+        xqy = __shfl_down_sync(full, qg[1].x, 1);
+        if ((threadIdx.x & 31) == 31 || x0 + 4 == g.L0) {
+            const bool edge = x0 + 4 == g.L0;
+            const long long ox = edge ? -(g.L0 - 4) : 4;
+            const float f = edge ? (float)g.bc[0] : 1.0f;
+            xpz = f * PG[2 * n3 + l + ox];
+            xqy = f * QG[1 * n3 + l + ox];
+        }
+    } else {
+        xpz = __shfl_up_sync(full, pg[2].w, 1);
+        xqy = __shfl_up_sync(full, qg[1].w, 1);
+        if ((threadIdx.x & 31) == 0 || x0 == 0) {
+            const bool edge = x0 == 0;
+            const long long ox = edge ? g.L0 - 1 : -1;
+            const float f = edge ? (float)g.bc[0] : 1.0f;
+            xpz = f * PG[2 * n3 + l + ox];
+            xqy = f * QG[1 * n3 + l + ox];
+        }
+    }
+    if (!live) return;
+    const float fx_in = 1.0f;
+    const bool pyzm = cf.pmask[cf.s1 + y] | cf.pmask[cf.s2 + z];
+    float gs[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    if (z == o.zq) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int px = x0 + i + g.L0 * y;
+            gs[0][i] = (float)sample_sens(o, b, EF ? 2 : 0, px, g.pl, k);
+            gs[1][i] = (float)sample_sens(o, b, EF ? 3 : 1, px, g.pl, k);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int x = x0 + i;
+        const bool split = cf.pmask[x] | pyzm;
+        /* neighbour along x of element i: phi_z, psi_y */
+        const float npz = EF ? (i == 3 ? xpz : e4(pg[2], i + 1)) : (i == 0 ? xpz : e4(pg[2], i - 1));
+        const float nqy = EF ? (i == 3 ? xqy : e4(qg[1], i + 1)) : (i == 0 ? xqy : e4(qg[1], i - 1));
+        float sv[3];
+        if (EF) { /* -(pl + mi), forward neighbours */
+            const float pl0 = fy * e4(qyz, i) - e4(qg[2], i), mi0 = e4(pg[1], i) - fz * e4(pzy, i);
+            const float pl1 = fz * e4(qzx, i) - e4(qg[0], i), mi1 = e4(pg[2], i) - fx_in * npz;
+            const float pl2 = fx_in * nqy - e4(qg[1], i), mi2 = e4(pg[0], i) - fy * e4(pyx, i);
+            sv[0] = -(pl0 + mi0) + gs[0][i];
+            sv[1] = -(pl1 + mi1) + gs[1][i];
+            sv[2] = -(pl2 + mi2);
+        } else { /* +(pl + mi), backward neighbours */
+            const float pl0 = e4(qg[2], i) - fy * e4(qyz, i), mi0 = -e4(pg[1], i) + fz * e4(pzy, i);
+            const float pl1 = e4(qg[0], i) - fz * e4(qzx, i), mi1 = -e4(pg[2], i) + fx_in * npz;
+            const float pl2 = e4(qg[1], i) - fx_in * nqy, mi2 = -e4(pg[0], i) + fy * e4(pyx, i);
+            sv[0] = pl0 + mi0 + gs[0][i];
+            sv[1] = pl1 + mi1 + gs[1][i];
+            sv[2] = pl2 + mi2;
+        }
+        long long bi = 0;
+        const bool design = EF && grad && in_box(bx, x, y, z, bi);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float Ap, Bp, Am, Bm;
+            coef32_elem(cf, EF, cq, i, c, split, x, y, z, Ap, Bp, Am, Bm);
+            const float phi = Ap * e4(pf[c], i) + Bp * sv[c];
+            s4(pf[c], i, phi);
+            s4(qf[c], i, Am * e4(qf[c], i) + Bm * sv[c]);
+            if (design && Bp != 0.0f) {
+                const long long r = ((long long)b * 3 + c) * bx.n + bi;
+                const double lam = (double)phi / (double)Bp;
+                grad[r] -= lam * ((double)rec1[r] - (double)Ap * (double)rec0[r]);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        stf4(PF + c * n3 + l, pf[c]);
+        stf4(QF + c * n3 + l, qf[c]);
+    }
+}
+
 } // namespace adj
 } // namespace smat
 
@@ -324,6 +498,25 @@ int zero_state(smat_fdtd_plan *p)
     if (p->d_acc)
         CK(cudaMemsetAsync(p->d_acc, 0, (size_t)p->batch * p->nfreq * p->nq * 4 * p->pl * 2 * 8, p->stream));
     return SMAT_OK;
+}
+
+/* the vectorised FP32 adjoint step where it applies (L0 % 4 == 0); false:
+ * the caller launches the scalar kernels */
+bool adj_launch_vec(smat_fdtd_plan *p, const Geo &g, int batch, const Coef32 &cf, const AState<float> &as,
+                    const Obj &o, int k, const Box &bx, const float *rec1, const float *rec0, double *grad)
+{
+    if (g.L0 % 4 != 0 || p->adj_scalar) return false;
+    const int by = 2;
+    const dim3 blk(32, by, 1), grd((g.L0 / 4 + 31) / 32, ((g.L1 + by - 1) / by) * batch, g.L2);
+    k_adj32v<true><<<grd, blk, 0, p->stream>>>(g, batch, cf, as, o, k, bx, rec1, rec0, grad);
+    k_adj32v<false><<<grd, blk, 0, p->stream>>>(g, batch, cf, as, o, k, bx, nullptr, nullptr, nullptr);
+    return true;
+}
+
+bool adj_launch_vec(smat_fdtd_plan *, const Geo &, int, const Coef64 &, const AState<double> &, const Obj &, int,
+                    const Box &, const double *, const double *, double *)
+{
+    return false;
 }
 
 template <class T, class C>
@@ -428,6 +621,9 @@ int adjoint_run(smat_fdtd_plan *p, const C &coef, int nsteps, int K, int f, int 
                                                         rec + rec_n * (k - k0 + 1));
         }
         for (int k = k1 - 1; k >= k0; k--) {
+            if (adj_launch_vec(p, g, batch, coef, as, o, k, bx, rec + rec_n * (k - k0 + 1), rec + rec_n * (k - k0),
+                               dgrad))
+                continue;
             k_adj_e<T, C><<<gc, 256, 0, p->stream>>>(g, batch, coef, as, o, k, bx, rec + rec_n * (k - k0 + 1),
                                                      rec + rec_n * (k - k0), dgrad);
             k_adj_h<T, C><<<gc, 256, 0, p->stream>>>(g, batch, coef, as, o, k);
@@ -491,6 +687,10 @@ extern "C" int smat_fdtd_adjoint_grad(smat_fdtd_plan *p, int nsteps, int K, int 
                     return smat_fail(SMAT_EINVAL, "adjoint: design cell %lld is a PML cell", l);
             }
     if (p->precision == SMAT_FP32) {
+        /* SMATRAN_ADJOINT_SCALAR=1: the one-cell-per-thread kernels even where
+         * the vectorised ones apply (for comparing the two) */
+        const char *sc = getenv("SMATRAN_ADJOINT_SCALAR");
+        p->adj_scalar = sc && sc[0] && sc[0] != '0';
         Coef32 c;
         c.bh = p->d_bh;
         c.be = p->d_be;

@@ -105,6 +105,7 @@ struct smat_fdtd_plan {
     std::vector<int> hgen_z, egen_z; /* [L2+1]: index of the first general cell of plane z */
     int szc = 0; /* sweeps (kernels 0, 2): planes per H/E chunk, 0 = whole grid */
     int sweep_mb = 5; /* vectorised sweep register bound: minimum resident blocks 5, 6 or 8 */
+    bool adj_scalar = false; /* FP32 adjoint: scalar kernels even where the vectorised ones apply */
     std::vector<int> hgen_host, egen_host; /* host copies of the general-cell lists */
     /* pipelined sweeps (kernel 4) */
     int pipe_by = 0, pipe_grid = 0, pipe_lag = 1, pipe_nxw = 32;

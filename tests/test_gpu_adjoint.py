@@ -208,3 +208,17 @@ def test_adjoint_sums_over_the_batch(built):
         J2, g2, _ = p.adjoint_grad(nsteps, 32, 0, 1, _column(mode), d.box)
     assert J2 == 2 * J1
     assert np.array_equal(g2 / d.eps, 2 * g1)
+
+
+def test_vectorised_fp32_adjoint_matches_the_scalar_one(built, monkeypatch):
+    """The float4 adjoint kernels (four x-cells per thread) against the
+    one-cell-per-thread ones on the all-face PML case: same J, gradients
+    within 1e-6 of the largest entry (the two may contract multiply-adds
+    differently)."""
+    F, _ = _mods()
+    d = _design(pml_xy=True)
+    Jv, gv, _ = _adjoint(d, d.eps, F.FP32, "pulse")
+    monkeypatch.setenv("SMATRAN_ADJOINT_SCALAR", "1")
+    Js, gs, _ = _adjoint(d, d.eps, F.FP32, "pulse")
+    assert Jv == Js
+    assert np.max(np.abs(gv - gs)) <= 1e-6 * np.max(np.abs(gs))
