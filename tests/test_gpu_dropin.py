@@ -65,3 +65,22 @@ def test_dropin_fp32_within_tolerance(built, tmp_path):
     big = max(b)
     for x, y in zip(a, b):
         assert abs(x - y) <= 1e-4 * big
+
+
+@pytest.mark.parametrize("name", DECKS)
+def test_dropin_with_deck_cache(built, tmp_path, name):
+    """With "FDTD_GPU: cache = y" the first run writes <prefix>.smatdeck and the
+    second reads it; both print the reference's report."""
+    src = os.path.join(GOLDEN, "decks", name)
+    if int(open(os.path.join(src, "reference_status.txt")).read()) != 0:
+        pytest.skip("a deck the reference rejects")
+    work = tmp_path / name
+    shutil.copytree(src, work)
+    with open(work / "input.txt", "a") as f:
+        f.write("\tFDTD_GPU: cache = y\n")
+    ref = _comparable(open(os.path.join(src, "reference_stderr.txt")).read())
+    for run in range(2):
+        r = subprocess.run([EXE, "input.txt"], cwd=work, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        assert _comparable(r.stderr) == ref, run
+        assert any(p.name.endswith(".smatdeck") for p in (work / "Data").iterdir())
