@@ -264,10 +264,11 @@ int smat_fdtd_group_sync(smat_fdtd_group *group);
 
 /* Adjoint gradient. ----------------------------------------------------------
  * No counterpart in the reference (it has no gradient).  The objective is
- *   J = sum_b |S_b|^2,  S_b = sum_r conj(t_r) x_r,  x = (HB_x, HB_y, -EB_y, EB_x)
+ *   J = sum_b |S_b|^2,  S_b = sum_r conj(t_b,r) x_b,r,  x = (HB_x, HB_y, -EB_y, EB_x)
  * of excitation b's DFT at frequency f on DFT plane slot q (the S_calc
- * projection, S_calc :437-445, of one mode column t = tilXi_col, 4*L0*L1
- * complex, rows in that order).  The call runs the plan's schedule from rest
+ * projection, S_calc :437-445) with mode columns tilXi_cols: ncols = 1 column
+ * for every excitation, or ncols = batch, column b for excitation b (4*L0*L1
+ * complex each, rows in that order; a weight w_b enters as sqrt(w_b) t_b).  The call runs the plan's schedule from rest
  * (fields and DFT zeroed) for nsteps steps with a checkpoint every K steps,
  * then runs the discrete adjoint backwards, recomputing each K-step segment
  * from its checkpoint.  Returns J and, for each cell i of the box
@@ -280,8 +281,8 @@ int smat_fdtd_group_sync(smat_fdtd_group *group);
  * stable-form (metal) cells.  Afterwards the DFT holds the forward result and
  * the fields are those of the first checkpoint segment.  Device memory: one
  * state copy per checkpoint (ceil(nsteps/K) copies) plus four field arrays. */
-int smat_fdtd_adjoint_grad(smat_fdtd_plan *plan, int nsteps, int K, int f, int q, const double *tilXi_col,
-                           const int box[6], double *grad, double *grad_c, double *J);
+int smat_fdtd_adjoint_grad(smat_fdtd_plan *plan, int nsteps, int K, int f, int q, int ncols,
+                           const double *tilXi_cols, const int box[6], double *grad, double *grad_c, double *J);
 
 /* The FDTD input deck and the drop-in program. ------------------------------
  * A deck is what the reference FDTD reads (main :44-99): input.txt (keys

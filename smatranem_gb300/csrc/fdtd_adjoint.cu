@@ -12,9 +12,9 @@
  * with pl/mi the two halves of the curl of the total field (backward
  * differences for H, :393-413, forward ones for E, :372-392), and a DFT sample
  * of the total H', E' on the monitor planes.  Objective
- *   J = sum_b |S_b|^2,  S_b = t^H x_b,  x_b = (HB_x, HB_y, -EB_y, EB_x)
+ *   J = sum_b |S_b|^2,  S_b = t_b^H x_b,  x_b = (HB_x, HB_y, -EB_y, EB_x)
  * of excitation b's DFT at one frequency and plane (the S_calc projection,
- * :437-445).
+ * :437-445), with one mode column t for all excitations or one per excitation.
  *
  * Adjoint: with L = dJ/d(state) and the weighted adjoints phi+- = B+- L+- that
  * neighbours read (the transpose of "read the total" sends the same value to
@@ -520,7 +520,7 @@ bool adj_launch_vec(smat_fdtd_plan *, const Geo &, int, const Coef64 &, const AS
 }
 
 template <class T, class C>
-int adjoint_run(smat_fdtd_plan *p, const C &coef, int nsteps, int K, int f, int q, const double *tcol,
+int adjoint_run(smat_fdtd_plan *p, const C &coef, int nsteps, int K, int f, int q, int ncols, const double *tcols,
                 const Box &bx, double *grad, double *grad_c, double *J)
 {
     Scratch sc;
@@ -570,6 +570,7 @@ int adjoint_run(smat_fdtd_plan *p, const C &coef, int nsteps, int K, int f, int 
     double Jv = 0.0;
     for (int b = 0; b < batch; b++) {
         if ((rc = smat_fdtd_get_dft(p, b, f, q, acc.data()))) return rc;
+        const double *tcol = tcols + (ncols == 1 ? 0 : (size_t)b * 8 * pl); /* 4*pl complex per column */
         std::complex<double> S = 0.0;
         /* rows of t: HB_x, HB_y, -EB_y, EB_x; DFT components v: H_x, H_y, E_x, E_y */
         const int row_of_v[4] = {0, 1, 3, 2};
@@ -652,11 +653,14 @@ int adjoint_run(smat_fdtd_plan *p, const C &coef, int nsteps, int K, int f, int 
 
 } // namespace
 
-extern "C" int smat_fdtd_adjoint_grad(smat_fdtd_plan *p, int nsteps, int K, int f, int q, const double *tilXi_col,
+extern "C" int smat_fdtd_adjoint_grad(smat_fdtd_plan *p, int nsteps, int K, int f, int q, int ncols, const double *tilXi_cols,
                                       const int box[6], double *grad, double *grad_c, double *J)
 {
     smat_clear_error();
-    if (!p || !tilXi_col || !box || !grad || !J) return smat_fail(SMAT_EINVAL, "adjoint: null argument");
+    if (!p || !tilXi_cols || !box || !grad || !J) return smat_fail(SMAT_EINVAL, "adjoint: null argument");
+    if (ncols != 1 && ncols != p->batch)
+        return smat_fail(SMAT_EINVAL, "adjoint: %d objective columns: give 1 or one per excitation (%d)", ncols,
+                         p->batch);
     if (nsteps < 1 || nsteps > p->nsched || !p->d_sched)
         return smat_fail(SMAT_EINVAL, "adjoint: nsteps %d outside the %d-step schedule", nsteps, p->nsched);
     if (K < 1) return smat_fail(SMAT_EINVAL, "adjoint: checkpoint interval K must be >= 1");
@@ -701,7 +705,7 @@ extern "C" int smat_fdtd_adjoint_grad(smat_fdtd_plan *p, int nsteps, int K, int 
         c.S = p->L[0] + p->L[1] + p->L[2];
         c.s1 = p->L[0];
         c.s2 = p->L[0] + p->L[1];
-        return adjoint_run<float>(p, c, nsteps, K, f, q, tilXi_col, bx, grad, grad_c, J);
+        return adjoint_run<float>(p, c, nsteps, K, f, q, ncols, tilXi_cols, bx, grad, grad_c, J);
     }
     Coef64 c;
     c.flags = p->d_flags;
@@ -709,5 +713,5 @@ extern "C" int smat_fdtd_adjoint_grad(smat_fdtd_plan *p, int nsteps, int K, int 
     c.cm = p->d_cm;
     c.ca = p->d_ca;
     c.lnotn = p->lnotn;
-    return adjoint_run<double>(p, c, nsteps, K, f, q, tilXi_col, bx, grad, grad_c, J);
+    return adjoint_run<double>(p, c, nsteps, K, f, q, ncols, tilXi_cols, bx, grad, grad_c, J);
 }

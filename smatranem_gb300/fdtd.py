@@ -80,7 +80,7 @@ def lib():
         L.smat_fdtd_dft_count.argtypes = [_P, _P, _P]
         L.smat_fdtd_dft_device.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P]
         L.smat_overlap.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, _P, _P, _P, _P]
-        L.smat_fdtd_adjoint_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P]
+        L.smat_fdtd_adjoint_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P]
         L.smat_fdtd_group_create.argtypes = [_P, C.c_int, _P]
         L.smat_fdtd_group_destroy.argtypes = [_P]
         L.smat_fdtd_group_set_tuning.argtypes = [_P, C.c_int, C.c_int]
@@ -363,19 +363,22 @@ class Plan:
         _check(lib().smat_fdtd_overlap(self._h, b, q, ncols, _ptr(t), _ptr(S)))
         return S
 
-    def adjoint_grad(self, nsteps, K, f, q, tilxi_col, box):
-        """J = sum_b |S_b|^2 of mode column tilxi_col (4*L0*L1 complex) on DFT
-        plane slot q at frequency f, and dJ/ds for every cell of box
-        (x0, x1, y0, y1, z0, z1), s scaling the cell's permittivity by (1 + s)
-        (smat_fdtd_adjoint_grad).  Returns (J, grad [nz, ny, nx], grad_c
-        [3, nz, ny, nx])."""
-        t = _c128(tilxi_col).reshape(-1)
+    def adjoint_grad(self, nsteps, K, f, q, tilxi_cols, box):
+        """J = sum_b |S_b|^2 of mode columns tilxi_cols (4*L0*L1 complex: one
+        column for every excitation, or a (batch, 4*L0*L1) array, row b for
+        excitation b) on DFT plane slot q at frequency f, and dJ/ds for every
+        cell of box (x0, x1, y0, y1, z0, z1), s scaling the cell's permittivity
+        by (1 + s) (smat_fdtd_adjoint_grad).  Returns (J, grad [nz, ny, nx],
+        grad_c [3, nz, ny, nx])."""
+        t = _c128(tilxi_cols)
+        ncols = 1 if t.ndim == 1 else t.shape[0]
+        t = t.reshape(-1)
         bx = _i32(box)
         shape = (int(bx[5] - bx[4]), int(bx[3] - bx[2]), int(bx[1] - bx[0]))
         g = np.zeros(shape)
         gc = np.zeros((3,) + shape)
         J = C.c_double(0)
-        _check(lib().smat_fdtd_adjoint_grad(self._h, nsteps, K, f, q, _ptr(t), _ptr(bx), _ptr(g), _ptr(gc),
+        _check(lib().smat_fdtd_adjoint_grad(self._h, nsteps, K, f, q, ncols, _ptr(t), _ptr(bx), _ptr(g), _ptr(gc),
                                             C.byref(J)))
         return J.value, g, gc
 

@@ -222,3 +222,28 @@ def test_vectorised_fp32_adjoint_matches_the_scalar_one(built, monkeypatch):
     Js, gs, _ = _adjoint(d, d.eps, F.FP32, "pulse")
     assert Jv == Js
     assert np.max(np.abs(gv - gs)) <= 1e-6 * np.max(np.abs(gs))
+
+
+def test_adjoint_with_a_column_per_excitation(built):
+    """One objective column per excitation: the same source twice, the second
+    projected on twice the mode column, gives J and the gradient 5 times those
+    of the first alone (|2 S|^2 = 4 |S|^2; FP64)."""
+    F, W = _mods()
+    d = _design(pml_xy=True, shape=(24, 20, 28), design=(6, 5, 4), pml=6)
+    J1, g1, _ = _adjoint(d, d.eps, F.FP64, "pulse", K=32)
+    s = d.with_eps(d.eps)
+    pr = W.prepare(s, dt_factor=1.0 / 0.99)
+    mode = W.mode_profiles(d, n_modes=1)[0]
+    nsteps = 8 * pr.n2pi
+    src, ph = W.pulse_schedule(nsteps, pr.dt, bandwidth=0.5, lams_um=[1.55])
+    col = _column(mode)
+    with F.Plan.create(s.L, s.iBc, (d.iB, d.iT, d.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                       precision=F.FP64, batch=2) as p:
+        for b in range(2):
+            p.set_incident(b, *mode)
+        p.set_schedule(src, planes=(d.iB, d.iT), phase=ph)
+        J2, g2, _ = p.adjoint_grad(nsteps, 32, 0, 1, np.stack([col, 2 * col]), d.box)
+        with pytest.raises(F.FdtdError):  # three columns for two excitations
+            p.adjoint_grad(nsteps, 32, 0, 1, np.stack([col, col, col]), d.box)
+    assert J2 == pytest.approx(5 * J1, rel=1e-13)
+    assert np.allclose(g2 / d.eps, 5 * g1, rtol=1e-12, atol=1e-12 * np.max(np.abs(g1)))
