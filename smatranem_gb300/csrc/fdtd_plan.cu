@@ -642,6 +642,19 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
             std::vector<Rec32> &recs = side ? erec : hrec;
             const double *m = side ? ep : mu;
             const double *A = side ? Ae : Ah, *B = side ? Be : Bh;
+            const bool lossless = m[2 * (3 * l + 0) + 1] == 0.0 && m[2 * (3 * l + 1) + 1] == 0.0 &&
+                                  m[2 * (3 * l + 2) + 1] == 0.0;
+            bool simple = false;
+            if (k == 'n')
+                simple = lossless && !(side == 1 && pec) && (float)A[3 * l] == 1.0f && (float)A[1 + 3 * l] == 1.0f &&
+                         (float)A[2 + 3 * l] == 1.0f;
+            else if (k == 'a')
+                simple = lossless;
+            if (simple) {
+                for (int c = 0; c < 3; c++) cf[c * n3 + l] = (float)(1. / (iR * m[2 * (3 * l + c)]));
+                continue;
+            }
+            /* a record: everything else (a few per mille of the cells) */
             Rec32 r;
             memset(&r, 0, sizeof r);
             for (int c = 0; c < 3; c++) {
@@ -652,27 +665,18 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
                     r.B1[c] = (float)B[aux(l, c)];
                 }
             }
-            const bool lossless = m[2 * (3 * l + 0) + 1] == 0.0 && m[2 * (3 * l + 1) + 1] == 0.0 &&
-                                  m[2 * (3 * l + 2) + 1] == 0.0;
-            bool simple = false;
             if (k == 'n') {
-                simple = lossless && !(side == 1 && pec) && r.A0[0] == 1.0f && r.A0[1] == 1.0f && r.A0[2] == 1.0f;
                 r.kind = RK_N;
             } else if (k == 'a') {
-                simple = lossless;
                 r.kind = RK_A;
             } else {
                 const bool stable_here = side == 0 ? (k == 'h' || k == 'b') : (k == 'e' || k == 'b');
                 r.kind = stable_here ? RK_STABLE : RK_FROZEN;
             }
-            if (simple) {
-                for (int c = 0; c < 3; c++) cf[c * n3 + l] = (float)(1. / (iR * m[2 * (3 * l + c)]));
-            } else {
-                if (side == 1 && pec) {
-                    for (int c = 0; c < 3; c++) r.A0[c] = r.B0[c] = 0.0f;
-                }
-                put_rec(cf, recs, l, r);
+            if (side == 1 && pec) {
+                for (int c = 0; c < 3; c++) r.A0[c] = r.B0[c] = 0.0f;
             }
+            put_rec(cf, recs, l, r);
         }
     }
     /* 1-D sigma tables: rows A_h, G_h, A_e, G_e over the three axes */

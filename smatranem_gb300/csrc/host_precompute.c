@@ -163,8 +163,10 @@ int smat_set_address(const int L[4], const double *sigma, const double *mu_, con
                 char k = (pml[0][j0] || pml[1][j1] || pml[2][j2]) ? 'a' : 'n';
                 /* lossy media override, the last component deciding (:200-210) */
                 for (int c = 0; c < 3; c++) {
-                    const int m = tan(carg(mu[c + 3 * l])) < -TINY;
-                    const int e = tan(carg(ep[c + 3 * l])) < -TINY;
+                    /* with a zero imaginary part tan(carg()) is 0 or +-1.2e-16,
+                     * never below -TINY: skip the trigonometry (same answer) */
+                    const int m = cimag(mu[c + 3 * l]) != 0.0 && tan(carg(mu[c + 3 * l])) < -TINY;
+                    const int e = cimag(ep[c + 3 * l]) != 0.0 && tan(carg(ep[c + 3 * l])) < -TINY;
                     if (m && e) k = 'b';
                     else if (m) k = 'h';
                     else if (e) k = 'e';
