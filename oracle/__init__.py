@@ -24,6 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle_fdtd.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_fdtd.so")
 REF_BIN = os.path.join(HERE, "_ref", "FDTD_ref")
+MCALC_BIN = os.path.join(HERE, "_ref", "Mcalc_ref")
 REF_DIR_DEFAULT = "/root/reference"
 
 _P = C.c_void_p
@@ -64,6 +65,38 @@ def build(with_reference: bool | None = None) -> None:
                         "-o", REF_LIB, "-lm"], check=True)
     if _newer(REF_BIN, [ref_src, shim]):
         subprocess.run(["gcc", *CFLAGS, "-w", ref_src, shim, "-o", REF_BIN, "-lm"], check=True)
+    _build_mcalc(ref_dir, shim)
+
+
+def _openblas():
+    """scipy's bundled OpenBLAS (the only LAPACK in this image), or None."""
+    import glob
+    try:
+        import scipy
+    except ImportError:
+        return None
+    libs = glob.glob(os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs",
+                                  "libscipy_openblas-*.so"))
+    return libs[0] if libs else None
+
+
+def _build_mcalc(ref_dir, blas_shim):
+    """The stock reference mode solver (ModeCalc: Mcalc.c with its long-double
+    eigen solvers) linked against scipy's OpenBLAS through lapack_shim.c.
+    Skipped where the sources or that library are absent."""
+    mdir = os.path.join(ref_dir, "ModeCalc")
+    srcs = [os.path.join(mdir, f) for f in ("Mcalc.c", "ldgeev20160825.c", "lzgeev20181003.c")]
+    blas = _openblas()
+    if not all(os.path.isfile(s) for s in srcs) or blas is None:
+        return
+    lshim = os.path.join(HERE, "lapack_shim.c")
+    if _newer(MCALC_BIN, srcs + [lshim, blas_shim]):
+        subprocess.run(["gcc", "-O2", "-std=c11", "-w", *srcs, lshim, blas_shim, blas,
+                        "-Wl,-rpath," + os.path.dirname(blas), "-o", MCALC_BIN, "-lm"], check=True)
+
+
+def mcalc_available() -> bool:
+    return os.path.isfile(MCALC_BIN)
 
 
 def reference_available() -> bool:

@@ -39,6 +39,37 @@ def layer_name(prefix, L, z):
     return f"{prefix}_MedT{z - (L2 - L3)}.dat"
 
 
+def write_layer(path: str, med, L, *, wavelength_m=1.55e-6, k0=1.0e7, u2=0.0, min_sqdt=1.0, factors=None):
+    """One Med layer file as the mesher chain writes it: a comment line, the
+    wavelength / k_0 / lattice header (Medium3DSi/Med3DSi.c:222-227 with
+    PMLgen's "PML num / min Dt^2" tail, PMLset/PMLcalc.c:331), then
+    2*L0*L1 lines "l m j2 Re Im Re Im Re Im fx fx fx".  med is (6, L0*L1)
+    complex in the file's column order (j2 = 0: mu00, mu11, eps22; j2 = 1:
+    eps11, eps00, mu22); factors (same shape, real) default to 1."""
+    L0, L1 = L[0], L[1]
+    L2 = L[2] if len(L) > 2 else 1
+    L3 = L[3] if len(L) > 3 else 0
+    med = np.asarray(med, np.complex128).reshape(6, L0 * L1)
+    fx = np.ones((6, L0 * L1)) if factors is None else np.asarray(factors, np.float64).reshape(6, L0 * L1)
+    lines = ["# Created by smatranem_gb300.decks",
+             f"# wavelength [m] = {wavelength_m:.20e}, temp. [K] = {298.15:.20e}, sinc_rad = 0",
+             f"# k_0 * u_2  = {u2:.20e} ; {u2 + 0.05:.20e} ; {u2 + 0.1:.20e}, k_0[m^-1] = {k0:.20e}",
+             f"# l < {L0}, m < {L1}, n + 2*outer < {L2}, media_no < 2, outer = {L3}, PML num = 1, "
+             f"min Dt^2 = {min_sqdt:.20e}",
+             "# l m 0 mu_u mu_v ep_w",
+             "# l m 1 ep_v ep_u mu_w"]
+    for j1 in range(L1):
+        for j0 in range(L0):
+            p = j0 + L0 * j1
+            for j2 in (0, 1):
+                vals = med[3 * j2:3 * j2 + 3, p]
+                nums = " ".join(f"{v.real:.20e} {v.imag:.20e}" for v in vals)
+                fs = " ".join(f"{x:.20e}" for x in fx[3 * j2:3 * j2 + 3, p])
+                lines.append(f"{j0} {j1} {j2} {nums} {fs}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def write_deck(root: str, s: Structure, *, prefix="Data/deck", wavelength_m=1.55e-6, k0=1.0e7, time_period=(1, 1, 3),
                inci_point="B2", inci_mode=1, targets=("B1", "T1"), nreal=(3, 3), seed=0, extra_lines=()):
     """Write a deck for structure s under directory root; returns input.txt's path."""
@@ -52,20 +83,9 @@ def write_deck(root: str, s: Structure, *, prefix="Data/deck", wavelength_m=1.55
     mu = s.mu.reshape(L2, pl, 3)
     ep = s.epsi.reshape(L2, pl, 3)
     for z in range(L2):
-        lines = [f"# wavelength [m] = {wavelength_m:.20e}, temp. [K] = {298.15:.20e}, sinc_rad = 0",
-                 f"# k_0 * u_2  = {z * 0.1:.20e} ; {z * 0.1 + 0.05:.20e} ; {z * 0.1 + 0.1:.20e}, "
-                 f"k_0[m^-1] = {k0:.20e}",
-                 f"# l < {L0}, m < {L1}, n + 2*outer < {L2}, media_no < 2, outer = {L3}, PML num = 1, "
-                 f"min Dt^2 = {sq:.20e}"]
         m, e = mu[z], ep[z]
-        for j1 in range(L1):
-            for j0 in range(L0):
-                p = j0 + L0 * j1
-                for j2, vals in ((0, (m[p, 0], m[p, 1], e[p, 2])), (1, (e[p, 1], e[p, 0], m[p, 2]))):
-                    nums = " ".join(f"{v.real:.20e} {v.imag:.20e}" for v in vals)
-                    lines.append(f"{j0} {j1} {j2} {nums} {1.0:.20e} {1.0:.20e} {1.0:.20e}")
-        with open(layer_name(pfx, L, z), "w") as f:
-            f.write("\n".join(lines) + "\n")
+        med = np.stack([m[:, 0], m[:, 1], e[:, 2], e[:, 1], e[:, 0], m[:, 2]])
+        write_layer(layer_name(pfx, L, z), med, L, wavelength_m=wavelength_m, k0=k0, u2=z * 0.1, min_sqdt=sq)
     rng = np.random.default_rng(seed)
     NA = 2 * pl
     for side, nr in zip("bt", nreal):

@@ -538,3 +538,30 @@ def large_structure(shape=(640, 640, 512), pml=12, radius_um=50.0, dx_um=0.02, e
     b = Bend(s=s, iB=pml + 1, iT=L2 - pml - 2, iI=pml + 3, pml=pml, u0=u0 * (2.0 / beam_um),
              u1=u1 * (2.0 / beam_um), n_eff=1.0)
     return b
+
+
+def port_layer(L0, L1, core=(4, 3), eps_core=12.11, eps_clad=2.085, seed=0, jitter=0.0, metric=0.0, loss=0.0):
+    """One synthetic z layer of port media for the mode solver: (6, L0*L1)
+    complex values in the Med file's column order (j2 = 0: mu00, mu11, eps22;
+    j2 = 1: eps11, eps00, mu22), metric factor included.
+
+    A core of core[0] x core[1] cells with relative permittivity eps_core,
+    centred, in eps_clad; jitter perturbs the core permittivity per cell by up
+    to that fraction, metric multiplies every value by a seeded factor in
+    [1 - metric, 1 + metric] (a non-uniform mesh), loss adds i*loss*eps to the
+    core permittivity (lossy media make the eigenproblem complex).  Seeded."""
+    rng = np.random.default_rng(seed)
+    n = L0 * L1
+    j0 = np.tile(np.arange(L0), L1)
+    j1 = np.repeat(np.arange(L1), L0)
+    c0, c1 = (L0 - core[0]) // 2, (L1 - core[1]) // 2
+    in_core = (j0 >= c0) & (j0 < c0 + core[0]) & (j1 >= c1) & (j1 < c1 + core[1])
+    eps = np.where(in_core, eps_core, eps_clad).astype(np.complex128)
+    if jitter:
+        eps = eps * np.where(in_core, 1.0 + jitter * (rng.random(n) - 0.5) * 2.0, 1.0)
+    if loss:
+        eps = eps + 1j * loss * np.where(in_core, eps.real, 0.0)
+    med = np.stack([np.ones(n), np.ones(n), eps, eps, eps, np.ones(n)]).astype(np.complex128)
+    if metric:
+        med = med * (1.0 + metric * (2.0 * rng.random((6, n)) - 1.0))
+    return med

@@ -42,7 +42,9 @@ def reference(built):
 
 
 def golden_cases():
-    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """The time-loop fixtures (the port-mode fixtures modes_*.npz have their own tests)."""
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(p).startswith("modes_"))
 
 
 def load_golden(name):
