@@ -48,8 +48,10 @@ METRIC = "Gcell-updates/s & S-cols/s: batched FP32 vs plain FP64 on 1 GB300 at s
 LAMS = list(np.linspace(1.50, 1.60, 21))
 FULL_STEPS = 8000
 BATCH = 8
+N_MODES = 4
 WORKLOAD = ("bend 256x192x160 curvilinear (R=2um, Si strip in SiO2), 12-cell split PML on 6 faces, "
-            "batch 8 = 2 ports x 4 modes, Gaussian pulse, FP64 DFT at 21 wavelengths on 2 port planes")
+            "batch 8 = 2 ports x 4 port eigenmodes (GPU mode solver), Gaussian pulse, "
+            "FP64 DFT at 21 wavelengths on 2 port planes")
 
 
 # DRAM traffic of one k_sweep32v launch on the bench workload, from one ncu
@@ -134,19 +136,36 @@ def measured_peak():
 # workload
 # ---------------------------------------------------------------------------
 
-def make_workload(shape=(256, 192, 160)):
+def make_workload(shape=(256, 192, 160), solve_modes=True):
+    """The bend, its precompute and its port modes: the first N_MODES
+    eigenmodes of the port layer from the GPU mode solver (forward sheets
+    for the bottom-port excitations, backward ones for the top port, and the
+    dual columns S is projected on).  solve_modes=False gives Gaussian
+    stand-in sheets instead (used where only the step time matters)."""
     from smatranem_gb300 import workloads as W
     bend = W.bend_structure(shape=shape)
     pr = W.prepare(bend.s, dt_factor=1.0 / 0.99)
-    modes = W.mode_profiles(bend)
+    if solve_modes:
+        ms = W.port_modes(bend, N_MODES)
+        k = ms.n_found
+        modes = {"fwd": [ms.incident(m) for m in range(1, k + 1)],
+                 "bwd": [ms.incident(-m) for m in range(1, k + 1)],
+                 "cols": np.array([ms.dual(m) for m in range(1, k + 1)] + [ms.dual(-m) for m in range(1, k + 1)]),
+                 "theta": ms.theta[:k].real.tolist(), "solver": ms.info}
+    else:
+        sheets = W.mode_profiles(bend, n_modes=N_MODES)
+        modes = {"fwd": sheets, "bwd": sheets, "cols": mode_columns(sheets), "theta": None, "solver": None}
     return bend, pr, modes
 
 
 def excitations(bend, modes):
-    """(port plane, inci_mode sign, Hinc, Einc) for 2 ports x 4 modes."""
+    """(port plane, inci_mode sign, Hinc, Einc) for 2 ports x 4 modes: forward
+    modes launched at the bottom port, backward ones at the top port (the
+    reference picks the backward Xi column for a negative inci_mode,
+    set_incident :497-499)."""
     out = []
-    for port, (plane, sign) in enumerate(((bend.iI, 1), (bend.iT - 2, -1))):
-        for Hinc, Einc in modes:
+    for plane, sign, key in ((bend.iI, 1, "fwd"), (bend.iT - 2, -1, "bwd")):
+        for Hinc, Einc in modes[key]:
             out.append((plane, sign, Hinc, Einc))
     return out
 
@@ -172,7 +191,7 @@ def make_plan(bend, pr, modes, precision, batch, nsteps, stream=None, tuning="au
 
 
 def mode_columns(modes):
-    """tilde-Xi style columns (4*npix rows: Hx, Hy, -Ey, Ex) of the mode sheets."""
+    """Overlap columns (4*npix rows: Hx, Hy, -Ey, Ex) of stand-in mode sheets."""
     cols = []
     for Hinc, Einc in modes:
         cols.append(np.concatenate([Hinc[0::2], Hinc[1::2], -Einc[1::2], Einc[0::2]]))
@@ -180,9 +199,8 @@ def mode_columns(modes):
 
 
 def s_parameters(p, bend, modes, b):
-    """Mode overlaps on the GPU (FP64): [port plane][lambda][mode]."""
-    cols = mode_columns(modes)
-    return np.stack([p.overlap(b, q, cols) for q in range(2)])
+    """Mode overlaps on the GPU (FP64): [port plane][lambda][mode column]."""
+    return np.stack([p.overlap(b, q, modes["cols"]) for q in range(2)])
 
 
 # ---------------------------------------------------------------------------
@@ -193,7 +211,7 @@ def _cpu_worker(args):
     """One process: `nsteps` oracle main_calc steps of the full bend, one excitation."""
     shape, nsteps, kind = args
     import oracle
-    bend, pr, modes = make_workload(shape)
+    bend, pr, modes = make_workload(shape, solve_modes=False)  # no GPU in this process
     o = oracle.Oracle(kind)
     Ah, Bh, Ae, Be = pr.coefficients()
     s = bend.s
@@ -201,7 +219,7 @@ def _cpu_worker(args):
     pl = s.L[0] * s.L[1]
     H = np.zeros(3 * (n3 + pr.lnotn + 1))
     E = np.zeros_like(H)
-    Hinc, Einc = modes[0]
+    Hinc, Einc = modes["fwd"][0]
     rng = np.random.default_rng(0)
     H[:3 * n3] = rng.standard_normal(3 * n3) * 1e-3
     mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
@@ -410,7 +428,9 @@ def run_ours(args):
                          "finite": finite32},
         "s_cols_speedup_fp32_vs_fp64": (batch / t_full32) / (1.0 / t_full64),
         "s_param_rel_err_fp32_vs_fp64": {"max_rel": s_rel, "max_abs_over_max": s_abs,
-                                         "over": "2 ports x 21 wavelengths x 4 modes, excitation 0, |S| > 1e-3 max"},
+                                         "over": "2 ports x 21 wavelengths x 4 modes x (+,-), excitation 0, "
+                                                 "|S| > 1e-3 max"},
+        "port_modes": {"theta": modes["theta"], "solver": modes["solver"]},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
@@ -593,9 +613,53 @@ def run_large(args):
     p.close()
 
 
+def run_modes(args):
+    """Port-mode solver (f)-3: the N_MODES propagating modes of the bend's
+    256 x 192 port layer (n = 98,304 unknowns) on the GPU, timed over
+    --steps solves after --warmup; the CPU side is the dense reference
+    algorithm (oracle restatement of Mcalc's calc_Xi) on the largest
+    cross-section it handles in seconds, scaled to the full size by n^3."""
+    import torch
+    from smatranem_gb300 import modes as M
+    from smatranem_gb300 import workloads as W
+    bend = W.bend_structure(shape=(256, 192, 64))
+    L0, L1 = 256, 192
+    for _ in range(max(1, args.warmup)):
+        M.solve(bend.port_med, bend.s.omega, L0, L1, (0, 0), N_MODES)
+    torch.cuda.synchronize()
+    times, infos = [], []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        ms = M.solve(bend.port_med, bend.s.omega, L0, L1, (0, 0), N_MODES)
+        times.append(time.perf_counter() - t0)
+        infos.append(ms.info)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import mode_oracle as MO
+        c0, c1 = 40, 30   # the same graded mesh around the core, cropped
+        sub = W.bend_structure(shape=(c0, c1, 64), core_cell0=c0 // 2)
+        V, _ = MO.set_V(sub.port_med, sub.s.omega)
+        maa, mbb = MO.set_M((0, 0), c0, c1, V)
+        A = (mbb @ maa).real
+        t0 = time.perf_counter()
+        MO.eigen(A, real=True)  # Mcalc's dominant step: dense dgeev of mbb*maa (Mcalc.c:884)
+        t_cpu = time.perf_counter() - t0
+        scale = (L0 * L1 / (c0 * c1)) ** 3
+        cpu = {"value": t_cpu * scale, "unit": "s per solve (dense eigen solve, extrapolated as n^3)",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": f"dgeev of the {2 * c0 * c1}x{2 * c0 * c1} mbb*maa of a {c0}x{c1} crop of the same mesh: "
+                         f"{t_cpu:.2f} s, x (n ratio)^3 = {scale:.3g}; the full {2 * L0 * L1}^2 matrix alone "
+                         f"would take {(2 * L0 * L1) ** 2 * 8 / 1e9:.0f} GB"}
+    print(json.dumps({
+        "mode": "modes", "config": f"bend port layer {L0}x{L1} (graded 15-25 nm mesh), BoundC 0, {N_MODES} modes",
+        "ms_per_solve": 1e3 * float(np.median(times)), "solves": len(times),
+        "theta": ms.theta[:ms.n_found].real.tolist(), "info": infos[-1],
+        "cpu_baseline": cpu}))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", default="main", choices=["main", "adjoint", "group", "large"],
+    ap.add_argument("--mode", default="main", choices=["main", "adjoint", "group", "large", "modes"],
                     help="main: the contract line; the others: the adjoint, batched-structures and large-domain "
                          "workloads (one summary line each)")
     ap.add_argument("--adj-steps", type=int, default=6000)
@@ -620,7 +684,7 @@ def main():
     if args.profile:
         run_profile(args)
     elif args.mode != "main":
-        {"adjoint": run_adjoint, "group": run_group, "large": run_large}[args.mode](args)
+        {"adjoint": run_adjoint, "group": run_group, "large": run_large, "modes": run_modes}[args.mode](args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -362,6 +362,66 @@ int smat_device_info(char *name, int name_len, int *sm_count, int *cc);
 /* Device bytes the plan holds. */
 long long smat_fdtd_device_bytes(const smat_fdtd_plan *plan);
 
+/* ---------------------------------------------------------------------------
+ * Port eigenmodes of one z layer (the reference mode solver, ModeCalc/Mcalc.c).
+ *
+ * Media `med`: 6*L0*L1 complex values (interleaved re, im) of the layer's Med
+ * file, value times metric factor, in the file's column order -- rows
+ * [0, L0L1): mu00, then mu11, eps22 (the j2 = 0 columns), eps11, eps00, mu22
+ * (the j2 = 1 columns), point p = l + L0*m within each row.  This is Vcomp of
+ * set_V (Mcalc.c:1123-1160) before its omega scaling.  The imaginary parts
+ * must be zero: the reference serves lossless port layers only (its sortXi
+ * exits on complex modes, :620-626).  BoundC[2] in {-1, 0, 1} as in set_D.
+ * --------------------------------------------------------------------------- */
+typedef struct smat_mode_opts {
+    double tol;              /* relative residual ||A x - l x|| / (rho ||x||); 0: 1e-12 */
+    int degree;              /* initial Chebyshev filter degree per iteration (it grows
+                                by that much every 4 iterations, up to 256, capped so
+                                the top mode grows at most e^13 per pass); 0: 24 */
+    int guard;               /* extra block vectors beyond nmodes; 0: max(8, nmodes/2) */
+    int max_iter;            /* outer iterations; 0: 2000 */
+    unsigned long long seed; /* start block; 0: fixed default */
+} smat_mode_opts;
+
+typedef struct smat_mode_info {
+    int n_found;          /* propagating modes returned (<= nmodes) */
+    int iterations;       /* outer (filter + Rayleigh-Ritz) iterations */
+    int degenerate_pairs; /* mode pairs degeneXi re-orthogonalised */
+    int block;            /* block size used */
+    long long matvecs;    /* applications of mbb*maa to one vector */
+    double max_residual;  /* largest relative residual among returned modes */
+    double spectral_radius;
+    double ms;            /* wall time of the call */
+} smat_mode_info;
+
+/* Replaces calc_Xi (Mcalc.c:256-347) for the propagating part of the spectrum:
+ * the nmodes eigenpairs of mbb*maa with the largest eigenvalues (those with a
+ * positive eigenvalue; fewer when the layer has fewer propagating modes),
+ * turned into Mcalc's outputs for those modes.  theta: 2*nmodes complex,
+ * theta[j] and theta[j + nmodes] = -theta[j] (makeXi :651-654), descending.
+ * Xi: (4*L0*L1) x (2*nmodes) complex, column-major -- forward column j =
+ * [e^{-i theta/2} H; E], backward column nmodes + j = [e^{+i theta/2} H; -E]
+ * with H rows (H0 of all points, H1 of all points), E = maa H / eiSin
+ * (makeE :731-757), power-normalised (normXi :529-561) and degenerate modes
+ * re-orthogonalised (degeneXi :417-467).  The sign of each eigenvector is
+ * fixed by making its largest H entry positive (dgeev leaves it open).
+ * Columns past info->n_found are zero.  opts and info may be NULL. */
+int smat_mode_solve(int L0, int L1, const int BoundC[2], double omega, const double *med, int nmodes,
+                    const smat_mode_opts *opts, double *theta, double *Xi, smat_mode_info *info);
+
+/* No counterpart in the reference: applies maa (which = 0), mbb (1) or
+ * mbb*maa (2) of the layer to the m columns of X (2*L0*L1 doubles each) on
+ * the GPU, into Y.  The stencils the solver uses, exposed for checking them
+ * against Mcalc's dense set_M matrices. */
+int smat_mode_apply(int L0, int L1, const int BoundC[2], double omega, const double *med, int which, int m,
+                    const double *X, double *Y);
+
+/* No counterpart in the reference: the host eigen solver of the mode solver's
+ * Rayleigh-Ritz step (complex Schur form by shifted QR), for testing.  B: m x m
+ * complex row-major; w: m eigenvalues; V: m x m, eigenvector k in column k
+ * (unit 2-norm).  Host only, no GPU needed. */
+int smat_mode_small_eig(int m, const double *B, double *w, double *V);
+
 #ifdef __cplusplus
 }
 #endif

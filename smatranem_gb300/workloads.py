@@ -239,6 +239,7 @@ class Bend:
     u0: np.ndarray   # cell-centre coordinates across (um), core centre at 0
     u1: np.ndarray
     n_eff: float = 2.4
+    port_med: np.ndarray | None = None  # (6, L0*L1) lossless Med values of a port layer (before the PML stretch)
 
 
 def bend_structure(shape=(256, 192, 160), pml=12, L3=16, radius_um=2.0, core=(0.45, 0.22), eps_core=12.11,
@@ -288,10 +289,15 @@ def bend_structure(shape=(256, 192, 160), pml=12, L3=16, radius_um=2.0, core=(0.
         th_lo, th_hi = float(d[:pml].sum()), float(d[n - pml:].sum())
         sig.append(pml_sigma(n, pml, pml, omega, th_lo, th_hi, sq_ref, power))
     mu_s, ep_s = stretch_media((L0, L1, L2), mu_r, eps_r, sig)
+    pl = L0 * L1
+    zi = min(pml + 3, L3 - 1)  # a straight port layer (every port layer has the same media)
+    m_l, e_l = mu_r[zi * pl:(zi + 1) * pl], eps_r[zi * pl:(zi + 1) * pl]
+    port_med = np.stack([m_l[:, 0], m_l[:, 1], e_l[:, 2], e_l[:, 1], e_l[:, 0], m_l[:, 2]]).astype(np.complex128)
     del mu_r, eps_r, fx
     s = Structure(L=(L0, L1, L2, L3), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=(0, 0, 0),
                   name=f"bend{L0}x{L1}x{L2}")
-    return Bend(s=s, iB=pml + 1, iT=L2 - pml - 2, iI=pml + 3, pml=pml, u0=u0 * INV_K0_UM, u1=u1 * INV_K0_UM)
+    return Bend(s=s, iB=pml + 1, iT=L2 - pml - 2, iI=pml + 3, pml=pml, u0=u0 * INV_K0_UM, u1=u1 * INV_K0_UM,
+                port_med=port_med)
 
 
 def mode_profiles(b: Bend, n_modes=4, w0_um=0.26, w1_um=0.16):
@@ -300,8 +306,8 @@ def mode_profiles(b: Bend, n_modes=4, w0_um=0.26, w1_um=0.16):
     Returns a list of (Hinc, Einc) complex planes (2*L0*L1, component v of pixel
     p at v + 2p) for propagation along +u2: TE modes carry E_x with
     H_y = n_eff E_x, TM modes E_y with H_x = -n_eff E_y.  Normalised to unit
-    overlap norm.  They stand in for the Mcalc eigenvectors (no mode solver in
-    this path)."""
+    overlap norm.  Stand-ins for the port eigenmodes where only the update
+    rate matters; port_modes() gives the eigenmodes themselves."""
     L0, L1 = b.s.L[0], b.s.L[1]
     x = b.u0[None, :] / w0_um
     y = b.u1[:, None] / w1_um
@@ -321,6 +327,14 @@ def mode_profiles(b: Bend, n_modes=4, w0_um=0.26, w1_um=0.16):
             Hinc[0::2] = -b.n_eff * f
         out.append((Hinc, Einc))
     return out
+
+
+def port_modes(b: Bend, n_modes=4, **solve_kw):
+    """The first n_modes propagating eigenmodes of the bend's port layer
+    (lossless media with their metric factors, PEC box) from the GPU mode
+    solver: a modes.Modes with Mcalc's theta and Xi columns."""
+    from . import modes as M
+    return M.solve(b.port_med, b.s.omega, b.s.L[0], b.s.L[1], b.s.iBc[:2], n_modes, **solve_kw)
 
 
 def pulse_schedule(nsteps, dt, lam0_um=1.55, bandwidth=0.2, lams_um=None, delay_sigmas=4.0):
@@ -565,3 +579,24 @@ def port_layer(L0, L1, core=(4, 3), eps_core=12.11, eps_clad=2.085, seed=0, jitt
     if metric:
         med = med * (1.0 + metric * (2.0 * rng.random((6, n)) - 1.0))
     return med
+
+
+def waveguide_structure(med, L0, L1, L2, L3, omega=0.405, pml_z=3, iBc=(0, 0, 0), sq_ref=1e-8):
+    """A straight guide along z: the port layer med ((6, L0*L1), from
+    port_layer) repeated on all L2 layers, a split PML of pml_z layers at each
+    z end and none across (the port layers stay lossless, as the mesher
+    chain's PMLgen leaves them, PMLset/PMLcalc.c:222).  With
+    modes.solve(med, omega, L0, L1, iBc[:2]) this is a deck whose incident
+    and overlap columns come from the layer's own eigenmodes."""
+    med = np.asarray(med, np.complex128).reshape(6, L0 * L1)
+    pl = L0 * L1
+    mu = np.zeros((L2 * pl, 3), np.complex128)
+    ep = np.zeros((L2 * pl, 3), np.complex128)
+    mu[:, 0], mu[:, 1], ep[:, 2] = (np.tile(med[k], L2) for k in (0, 1, 2))
+    ep[:, 1], ep[:, 0], mu[:, 2] = (np.tile(med[k], L2) for k in (3, 4, 5))
+    min_dt = cfl_min_dt(mu.real, ep.real)
+    sig = [np.zeros((2, L0)), np.zeros((2, L1)),
+           pml_sigma(L2, pml_z, pml_z, omega, float(pml_z), float(pml_z), sq_ref)]
+    mu_s, ep_s = stretch_media((L0, L1, L2), mu, ep, sig)
+    return Structure(L=(L0, L1, L2, L3), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=tuple(iBc),
+                     name=f"guide{L0}x{L1}x{L2}")
