@@ -39,6 +39,9 @@ struct smat_deck {
     char prefix[BUF], target[2][BUF], inci_point[BUF];
     int precision; /* extra key "FDTD_GPU: precision = FP32" (ignored by the reference) */
     int use_cache;  /* extra key "FDTD_GPU: cache = y": keep a binary copy of the parsed deck */
+    int solve_modes; /* extra key "FDTD_GPU: modes = solve[, nmodes = K]": port modes from the
+                        GPU mode solver on the monitor layers instead of the Mode / Xi files */
+    int nmodes_req;  /* K: at most this many propagating modes per side (default 64) */
     int from_cache; /* this load came from that copy */
     double complex *mu, *epsi;
     double complex *Hinc, *Einc;
@@ -119,6 +122,14 @@ static int read_input(smat_deck *d, const char *path)
                     ;
                 d->use_cache = *c == 'y' || *c == 'Y' || *c == '1';
             }
+            const char *m = strstr(buf, "modes");
+            if (m && (m = strchr(m, '=')) != NULL) {
+                while (*++m == ' ')
+                    ;
+                d->solve_modes = strncmp(m, "solve", 5) == 0;
+            }
+            const char *k = strstr(buf, "nmodes");
+            if (k && (k = strchr(k, '=')) != NULL) d->nmodes_req = atoi(k + 1);
         } else if (!(seen & 8) && strncmp(buf, "FDTD", 4) == 0 &&
                    sscanf(buf,
                           "%*[^=] %*[=] %d %*[^=] %*[=] %d %*[^=] %*[=] %d %*[^=] %*[=] %s %*[^=] %*[=] %d "
@@ -153,6 +164,9 @@ static int read_geometry(smat_deck *d)
     fclose(f);
     if (n < 0) return smat_fail(SMAT_EINVAL, "L,M,N,N_outer can not be read at Scatterer @ input_file0!");
     d->omega = TWO_PI_LD / (d->wavelength * d->k0);
+    if (d->L[0] <= 0 || d->L[1] <= 0 || d->L[2] <= 0 || d->L[3] < 0)
+        return smat_fail(SMAT_EINVAL, "bad lattice numbers %d %d %d %d", d->L[0], d->L[1], d->L[2], d->L[3]);
+    if (d->solve_modes) return SMAT_OK; /* modes computed at this omega: no Mode file to check against */
     snprintf(name, sizeof name, "%s_bMode.dat", d->prefix);
     f = fopen(name, "r");
     if (!f) return smat_fail(SMAT_EINVAL, "open error for %s", name);
@@ -433,6 +447,70 @@ void smat_deck_free(smat_deck *d)
     free(d);
 }
 
+/* Port modes of one side from the GPU mode solver (smat_mode_solve, the
+ * few-mode counterpart of ModeCalc/Mcalc.c calc_Xi) on monitor layer z: the
+ * layer's Med values in Mcalc's set_V order, at most d->nmodes_req
+ * propagating modes.  Fills what the Mode / Xi files would have given:
+ * N_real, the tilde-Xi columns of set_tilXi (:617-619) and, on the incident
+ * side, the incident sheets of set_incident (:497-510). */
+static int solve_side(smat_deck *d, int side, int z, int incident)
+{
+    const int *L = d->L;
+    const long pl = (long)L[0] * L[1], NA = 2 * pl;
+    int K = d->nmodes_req > 0 ? d->nmodes_req : 64;
+    if (K > 85) K = 85; /* with the solver's guard vectors the block stays within 128 */
+    if (K > NA) K = (int)NA;
+    const int am = abs(d->inci_mode);
+    if (incident && am > K) K = am;
+    double complex *med = malloc(sizeof(double complex) * 6 * pl);
+    double complex *theta = malloc(sizeof(double complex) * 2 * K);
+    double complex *xi = malloc(sizeof(double complex) * (size_t)2 * NA * 2 * K);
+    int rc = SMAT_OK;
+    if (!med || !theta || !xi) rc = smat_fail(SMAT_ENOMEM, "deck_load: out of host memory");
+    if (!rc) {
+        const double complex *mu = d->mu + 3 * pl * z, *ep = d->epsi + 3 * pl * z;
+        for (long p = 0; p < pl; p++) {
+            med[0 * pl + p] = mu[3 * p + 0];
+            med[1 * pl + p] = mu[3 * p + 1];
+            med[2 * pl + p] = ep[3 * p + 2];
+            med[3 * pl + p] = ep[3 * p + 1];
+            med[4 * pl + p] = ep[3 * p + 0];
+            med[5 * pl + p] = mu[3 * p + 2];
+        }
+        smat_mode_info info;
+        const int bc[2] = {d->iBc[0], d->iBc[1]};
+        rc = smat_mode_solve(L[0], L[1], bc, d->omega, (const double *)med, K, NULL, (double *)theta, (double *)xi,
+                             &info);
+        if (!rc) {
+            const int nr = info.n_found;
+            d->nreal[side] = nr;
+            if (incident && am > nr) rc = smat_fail(SMAT_EINVAL, "inci_mode = %d > %d", d->inci_mode, nr);
+            d->ncols[side] = 2 * nr;
+            d->tilxi[side] = calloc((size_t)2 * nr * 2 * NA + 1, sizeof(double complex));
+            if (!rc && !d->tilxi[side]) rc = smat_fail(SMAT_ENOMEM, "deck_load: out of host memory");
+            for (int j = 0; j < nr && !rc; j++)
+                for (long row = 0; row < 2 * NA; row++) {
+                    const long r = (row + NA) % (2 * NA);
+                    d->tilxi[side][(size_t)j * 2 * NA + r] = xi[(size_t)j * 2 * NA + row];
+                    d->tilxi[side][(size_t)(nr + j) * 2 * NA + r] = -xi[(size_t)(K + j) * 2 * NA + row];
+                }
+            if (!rc && incident) {
+                const double complex *c = xi + (size_t)(d->inci_mode > 0 ? am - 1 : K + am - 1) * 2 * NA;
+                for (long row = NA; row < 2 * NA && !rc; row++)
+                    if (cimag(c[row]) != 0.) rc = smat_fail(SMAT_EINVAL, "incident wave is not real number!");
+                for (long r = 0; r < pl && !rc; r++) {
+                    d->Hinc[0 + 2 * r] = c[r + 0 * pl];
+                    d->Hinc[1 + 2 * r] = c[r + 1 * pl];
+                    d->Einc[1 + 2 * r] = -c[r + 2 * pl];
+                    d->Einc[0 + 2 * r] = c[r + 3 * pl];
+                }
+            }
+        }
+    }
+    free(med), free(theta), free(xi);
+    return rc;
+}
+
 int smat_deck_load(const char *input_txt, smat_deck **out)
 {
     smat_clear_error();
@@ -510,6 +588,10 @@ int smat_deck_load(const char *input_txt, smat_deck **out)
     d->Einc = calloc(2 * pl, sizeof(double complex));
     for (int side = 0; side < 2 && !rc; side++) {
         if (!need_side[side]) continue;
+        if (d->solve_modes) {
+            rc = solve_side(d, side, side == 0 ? d->iB : d->iT, side == inc_side);
+            continue;
+        }
         char xi[BUF + 32], mode[BUF + 32];
         xi_names(d, side, xi, mode);
         rc = read_nreal(mode, L, &d->nreal[side]);

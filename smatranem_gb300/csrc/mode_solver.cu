@@ -737,7 +737,7 @@ extern "C" int smat_mode_solve(int L0, int L1, const int BoundC[2], double omega
          * e^13 per pass, so that the block keeps its rank (the Gram
          * truncation below drops directions under 1e-13) */
         const double xt = (ltop - c) / e;
-        if (std::isfinite(xt) && xt > 1.0) degree = std::min(degree, std::max(degree0, (int)(13.0 / std::acosh(xt))));
+        if (std::isfinite(xt) && xt > 1.0) degree = std::min(degree, std::max(4, (int)(13.0 / std::acosh(xt))));
         double *prev = X, *cur = F[0];
         if ((rc = S.maa(prev, W, mb)) || (rc = S.mbb(W, prev, nullptr, cur, mb, 1.0 / e, c, 0.0))) return rc;
         for (int k = 1; k < degree; k++) {

@@ -105,6 +105,39 @@ def make_deck(name, L, seed, kw, dkw):
     print(f"{name}: " + r.stderr.strip().splitlines()[-1])
 
 
+def make_mode_deck(name="deck_modes", L=(5, 4, 14, 4), seed=51):
+    """A straight guide whose Mode / Xi files are the stock reference mode
+    solver's (oracle/_ref/Mcalc_ref) for the two monitor layers, then the
+    stock FDTD run on it: the Mcalc -> FDTD chain of the reference end to end.
+    The drop-in checks its report both reading these files and solving the
+    port modes itself (FDTD_GPU: modes = solve)."""
+    import shutil
+    import subprocess
+    from smatranem_gb300 import decks
+    root = os.path.join(HERE, "decks", name)
+    shutil.rmtree(root, ignore_errors=True)
+    L0, L1, L2, L3 = L
+    om = decks.omega_of(1.55e-6, 1.0e7)
+    med = W.port_layer(L0, L1, core=(2, 2), eps_core=12.11, eps_clad=2.085, seed=seed, jitter=0.25)
+    s = W.waveguide_structure(med, L0, L1, L2, L3, omega=om, pml_z=2)
+    decks.write_deck(root, s, seed=seed, time_period=(1, 2, 6), inci_point="B3", inci_mode=1,
+                     targets=("B2", "T1"), nreal=(1, 1),
+                     extra_lines=("\tinv_k0 = 1.00000000000000000000e-07 m",
+                                  "\tMediumPara: wavelength= 1.55000000000000000000e-06 m, temperature= 25 degC"))
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+    r = subprocess.run([oracle.MCALC_BIN, "input.txt"], cwd=root, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"{name}: Mcalc failed\n{r.stderr}")
+    r = subprocess.run([oracle.REF_BIN, "input.txt"], cwd=root, capture_output=True, text=True)
+    with open(os.path.join(root, "reference_stderr.txt"), "w") as f:
+        f.write(r.stderr)
+    with open(os.path.join(root, "reference_status.txt"), "w") as f:
+        f.write(f"{r.returncode}\n")
+    np.savez_compressed(os.path.join(root, "media.npz"), mu=s.mu.reshape(-1), epsi=s.epsi.reshape(-1),
+                        min_dt=s.min_dt, port_med=med)
+    print(f"{name}: " + " | ".join(r.stderr.strip().splitlines()[-6:]))
+
+
 def main():
     oracle.build(with_reference=True)
     ref, port = oracle.Oracle("reference"), oracle.Oracle("port")
@@ -112,7 +145,12 @@ def main():
         run_case(ref, port, *case)
     for deck in DECKS:
         make_deck(*deck)
+    make_mode_deck()
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["modes"]:
+        oracle.build(with_reference=True)
+        make_mode_deck()
+    else:
+        main()

@@ -84,3 +84,37 @@ def test_dropin_with_deck_cache(built, tmp_path, name):
         assert r.returncode == 0, r.stderr
         assert _comparable(r.stderr) == ref, run
         assert any(p.name.endswith(".smatdeck") for p in (work / "Data").iterdir())
+
+
+def _table(text):
+    rows = []
+    for l in text.splitlines():
+        parts = [p.strip() for p in l.split(",")]
+        if len(parts) == 4 and parts[0][:1] in "+-":
+            rows.append((parts[0], float(parts[1]), parts[2], float(parts[3])))
+    return rows
+
+
+def test_dropin_solves_port_modes(built, tmp_path):
+    """"FDTD_GPU: modes = solve": the drop-in computes the port modes of the two
+    monitor layers with the GPU mode solver instead of reading the Mode / Xi
+    files (deleted here), and reports the same |S|^2 as the reference FDTD fed
+    with the stock Mcalc's files -- same modes, same N_real, values within
+    1e-8 relative (the modes agree to the solver's residual, not bit for bit)."""
+    name = "deck_modes"
+    src = os.path.join(GOLDEN, "decks", name)
+    work = tmp_path / name
+    shutil.copytree(src, work)
+    for fn in os.listdir(work / "Data"):
+        if fn.endswith(("Mode.dat", "Xi.dat")):
+            os.remove(work / "Data" / fn)
+    with open(work / "input.txt", "a") as f:
+        f.write("\tFDTD_GPU: modes = solve, nmodes = 16\n")
+    r = subprocess.run([EXE, "input.txt"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    a, b = _table(r.stderr), _table(open(os.path.join(src, "reference_stderr.txt")).read())
+    assert len(a) == len(b) == 4
+    big = max(max(x[1], x[3]) for x in b)
+    for x, y in zip(a, b):
+        assert x[0] == y[0] and x[2] == y[2]
+        assert abs(x[1] - y[1]) <= 1e-8 * big and abs(x[3] - y[3]) <= 1e-8 * big

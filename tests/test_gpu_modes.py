@@ -193,3 +193,18 @@ def test_fdtd_with_solver_modes_matches_oracle_modes(built):
     assert np.abs(s1 - s2).max() <= 1e-9 * s2.max()
     # the excited mode carries most of the transmitted power
     assert s1[2 * k] > 10 * max(s1[2 * k + 2:].max(), 1e-30), s1
+
+
+@pytest.mark.parametrize("k", [2, 3, 16, 40])
+def test_fewer_propagating_modes_than_asked(built, k):
+    """A 5 x 4 layer with two propagating modes (the golden mode deck's port):
+    asking for more returns those two; a block as large as the space works."""
+    g = np.load(os.path.join(HERE, "golden", "decks", "deck_modes", "media.npz"))
+    med = g["port_med"]
+    om = 2 * np.pi / (1.55e-6 * 1.0e7)
+    ref = MO.calc_Xi(med, om, 5, 4, (0, 0))
+    assert ref["num_real"] == 2
+    ms = modes.solve(med, om, 5, 4, (0, 0), k)
+    assert ms.n_found == 2, ms.info
+    np.testing.assert_allclose(ms.theta[:2], ref["theta"][:2], rtol=0, atol=1e-10)
+    assert np.all(ms.Xi[:, 2:k] == 0) and np.all(ms.Xi[:, k + 2:] == 0)
