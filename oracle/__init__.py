@@ -25,6 +25,7 @@ PORT_LIB = os.path.join(HERE, "_build", "liboracle_fdtd.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_fdtd.so")
 REF_BIN = os.path.join(HERE, "_ref", "FDTD_ref")
 MCALC_BIN = os.path.join(HERE, "_ref", "Mcalc_ref")
+SCALC_BIN = os.path.join(HERE, "_ref", "Scalc_ref")
 REF_DIR_DEFAULT = "/root/reference"
 
 _P = C.c_void_p
@@ -66,6 +67,7 @@ def build(with_reference: bool | None = None) -> None:
     if _newer(REF_BIN, [ref_src, shim]):
         subprocess.run(["gcc", *CFLAGS, "-w", ref_src, shim, "-o", REF_BIN, "-lm"], check=True)
     _build_mcalc(ref_dir, shim)
+    _build_scalc(ref_dir)
 
 
 def _openblas():
@@ -93,6 +95,23 @@ def _build_mcalc(ref_dir, blas_shim):
     if _newer(MCALC_BIN, srcs + [lshim, blas_shim]):
         subprocess.run(["gcc", "-O2", "-std=c11", "-w", *srcs, lshim, blas_shim, blas,
                         "-Wl,-rpath," + os.path.dirname(blas), "-o", MCALC_BIN, "-lm"], check=True)
+
+
+def _build_scalc(ref_dir):
+    """The stock reference S-matrix program (Smat/Scalc.c) with zgesv_ from
+    lapack_shim.c and zgemm_/dznrm2_ from blas_fwd.c, both on scipy's OpenBLAS."""
+    src = os.path.join(ref_dir, "Smat", "Scalc.c")
+    blas = _openblas()
+    if not os.path.isfile(src) or blas is None:
+        return
+    deps = [src, os.path.join(HERE, "lapack_shim.c"), os.path.join(HERE, "blas_fwd.c")]
+    if _newer(SCALC_BIN, deps):
+        subprocess.run(["gcc", "-O2", "-std=c11", "-w", *deps, blas, "-Wl,-rpath," + os.path.dirname(blas),
+                        "-o", SCALC_BIN, "-lm"], check=True)
+
+
+def scalc_available() -> bool:
+    return os.path.isfile(SCALC_BIN)
 
 
 def mcalc_available() -> bool:

@@ -35,3 +35,12 @@ void zgeev_(char *jobvl, char *jobvr, long *n, double complex *a, long *lda, dou
     scipy_zgeev_(jobvl, jobvr, &n_, a, &lda_, w, vl, &ldvl_, vr, &ldvr_, work, &lwork_, rwork, &info_, 1, 1);
     *info = info_;
 }
+
+extern void scipy_zgesv_(const int *n, const int *nrhs, double complex *a, const int *lda, int *ipiv,
+                         double complex *b, const int *ldb, int *info);
+
+/* Smat/Scalc.c declares zgesv_ with int arguments (:315): a plain forward */
+void zgesv_(int *n, int *nrhs, double complex *a, int *lda, int *ipiv, double complex *b, int *ldb, int *info)
+{
+    scipy_zgesv_(n, nrhs, a, lda, ipiv, b, ldb, info);
+}
