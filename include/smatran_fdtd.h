@@ -422,6 +422,35 @@ int smat_mode_apply(int L0, int L1, const int BoundC[2], double omega, const dou
  * (unit 2-norm).  Host only, no GPU needed. */
 int smat_mode_small_eig(int m, const double *B, double *w, double *V);
 
+/* ---------------------------------------------------------------------------
+ * Frequency-domain S matrix by layer transfer (the reference's Smat/Scalc.c).
+ * --------------------------------------------------------------------------- */
+typedef struct smat_scalc_info {
+    double ms;         /* wall time of the call */
+    int solves;        /* dense eliminations (inv_process) performed */
+    double unitarity;  /* ||S^H S - 1||_F   (check_Smat :885-912) */
+    double transpose;  /* ||S - S^T||_F */
+} smat_scalc_info;
+
+/* Scalc's main (:74-96): the S matrix between the bottom port layer iB and the
+ * top port layer iT.  meds: nlayers = iT - iB + 1 layers in z order, each
+ * 6*L0*L1 complex Med values as set_V reads them (the port layers must be
+ * lossless, inner layers may be lossy); XiB / XiT: the full mode matrices of
+ * the two port layers, (4*L0*L1) x (4*L0*L1) complex column-major as Mcalc's
+ * Xi file holds them (column j forward mode j, column j + 2*L0*L1 backward);
+ * nB / nT: their N_real.  both_ways = 0 computes the first nB columns only
+ * (the forward pass).  S: (nB+nT)^2 complex, column-major, Smat_calc's
+ * layout.  Dense in 2*L0*L1, as the reference: cross-sections up to a few
+ * thousand unknowns. */
+int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int nlayers, const double *meds,
+               const double *XiB, int nB, const double *XiT, int nT, int both_ways, double *S,
+               smat_scalc_info *info);
+
+/* No counterpart in the reference: the GPU LU solve behind smat_scalc (zgesv
+ * semantics) on host arrays, for testing.  A: n x n, B and X: n x nrhs, all
+ * complex column-major; *info = first zero pivot (1-based) or 0. */
+int smat_zgesv(int n, int nrhs, const double *A, const double *B, double *X, int *info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,9 +42,10 @@ def reference(built):
 
 
 def golden_cases():
-    """The time-loop fixtures (the port-mode fixtures modes_*.npz have their own tests)."""
+    """The time-loop fixtures (the mode-solver and S-matrix fixtures, modes_*.npz
+    and scalc_*.npz, have their own tests)."""
     return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith("modes_"))
+                  if not os.path.basename(p).startswith(("modes_", "scalc_")))
 
 
 def load_golden(name):
