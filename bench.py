@@ -657,9 +657,65 @@ def run_modes(args):
         "cpu_baseline": cpu}))
 
 
+def run_scalc(args):
+    """Layer-transfer S matrix (Scalc, (f)-4) on the GPU: a periodic grating
+    between uniform ports, --shape L0,L1,nlayers (default 32x32, 10 layers:
+    dense matrices of order NA = 2*L0*L1 = 2048, all propagating modes of the
+    ports in S), both directions.  CPU side: the same dense steps (zgesv of
+    B2^T with NA + N_real right-hand sides, the projection zgemm) through
+    LAPACK / BLAS on the host cores, one of each timed at full size and
+    multiplied by their counts."""
+    import torch
+    from smatranem_gb300 import scalc as SC
+    from smatranem_gb300 import workloads as W
+    parts = [int(x) for x in args.shape.split(",")] if args.shape != "256,192,48" else [32, 32, 10]
+    L0, L1, nl = parts[:3]
+    om = 0.405
+    t0 = time.perf_counter()
+    theta, Xi, nr = W.plane_wave_basis(L0, L1, omega=om)
+    meds = W.grating_layers(L0, L1, nl, seed=7)
+    t_setup = time.perf_counter() - t0
+    NA = 2 * L0 * L1
+    SC.smatrix(meds[:2], om, L0, L1, (1, 1), Xi, nr, Xi, nr)  # warm-up (allocations, module load)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        S, info = SC.smatrix(meds, om, L0, L1, (1, 1), Xi, nr, Xi, nr)
+        times.append(time.perf_counter() - t0)
+    solves = info["solves"]
+    flops = solves * (8.0 / 3.0 * 4 * NA ** 3 + 8.0 * NA ** 2 * (NA + nr)) + 2 * 8.0 * (2 * NA) ** 2 * (NA + nr)
+    cpu = None
+    if not args.no_cpu:
+        import scipy.linalg as sl
+        rng = np.random.default_rng(0)
+        A = rng.standard_normal((NA, NA)) + 1j * rng.standard_normal((NA, NA))
+        B = rng.standard_normal((NA, NA + nr)) + 1j * rng.standard_normal((NA, NA + nr))
+        t0 = time.perf_counter()
+        sl.solve(A, B, check_finite=False)
+        t_solve = time.perf_counter() - t0
+        P = rng.standard_normal((2 * NA, 2 * NA)) + 1j * rng.standard_normal((2 * NA, 2 * NA))
+        F = rng.standard_normal((2 * NA, NA + nr)) + 1j * rng.standard_normal((2 * NA, NA + nr))
+        t0 = time.perf_counter()
+        P.conj().T @ F
+        t_mm = time.perf_counter() - t0
+        est = solves * t_solve + 2 * t_mm
+        cpu = {"value": est, "unit": "s per S matrix (LAPACK zgesv x solves + 2 projection zgemm)",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": f"one zgesv of order {NA} with {NA + nr} right-hand sides: {t_solve:.2f} s (x {solves}); "
+                         f"one {2 * NA}^2 x {NA + nr} zgemm: {t_mm:.2f} s (x 2); threads of the host BLAS"}
+    best = float(min(times))
+    print(json.dumps({
+        "mode": "scalc", "config": f"periodic grating {L0}x{L1}, {nl} layers, uniform ports eps 2.085, "
+                                   f"NA = {NA}, N_real = {nr} per port, both directions",
+        "s_per_smatrix": best, "runs": len(times), "solves": solves,
+        "fp64_tflops": flops / best / 1e12, "unitarity": info["unitarity"], "transpose": info["transpose"],
+        "setup_s": t_setup, "cpu_baseline": cpu}))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", default="main", choices=["main", "adjoint", "group", "large", "modes"],
+    ap.add_argument("--mode", default="main", choices=["main", "adjoint", "group", "large", "modes", "scalc"],
                     help="main: the contract line; the others: the adjoint, batched-structures and large-domain "
                          "workloads (one summary line each)")
     ap.add_argument("--adj-steps", type=int, default=6000)
@@ -684,7 +740,8 @@ def main():
     if args.profile:
         run_profile(args)
     elif args.mode != "main":
-        {"adjoint": run_adjoint, "group": run_group, "large": run_large, "modes": run_modes}[args.mode](args)
+        {"adjoint": run_adjoint, "group": run_group, "large": run_large, "modes": run_modes,
+         "scalc": run_scalc}[args.mode](args)
     elif args.impl == "reference":
         run_reference(args)
     else:

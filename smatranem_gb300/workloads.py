@@ -600,3 +600,89 @@ def waveguide_structure(med, L0, L1, L2, L3, omega=0.405, pml_z=3, iBc=(0, 0, 0)
     mu_s, ep_s = stretch_media((L0, L1, L2), mu, ep, sig)
     return Structure(L=(L0, L1, L2, L3), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=tuple(iBc),
                      name=f"guide{L0}x{L1}x{L2}")
+
+
+def plane_wave_basis(L0, L1, eps=2.085, omega=0.405):
+    """The full mode matrix Xi of a uniform, isotropic, periodic port layer
+    (BoundC = (1, 1), mu = 1, unit cells) in Mcalc's conventions, built in
+    closed form instead of by a dense eigen solve.  For wavevector k the
+    forward differences have the symbols d_a = e^{i k_a} - 1, maa the
+    Hermitian symbol M = w mu - (1/(w eps)) c^H c with c = (d1, -d0), and
+    mbb*maa the eigenvalue w^2 eps mu - |d|^2 on both polarizations
+    (u1 = c^H / |c| and u2 = (d0, d1) / |d|, eigenvectors of M; e_x, e_y at
+    k = 0).  Then Mcalc's steps: eiSin = the root with Im >= 0, theta =
+    2 asin(eiSin / 2), E = maa H / eiSin, forward [e^{-i theta/2} H; E] and
+    backward [e^{i theta/2} H; -E] columns, propagating modes first by
+    descending theta and evanescent ones by ascending Im theta, and normXi's
+    normalisations (unit power flow; unit cross flow of an evanescent pair).
+    Returns (theta (2N,), Xi (2N, 2N), num_real), N = 2*L0*L1."""
+    NA1 = L0 * L1
+    N = 2 * NA1
+    w = omega
+    j0 = np.tile(np.arange(L0), L1)
+    j1 = np.repeat(np.arange(L1), L0)
+    modes = []
+    for q in range(L1):
+        for p in range(L0):
+            k0, k1 = 2 * math.pi * p / L0, 2 * math.pi * q / L1
+            d0, d1 = np.exp(1j * k0) - 1, np.exp(1j * k1) - 1
+            c = np.array([d1, -d0])
+            M = w * np.eye(2) - np.outer(np.conj(c), c) / (w * eps)
+            lam = w * w * eps - (abs(d0) ** 2 + abs(d1) ** 2)
+            ph = np.exp(1j * (k0 * j0 + k1 * j1)) / math.sqrt(NA1)
+            nd = math.sqrt(abs(d0) ** 2 + abs(d1) ** 2)
+            pols = [np.array([1.0, 0.0]), np.array([0.0, 1.0])] if nd == 0.0 else \
+                [np.conj(c) / nd, np.array([d0, d1]) / nd]
+            for u in pols:
+                modes.append((lam, u, M @ u, ph))
+    real = sorted([m for m in modes if m[0] > 0], key=lambda m: -m[0])
+    evan = sorted([m for m in modes if m[0] <= 0], key=lambda m: -m[0])
+    theta = np.zeros(2 * N, np.complex128)
+    Xi = np.zeros((2 * N, 2 * N), np.complex128)
+    for col, (lam, u, Mu, ph) in enumerate(real + evan):
+        s = np.sqrt(complex(lam, 0.0))
+        H = np.concatenate([u[0] * ph, u[1] * ph])
+        E = np.concatenate([Mu[0] * ph, Mu[1] * ph]) / s
+        t = 2.0 * np.arcsin(0.5 * s)
+        theta[col], theta[col + N] = t, -t
+        Xi[:N, col] = np.exp(-0.5j * t) * H
+        Xi[N:, col] = E
+        Xi[:N, col + N] = np.exp(0.5j * t) * H
+        Xi[N:, col + N] = -E
+    nr = len(real)
+    for col in range(N):
+        f, b = Xi[:, col], Xi[:, col + N]
+        if col < nr:
+            for v in (f, b):
+                z = np.vdot(v[:N], v[N:]) + np.vdot(v[N:], v[:N])
+                v *= 1.0 / math.sqrt(abs(z.real))
+        else:
+            z = np.sqrt(np.vdot(b[:N], f[N:]) + np.vdot(b[N:], f[:N]))
+            z = np.conj(z) / (z.real ** 2 + z.imag ** 2)
+            f *= z
+            b *= np.conj(z)
+    return theta, Xi, nr
+
+
+def grating_layers(L0, L1, nlayers, eps_port=2.085, eps_grating=(2.085, 12.11), fill=0.4, seed=0):
+    """Media of nlayers z layers (6, L0*L1) each for the layer-transfer S
+    matrix: uniform ports (the first and last layer, matching
+    plane_wave_basis) around a seeded two-material pattern (a random
+    rectangle of the second material covering about `fill` of each inner
+    layer).  Unit cells, mu = 1."""
+    rng = np.random.default_rng(seed)
+    n = L0 * L1
+    j0 = np.tile(np.arange(L0), L1)
+    j1 = np.repeat(np.arange(L1), L0)
+    out = []
+    for z in range(nlayers):
+        eps = np.full(n, eps_port, np.complex128)
+        if 0 < z < nlayers - 1:
+            w0 = max(1, int(round(L0 * math.sqrt(fill))))
+            w1 = max(1, int(round(L1 * math.sqrt(fill))))
+            a0, a1 = rng.integers(0, L0), rng.integers(0, L1)
+            inside = (((j0 - a0) % L0) < w0) & (((j1 - a1) % L1) < w1)
+            eps = np.where(inside, eps_grating[1], eps_grating[0]).astype(np.complex128)
+        one = np.ones(n, np.complex128)
+        out.append(np.stack([one, one, eps, eps, eps, one]))
+    return np.array(out)

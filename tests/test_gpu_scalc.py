@@ -98,3 +98,14 @@ def test_smatrix_argument_checks(built):
     assert e.value.code == -1
     with pytest.raises(fdtd.FdtdError):
         scalc.smatrix(g["meds"][:1], float(g["omega"]), int(L[0]), int(L[1]), (0, 0), g["XiB"], nB, g["XiT"], nT)
+
+
+def test_grating_with_plane_wave_ports(built):
+    """The bench's workload form at a small size: closed-form port basis, seeded grating."""
+    L0, L1, om = 10, 8, 0.405
+    th, Xi, nr = W.plane_wave_basis(L0, L1, omega=om)
+    meds = W.grating_layers(L0, L1, 6, seed=7)
+    ref = SO.smatrix(list(meds), om, L0, L1, (1, 1), Xi, nr, Xi, nr)
+    S, info = scalc.smatrix(meds, om, L0, L1, (1, 1), Xi, nr, Xi, nr)
+    assert np.abs(S - ref).max() < 1e-10
+    assert info["unitarity"] < 1e-10
