@@ -451,6 +451,11 @@ int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int nlayers, c
  * complex column-major; *info = first zero pivot (1-based) or 0. */
 int smat_zgesv(int n, int nrhs, const double *A, const double *B, double *X, int *info);
 
+/* The drop-in S-matrix program: `Scalc input.txt` reads the keys, Med layers,
+ * Mode and Xi files Scalc reads (Smat/Scalc.c main :27-96) and writes
+ * <prefix>_Smatrix.dat in Out_Smat's format (:113-140); returns the exit status. */
+int smat_scalc_main(int argc, char **argv);
+
 #ifdef __cplusplus
 }
 #endif

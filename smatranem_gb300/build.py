@@ -5,6 +5,8 @@ Outputs (git-ignored) under smatranem_gb300/_build/:
                        sm_103a + host precompute + deck I/O)
   FDTD                 the drop-in command-line solver (reads input.txt and the
                        Data/ files of the SMatrAnEM mesher chain)
+  Scalc                the drop-in S-matrix program (same input.txt, Med, Mode
+                       and Xi files as SMatrAnEM's Scalc; writes _Smatrix.dat)
 
 Only nvcc and gcc are used, one -gencode (sm_103a), translation units compiled
 in parallel.  Run ``python -m smatranem_gb300.build``.
@@ -24,6 +26,7 @@ INC = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libsmatran_fdtd.so")
 EXE = os.path.join(OUT, "FDTD")
+SCALC_EXE = os.path.join(OUT, "Scalc")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host C: the reference's flags (-O2 -std=c11) plus no FMA contraction, so the
@@ -90,6 +93,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     main_c = os.path.join(CSRC, "fdtd_main.c")
     if os.path.exists(main_c) and (force or _stale(EXE, [main_c, LIB] + headers)):
         _run(["gcc"] + CFLAGS + [main_c, "-o", EXE, "-L" + OUT, "-lsmatran_fdtd", "-Wl,-rpath,$ORIGIN", "-lm"], log)
+    cli_c = os.path.join(CSRC, "scalc_cli.c")
+    if os.path.exists(cli_c) and (force or _stale(SCALC_EXE, [cli_c, LIB] + headers)):
+        _run(["gcc"] + CFLAGS + [cli_c, "-o", SCALC_EXE, "-L" + OUT, "-lsmatran_fdtd", "-Wl,-rpath,$ORIGIN", "-lm"],
+             log)
     if verbose:
         for cmd, out in log:
             print(" ".join(cmd))

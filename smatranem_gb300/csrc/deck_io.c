@@ -860,3 +860,225 @@ done:
     smat_deck_free(d);
     return status;
 }
+
+/* ---- the drop-in S-matrix program (Smat/Scalc.c main :27-96) ---------------- */
+
+/* input_file0 of Scalc (:657-686): Prefix, BoundaryCondition (B0, B1), ModeP's
+ * two targets, Smatrix (both-ways, LAPACK solver) */
+static int scalc_input(const char *path, char *prefix, int bc[2], char target[2][BUF], char *both, char *solv)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) return smat_fail(SMAT_EINVAL, "open error!: open input-file0!");
+    char buf[BUF];
+    int seen = 0;
+    while (fgets(buf, sizeof buf, f) && seen != 15) {
+        strip_leading_space(buf);
+        if (!(seen & 1) && strncmp(buf, "Prefix", 6) == 0 && sscanf(buf, "%*[^=] %*[=] %s", prefix) == 1) {
+            cut_at_comma(prefix);
+            seen |= 1;
+        } else if (!(seen & 2) && strncmp(buf, "BoundaryCondition", 17) == 0 &&
+                   sscanf(buf, "%*[^=] %*[=] %d %*[^=] %*[=] %d", &bc[0], &bc[1]) == 2) {
+            seen |= 2;
+        } else if (!(seen & 4) && strncmp(buf, "ModeP", 5) == 0 &&
+                   sscanf(buf, "%*[^=] %*[=] %*[^=] %*[=] %*[^=] %*[=] %s", target[0]) == 1) {
+            cut_at_comma(target[0]);
+            if (sscanf(buf, "%*[^=] %*[=] %*[^=] %*[=] %*[^=] %*[=] %*[^=] %*[=] %s", target[1]) != 1)
+                sscanf(target[0], "%s", target[1]);
+            else cut_at_comma(target[1]);
+            seen |= 4;
+        } else if (!(seen & 8) && strncmp(buf, "Smatrix", 7) == 0 &&
+                   sscanf(buf, "%*[^=] %*[=] %s %*[^=] %*[=] %s", both, solv) == 2) {
+            cut_at_comma(both);
+            cut_at_comma(solv);
+            seen |= 8;
+        }
+    }
+    fclose(f);
+    if (seen != 15) return smat_fail(SMAT_EINVAL, "4 control commands cannot be read in input_file1!");
+    return SMAT_OK;
+}
+
+/* N_real and omega of a Mode file (get_RealNum05omega :599-626) */
+static int scalc_mode_file(const char *name, const int L[4], int *nreal, double *omega)
+{
+    FILE *f = fopen(name, "r");
+    if (!f) return smat_fail(SMAT_EINVAL, "open error for %s", name);
+    char buf[BUF];
+    int need = 2, nc = 0;
+    while (need > 0 && fgets(buf, sizeof buf, f)) {
+        if (strncmp(buf, "# Omega", 7) == 0 && sscanf(buf, "%*[^=] %*[=] %lf", omega) == 1) need--;
+        if (strncmp(buf, "# Eigen-value", 13) == 0 && sscanf(buf, "%*[^=] %*[=] %d %*[^=] %*[=] %d", nreal, &nc) == 2)
+            need--;
+    }
+    fclose(f);
+    if (need != 0 || *nreal + nc != 2 * L[0] * L[1])
+        return smat_fail(SMAT_EINVAL, "RealNum05 cannot be read in get_RealNum05! (%s)", name);
+    return SMAT_OK;
+}
+
+/* a whole Xi file as the (2NA x 2NA) column-major mode matrix */
+static int scalc_xi(const char *name, int NA, double complex **out)
+{
+    double complex *blk = malloc(sizeof(double complex) * (size_t)NA * 2 * NA * 2);
+    double complex *xi = malloc(sizeof(double complex) * (size_t)2 * NA * 2 * NA);
+    if (!blk || !xi) {
+        free(blk), free(xi);
+        return smat_fail(SMAT_ENOMEM, "Scalc: out of host memory for %s", name);
+    }
+    int rc = read_xi_blocks(name, NA, NA, blk);
+    for (long j = 0; j < NA && !rc; j++)
+        for (long r = 0; r < 2 * NA; r++) {
+            xi[r + 2 * NA * j] = blk[(j * 2 * NA + r) * 2 + 0];
+            xi[r + 2 * NA * (j + NA)] = blk[(j * 2 * NA + r) * 2 + 1];
+        }
+    free(blk);
+    if (rc) {
+        free(xi);
+        return rc;
+    }
+    *out = xi;
+    return SMAT_OK;
+}
+
+int smat_scalc_main(int argc, char **argv)
+{
+    time_t t_ini = time(0);
+    fprintf(stderr, "# Start time of mode calculation = %s\n", ctime(&t_ini));
+    if (argc != 2) {
+        fprintf(stderr, "error: number of files \n");
+        return EXIT_FAILURE;
+    }
+    if (strncmp(argv[1], "-v", 2) == 0 || strcmp(argv[1], "--version") == 0) {
+        fprintf(stderr, "The '%s' creates scattering matrix by layer transfer on the GPU.\n", argv[0]);
+        fprintf(stderr, " smatranem_gb300 (sm_103a); input and output formats of SMatrAnEM Scalc.\n");
+        fprintf(stderr, "There is NO warranty.\n");
+        return EXIT_SUCCESS;
+    }
+    char prefix[BUF], target[2][BUF], both[BUF], solv[BUF];
+    int bc[2], L[4] = {0, 0, 0, 0};
+    int rc = scalc_input(argv[1], prefix, bc, target, both, solv);
+    double complex *meds = NULL, *xiB = NULL, *xiT = NULL, *S = NULL, *mu = NULL, *ep = NULL;
+    if (!rc) { /* input_file1 :643-653 */
+        char name[BUF + 32], buf[BUF];
+        snprintf(name, sizeof name, "%s_Med%s.dat", prefix, target[0]);
+        FILE *f = fopen(name, "r");
+        if (!f) rc = smat_fail(SMAT_EINVAL, "open error!: open input-file1!");
+        int got = 0;
+        while (!rc && !got && fgets(buf, sizeof buf, f))
+            if (strncmp(buf, "# l <", 5) == 0 &&
+                sscanf(buf, "%*[^<] %*[<] %d %*[^<] %*[<] %d %*[^<] %*[<] %d %*[^=] %*[=] %d", &L[0], &L[1], &L[2],
+                       &L[3]) == 4)
+                got = 1;
+        if (f) fclose(f);
+        if (!rc && !got) rc = smat_fail(SMAT_EINVAL, "L[4] cannot be read in input_file1!");
+    }
+    int iB = 0, iT = 0, nreal[2] = {0, 0};
+    double omega = 0;
+    const int same = !rc && strcmp(target[0], target[1]) == 0;
+    if (!rc) {
+        iB = plane_index(L, target[0]);
+        iT = plane_index(L, target[1]);
+        if (iB == iT) {
+            iT = (L[2] - 1) - iB;
+            fprintf(stderr, "The 2nd target ' %s ' is the same as the 1st, and iT is changed to %d\n", target[1], iT);
+        }
+        if (iB >= iT)
+            rc = smat_fail(SMAT_EINVAL, "Target_B = %d for %s is larger than or equal to Target_T = %d for %s", iB,
+                           target[0], iT, target[1]);
+        else fprintf(stderr, "Target_B = %d for %s, Target_T = %d for %s\n", iB, target[0], iT, target[1]);
+    }
+    for (int side = 0; side < (same ? 1 : 2) && !rc; side++) {
+        char name[BUF + 32];
+        double om = 0;
+        snprintf(name, sizeof name, "%s_%cMode.dat", prefix, side ? 't' : 'b');
+        rc = scalc_mode_file(name, L, &nreal[side], &om);
+        if (!rc) fprintf(stderr, "RealNum05 for %s = %d\n", name, nreal[side]);
+        if (!rc && side == 1 && om != omega)
+            rc = smat_fail(SMAT_EINVAL, "Top omega = %.5e != Bottom omega = %.5e", om, omega);
+        omega = om;
+    }
+    if (!rc && same) nreal[1] = nreal[0];
+    if (!rc) fprintf(stderr, "Omega = k/k0 = %.20e\n", omega);
+    const long pl = (long)L[0] * L[1];
+    const int NA = 2 * (int)pl, nl = iT - iB + 1;
+    if (!rc) { /* the layers iB..iT in Mcalc's set_V order */
+        meds = malloc(sizeof(double complex) * 6 * pl * (nl > 0 ? nl : 1));
+        mu = malloc(sizeof(double complex) * 3 * pl);
+        ep = malloc(sizeof(double complex) * 3 * pl);
+        if (!meds || !mu || !ep) rc = smat_fail(SMAT_ENOMEM, "Scalc: out of host memory");
+        for (int z = iB; z <= iT && !rc; z++) {
+            char name[BUF];
+            double sq;
+            layer_file(prefix, L, z, name);
+            rc = read_layer(name, L, &sq, mu, ep);
+            double complex *m = meds + 6 * pl * (z - iB);
+            for (long p = 0; p < pl && !rc; p++) {
+                m[0 * pl + p] = mu[3 * p + 0];
+                m[1 * pl + p] = mu[3 * p + 1];
+                m[2 * pl + p] = ep[3 * p + 2];
+                m[3 * pl + p] = ep[3 * p + 1];
+                m[4 * pl + p] = ep[3 * p + 0];
+                m[5 * pl + p] = mu[3 * p + 2];
+            }
+        }
+    }
+    /* Xi files (initial_calc :190-191, final_calc :298-299): the bottom port's for
+     * both ends when the targets are the same or the second is a bottom layer */
+    const int top_xi = !same && target[1][0] != 'B';
+    if (!rc) {
+        char name[BUF + 32];
+        snprintf(name, sizeof name, "%s_bXi.dat", prefix);
+        rc = scalc_xi(name, NA, &xiB);
+        if (!rc && top_xi) {
+            snprintf(name, sizeof name, "%s_tXi.dat", prefix);
+            rc = scalc_xi(name, NA, &xiT);
+        }
+    }
+    const int N = nreal[0] + nreal[1];
+    const int both_ways = both[0] == 'Y' || both[0] == 'y';
+    smat_scalc_info info = {0, 0, 0, 0};
+    if (!rc) {
+        S = calloc((size_t)N * N, sizeof(double complex));
+        if (!S) rc = smat_fail(SMAT_ENOMEM, "Scalc: out of host memory");
+    }
+    if (!rc) {
+        fprintf(stderr, "Forward calc.: iway = 1%s\n", both_ways ? ", then Backward calc.: iway = -1" : "");
+        rc = smat_scalc(L[0], L[1], bc, omega, nl, (const double *)meds, (const double *)xiB, nreal[0],
+                        (const double *)(top_xi ? xiT : xiB), nreal[1], both_ways, (double *)S, &info);
+    }
+    if (!rc) { /* Out_Smat :113-140 */
+        char name[BUF + 32];
+        snprintf(name, sizeof name, "%s_Smatrix.dat", prefix);
+        FILE *f = fopen(name, "w");
+        if (!f) rc = smat_fail(SMAT_EINVAL, "open error!: open o-file!");
+        else {
+            time_t t_f = time(0);
+            fprintf(f, "# This file          : ' %s ' on %s", name, ctime(&t_f));
+            fprintf(f, "# Exec. file         : ' %s ' (smatranem_gb300, GPU layer transfer)\n", argv[0]);
+            fprintf(f, "# Calc. time         : Exec. time = %1.0f s\n", difftime(t_f, t_ini));
+            fprintf(f, "# Parameter file     : ' %s ' for prefix, boundary conditions and internal precision\n",
+                    argv[1]);
+            fprintf(f, "# Omega              : k/k_0 = %.20e\n", omega);
+            fprintf(f, "# Boundary conditions: B0 = %d, B1 = %d\n", bc[0], bc[1]);
+            fprintf(f, "# Target layers      : Bottom = %s, Top = %s\n", target[0], target[1]);
+            fprintf(f, "# Mode numbers       : Bottom = %d, Top = %d\n", nreal[0], nreal[1]);
+            fprintf(f, "# Calc. mode         : both ways = %s, 'zgesv' = %s\n", both, solv);
+            fprintf(f, "# Smat. residual norm: unitarity = %.16e, transpose = %.16e\n", info.unitarity,
+                    info.transpose);
+            fprintf(f, "# m n real(S_mn) imag(S_mn) |S_mn|^2 for m,n < %d\n", N);
+            for (int c = 0; c < N; c++)
+                for (int r = 0; r < N; r++) {
+                    const double complex v = S[r + (size_t)N * c];
+                    const double a = cabs(v);
+                    fprintf(f, "%d %d %.20e %.20e %.20e\n", r, c, creal(v), cimag(v), a * a);
+                }
+            fclose(f);
+        }
+    }
+    free(meds), free(mu), free(ep), free(xiB), free(xiT), free(S);
+    if (rc) {
+        fprintf(stderr, "%s\n", smat_last_error());
+        return EXIT_FAILURE;
+    }
+    return EXIT_SUCCESS;
+}

@@ -106,11 +106,13 @@ def make_deck(name, L, seed, kw, dkw):
 
 
 def make_mode_deck(name="deck_modes", L=(5, 4, 14, 4), seed=51):
-    """A straight guide whose Mode / Xi files are the stock reference mode
-    solver's (oracle/_ref/Mcalc_ref) for the two monitor layers, then the
-    stock FDTD run on it: the Mcalc -> FDTD chain of the reference end to end.
-    The drop-in checks its report both reading these files and solving the
-    port modes itself (FDTD_GPU: modes = solve)."""
+    """A guide with a dielectric block beside the core, whose Mode / Xi files
+    are the stock reference mode solver's (oracle/_ref/Mcalc_ref) for the two
+    monitor layers; then the stock FDTD and the stock S-matrix program
+    (oracle/_ref/Scalc_ref) run on it: the Mcalc -> FDTD / Scalc chains of
+    the reference end to end.  The drop-ins check their outputs against
+    reference_stderr.txt (FDTD, reading these files or solving the port modes
+    itself) and reference_Smatrix.dat (Scalc)."""
     import shutil
     import subprocess
     from smatranem_gb300 import decks
@@ -120,14 +122,25 @@ def make_mode_deck(name="deck_modes", L=(5, 4, 14, 4), seed=51):
     om = decks.omega_of(1.55e-6, 1.0e7)
     med = W.port_layer(L0, L1, core=(2, 2), eps_core=12.11, eps_clad=2.085, seed=seed, jitter=0.25)
     s = W.waveguide_structure(med, L0, L1, L2, L3, omega=om, pml_z=2)
+    pl = L0 * L1
+    ep = s.epsi.reshape(L2, pl, 3)
+    for z in range(L3 + 1, L2 - L3 - 1):  # a dielectric block beside the core in the scatterer layers
+        for j1 in range(0, 2):
+            for j0 in range(3, 5):
+                ep[z, j0 + L0 * j1, :] = 6.5
     decks.write_deck(root, s, seed=seed, time_period=(1, 2, 6), inci_point="B3", inci_mode=1,
                      targets=("B2", "T1"), nreal=(1, 1),
                      extra_lines=("\tinv_k0 = 1.00000000000000000000e-07 m",
-                                  "\tMediumPara: wavelength= 1.55000000000000000000e-06 m, temperature= 25 degC"))
+                                  "\tMediumPara: wavelength= 1.55000000000000000000e-06 m, temperature= 25 degC",
+                                  "\tSmatrix: both-ways = y, LAPACK solver = y"))
     env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
     r = subprocess.run([oracle.MCALC_BIN, "input.txt"], cwd=root, capture_output=True, text=True, env=env)
     if r.returncode != 0:
         raise RuntimeError(f"{name}: Mcalc failed\n{r.stderr}")
+    r = subprocess.run([oracle.SCALC_BIN, "input.txt"], cwd=root, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError(f"{name}: Scalc failed\n{r.stderr}")
+    os.replace(os.path.join(root, "Data", "deck_Smatrix.dat"), os.path.join(root, "reference_Smatrix.dat"))
     r = subprocess.run([oracle.REF_BIN, "input.txt"], cwd=root, capture_output=True, text=True)
     with open(os.path.join(root, "reference_stderr.txt"), "w") as f:
         f.write(r.stderr)

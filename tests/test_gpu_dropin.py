@@ -118,3 +118,49 @@ def test_dropin_solves_port_modes(built, tmp_path):
     for x, y in zip(a, b):
         assert x[0] == y[0] and x[2] == y[2]
         assert abs(x[1] - y[1]) <= 1e-8 * big and abs(x[3] - y[3]) <= 1e-8 * big
+
+
+SCALC_EXE = os.path.join(ROOT, "smatranem_gb300", "_build", "Scalc")
+
+
+def _smatrix_file(path):
+    rows = {}
+    header = {}
+    for line in open(path):
+        if line.startswith("# Mode numbers") or line.startswith("# Target layers") or line.startswith("# Omega"):
+            header[line.split(":")[0].strip()] = line.split(":", 1)[1].strip()
+        if line.startswith("#"):
+            continue
+        m, n, re_, im_, a2 = line.split()
+        rows[(int(m), int(n))] = (float(re_), float(im_), float(a2))
+    return header, rows
+
+
+def test_scalc_dropin_matches_reference(built, tmp_path):
+    """The drop-in `Scalc input.txt` on the golden mode deck (Mode / Xi files from
+    the stock Mcalc): the same header facts and every S entry of the stock
+    Scalc's <prefix>_Smatrix.dat within 1e-10."""
+    src = os.path.join(GOLDEN, "decks", "deck_modes")
+    work = tmp_path / "deck_modes"
+    shutil.copytree(src, work)
+    r = subprocess.run([SCALC_EXE, "input.txt"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    h1, s1 = _smatrix_file(work / "Data" / "deck_Smatrix.dat")
+    h2, s2 = _smatrix_file(os.path.join(src, "reference_Smatrix.dat"))
+    assert h1 == h2
+    assert s1.keys() == s2.keys() and len(s1) == 16
+    for k in s2:
+        assert all(abs(a - b) < 1e-10 for a, b in zip(s1[k], s2[k])), (k, s1[k], s2[k])
+
+
+def test_scalc_dropin_errors(built, tmp_path):
+    src = os.path.join(GOLDEN, "decks", "deck_modes")
+    work = tmp_path / "deck_modes"
+    shutil.copytree(src, work)
+    os.remove(work / "Data" / "deck_tXi.dat")
+    r = subprocess.run([SCALC_EXE, "input.txt"], cwd=work, capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0 and "open error" in r.stderr
+    r = subprocess.run([SCALC_EXE], cwd=work, capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0
+    r = subprocess.run([SCALC_EXE, "-v"], cwd=work, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "scattering matrix" in r.stderr
