@@ -381,6 +381,9 @@ typedef struct smat_mode_opts {
     int guard;               /* extra block vectors beyond nmodes; 0: max(8, nmodes/2) */
     int max_iter;            /* outer iterations; 0: 2000 */
     unsigned long long seed; /* start block; 0: fixed default */
+    int precision;           /* 0: FP32 filter passes until the wanted residuals are below
+                                1e-6, then FP64 (default); 1: FP64 passes throughout.
+                                The Rayleigh-Ritz step and the result are FP64 either way */
 } smat_mode_opts;
 
 typedef struct smat_mode_info {
@@ -388,10 +391,11 @@ typedef struct smat_mode_info {
     int iterations;       /* outer (filter + Rayleigh-Ritz) iterations */
     int degenerate_pairs; /* mode pairs degeneXi re-orthogonalised */
     int block;            /* block size used */
-    long long matvecs;    /* applications of mbb*maa to one vector */
+    long long matvecs;    /* applications of mbb*maa to one vector (FP32 and FP64) */
     double max_residual;  /* largest relative residual among returned modes */
     double spectral_radius;
     double ms;            /* wall time of the call */
+    long long matvecs_fp32; /* of matvecs, those done in FP32 filter passes */
 } smat_mode_info;
 
 /* Replaces calc_Xi (Mcalc.c:256-347) for the propagating part of the spectrum:

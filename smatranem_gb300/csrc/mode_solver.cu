@@ -54,38 +54,39 @@ using cplx = std::complex<double>;
 
 struct Op {
     int L0, L1, NA1;
-    const double *V;  // 6*NA1: w mu00, w mu11, 1/(w eps22), w eps11, w eps00, 1/(w mu22)
+    const double *V;  // 6*NA1: w mu00, w mu11, 1/(w eps22), w eps11, w eps00, 1/(w mu22) (FP64 copy)
     double s0, s1;    // diagonal of Dup0 / Dup1: -1, or BoundC when the axis has one cell
     double e0, e1;    // Dup's wrap coefficient at the last column / row (0 for a one-cell axis)
 };
-
-__device__ __forceinline__ double cw(int i, int La, double e) { return i < La - 1 ? 1.0 : e; }
 
 /* Y = maa X for the m columns of X (column j at X + j*ld).  One thread per
  * point p = i0 + L0*i1; w = (1/(w eps22)) (Dup1 x0 - Dup0 x1) is evaluated at
  * p and at its -e0 and -e1 neighbours, then
  *     y0 = V0 x0 + Ddown1 w,   y1 = V1 x1 - Ddown0 w,
  * with (Ddown_a w)(p) = -s_a w(p) - c_a(p - e_a) w(p - e_a). */
-__global__ void k_maa(Op op, const double *__restrict__ X, double *__restrict__ Y, long long ld)
+template <class T>
+__global__ void k_maa(Op op, const T *__restrict__ Vt, const T *__restrict__ X, T *__restrict__ Y, long long ld)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= op.NA1) return;
     const int L0 = op.L0, L1 = op.L1, NA1 = op.NA1;
     const int i0 = p % L0, i1 = p / L0;
     const int i0m = i0 == 0 ? L0 - 1 : i0 - 1, i1m = i1 == 0 ? L1 - 1 : i1 - 1;
-    const double *x0 = X + (long long)blockIdx.y * ld, *x1 = x0 + NA1;
-    const double *V2 = op.V + 2 * (long long)NA1;
+    const T s0 = (T)op.s0, s1 = (T)op.s1, e0 = (T)op.e0, e1 = (T)op.e1;
+    const T *x0 = X + (long long)blockIdx.y * ld, *x1 = x0 + NA1;
+    const T *V2 = Vt + 2 * (long long)NA1;
+    auto cwt = [](int i, int La, T e) { return i < La - 1 ? (T)1 : e; };
     auto curl = [&](int j0, int j1) {  // w at (j0, j1)
         const int q = j0 + L0 * j1;
         const int q0 = (j0 + 1 == L0 ? 0 : j0 + 1) + L0 * j1, q1 = j0 + L0 * (j1 + 1 == L1 ? 0 : j1 + 1);
-        const double d1 = op.s1 * __ldg(x0 + q) + cw(j1, L1, op.e1) * __ldg(x0 + q1);
-        const double d0 = op.s0 * __ldg(x1 + q) + cw(j0, L0, op.e0) * __ldg(x1 + q0);
+        const T d1 = s1 * __ldg(x0 + q) + cwt(j1, L1, e1) * __ldg(x0 + q1);
+        const T d0 = s0 * __ldg(x1 + q) + cwt(j0, L0, e0) * __ldg(x1 + q0);
         return __ldg(V2 + q) * (d1 - d0);
     };
-    const double wp = curl(i0, i1), wm0 = curl(i0m, i1), wm1 = curl(i0, i1m);
-    double *y0 = Y + (long long)blockIdx.y * ld, *y1 = y0 + NA1;
-    y0[p] = __ldg(op.V + p) * __ldg(x0 + p) + (-op.s1 * wp - cw(i1m, L1, op.e1) * wm1);
-    y1[p] = __ldg(op.V + NA1 + p) * __ldg(x1 + p) - (-op.s0 * wp - cw(i0m, L0, op.e0) * wm0);
+    const T wp = curl(i0, i1), wm0 = curl(i0m, i1), wm1 = curl(i0, i1m);
+    T *y0 = Y + (long long)blockIdx.y * ld, *y1 = y0 + NA1;
+    y0[p] = __ldg(Vt + p) * __ldg(x0 + p) + (-s1 * wp - cwt(i1m, L1, e1) * wm1);
+    y1[p] = __ldg(Vt + NA1 + p) * __ldg(x1 + p) - (-s0 * wp - cwt(i0m, L0, e0) * wm0);
 }
 
 /* out = mbb W (W = maa Ycur), then Ynew = alpha*(out - c*Ycur) - beta*Yprev.
@@ -93,37 +94,48 @@ __global__ void k_maa(Op op, const double *__restrict__ X, double *__restrict__ 
  *     out0 = V3 w0 + Dup0 u,   out1 = V4 w1 + Dup1 u.
  * alpha = 1, c = 0, beta = 0 gives the plain product A Ycur = mbb maa Ycur.
  * Ynew may alias Yprev (each thread reads its own entries before writing). */
-__global__ void k_mbb(Op op, const double *__restrict__ W, const double *Ycur, const double *Yprev, double *Ynew,
-                      long long ld, double alpha, double c, double beta)
+template <class T>
+__global__ void k_mbb(Op op, const T *__restrict__ Vt, const T *__restrict__ W, const T *Ycur, const T *Yprev, T *Ynew,
+                      long long ld, T alpha, T c, T beta)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= op.NA1) return;
     const int L0 = op.L0, L1 = op.L1, NA1 = op.NA1;
     const int i0 = p % L0, i1 = p / L0;
+    const T s0 = (T)op.s0, s1 = (T)op.s1, e0 = (T)op.e0, e1 = (T)op.e1;
     const long long col = (long long)blockIdx.y * ld;
-    const double *w0 = W + col, *w1 = w0 + NA1;
-    const double *V5 = op.V + 5 * (long long)NA1;
+    const T *w0 = W + col, *w1 = w0 + NA1;
+    const T *V5 = Vt + 5 * (long long)NA1;
+    auto cwt = [](int i, int La, T e) { return i < La - 1 ? (T)1 : e; };
     auto div = [&](int j0, int j1) {  // u at (j0, j1)
         const int q = j0 + L0 * j1;
         const int j0m = j0 == 0 ? L0 - 1 : j0 - 1, j1m = j1 == 0 ? L1 - 1 : j1 - 1;
-        const double a0 = -op.s0 * __ldg(w0 + q) - cw(j0m, L0, op.e0) * __ldg(w0 + j0m + L0 * j1);
-        const double a1 = -op.s1 * __ldg(w1 + q) - cw(j1m, L1, op.e1) * __ldg(w1 + j0 + L0 * j1m);
+        const T a0 = -s0 * __ldg(w0 + q) - cwt(j0m, L0, e0) * __ldg(w0 + j0m + L0 * j1);
+        const T a1 = -s1 * __ldg(w1 + q) - cwt(j1m, L1, e1) * __ldg(w1 + j0 + L0 * j1m);
         return __ldg(V5 + q) * (a0 + a1);
     };
     const int i0p = i0 + 1 == L0 ? 0 : i0 + 1, i1p = i1 + 1 == L1 ? 0 : i1 + 1;
-    const double up = div(i0, i1), up0 = div(i0p, i1), up1 = div(i0, i1p);
-    const double o0 = __ldg(op.V + 3 * (long long)NA1 + p) * __ldg(w0 + p) + (op.s0 * up + cw(i0, L0, op.e0) * up0);
-    const double o1 = __ldg(op.V + 4 * (long long)NA1 + p) * __ldg(w1 + p) + (op.s1 * up + cw(i1, L1, op.e1) * up1);
-    const double *yc = Ycur + col;
-    double r0 = alpha * (o0 - c * yc[p]), r1 = alpha * (o1 - c * yc[p + NA1]);
-    if (beta != 0.0) {
-        const double *yp = Yprev + col;
+    const T up = div(i0, i1), up0 = div(i0p, i1), up1 = div(i0, i1p);
+    const T o0 = __ldg(Vt + 3 * (long long)NA1 + p) * __ldg(w0 + p) + (s0 * up + cwt(i0, L0, e0) * up0);
+    const T o1 = __ldg(Vt + 4 * (long long)NA1 + p) * __ldg(w1 + p) + (s1 * up + cwt(i1, L1, e1) * up1);
+    const T *yc = Ycur + col;
+    T r0 = alpha * (o0 - c * yc[p]), r1 = alpha * (o1 - c * yc[p + NA1]);
+    if (beta != (T)0) {
+        const T *yp = Yprev + col;
         r0 -= beta * yp[p];
         r1 -= beta * yp[p + NA1];
     }
-    double *yn = Ynew + col;
+    T *yn = Ynew + col;
     yn[p] = r0;
     yn[p + NA1] = r1;
+}
+
+/* column-major block conversion between FP64 and FP32 */
+template <class A, class B>
+__global__ void k_cvt(const A *__restrict__ in, B *__restrict__ out, long long count)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) out[t] = (B)in[t];
 }
 
 constexpr int GT = 256;       // threads of the reduction kernels
@@ -207,7 +219,8 @@ __global__ void k_gemm(const double *__restrict__ X, const double *__restrict__ 
 
 /* per column j: sum_r (A[r,j] - lam[j] B[r,j])^2 (lam == nullptr: sum A^2),
  * partial sums per CTA into P[blk][j] */
-__global__ void k_colres(const double *__restrict__ A, const double *__restrict__ B, const double *__restrict__ lam,
+template <class T>
+__global__ void k_colres(const T *__restrict__ A, const T *__restrict__ B, const double *__restrict__ lam,
                          long long n, long long ld, int m, double *__restrict__ P)
 {
     __shared__ double red[GT];
@@ -217,7 +230,7 @@ __global__ void k_colres(const double *__restrict__ A, const double *__restrict_
         const double l = lam ? lam[j] : 0.0;
         double s = 0.0;
         for (long long r = r0 + threadIdx.x; r < r1; r += GT) {
-            const double v = lam ? A[r + ld * j] - l * B[r + ld * j] : A[r + ld * j];
+            const double v = lam ? (double)A[r + ld * j] - l * (double)B[r + ld * j] : (double)A[r + ld * j];
             s = fma(v, v, s);
         }
         red[threadIdx.x] = s;
@@ -233,12 +246,13 @@ __global__ void k_colres(const double *__restrict__ A, const double *__restrict_
 
 /* column j of A and of B scaled by s[j] (keeps the Chebyshev recurrence's
  * last two terms bounded; the recurrence is linear per column) */
-__global__ void k_scale2(double *A, double *B, const double *__restrict__ s, long long n, long long ld, int m)
+template <class T>
+__global__ void k_scale2(T *A, T *B, const double *__restrict__ s, long long n, long long ld, int m)
 {
     const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     for (int j = 0; j < m; j++) {
-        const double f = s[j];
+        const T f = (T)s[j];
         A[r + ld * j] *= f;
         B[r + ld * j] *= f;
     }
@@ -478,19 +492,26 @@ int small_eig(int m, std::vector<cplx> &A, std::vector<cplx> &w, std::vector<cpl
     return 0;
 }
 
+template <class T> struct nd {
+    using type = T;
+};
+
 struct Solver {
     Op op{};
     cudaStream_t st = nullptr;
     long long n = 0, ld = 0;
     int mb = 0, nblk = 0;
     double *dV = nullptr, *bufs[7] = {}, *dP = nullptr, *dG = nullptr, *dC = nullptr, *dL = nullptr;
-    long long matvecs = 0;
+    float *dVf = nullptr, *fbufs[4] = {};  /* FP32 copy of the coefficients; FP32 filter buffers */
+    long long matvecs = 0, matvecs32 = 0;
 
     ~Solver()
     {
         if (st) cudaStreamSynchronize(st);
         cudaFree(dV);
+        cudaFree(dVf);
         for (double *b : bufs) cudaFree(b);
+        for (float *b : fbufs) cudaFree(b);
         cudaFree(dP);
         cudaFree(dG);
         cudaFree(dC);
@@ -499,15 +520,24 @@ struct Solver {
     }
     dim3 pgrid(int m) const { return dim3((unsigned)((op.NA1 + 127) / 128), (unsigned)m); }
 
-    int maa(const double *X, double *Y, int m)
+    const double *coef(const double *) const { return dV; }
+    const float *coef(const float *) const { return dVf; }
+    template <class T> int maa(const T *X, T *Y, int m)
     {
-        k_maa<<<pgrid(m), 128, 0, st>>>(op, X, Y, ld);
+        k_maa<T><<<pgrid(m), 128, 0, st>>>(op, coef(X), X, Y, ld);
         return cudaPeekAtLastError() == cudaSuccess ? SMAT_OK : smat_fail(SMAT_ECUDA, "k_maa launch");
     }
-    int mbb(const double *W, const double *Yc, const double *Yp, double *Yn, int m, double alpha, double c, double beta)
+    template <class T>
+    int mbb(const T *W, const T *Yc, const typename nd<T>::type *Yp, T *Yn, int m, double alpha, double c, double beta)
     {
-        k_mbb<<<pgrid(m), 128, 0, st>>>(op, W, Yc, Yp, Yn, ld, alpha, c, beta);
+        k_mbb<T><<<pgrid(m), 128, 0, st>>>(op, coef(W), W, Yc, Yp, Yn, ld, (T)alpha, (T)c, (T)beta);
         return cudaPeekAtLastError() == cudaSuccess ? SMAT_OK : smat_fail(SMAT_ECUDA, "k_mbb launch");
+    }
+    template <class A, class B> int convert(const A *in, B *out, int m)
+    {
+        const long long count = n * m;
+        k_cvt<A, B><<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in, out, count);
+        return cudaPeekAtLastError() == cudaSuccess ? SMAT_OK : smat_fail(SMAT_ECUDA, "k_cvt launch");
     }
     /* G (host, mx x my row-major by i*my + j) = X^T Y */
     int gram(const double *X, const double *Y, int mx, int my, std::vector<double> &G)
@@ -536,12 +566,14 @@ struct Solver {
         return SMAT_OK;
     }
     /* per column: ||A_j - lam_j B_j||^2 (lam empty: ||A_j||^2) */
-    int colres(const double *A, const double *B, const std::vector<double> &lam, int m, std::vector<double> &out)
+    template <class T>
+    int colres(const T *A, const typename nd<T>::type *B, const std::vector<double> &lam, int m,
+               std::vector<double> &out)
     {
         if (!lam.empty() &&
             cudaMemcpyAsync(dL, lam.data(), (size_t)m * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
             return smat_fail(SMAT_ECUDA, "colres upload");
-        k_colres<<<nblk, GT, 0, st>>>(A, B, lam.empty() ? nullptr : dL, n, ld, m, dP);
+        k_colres<T><<<nblk, GT, 0, st>>>(A, B, lam.empty() ? nullptr : dL, n, ld, m, dP);
         k_sum_blocks<<<(m + 255) / 256, 256, 0, st>>>(dP, nblk, m, dG);
         out.resize(m);
         if (cudaMemcpyAsync(out.data(), dG, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -550,15 +582,15 @@ struct Solver {
         return SMAT_OK;
     }
     /* rescale columns of cur (and prev alike) to unit norm */
-    int rescale(double *cur, double *prev, int m)
+    template <class T> int rescale(T *cur, T *prev, int m)
     {
         std::vector<double> nv;
-        int rc = colres(cur, nullptr, {}, m, nv);
+        int rc = colres<T>(cur, nullptr, {}, m, nv);
         if (rc) return rc;
         for (double &v : nv) v = (v > 0 && std::isfinite(v)) ? 1.0 / std::sqrt(v) : 1.0;
         if (cudaMemcpyAsync(dL, nv.data(), (size_t)m * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
             return smat_fail(SMAT_ECUDA, "rescale upload");
-        k_scale2<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(cur, prev, dL, n, ld, m);
+        k_scale2<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(cur, prev, dL, n, ld, m);
         if (cudaStreamSynchronize(st) != cudaSuccess) return smat_fail(SMAT_ECUDA, "k_scale2");
         return SMAT_OK;
     }
@@ -567,6 +599,27 @@ struct Solver {
         if (j0 < m) k_random<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(X, n, ld, j0, m, seed);
     }
 };
+
+/* Chebyshev filter of degree d on [c - e, c + e], Y = T_d((A - c)/e) X0, in
+ * the precision of T; Fa, Fb rotate with X0 (left untouched after the first
+ * step), Wt holds maa Y_k; *out receives the buffer with the result */
+template <class T>
+int chebyshev(Solver &S, const T *X0, T *Fa, T *Fb, T *Wt, int mb, int degree, double c, double e, T **out)
+{
+    int rc;
+    const T *prev = X0;
+    T *cur = Fa;
+    if ((rc = S.maa(prev, Wt, mb)) || (rc = S.mbb(Wt, prev, nullptr, cur, mb, 1.0 / e, c, 0.0))) return rc;
+    for (int k = 1; k < degree; k++) {
+        T *nxt = (prev == X0) ? Fb : const_cast<T *>(prev);
+        if ((rc = S.maa(cur, Wt, mb)) || (rc = S.mbb(Wt, cur, prev, nxt, mb, 2.0 / e, c, 1.0))) return rc;
+        prev = cur;
+        cur = nxt;
+        if (k % 32 == 0 && k + 1 < degree && (rc = S.rescale(cur, const_cast<T *>(prev), mb))) return rc;
+    }
+    *out = cur;
+    return SMAT_OK;
+}
 
 int check_media(int L0, int L1, const int *bc, double omega, const double *med, std::vector<double> &V)
 {
@@ -614,6 +667,13 @@ int setup(Solver &S, int L0, int L1, const int *bc, const std::vector<double> &V
     MCK(cudaMemcpyAsync(S.dV, V.data(), V.size() * sizeof(double), cudaMemcpyHostToDevice, S.st));
     S.op.V = S.dV;
     for (double *&b : S.bufs) MCK(cudaMalloc(&b, (size_t)S.n * mb * sizeof(double)));
+    for (float *&b : S.fbufs) MCK(cudaMalloc(&b, (size_t)S.n * mb * sizeof(float)));
+    MCK(cudaMalloc(&S.dVf, V.size() * sizeof(float)));
+    {
+        std::vector<float> vf(V.begin(), V.end());
+        MCK(cudaMemcpyAsync(S.dVf, vf.data(), vf.size() * sizeof(float), cudaMemcpyHostToDevice, S.st));
+        MCK(cudaStreamSynchronize(S.st));
+    }
     MCK(cudaMalloc(&S.dP, (size_t)S.nblk * mb * mb * sizeof(double)));
     MCK(cudaMalloc(&S.dG, (size_t)mb * mb * sizeof(double)));
     MCK(cudaMalloc(&S.dC, (size_t)mb * mb * sizeof(double)));
@@ -724,6 +784,7 @@ extern "C" int smat_mode_solve(int L0, int L1, const int BoundC[2], double omega
 
     std::vector<double> lam, res, relres, Cm;
     double ltop = -INFINITY;  // largest Ritz value seen (estimate of the top eigenvalue)
+    bool use32 = o.precision == 0;
     int iters = 0, found = 0, r = 0;
     bool done = false;
     for (iters = 1; iters <= max_iter && !done; iters++) {
@@ -738,17 +799,22 @@ extern "C" int smat_mode_solve(int L0, int L1, const int BoundC[2], double omega
          * truncation below drops directions under 1e-13) */
         const double xt = (ltop - c) / e;
         if (std::isfinite(xt) && xt > 1.0) degree = std::min(degree, std::max(4, (int)(13.0 / std::acosh(xt))));
-        double *prev = X, *cur = F[0];
-        if ((rc = S.maa(prev, W, mb)) || (rc = S.mbb(W, prev, nullptr, cur, mb, 1.0 / e, c, 0.0))) return rc;
-        for (int k = 1; k < degree; k++) {
-            double *nxt = (prev == X) ? F[1] : prev;
-            if ((rc = S.maa(cur, W, mb)) || (rc = S.mbb(W, cur, prev, nxt, mb, 2.0 / e, c, 1.0))) return rc;
-            prev = cur;
-            cur = nxt;
-            if (k % 32 == 0 && k + 1 < degree && prev != X && (rc = S.rescale(cur, prev, mb))) return rc;
+        /* FP32 passes while the wanted residuals are above 1e-6 (the filter
+         * only shapes the subspace; GB300's FP32 rate is many times its FP64
+         * rate), FP64 passes to finish; the Rayleigh-Ritz step is FP64 always */
+        double *Y = nullptr;
+        if (use32) {
+            float *yf = nullptr;
+            if ((rc = S.convert(X, S.fbufs[0], mb)) ||
+                (rc = chebyshev<float>(S, S.fbufs[0], S.fbufs[1], S.fbufs[2], S.fbufs[3], mb, degree, c, e, &yf)) ||
+                (rc = S.convert(yf, F[0], mb)))
+                return rc;
+            Y = F[0];
+            S.matvecs32 += (long long)degree * mb;
+        } else {
+            if ((rc = chebyshev<double>(S, X, F[0], F[1], W, mb, degree, c, e, &Y))) return rc;
+            S.matvecs += (long long)degree * mb;
         }
-        S.matvecs += (long long)degree * mb;
-        double *Y = cur;
         /* Rayleigh-Ritz on an orthonormal basis of the filtered block:
          * Q = Y T (T from the Gram matrix's eigen-decomposition, directions
          * below 1e-13 of the largest dropped), B = Q^T A Q, Ritz pairs from
@@ -838,6 +904,12 @@ extern "C" int smat_mode_solve(int L0, int L1, const int BoundC[2], double omega
             relres[j] = is_c[j] ? INFINITY : std::sqrt(res[j]) / (rho * std::sqrt(xn[j]));
         found = 0;
         while (found < r && found < nmodes && lam[found] > 0.0 && relres[found] <= tol) found++;
+        if (use32) {
+            double worst = 0.0;
+            for (int j = 0; j < std::min(nmodes, r); j++)
+                if (lam[j] > 0.0) worst = std::max(worst, relres[j]);
+            if (worst <= 1e-6) use32 = false;
+        }
         /* stop: all wanted found, or the next Ritz pair is a converged
          * non-propagating one (the layer has no more propagating modes) */
         if (found >= nmodes || (found < r && lam[found] <= 0.0 && relres[found] <= tol && iters > 3)) done = true;
@@ -938,7 +1010,8 @@ extern "C" int smat_mode_solve(int L0, int L1, const int BoundC[2], double omega
     if (info) {
         info->n_found = k;
         info->iterations = iters - 1;
-        info->matvecs = S.matvecs;
+        info->matvecs = S.matvecs + S.matvecs32;
+        info->matvecs_fp32 = S.matvecs32;
         info->max_residual = max_res;
         info->spectral_radius = rho;
         info->degenerate_pairs = ndegen;

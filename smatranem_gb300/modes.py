@@ -22,13 +22,13 @@ _P = C.c_void_p
 
 class ModeOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("degree", C.c_int), ("guard", C.c_int), ("max_iter", C.c_int),
-                ("seed", C.c_ulonglong)]
+                ("seed", C.c_ulonglong), ("precision", C.c_int)]
 
 
 class ModeInfo(C.Structure):
     _fields_ = [("n_found", C.c_int), ("iterations", C.c_int), ("degenerate_pairs", C.c_int), ("block", C.c_int),
                 ("matvecs", C.c_longlong), ("max_residual", C.c_double), ("spectral_radius", C.c_double),
-                ("ms", C.c_double)]
+                ("ms", C.c_double), ("matvecs_fp32", C.c_longlong)]
 
 
 def _lib():
@@ -85,18 +85,20 @@ def _med(med, L0, L1):
 
 
 def solve(med, omega: float, L0: int, L1: int, bc=(0, 0), nmodes: int = 4, *, tol: float = 0.0, degree: int = 0,
-          guard: int = 0, max_iter: int = 0, seed: int = 0) -> Modes:
+          guard: int = 0, max_iter: int = 0, seed: int = 0, fp64_only: bool = False) -> Modes:
     """The nmodes propagating modes of one z layer (smat_mode_solve).
 
     med: (6, L0*L1) complex Med values (mu00, mu11, eps22, eps11, eps00,
     mu22; value times metric factor), imaginary parts zero.  omega = k/k0 of
-    the Mode file (2 pi / (lambda k0)); bc = (BoundC[0], BoundC[1])."""
+    the Mode file (2 pi / (lambda k0)); bc = (BoundC[0], BoundC[1]).
+    fp64_only keeps every filter pass in FP64 (default: FP32 passes until the
+    wanted residuals reach 1e-6, FP64 passes after)."""
     m = _med(med, L0, L1)
     bcv = np.ascontiguousarray(bc, np.int32)
     n = 2 * L0 * L1
     theta = np.zeros(2 * nmodes, np.complex128)
     Xi = np.zeros((2 * nmodes, 2 * n), np.complex128)  # column-major (4*L0*L1) x (2*nmodes)
-    opts = ModeOpts(tol, degree, guard, max_iter, seed)
+    opts = ModeOpts(tol, degree, guard, max_iter, seed, 1 if fp64_only else 0)
     info = ModeInfo()
     fdtd._check(_lib().smat_mode_solve(L0, L1, bcv.ctypes.data_as(_P), float(omega), m.ctypes.data_as(_P), nmodes,
                                        C.byref(opts), theta.ctypes.data_as(_P), Xi.ctypes.data_as(_P),

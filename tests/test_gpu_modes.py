@@ -208,3 +208,15 @@ def test_fewer_propagating_modes_than_asked(built, k):
     assert ms.n_found == 2, ms.info
     np.testing.assert_allclose(ms.theta[:2], ref["theta"][:2], rtol=0, atol=1e-10)
     assert np.all(ms.Xi[:, 2:k] == 0) and np.all(ms.Xi[:, k + 2:] == 0)
+
+
+def test_fp32_filter_passes_give_the_fp64_result(built):
+    """The default FP32 filter passes (until the residuals reach 1e-6) end at the
+    same eigenpairs as FP64 passes throughout."""
+    med = W.port_layer(24, 18, core=(8, 5), eps_core=12.11, eps_clad=2.085, seed=11, metric=0.15)
+    a = modes.solve(med, 0.405, 24, 18, (0, 0), 5)
+    b = modes.solve(med, 0.405, 24, 18, (0, 0), 5, fp64_only=True)
+    assert a.info["matvecs_fp32"] > 0 and b.info["matvecs_fp32"] == 0
+    np.testing.assert_allclose(a.theta, b.theta, rtol=0, atol=1e-12)
+    for j in range(5):
+        assert np.abs(_fit_sign(a.Xi[:, j], b.Xi[:, j]) - b.Xi[:, j]).max() < 1e-9
