@@ -42,6 +42,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -116,6 +117,89 @@ __global__ void k_mbb(Op op, const T *__restrict__ Vt, const T *__restrict__ W, 
     };
     const int i0p = i0 + 1 == L0 ? 0 : i0 + 1, i1p = i1 + 1 == L1 ? 0 : i1 + 1;
     const T up = div(i0, i1), up0 = div(i0p, i1), up1 = div(i0, i1p);
+    const T o0 = __ldg(Vt + 3 * (long long)NA1 + p) * __ldg(w0 + p) + (s0 * up + cwt(i0, L0, e0) * up0);
+    const T o1 = __ldg(Vt + 4 * (long long)NA1 + p) * __ldg(w1 + p) + (s1 * up + cwt(i1, L1, e1) * up1);
+    const T *yc = Ycur + col;
+    T r0 = alpha * (o0 - c * yc[p]), r1 = alpha * (o1 - c * yc[p + NA1]);
+    if (beta != (T)0) {
+        const T *yp = Yprev + col;
+        r0 -= beta * yp[p];
+        r1 -= beta * yp[p + NA1];
+    }
+    T *yn = Ynew + col;
+    yn[p] = r0;
+    yn[p + NA1] = r1;
+}
+
+/* The same operators in two passes each, every curl w (resp. divergence u)
+ * evaluated once per point instead of at three points: half the FP64
+ * operations (the stencils are FP64-pipe bound), the same expressions, so
+ * the results are bit-identical to k_maa / k_mbb. */
+template <class T>
+__global__ void k_curl(Op op, const T *__restrict__ Vt, const T *__restrict__ X, T *__restrict__ Wc, long long ld)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= op.NA1) return;
+    const int L0 = op.L0, L1 = op.L1, NA1 = op.NA1;
+    const int j0 = p % L0, j1 = p / L0;
+    const T s0 = (T)op.s0, s1 = (T)op.s1, e0 = (T)op.e0, e1 = (T)op.e1;
+    const T *x0 = X + (long long)blockIdx.y * ld, *x1 = x0 + NA1;
+    auto cwt = [](int i, int La, T e) { return i < La - 1 ? (T)1 : e; };
+    const int q0 = (j0 + 1 == L0 ? 0 : j0 + 1) + L0 * j1, q1 = j0 + L0 * (j1 + 1 == L1 ? 0 : j1 + 1);
+    const T d1 = s1 * __ldg(x0 + p) + cwt(j1, L1, e1) * __ldg(x0 + q1);
+    const T d0 = s0 * __ldg(x1 + p) + cwt(j0, L0, e0) * __ldg(x1 + q0);
+    Wc[(long long)blockIdx.y * ld + p] = __ldg(Vt + 2 * (long long)NA1 + p) * (d1 - d0);
+}
+
+template <class T>
+__global__ void k_maa2(Op op, const T *__restrict__ Vt, const T *__restrict__ X, const T *__restrict__ Wc,
+                       T *__restrict__ Y, long long ld)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= op.NA1) return;
+    const int L0 = op.L0, L1 = op.L1, NA1 = op.NA1;
+    const int i0 = p % L0, i1 = p / L0;
+    const int i0m = i0 == 0 ? L0 - 1 : i0 - 1, i1m = i1 == 0 ? L1 - 1 : i1 - 1;
+    const T s0 = (T)op.s0, s1 = (T)op.s1, e0 = (T)op.e0, e1 = (T)op.e1;
+    auto cwt = [](int i, int La, T e) { return i < La - 1 ? (T)1 : e; };
+    const long long col = (long long)blockIdx.y * ld;
+    const T *x0 = X + col, *x1 = x0 + NA1, *w = Wc + col;
+    const T wp = __ldg(w + p), wm0 = __ldg(w + i0m + L0 * i1), wm1 = __ldg(w + i0 + L0 * i1m);
+    T *y0 = Y + col, *y1 = y0 + NA1;
+    y0[p] = __ldg(Vt + p) * __ldg(x0 + p) + (-s1 * wp - cwt(i1m, L1, e1) * wm1);
+    y1[p] = __ldg(Vt + NA1 + p) * __ldg(x1 + p) - (-s0 * wp - cwt(i0m, L0, e0) * wm0);
+}
+
+template <class T>
+__global__ void k_div(Op op, const T *__restrict__ Vt, const T *__restrict__ W, T *__restrict__ U, long long ld)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= op.NA1) return;
+    const int L0 = op.L0, L1 = op.L1, NA1 = op.NA1;
+    const int j0 = p % L0, j1 = p / L0;
+    const T s0 = (T)op.s0, s1 = (T)op.s1, e0 = (T)op.e0, e1 = (T)op.e1;
+    auto cwt = [](int i, int La, T e) { return i < La - 1 ? (T)1 : e; };
+    const T *w0 = W + (long long)blockIdx.y * ld, *w1 = w0 + NA1;
+    const int j0m = j0 == 0 ? L0 - 1 : j0 - 1, j1m = j1 == 0 ? L1 - 1 : j1 - 1;
+    const T a0 = -s0 * __ldg(w0 + p) - cwt(j0m, L0, e0) * __ldg(w0 + j0m + L0 * j1);
+    const T a1 = -s1 * __ldg(w1 + p) - cwt(j1m, L1, e1) * __ldg(w1 + j0 + L0 * j1m);
+    U[(long long)blockIdx.y * ld + p] = __ldg(Vt + 5 * (long long)NA1 + p) * (a0 + a1);
+}
+
+template <class T>
+__global__ void k_mbb2(Op op, const T *__restrict__ Vt, const T *__restrict__ W, const T *__restrict__ Uc,
+                       const T *Ycur, const T *Yprev, T *Ynew, long long ld, T alpha, T c, T beta)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= op.NA1) return;
+    const int L0 = op.L0, L1 = op.L1, NA1 = op.NA1;
+    const int i0 = p % L0, i1 = p / L0;
+    const T s0 = (T)op.s0, s1 = (T)op.s1, e0 = (T)op.e0, e1 = (T)op.e1;
+    auto cwt = [](int i, int La, T e) { return i < La - 1 ? (T)1 : e; };
+    const long long col = (long long)blockIdx.y * ld;
+    const T *w0 = W + col, *w1 = w0 + NA1, *u = Uc + col;
+    const int i0p = i0 + 1 == L0 ? 0 : i0 + 1, i1p = i1 + 1 == L1 ? 0 : i1 + 1;
+    const T up = __ldg(u + p), up0 = __ldg(u + i0p + L0 * i1), up1 = __ldg(u + i0 + L0 * i1p);
     const T o0 = __ldg(Vt + 3 * (long long)NA1 + p) * __ldg(w0 + p) + (s0 * up + cwt(i0, L0, e0) * up0);
     const T o1 = __ldg(Vt + 4 * (long long)NA1 + p) * __ldg(w1 + p) + (s1 * up + cwt(i1, L1, e1) * up1);
     const T *yc = Ycur + col;
@@ -503,6 +587,8 @@ struct Solver {
     int mb = 0, nblk = 0;
     double *dV = nullptr, *bufs[7] = {}, *dP = nullptr, *dG = nullptr, *dC = nullptr, *dL = nullptr;
     float *dVf = nullptr, *fbufs[4] = {};  /* FP32 copy of the coefficients; FP32 filter buffers */
+    double *aux = nullptr;                 /* w or u of every point and column (two-pass stencils) */
+    float *auxf = nullptr;
     long long matvecs = 0, matvecs32 = 0;
 
     ~Solver()
@@ -512,6 +598,8 @@ struct Solver {
         cudaFree(dVf);
         for (double *b : bufs) cudaFree(b);
         for (float *b : fbufs) cudaFree(b);
+        cudaFree(aux);
+        cudaFree(auxf);
         cudaFree(dP);
         cudaFree(dG);
         cudaFree(dC);
@@ -522,15 +610,30 @@ struct Solver {
 
     const double *coef(const double *) const { return dV; }
     const float *coef(const float *) const { return dVf; }
+    double *scratch(const double *) const { return aux; }
+    float *scratch(const float *) const { return auxf; }
+    bool two_pass = true;
     template <class T> int maa(const T *X, T *Y, int m)
     {
-        k_maa<T><<<pgrid(m), 128, 0, st>>>(op, coef(X), X, Y, ld);
+        if (two_pass) {
+            T *w = scratch(X);
+            k_curl<T><<<pgrid(m), 128, 0, st>>>(op, coef(X), X, w, ld);
+            k_maa2<T><<<pgrid(m), 128, 0, st>>>(op, coef(X), X, w, Y, ld);
+        } else {
+            k_maa<T><<<pgrid(m), 128, 0, st>>>(op, coef(X), X, Y, ld);
+        }
         return cudaPeekAtLastError() == cudaSuccess ? SMAT_OK : smat_fail(SMAT_ECUDA, "k_maa launch");
     }
     template <class T>
     int mbb(const T *W, const T *Yc, const typename nd<T>::type *Yp, T *Yn, int m, double alpha, double c, double beta)
     {
-        k_mbb<T><<<pgrid(m), 128, 0, st>>>(op, coef(W), W, Yc, Yp, Yn, ld, (T)alpha, (T)c, (T)beta);
+        if (two_pass) {
+            T *u = scratch(W);
+            k_div<T><<<pgrid(m), 128, 0, st>>>(op, coef(W), W, u, ld);
+            k_mbb2<T><<<pgrid(m), 128, 0, st>>>(op, coef(W), W, u, Yc, Yp, Yn, ld, (T)alpha, (T)c, (T)beta);
+        } else {
+            k_mbb<T><<<pgrid(m), 128, 0, st>>>(op, coef(W), W, Yc, Yp, Yn, ld, (T)alpha, (T)c, (T)beta);
+        }
         return cudaPeekAtLastError() == cudaSuccess ? SMAT_OK : smat_fail(SMAT_ECUDA, "k_mbb launch");
     }
     template <class A, class B> int convert(const A *in, B *out, int m)
@@ -666,8 +769,14 @@ int setup(Solver &S, int L0, int L1, const int *bc, const std::vector<double> &V
     MCK(cudaMalloc(&S.dV, V.size() * sizeof(double)));
     MCK(cudaMemcpyAsync(S.dV, V.data(), V.size() * sizeof(double), cudaMemcpyHostToDevice, S.st));
     S.op.V = S.dV;
+    {   /* SMATRAN_MODE_ONE_PASS=1: the one-pass stencils (same results, for comparison) */
+        const char *env = getenv("SMATRAN_MODE_ONE_PASS");
+        S.two_pass = !(env && env[0] == '1');
+    }
     for (double *&b : S.bufs) MCK(cudaMalloc(&b, (size_t)S.n * mb * sizeof(double)));
     for (float *&b : S.fbufs) MCK(cudaMalloc(&b, (size_t)S.n * mb * sizeof(float)));
+    MCK(cudaMalloc(&S.aux, (size_t)S.n * mb * sizeof(double)));
+    MCK(cudaMalloc(&S.auxf, (size_t)S.n * mb * sizeof(float)));
     MCK(cudaMalloc(&S.dVf, V.size() * sizeof(float)));
     {
         std::vector<float> vf(V.begin(), V.end());

@@ -220,3 +220,22 @@ def test_fp32_filter_passes_give_the_fp64_result(built):
     np.testing.assert_allclose(a.theta, b.theta, rtol=0, atol=1e-12)
     for j in range(5):
         assert np.abs(_fit_sign(a.Xi[:, j], b.Xi[:, j]) - b.Xi[:, j]).max() < 1e-9
+
+
+def test_one_and_two_pass_stencils_agree_bit_for_bit(built):
+    """The two-pass stencils (curl / divergence once per point, the default)
+    and the one-pass ones (SMATRAN_MODE_ONE_PASS=1) evaluate the same
+    expressions: identical eigenpairs."""
+    import subprocess
+    import sys
+    code = ("import numpy as np, sys; sys.path.insert(0, %r); from smatranem_gb300 import modes, workloads as W; "
+            "med = W.port_layer(20, 16, core=(6, 4), seed=3, metric=0.1); "
+            "ms = modes.solve(med, 0.405, 20, 16, (1, 0), 4); np.save(sys.argv[1], ms.Xi)") % os.path.dirname(HERE)
+    out = {}
+    for flag in ("0", "1"):
+        path = os.path.join(os.environ.get("TMPDIR", "/tmp"), f"xi_pass{flag}_{os.getpid()}.npy")
+        env = dict(os.environ, SMATRAN_MODE_ONE_PASS=flag)
+        subprocess.run([sys.executable, "-c", code, path], check=True, env=env)
+        out[flag] = np.load(path)
+        os.remove(path)
+    assert np.array_equal(out["0"], out["1"])
