@@ -61,9 +61,10 @@ SWEEP32V_TRAFFIC_PER_LAUNCH = 1.95e9 + 0.977e9
 
 
 def launches_per_step(tuning, L2):
-    """Update-kernel launches of one step: one fused launch (kernels 1, 3), or
-    an H and an E sweep per z-chunk (kernels 0, 2; z_chunk 0 = one chunk)."""
-    if tuning[0] in (1, 3, 5):
+    """Update-kernel launches of one step: one fused launch (kernels 1, 3, 5,
+    6), or an H and an E sweep per z-chunk (kernels 0, 2; z_chunk 0 = one
+    chunk)."""
+    if tuning[0] in (1, 3, 5, 6):
         return 1
     zc = tuning[2]
     return 2 * (1 if zc <= 0 or zc >= L2 else math.ceil(L2 / zc))
@@ -416,6 +417,8 @@ def run_ours(args):
                                 3: "k_fused32t (one fused H+E launch per step, TMA-staged planes)",
                                 4: "k_pipe32v (pipelined H/E sweeps in one cooperative launch)",
                                 5: "k_zm32 (one fused H+E launch per step: 128x4 tiles, TMA producer warp)",
+                                6: f"k_row32 (one fused H+E launch per step: z-march of {tuning[1]} whole x rows"
+                                   f" per CTA, float4 quads)",
                                 0: "k_sweep32 (H, E)"}[tuning[0]],
                      "tuning": {"kernel": tuning[0], "tile_y": tuning[1], "z_chunk": tuning[2],
                                 "ctas_per_sm": tuning[3], "slots": tuning[4]},

@@ -152,6 +152,15 @@ struct Fused32T {
     int *err;
 };
 
+/* launch form 6: the fused step over whole x rows (fdtd_row32.cu); reads the
+ * field set in p, writes the other set */
+struct Row32 {
+    P32 p;
+    float *Hn, *En, *Han, *Ean; /* new set */
+    int ty, zc;                 /* rows per tile, planes per z chunk */
+    int nyt, nzc, nitems;       /* row tiles, z chunks, work items (= CTAs) */
+};
+
 /* launchers (one translation unit per precision) */
 void launch_h64(const P64 &p, int rel, cudaStream_t st);
 void launch_e64(const P64 &p, int rel, cudaStream_t st);
@@ -176,6 +185,13 @@ int zm32_max_ctas_per_sm();
 size_t fused32t_smem(int ty, int ns);
 int fused32t_max_ctas_per_sm(int ty, int ns);
 int fused32_max_ctas_per_sm(int ty, int ns);
+/* form 6: threads along x (four cells each, a multiple of 32), shared memory,
+ * resident CTAs of ty rows and z chunks of zc planes at register bound mb
+ * (1, 2 or 3 CTAs per SM) */
+int row32_threads_x(int L0);
+size_t row32_smem(int L0, int ty, int zc);
+int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc);
+void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st);
 void launch_bump(int *base, int by, cudaStream_t st);
 void launch_set(int *base, int value, cudaStream_t st);
 void launch_maxabs(const void *x, long long n, int is_double, double *out, cudaStream_t st);

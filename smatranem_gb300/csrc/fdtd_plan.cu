@@ -128,6 +128,23 @@ Fused32 make_fused(const smat_fdtd_plan *p, bool xp)
     return f;
 }
 
+/* launch form 6: whole-row tiles of ty rows, z chunks of zc planes */
+Row32 make_row(const smat_fdtd_plan *p, bool xp)
+{
+    Row32 r;
+    r.p = make_p32(p, xp);
+    r.Hn = p->cur ? p->d_H32 : p->d_H32b;
+    r.En = p->cur ? p->d_E32 : p->d_E32b;
+    r.Han = p->cur ? p->d_Ha32 : p->d_Ha32b;
+    r.Ean = p->cur ? p->d_Ea32 : p->d_Ea32b;
+    r.ty = p->ty;
+    r.zc = p->zc;
+    r.nyt = (p->L[1] + p->ty - 1) / p->ty;
+    r.nzc = (p->L[2] + p->zc - 1) / p->zc;
+    r.nitems = p->batch * r.nyt * r.nzc;
+    return r;
+}
+
 int sm_count()
 {
     int dev = 0, n = 0;
@@ -282,6 +299,12 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
         for (int i = 0; i < n; i++) {
             const Fused32T ft = make_zm(p, xp);
             launch_zm32(ft, rel0 + i, fused_grid(p, ft.f), p->stream);
+            p->cur ^= 1;
+        }
+        launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
+    } else if (p->fused == 6) {
+        for (int i = 0; i < n; i++) {
+            launch_row32(make_row(p, xp), rel0 + i, p->ctas_per_sm, p->stream);
             p->cur ^= 1;
         }
         launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
@@ -1086,7 +1109,7 @@ extern "C" int smat_fdtd_run(smat_fdtd_plan *p, int k_begin, int k_end)
     if (k_end > p->nsched) return smat_fail(SMAT_EINVAL, "run: k_end %d beyond the %d-step schedule", k_end, p->nsched);
     launch_set(p->d_base, k_begin, p->stream);
     int n = k_end - k_begin;
-    if (p->precision == SMAT_FP32 && (p->fused == 1 || p->fused == 3 || p->fused == 5) && p->cur != 0 &&
+    if (p->precision == SMAT_FP32 && (p->fused == 1 || p->fused == 3 || p->fused == 5 || p->fused == 6) && p->cur != 0 &&
         n >= GRAPH_STEPS + 1) {
         /* graphs are captured from field set 0: take one step to get there */
         enqueue_steps(p, 0, 1, false);
@@ -1140,6 +1163,9 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
             const Fused32T ft = make_zm(p, false);
             launch_zm32(ft, i, fused_grid(p, ft.f), p->stream);
             p->cur ^= 1;
+        } else if (p->fused == 6) {
+            launch_row32(make_row(p, false), i, p->ctas_per_sm, p->stream);
+            p->cur ^= 1;
         } else if (p->fused == 4) {
             launch_pipe32v(q32, i, make_pipe(p), p->pipe_grid, p->stream);
         } else if (p->szc > 0 && p->szc < p->L[2]) {
@@ -1182,9 +1208,10 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
 {
     smat_clear_error();
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
-    if (fused < 0 || fused > 5)
+    if (fused < 0 || fused > 6)
         return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps), 3 (fused, TMA), "
-                                      "4 (pipelined vector sweeps), 5 (fused, 128x4 tiles, TMA producer warp)");
+                                      "4 (pipelined vector sweeps), 5 (fused, 128x4 tiles, TMA producer warp), "
+                                      "6 (fused, whole rows)");
     if (fused == 5) {
         if (p->L[0] % 4 != 0 || p->iBc[0] != 0 || p->iBc[1] != 0 || p->iBc[2] != 0 || z_chunk < 1)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 5 needs L0 %% 4 == 0, iBc = (0,0,0) and z_chunk >= 1");
@@ -1195,6 +1222,24 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         p->ctas_per_sm = 1;
         p->max_ctas = 1;
         p->fused = 5;
+        drop_graph(p);
+        return SMAT_OK;
+    }
+    if (fused == 6) {
+        /* whole-row fused step: tile_y rows per CTA, z chunks, ctas_per_sm = register bound 1..3 */
+        if (p->L[0] % 4 != 0 || p->nhgen > 0 || p->negen > 0 || p->nstable > 0)
+            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 needs L0 %% 4 == 0 and a plan without record cells");
+        if (tile_y < 1 || tile_y > 16 || z_chunk < 1 || ctas_per_sm < 1 || ctas_per_sm > 3)
+            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 takes tile_y in 1..16, z_chunk >= 1 and "
+                                          "ctas_per_sm (register bound) 1..3");
+        if (row32_max_ctas_per_sm(p->L[0], tile_y, ctas_per_sm, z_chunk < p->L[2] ? z_chunk : p->L[2]) < 1)
+            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 with %d rows of %d cells does not fit an SM at %d "
+                                          "CTAs per SM", tile_y, p->L[0], ctas_per_sm);
+        p->ty = tile_y;
+        p->zc = z_chunk < p->L[2] ? z_chunk : p->L[2];
+        p->ctas_per_sm = ctas_per_sm;
+        p->max_ctas = ctas_per_sm;
+        p->fused = 6;
         drop_graph(p);
         return SMAT_OK;
     }
@@ -1293,6 +1338,12 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
         for (int rows : {2, 4, 8})
             for (int lag : {0, 4, 8})
                 if (rows <= p->L[1] && lag <= L2) cands.push_back({4, rows, lag, 0, 0});
+    /* whole-row fused step (plans without record cells) */
+    if (p->L[0] % 4 == 0 && p->nhgen == 0 && p->negen == 0 && p->nstable == 0)
+        for (int ty : {2, 3, 4, 5, 6, 7})
+            for (int mb : {1, 2})
+                for (int zc : {L2, 40, 32, 20})
+                    if (zc <= L2 && !(zc < 48 && zc >= L2)) cands.push_back({6, ty, zc, mb, 0});
     cands.push_back({0, 4, 0, 0, 4});
     cands.push_back({0, 8, 0, 0, 4});
     cands.push_back({0, 4, 4 < L2 ? 4 : 0, 0, 4});
@@ -1364,8 +1415,13 @@ extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
 {
     if (!p || !out) return smat_fail(SMAT_EINVAL, "get_tuning: bad arguments");
     out[0] = p->fused;
-    out[1] = (p->fused == 1 || p->fused == 3) ? p->ty : p->fused == 4 ? p->pipe_by : p->fused == 5 ? 4 : p->by32;
-    out[2] = (p->fused == 1 || p->fused == 3 || p->fused == 5) ? p->zc : p->fused == 4 ? p->pipe_lag : p->szc;
+    out[1] = (p->fused == 1 || p->fused == 3 || p->fused == 6) ? p->ty
+             : p->fused == 4                                    ? p->pipe_by
+             : p->fused == 5                                    ? 4
+                                                                : p->by32;
+    out[2] = (p->fused == 1 || p->fused == 3 || p->fused == 5 || p->fused == 6) ? p->zc
+             : p->fused == 4                                                    ? p->pipe_lag
+                                                                                : p->szc;
     out[3] = (p->fused == 0 || p->fused == 2) ? p->sweep_mb : p->ctas_per_sm;
     out[4] = p->ns;
     return SMAT_OK;

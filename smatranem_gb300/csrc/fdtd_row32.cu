@@ -1,0 +1,533 @@
+/*
+ * FP32 split-field FDTD: one fused launch per Yee step over whole x rows
+ * (launch form 6).
+ *
+ * Same update as the two FP32 sweeps of fdtd_f32.cu (the reference main_calc,
+ * FDTDcalc/FDTDsplitfieldMetal.c:242-329, in total-field form), with the same
+ * floating point expressions, so the results are bit-identical to them.  For
+ * plans without record cells and with L0 % 4 == 0.
+ *
+ *   - a CTA owns TY whole x rows (y0 .. y0+TY-1) of one excitation and marches
+ *     along z through a chunk of planes [z0, z1).  At stage z it computes
+ *     H_new(z) on its rows plus one halo row (y0+TY, recomputed, never stored),
+ *     then E_new(z-1) on its rows, which needs H_new of planes z-1 and z: of
+ *     plane z on its own column from registers, of plane z-1 (its own cells,
+ *     the row above, the quad to the right) from a two-plane ring in shared
+ *     memory.  One barrier a stage.
+ *   - a thread owns one quad (four x-cells, float4) of one row for the whole
+ *     march.  Each field value is read once and written once per step (48 B
+ *     per cell and excitation, plus the coefficient stream and the aux slots
+ *     of split cells): the compulsory traffic of a step, where the two sweeps
+ *     move 72 B.
+ *   - the inputs of the next plane are in flight while the current one is
+ *     computed: at stage z every thread issues cp.async copies of its quad's
+ *     H-update inputs of plane z+1 (coefficients, H, E, H aux) and of the
+ *     E-update inputs of plane z (coefficients, E aux; used at stage z+1) into
+ *     double-buffered shared memory, so the stage barrier never waits on a
+ *     DRAM round trip and no registers are held by loads in flight.  The y-1
+ *     and x-1 neighbours of the H update come from the neighbouring threads'
+ *     staged E (the first row also stages the E row above the tile).
+ *   - whole rows: the x wrap is inside the row.
+ *   - fields are double-buffered (read the current set, write the other), so
+ *     the halo reads of a neighbouring CTA never see an advanced value.
+ *   - the plane z1 closing a chunk: H_new(z1) is recomputed, not stored; at
+ *     z1 = L2 it is iBc_z * H_new(0), which is what the sweeps read through the
+ *     wrapped z boundary (:334, :355); a wrapped halo row likewise holds
+ *     iBc_y * H_new(row 0).
+ */
+#include <cuda_runtime.h>
+
+#include "fdtd_internal.cuh"
+
+namespace smat {
+namespace {
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float el(const float4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+__device__ __forceinline__ void set_el(float4 &v, int i, float x)
+{
+    if (i == 0) v.x = x;
+    else if (i == 1) v.y = x;
+    else if (i == 2) v.z = x;
+    else v.w = x;
+}
+__device__ __forceinline__ float4 scale4(float4 v, float f) { return make_float4(f * v.x, f * v.y, f * v.z, f * v.w); }
+
+/* 16-byte global -> shared copy that bypasses L1 (each staged value is read
+ * from shared memory only) */
+__device__ __forceinline__ void cpa16(float4 *dst, const float *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cpa_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+/* all but this thread's two most recent groups complete */
+__device__ __forceinline__ void cpa_wait2() { asm volatile("cp.async.wait_group 2;\n" ::: "memory"); }
+
+/* the source sheet of step k (the sweeps' expression) */
+__device__ __forceinline__ double row_sheet(const Src &s, int pl, int b, int k, bool efield, int v, int p)
+{
+    if (s.xsrc) return s.xsrc[(efield ? 2 * pl : 0) + v + 2 * p];
+    const double *sc = s.sched + 6 * (long long)k + (efield ? 0 : 3);
+    const double *w = s.inc + (long long)b * 8 * pl + (efield ? 4 * pl : 0) + 2 * (v + 2 * p);
+    return sc[0] * (sc[1] * w[0] + sc[2] * w[1]);
+}
+
+__device__ __forceinline__ int row_monitor(const Dft &d, int j2)
+{
+    int q = -1;
+#pragma unroll
+    for (int i = 0; i < MAX_PLANES; i++)
+        if (i < d.nq && d.planes[i] == j2) q = i;
+    return q;
+}
+
+__device__ __forceinline__ float *row_ring(const Dft &d, int pl, int b, int k, int q, int v)
+{
+    const int slot = k % d.ringK;
+    return d.ring + ((((long long)b * d.ringK + slot) * d.nq + q) * 4 + v) * (long long)pl;
+}
+
+/* The update of one quad -- H (EF = false) or E (EF = true) of cells x0..x0+3
+ * of row j1, plane j2 -- in place in out (total field) and aux (split cells),
+ * from the other field at the cells (gh), its y and z neighbours (gy0, gy2:
+ * components 0 and 2 one row away; gz0, gz1: components 0 and 1 one plane
+ * away, both already scaled by the boundary factor) and the outer x neighbour
+ * of the quad (xn1, xn2: components 1 and 2).  The expressions of the
+ * vectorised sweep (fdtd_f32.cu), element by element. */
+/* The 1-D split-PML factors A(sigma), G(sigma) of one field at a quad's four
+ * x indices, its row and its plane, and the PML bits of the four x indices:
+ * loaded once per thread (the plane's once per stage) instead of per element. */
+struct QuadTab {
+    float ax[4], gx[4];
+    float ay, gy, az, gz;
+    unsigned xm;
+};
+
+template <bool EF>
+__device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b, const int j1, const int j2,
+                                         const int x0, const bool on_src, const QuadTab &tq, const float4 c[3],
+                                         float4 out[3], const float4 gh[3], float4 aux[3], const float4 gy0,
+                                         const float4 gy2, const float4 gz0, const float4 gz1, const float xn1,
+                                         const float xn2, const bool pyz)
+{
+    const Geo &g = p.g;
+    const float sg = EF ? 1.0f : -1.0f;
+    const int px0 = x0 + g.L0 * j1;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float h0 = el(gh[0], i), h1 = el(gh[1], i), h2 = el(gh[2], i);
+        float n1x, n2x;
+        if (!EF) {
+            n1x = i == 0 ? xn1 : el(gh[1], i - 1);
+            n2x = i == 0 ? xn2 : el(gh[2], i - 1);
+        } else {
+            n1x = i == 3 ? xn1 : el(gh[1], i + 1);
+            n2x = i == 3 ? xn2 : el(gh[2], i + 1);
+        }
+        float pl[3], mi[3];
+        if (!EF) { /* backward differences */
+            pl[0] = h2 - el(gy2, i);
+            mi[0] = el(gz1, i) - h1;
+            pl[1] = h0 - el(gz0, i);
+            mi[1] = n2x - h2;
+            pl[2] = h1 - n1x;
+            mi[2] = el(gy0, i) - h0;
+        } else { /* forward differences */
+            pl[0] = el(gy2, i) - h2;
+            mi[0] = h1 - el(gz1, i);
+            pl[1] = el(gz0, i) - h0;
+            mi[1] = h2 - n2x;
+            pl[2] = n1x - h1;
+            mi[2] = h0 - el(gy0, i);
+        }
+        const float bn[3] = {el(c[0], i), el(c[1], i), el(c[2], i)};
+        if (!(((tq.xm >> i) & 1u) | pyz)) {
+            float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+            if (on_src) {
+                W[0] += (float)(p.s.sgn[b] * row_sheet(p.s, g.pl, b, k, !EF, 1, px0 + i));
+                W[1] -= (float)(p.s.sgn[b] * row_sheet(p.s, g.pl, b, k, !EF, 0, px0 + i));
+            }
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) set_el(out[cc], i, fmaf(sg * bn[cc], W[cc], el(out[cc], i)));
+        } else {
+            /* the factors of axis a: x (0), y (1), z (2) */
+            const float tA[3] = {tq.ax[i], tq.ay, tq.az}, tG[3] = {tq.gx[i], tq.gy, tq.gz};
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+                const int i1 = (cc + 1) % 3, i2 = (cc + 2) % 3;
+                const float Ap = tA[i1], Bp = sg * bn[cc] * tG[i1];
+                const float Am = tA[i2], Bm = sg * bn[cc] * tG[i2];
+                const float m = el(aux[cc], i);
+                const float pp = el(out[cc], i) - m;
+                const float np = fmaf(Bp, pl[cc], Ap * pp);
+                const float nm = fmaf(Bm, mi[cc], Am * m);
+                set_el(out[cc], i, np + nm);
+                set_el(aux[cc], i, nm);
+            }
+        }
+    }
+}
+
+
+/* Shared memory (float4 units; T = threads of the CTA, tid = ry * NX + xq):
+ *   es  [2][3][T]        staged E of a plane (read by the neighbouring threads:
+ *                        double-buffered, slot z & 1)
+ *   ph  [3][3][T]        staged bh, H, H aux of the next plane (read by their
+ *                        own thread only: one slot, refilled right after use)
+ *   pe  [2][3][T]        staged be, E aux of the plane whose E update is next
+ *   top [2][2][NX]       E components 0 and 2 of the row above the tile
+ *   hs  [2][TY+1][3][NQ] H_new of the last two planes (the halo row last)
+ * cp.async groups, three a stage, in this order: E of plane z+1 (G1), bh/H/aux
+ * of plane z+1 (G2, after the H update), be/E aux of plane z (G3, after the E
+ * update).  Each wait leaves the two most recent groups in flight. */
+size_t row_smem_f4(int L0, int ty, int zc)
+{
+    const size_t nq = L0 / 4, nx = ((nq + 31) / 32) * 32, t = nx * (ty + 1);
+    return 21 * t + 4 * nx + 6 * (ty + 1) * nq + 2 * (size_t)(zc + 1);
+}
+
+/* per plane of a chunk: the 1-D split-PML factors of its z index (H: A, G;
+ * E: A, G), whether it lies in a PML and its monitor index (or -1) */
+struct PlaneInfo {
+    float ah, gh, ae, ge;
+    int pm, q, pad0, pad1;
+};
+
+template <int MAXT, int MB>
+__global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel)
+{
+    extern __shared__ float4 sm4[];
+    const P32 &p = r.p;
+    const Geo &g = p.g;
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2, NQ = L0 >> 2, TY = r.ty, NR = TY + 1;
+    const int NX = blockDim.x, T = NX * NR;
+    const long long n3 = g.n3, bs = 3 * n3, pl = g.pl;
+    const int s1 = L0, s2 = L0 + L1;
+    const int xq = threadIdx.x, ry = threadIdx.y, tid = ry * NX + xq;
+    float4 *const es = sm4, *const ph = sm4 + 6 * T, *const pe = sm4 + 15 * T, *const top = sm4 + 21 * T,
+                  *const hs = top + 4 * NX;
+    PlaneInfo *const pinfo = reinterpret_cast<PlaneInfo *>(hs + 6 * NR * NQ); /* planes z0 .. z1 */
+#define ES(s, c) es[((s) * 3 + (c)) * T]
+#define PH(f, c) ph[((f) * 3 + (c)) * T]
+#define PE(f, c) pe[((f) * 3 + (c)) * T]
+#define TOP(s, c) top[((s) * 2 + (c)) * NX]
+#define HS(z, row, c) hs[((((z) & 1) * NR + (row)) * 3 + (c)) * NQ]
+
+    /* the item: excitation fastest (the coefficient stream is shared), then
+     * the row tile, then the z chunk */
+    int t = blockIdx.x;
+    const int b = t % p.batch;
+    t /= p.batch;
+    const int yt = t % r.nyt;
+    const int zci = t / r.nyt;
+    const int Y0 = yt * TY, h = min(TY, L1 - Y0);
+    const int z0 = zci * r.zc, z1 = min(z0 + r.zc, L2);
+
+    /* this thread's row: own rows 0..h-1, rows h..TY-1 idle (a partial last
+     * tile), row TY the halo row y0+h; lanes past the row idle too */
+    const bool halo = ry == TY;
+    const bool xlive = xq < NQ;
+    const bool own = !halo && ry < h && xlive;
+    const bool act = own || (halo && xlive); /* stages and computes H_new */
+    int gy = halo ? Y0 + h : min(Y0 + ry, L1 - 1);
+    float fyw = 1.0f; /* the halo row wrapped to row 0 holds iBc_y * H_new */
+    if (gy == L1) {
+        gy = 0;
+        fyw = (float)g.bc[1];
+    }
+    const int xs = xlive ? xq : NQ - 1;
+    const int x0 = 4 * xs;
+    const int rown = ry + 1 == h ? TY : ry + 1; /* H_new row of the y+1 neighbour */
+    const int yb = halo ? h - 1 : ry - 1;       /* staged E row of the y-1 neighbour (ry = 0: top) */
+    const int k = *p.s.base + rel;
+    const long long lr = x0 + (long long)L0 * gy + b * bs;
+    const int px0 = x0 + L0 * gy;
+    const float fy = gy == 0 ? (float)g.bc[1] : 1.0f; /* y-1 neighbour wrapped with iBc_y */
+    const int gtop = Y0 == 0 ? L1 - 1 : Y0 - 1;         /* the row above the tile */
+    const float fxm = x0 == 0 ? (float)g.bc[0] : 1.0f;  /* x-1 neighbour wrapped with iBc_x */
+    const int xl = x0 == 0 ? NQ - 1 : xs - 1;
+    const bool xe1 = x0 + 4 == L0;
+    const float fxp = xe1 ? (float)g.bc[0] : 1.0f; /* x+1 neighbour of the E update */
+    const int xqn = xe1 ? 0 : xs + 1;
+    const bool pmy = p.pmask[s1 + gy];
+    const int S = L0 + L1 + L2;
+    QuadTab th, te; /* split-PML factors of the H and the E update */
+    th.xm = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        th.xm |= (unsigned)(p.pmask[x0 + i] != 0) << i;
+        th.ax[i] = p.tab[x0 + i];
+        th.gx[i] = p.tab[S + x0 + i];
+        te.ax[i] = p.tab[2 * S + x0 + i];
+        te.gx[i] = p.tab[3 * S + x0 + i];
+    }
+    te.xm = th.xm;
+    const bool pmx = th.xm != 0;
+    th.ay = p.tab[s1 + gy];
+    th.gy = p.tab[S + s1 + gy];
+    te.ay = p.tab[2 * S + s1 + gy];
+    te.gy = p.tab[3 * S + s1 + gy];
+    const int iIb = p.s.iI[b]; /* the excitation's source plane */
+    const int lane = xq & 31;
+    /* the lanes of this warp that compute (a row is whole warps; the last
+     * warp of a row may have idle lanes past L0, which sit at its end) */
+    const unsigned amask = __ballot_sync(0xffffffffu, act);
+
+    /* G1: E of stage z (plane z, or 0 for z = L2) and the row above */
+    auto stage_e_old = [&](int z) {
+        const int zr = z == L2 ? 0 : z, s = z & 1;
+        const long long l = lr + pl * zr;
+#pragma unroll
+        for (int i = 0; i < 3; i++) cpa16(&ES(s, i) + tid, p.E + i * n3 + l);
+        if (ry == 0) {
+            const long long lt = x0 + (long long)L0 * gtop + b * bs + pl * zr;
+            cpa16(&TOP(s, 0) + xq, p.E + lt);
+            cpa16(&TOP(s, 1) + xq, p.E + 2 * n3 + lt);
+        }
+    };
+    /* G2: bh, H, H aux of stage z */
+    auto stage_h = [&](int z) {
+        const int zr = z == L2 ? 0 : z;
+        const long long l = lr + pl * zr, lc = l - b * bs;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            cpa16(&PH(0, i) + tid, p.bh + i * n3 + lc);
+            cpa16(&PH(1, i) + tid, p.H + i * n3 + l);
+        }
+        if (pmy | pinfo[z - z0].pm | pmx) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) cpa16(&PH(2, i) + tid, p.Ha + i * n3 + l);
+        }
+    };
+    /* G3: be, E aux of plane z (its E update runs at stage z + 1) */
+    auto stage_e = [&](int z) {
+        const long long l = lr + pl * z, lc = l - b * bs;
+#pragma unroll
+        for (int i = 0; i < 3; i++) cpa16(&PE(0, i) + tid, p.be + i * n3 + lc);
+        if (pmy | pinfo[z - z0].pm | pmx) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) cpa16(&PE(1, i) + tid, p.Ea + i * n3 + l);
+        }
+    };
+
+    /* the plane table of the chunk (z1 = L2 is plane 0) */
+    for (int j = tid; j <= z1 - z0; j += T) {
+        const int zz = z0 + j == L2 ? 0 : z0 + j;
+        PlaneInfo pi;
+        pi.ah = p.tab[s2 + zz];
+        pi.gh = p.tab[S + s2 + zz];
+        pi.ae = p.tab[2 * S + s2 + zz];
+        pi.ge = p.tab[3 * S + s2 + zz];
+        pi.pm = p.pmask[s2 + zz] != 0;
+        pi.q = row_monitor(p.d, zz);
+        pi.pad0 = pi.pad1 = 0;
+        pinfo[j] = pi;
+    }
+    __syncthreads();
+
+    /* E_old(z0-1), components 0 and 1 (the z-1 neighbour of H_new(z0)), and
+     * the inputs of the first stage */
+    float4 Ep[3];
+    Ep[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (act) {
+        int zp = z0 - 1;
+        float fz = 1.0f;
+        if (zp < 0) {
+            zp = L2 - 1;
+            fz = (float)g.bc[2];
+        }
+        const long long l = lr + pl * zp;
+        Ep[0] = scale4(ld4(p.E + l), fz);
+        Ep[1] = scale4(ld4(p.E + n3 + l), fz);
+        stage_e_old(z0);
+        stage_h(z0);
+    }
+    cpa_commit();
+    cpa_wait_all();
+    __syncthreads();
+
+    for (int z = z0; z <= z1; z++) {
+        const bool wz = z == L2; /* the closing plane wraps to 0 */
+        const int zr = wz ? 0 : z, s = z & 1;
+        const float fzw = wz ? (float)g.bc[2] : 1.0f;
+        /* G1: the next plane's E leaves now (its slot was last read before
+         * the previous barrier) */
+        if (act && z < z1) stage_e_old(z + 1);
+        cpa_commit();
+        float4 o[3], e[3];
+        if (act) {
+            /* this thread's bh, H, aux of plane z (the previous stage's G2) */
+            cpa_wait2();
+            const PlaneInfo zi = pinfo[z - z0];
+            const bool pyz = pmy | zi.pm;
+            const bool qs = pyz | pmx;
+            float4 c[3], a[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                c[i] = (&PH(0, i))[tid];
+                o[i] = (&PH(1, i))[tid];
+                e[i] = (&ES(s, i))[tid];
+            }
+            if (qs) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) a[i] = (&PH(2, i))[tid];
+            }
+            float4 gy0, gy2;
+            if (ry == 0) {
+                gy0 = scale4((&TOP(s, 0))[xq], fy);
+                gy2 = scale4((&TOP(s, 1))[xq], fy);
+            } else {
+                gy0 = scale4((&ES(s, 0))[yb * NX + xs], fy);
+                gy2 = scale4((&ES(s, 2))[yb * NX + xs], fy);
+            }
+            /* x-1 neighbour: the lane to the left, or staged E at a warp's first lane */
+            float xn1 = __shfl_up_sync(amask, e[1].w, 1), xn2 = __shfl_up_sync(amask, e[2].w, 1);
+            if (lane == 0 || x0 == 0) {
+                xn1 = fxm * (&ES(s, 1))[ry * NX + xl].w;
+                xn2 = fxm * (&ES(s, 2))[ry * NX + xl].w;
+            }
+            const float4 gz0 = scale4(Ep[0], fzw), gz1 = scale4(Ep[1], fzw);
+            th.az = zi.ah;
+            th.gz = zi.gh;
+            row_quad<false>(p, k, b, gy, zr, x0, zr == iIb, th, c, o, e, a, gy0, gy2, gz0, gz1, xn1, xn2, pyz);
+            /* the private slot is free: plane z+1's bh, H, aux leave */
+            if (z < z1) stage_h(z + 1);
+            const long long l = lr + pl * zr;
+            if (own && z < z1) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) st4(r.Hn + i * n3 + l, o[i]);
+                if (qs) {
+#pragma unroll
+                    for (int i = 0; i < 3; i++) st4(r.Han + i * n3 + l, a[i]);
+                }
+                const int q = zi.q;
+                if (q >= 0) {
+                    st4(row_ring(p.d, g.pl, b, k, q, 0) + px0, o[0]);
+                    st4(row_ring(p.d, g.pl, b, k, q, 1) + px0, o[1]);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++) (&HS(z, ry, i))[xs] = scale4(o[i], fyw);
+        }
+        cpa_commit(); /* G2 */
+        if (own && z > z0) {
+            /* this thread's be, E aux of plane z-1 (the previous stage's G3) */
+            cpa_wait2();
+            const int ze = z - 1;
+            const long long le = lr + pl * ze;
+            const PlaneInfo zi = pinfo[ze - z0];
+            const bool pyze = pmy | zi.pm;
+            const bool qse = pyze | pmx;
+            float4 ce[3], ae[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) ce[i] = (&PE(0, i))[tid];
+            if (qse) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) ae[i] = (&PE(1, i))[tid];
+            }
+            /* H_new of plane z-1 (own quad, row above, quad to the right) from
+             * shared memory, of plane z from registers */
+            const float4 hp[3] = {(&HS(ze, ry, 0))[xs], (&HS(ze, ry, 1))[xs], (&HS(ze, ry, 2))[xs]};
+            const float4 ey0 = (&HS(ze, rown, 0))[xs], ey2 = (&HS(ze, rown, 2))[xs];
+            const float4 ez0 = scale4(o[0], fzw), ez1 = scale4(o[1], fzw);
+            /* x+1 neighbour: the lane to the right, or H_new(z-1) in shared
+             * memory at a warp's last lane and at the row end */
+            float xp1 = __shfl_down_sync(amask, hp[1].x, 1), xp2 = __shfl_down_sync(amask, hp[2].x, 1);
+            if (lane == 31 || xe1) {
+                xp1 = fxp * (&HS(ze, ry, 1))[xqn].x;
+                xp2 = fxp * (&HS(ze, ry, 2))[xqn].x;
+            }
+            te.az = zi.ae;
+            te.gz = zi.ge;
+            row_quad<true>(p, k, b, gy, ze, x0, ze == iIb, te, ce, Ep, hp, ae, ey0, ey2, ez0, ez1, xp1, xp2, pyze);
+#pragma unroll
+            for (int i = 0; i < 3; i++) st4(r.En + i * n3 + le, Ep[i]);
+            if (qse) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) st4(r.Ean + i * n3 + le, ae[i]);
+            }
+            const int q = zi.q;
+            if (q >= 0) {
+                st4(row_ring(p.d, g.pl, b, k, q, 2) + px0, Ep[0]);
+                st4(row_ring(p.d, g.pl, b, k, q, 3) + px0, Ep[1]);
+            }
+        }
+        /* the private slot is free: plane z's be, E aux leave (G3) */
+        if (own && z < z1) stage_e(z);
+        cpa_commit();
+        if (act) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) Ep[i] = e[i];
+        }
+        /* the next plane's E (G1) complete, then visible to the neighbours */
+        cpa_wait2();
+        __syncthreads();
+    }
+#undef ES
+#undef PH
+#undef PE
+#undef TOP
+#undef HS
+}
+
+template <int MAXT, int MB> const void *row_fn() { return (const void *)k_row32<MAXT, MB>; }
+
+/* the instantiation for a block of `threads` at register bound mb (at least
+ * mb resident CTAs of MAXT threads: 65536 / (MAXT * mb) registers), or null */
+const void *row_kernel(int threads, int mb)
+{
+    switch (mb) {
+    case 1:
+        if (threads <= 384) return row_fn<384, 1>();
+        if (threads <= 448) return row_fn<448, 1>();
+        if (threads <= 512) return row_fn<512, 1>();
+        if (threads <= 640) return row_fn<640, 1>();
+        if (threads <= 1024) return row_fn<1024, 1>();
+        return nullptr;
+    case 2:
+        if (threads <= 192) return row_fn<192, 2>();
+        if (threads <= 384) return row_fn<384, 2>();
+        return nullptr;
+    case 3: return threads <= 256 ? row_fn<256, 3>() : nullptr;
+    default: return nullptr;
+    }
+}
+
+} // namespace
+
+int row32_threads_x(int L0) { return ((L0 / 4 + 31) / 32) * 32; }
+
+size_t row32_smem(int L0, int ty, int zc) { return sizeof(float4) * row_smem_f4(L0, ty, zc); }
+
+int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc)
+{
+    const int threads = row32_threads_x(L0) * (ty + 1);
+    const void *fn = row_kernel(threads, mb);
+    if (!fn) return 0;
+    const size_t sm = row32_smem(L0, ty, zc);
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, sm) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st)
+{
+    const int nx = row32_threads_x(r.p.g.L0);
+    const dim3 blk(nx, r.ty + 1);
+    const void *fn = row_kernel(nx * (r.ty + 1), mb);
+    const size_t sm = row32_smem(r.p.g.L0, r.ty, r.zc);
+    void *args[] = {(void *)&r, (void *)&rel};
+    cudaLaunchKernel(fn, dim3(r.nitems), blk, args, sm, st);
+}
+
+} // namespace smat

@@ -373,6 +373,65 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
                 assert np.array_equal(a, b_), tuning
 
 
+ROW_CASES = [
+    # record-free structures (launch form 6): (L, seed, structure kwargs, iBTIin)
+    ((40, 17, 19, 3), 31, dict(pml=(4, 4, 4), iBc=(1, 1, -1)), (5, 13, 7, -1)),
+    ((36, 9, 12, 2), 32, dict(pml=(0, 0, 2), pml_z_only=True, iBc=(0, -1, 0)), (3, 8, 5, 1)),
+    ((64, 24, 20, 3), 33, dict(pml=(5, 5, 4), iBc=(0, 0, 0)), (5, 14, 7, 1)),
+    # rows of two warps with idle lanes (34 quads), odd row count
+    ((136, 13, 17, 2), 34, dict(pml=(4, 3, 3), iBc=(-1, 1, 1)), (4, 12, 6, 1)),
+    ((8, 5, 3, 1), 35, dict(pml=(0, 0, 0), iBc=(1, -1, 1)), (0, 2, 1, 1)),
+]
+
+
+def _row_fits(L0, ty, mb, zc):
+    """Kernel 6 launch shape: a warp per 128 cells of a row, tile_y + 1 rows,
+    staging rings in shared memory (at most 227 KB per CTA)."""
+    nq = L0 // 4
+    nx = ((nq + 31) // 32) * 32
+    threads = nx * (ty + 1)
+    smem = 16 * (21 * threads + 4 * nx + 6 * (ty + 1) * nq + 2 * (zc + 1))
+    return threads <= {1: 1024, 2: 384, 3: 256}[mb] and smem <= 232448
+
+
+@pytest.mark.parametrize("case", range(len(ROW_CASES)))
+def test_row_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
+    """The whole-row fused step (kernel 6) reproduces the scalar FP32 sweeps
+    bit for bit: partial last row tiles, z chunks of 1 plane to the whole
+    grid, every register bound, iBc = -1/0/1 wraps on each axis (the halo row
+    and closing plane hold iBc * H_new), split PML on all faces, per-excitation
+    source planes and DFT planes, across field-set swaps."""
+    from smatranem_gb300 import workloads as W
+    L, seed, kw, iBTIin = ROW_CASES[case]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    nsteps = 37
+    ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
+    tunings = [(6, ty, zc, mb, 0) for ty, zc, mb in
+               [(1, L[2], 1), (2, 5, 2), (4, 3, 1), (3, 1, 3), (4, 7, 2), (8, 40, 1), (2, 2, 3), (5, L[2], 1),
+                (1, 4, 3), (1, 2, 2)]
+               if _row_fits(L[0], ty, mb, min(zc, L[2]))]
+    assert len(tunings) >= 5
+    for tuning in tunings:
+        got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
+        for rb, gb in zip(ref, got):
+            for a, b_ in zip(rb, gb):
+                assert np.array_equal(a, b_), tuning
+
+
+def test_row_fused_refuses_record_cells(built):
+    """Kernel 6 has no record-cell path: a plan with lossy or PEC cells is refused."""
+    from smatranem_gb300 import workloads as W
+    f = _fdtd()
+    L, seed, kw, iBTIin = FUSED_CASES[4]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=f.FP32,
+                       pec=s.pec) as p:
+        with pytest.raises(f.FdtdError):
+            p.set_tuning(6, 2, 4, 1, 0)
+
+
 def test_fused_fp32_within_tolerance_of_fp64_long_run(built):
     """A 300-step run with PML on all faces: FP32 (fused) vs the FP64 plan."""
     f = _fdtd()
@@ -502,6 +561,9 @@ def test_degenerate_grids(built, port, case):
         tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (3, 2, 2, 0, 4), (4, 1, 0, 0, 0)]
         if tuple(iBc) == (0, 0, 0):
             tunings += [(5, 4, 2, 1, 4)]
+
+    if L[0] % 4 == 0:
+        tunings += [(6, 1, 1, 1, 0), (6, 2, 2, 2, 0), (6, 1, L[2], 3, 0)]
     for tuning in tunings:
         got = _run_fp32(s, pr, fp32_planes, tuning, 20, batch=1)
         for rb, gb in zip(ref, got):
