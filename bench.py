@@ -54,10 +54,17 @@ WORKLOAD = ("bend 256x192x160 curvilinear (R=2um, Si strip in SiO2), 12-cell spl
             "FP64 DFT at 21 wavelengths on 2 port planes")
 
 
-# DRAM traffic of one k_sweep32v launch on the bench workload, from one ncu
-# capture of the full-size workload (dram__bytes_read.sum + dram__bytes_write.sum,
-# a one-pass metric set; the summary is kept with the other ncu summaries)
-SWEEP32V_TRAFFIC_PER_LAUNCH = 1.95e9 + 0.977e9
+# DRAM traffic per update launch on the bench workload (dram__bytes_read.sum +
+# dram__bytes_write.sum from one ncu capture of the full-size workload, a
+# one-pass metric set; the summaries are kept with the other ncu summaries),
+# keyed by (kernel, tile_y, z_chunk) of the launch configuration
+TRAFFIC_PER_LAUNCH = {
+    (2, 1, 0): 1.95e9 + 0.977e9,              # k_sweep32v, H or E sweep
+    (6, 5, 32): 2.594e9 + 2.008e9,            # k_row32, one fused step
+    (6, 5, 24): 2.619e9 + 2.007e9,
+    (6, 5, 20): 2.617e9 + 2.007e9,
+    (6, 4, 32): 2.582e9 + 2.008e9,
+}
 
 
 def launches_per_step(tuning, L2):
@@ -409,7 +416,7 @@ def run_ours(args):
                                                           f"{t_e2e:.2f} s"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
-                     "traffic": SWEEP32V_TRAFFIC_PER_LAUNCH if tuning[0] == 2 and batch == BATCH else None,
+                     "traffic": TRAFFIC_PER_LAUNCH.get(tuple(tuning[:3])) if batch == BATCH else None,
                      "traffic_per": "launch (ncu, dram read + write)",
                      "kernel": {1: "k_fused32 (one fused H+E launch per step)",
                                 2: "k_sweep32v (H, E; float4)" + (f", z-chunks of {tuning[2]} planes"

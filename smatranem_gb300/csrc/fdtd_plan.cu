@@ -1340,9 +1340,9 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
                 if (rows <= p->L[1] && lag <= L2) cands.push_back({4, rows, lag, 0, 0});
     /* whole-row fused step (plans without record cells) */
     if (p->L[0] % 4 == 0 && p->nhgen == 0 && p->negen == 0 && p->nstable == 0)
-        for (int ty : {2, 3, 4, 5, 6, 7})
+        for (int ty : {2, 4, 5})
             for (int mb : {1, 2})
-                for (int zc : {L2, 40, 32, 20})
+                for (int zc : {L2, 40, 32, 24, 20})
                     if (zc <= L2 && !(zc < 48 && zc >= L2)) cands.push_back({6, ty, zc, mb, 0});
     cands.push_back({0, 4, 0, 0, 4});
     cands.push_back({0, 8, 0, 0, 4});
