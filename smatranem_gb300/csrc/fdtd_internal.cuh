@@ -159,6 +159,8 @@ struct Row32 {
     float *Hn, *En, *Han, *Ean; /* new set */
     int ty, zc;                 /* rows per tile, planes per z chunk */
     int nyt, nzc, nitems;       /* row tiles, z chunks, work items (= CTAs) */
+    const int *qorder;          /* [L0/4]: quads whose x index lies in a PML, then the others */
+    int nqp;                    /* how many of the first kind */
 };
 
 /* launchers (one translation unit per precision) */
@@ -185,10 +187,10 @@ int zm32_max_ctas_per_sm();
 size_t fused32t_smem(int ty, int ns);
 int fused32t_max_ctas_per_sm(int ty, int ns);
 int fused32_max_ctas_per_sm(int ty, int ns);
-/* form 6: threads along x (four cells each, a multiple of 32), shared memory,
- * resident CTAs of ty rows and z chunks of zc planes at register bound mb
- * (1, 2 or 3 CTAs per SM) */
-int row32_threads_x(int L0);
+/* form 6: threads of a CTA (one per quad of its ty + 1 rows, rounded up to
+ * whole warps), shared memory, resident CTAs of ty rows and z chunks of zc
+ * planes at register bound mb (1, 2 or 3 CTAs per SM) */
+int row32_threads(int L0, int ty);
 size_t row32_smem(int L0, int ty, int zc);
 int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc);
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st);

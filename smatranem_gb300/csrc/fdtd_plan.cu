@@ -142,6 +142,8 @@ Row32 make_row(const smat_fdtd_plan *p, bool xp)
     r.nyt = (p->L[1] + p->ty - 1) / p->ty;
     r.nzc = (p->L[2] + p->zc - 1) / p->zc;
     r.nitems = p->batch * r.nyt * r.nzc;
+    r.qorder = p->d_qorder;
+    r.nqp = p->nqp;
     return r;
 }
 
@@ -759,6 +761,17 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
     if (p->L[0] % 4 == 0) {
         p->fused = 2; /* default: vectorised sweeps where they apply */
         p->by32 = 2;
+        /* kernel 6 thread order: quads with a split-PML x index first */
+        const int nq = p->L[0] / 4;
+        std::vector<int> qorder;
+        for (int pass = 0; pass < 2; pass++)
+            for (int q = 0; q < nq; q++) {
+                const bool px = pmask[4 * q] | pmask[4 * q + 1] | pmask[4 * q + 2] | pmask[4 * q + 3];
+                if (px == (pass == 0)) qorder.push_back(q);
+                if (pass == 0 && px) p->nqp++;
+            }
+        if ((rc = p->alloc(&p->d_qorder, (size_t)nq))) return rc;
+        CK(cudaMemcpyAsync(p->d_qorder, qorder.data(), nq * sizeof(int), cudaMemcpyHostToDevice, p->stream));
     }
     if ((rc = p->alloc(&p->d_stable, stable.size() + 1))) return rc;
     if (!stable.empty())

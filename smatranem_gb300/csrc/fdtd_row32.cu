@@ -172,21 +172,34 @@ __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b,
 }
 
 
-/* Shared memory (float4 units; T = threads of the CTA, tid = ry * NX + xq):
- *   es  [2][3][T]        staged E of a plane (read by the neighbouring threads:
+/* Shared memory (float4 units):
+ *   es  [2][3][NC]       staged E of a plane (read by the neighbouring threads:
  *                        double-buffered, slot z & 1)
- *   ph  [3][3][T]        staged bh, H, H aux of the next plane (read by their
+ *   ph  [3][3][NC]       staged bh, H, H aux of the next plane (read by their
  *                        own thread only: one slot, refilled right after use)
- *   pe  [2][3][T]        staged be, E aux of the plane whose E update is next
- *   top [2][2][NX]       E components 0 and 2 of the row above the tile
+ *   pe  [2][3][NC]       staged be, E aux of the plane whose E update is next
+ *   top [2][2][NQ]       E components 0 and 2 of the row above the tile
  *   hs  [2][TY+1][3][NQ] H_new of the last two planes (the halo row last)
+ *   the plane table of the chunk
+ * with NC = (TY+1) * NQ quads, quad q of tile row r at r * NQ + q.
  * cp.async groups, three a stage, in this order: E of plane z+1 (G1), bh/H/aux
  * of plane z+1 (G2, after the H update), be/E aux of plane z (G3, after the E
  * update).  Each wait leaves the two most recent groups in flight. */
 size_t row_smem_f4(int L0, int ty, int zc)
 {
-    const size_t nq = L0 / 4, nx = ((nq + 31) / 32) * 32, t = nx * (ty + 1);
-    return 21 * t + 4 * nx + 6 * (ty + 1) * nq + 2 * (size_t)(zc + 1);
+    const size_t nq = L0 / 4, nc = nq * (ty + 1);
+    return 21 * nc + 4 * nq + 6 * nc + 2 * (size_t)(zc + 1);
+}
+
+__device__ __forceinline__ float4 lds4(const float4 *a)
+{
+    float4 v;
+    const unsigned s = (unsigned)__cvta_generic_to_shared(a);
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];\n"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(s)
+                 : "memory");
+    return v;
 }
 
 /* per plane of a chunk: the 1-D split-PML factors of its z index (H: A, G;
@@ -203,17 +216,17 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
     const P32 &p = r.p;
     const Geo &g = p.g;
     const int L0 = g.L0, L1 = g.L1, L2 = g.L2, NQ = L0 >> 2, TY = r.ty, NR = TY + 1;
-    const int NX = blockDim.x, T = NX * NR;
+    const int NC = NR * NQ, T = blockDim.x;
     const long long n3 = g.n3, bs = 3 * n3, pl = g.pl;
     const int s1 = L0, s2 = L0 + L1;
-    const int xq = threadIdx.x, ry = threadIdx.y, tid = ry * NX + xq;
-    float4 *const es = sm4, *const ph = sm4 + 6 * T, *const pe = sm4 + 15 * T, *const top = sm4 + 21 * T,
-                  *const hs = top + 4 * NX;
-    PlaneInfo *const pinfo = reinterpret_cast<PlaneInfo *>(hs + 6 * NR * NQ); /* planes z0 .. z1 */
-#define ES(s, c) es[((s) * 3 + (c)) * T]
-#define PH(f, c) ph[((f) * 3 + (c)) * T]
-#define PE(f, c) pe[((f) * 3 + (c)) * T]
-#define TOP(s, c) top[((s) * 2 + (c)) * NX]
+    const int tid = threadIdx.x;
+    float4 *const es = sm4, *const ph = sm4 + 6 * NC, *const pe = sm4 + 15 * NC, *const top = sm4 + 21 * NC,
+                  *const hs = top + 4 * NQ;
+    PlaneInfo *const pinfo = reinterpret_cast<PlaneInfo *>(hs + 6 * NC); /* planes z0 .. z1 */
+#define ES(s, c) es[((s) * 3 + (c)) * NC]
+#define PH(f, c) ph[((f) * 3 + (c)) * NC]
+#define PE(f, c) pe[((f) * 3 + (c)) * NC]
+#define TOP(s, c) top[((s) * 2 + (c)) * NQ]
 #define HS(z, row, c) hs[((((z) & 1) * NR + (row)) * 3 + (c)) * NQ]
 
     /* the item: excitation fastest (the coefficient stream is shared), then
@@ -226,10 +239,25 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
     const int Y0 = yt * TY, h = min(TY, L1 - Y0);
     const int z0 = zci * r.zc, z1 = min(z0 + r.zc, L2);
 
-    /* this thread's row: own rows 0..h-1, rows h..TY-1 idle (a partial last
-     * tile), row TY the halo row y0+h; lanes past the row idle too */
+    /* this thread's quad: the quads of the tile's rows whose x index lies in
+     * a PML (split cells) take the first threads, row by row, the others the
+     * rest, so that whole warps run the ordinary update with no split-cell
+     * branch (in x order within each group: r.qorder) */
+    const int nqp = r.nqp, nqi = NQ - nqp;
+    int ry = TY, xq = NQ - 1;
+    const bool xlive = tid < NC; /* threads past the tile's quads idle */
+    if (tid < NR * nqp) {
+        ry = tid / nqp;
+        xq = r.qorder[tid % nqp];
+    } else if (xlive) {
+        const int u = tid - NR * nqp;
+        ry = u / nqi;
+        xq = r.qorder[nqp + u % nqi];
+    }
+    const int sid = ry * NQ + xq; /* its staging slot */
+    /* its row: own rows 0..h-1, rows h..TY-1 idle (a partial last tile), row
+     * TY the halo row y0+h */
     const bool halo = ry == TY;
-    const bool xlive = xq < NQ;
     const bool own = !halo && ry < h && xlive;
     const bool act = own || (halo && xlive); /* stages and computes H_new */
     int gy = halo ? Y0 + h : min(Y0 + ry, L1 - 1);
@@ -238,7 +266,7 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
         gy = 0;
         fyw = (float)g.bc[1];
     }
-    const int xs = xlive ? xq : NQ - 1;
+    const int xs = xq;
     const int x0 = 4 * xs;
     const int rown = ry + 1 == h ? TY : ry + 1; /* H_new row of the y+1 neighbour */
     const int yb = halo ? h - 1 : ry - 1;       /* staged E row of the y-1 neighbour (ry = 0: top) */
@@ -271,17 +299,13 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
     te.ay = p.tab[2 * S + s1 + gy];
     te.gy = p.tab[3 * S + s1 + gy];
     const int iIb = p.s.iI[b]; /* the excitation's source plane */
-    const int lane = xq & 31;
-    /* the lanes of this warp that compute (a row is whole warps; the last
-     * warp of a row may have idle lanes past L0, which sit at its end) */
-    const unsigned amask = __ballot_sync(0xffffffffu, act);
 
     /* G1: E of stage z (plane z, or 0 for z = L2) and the row above */
     auto stage_e_old = [&](int z) {
         const int zr = z == L2 ? 0 : z, s = z & 1;
         const long long l = lr + pl * zr;
 #pragma unroll
-        for (int i = 0; i < 3; i++) cpa16(&ES(s, i) + tid, p.E + i * n3 + l);
+        for (int i = 0; i < 3; i++) cpa16(&ES(s, i) + sid, p.E + i * n3 + l);
         if (ry == 0) {
             const long long lt = x0 + (long long)L0 * gtop + b * bs + pl * zr;
             cpa16(&TOP(s, 0) + xq, p.E + lt);
@@ -294,22 +318,22 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
         const long long l = lr + pl * zr, lc = l - b * bs;
 #pragma unroll
         for (int i = 0; i < 3; i++) {
-            cpa16(&PH(0, i) + tid, p.bh + i * n3 + lc);
-            cpa16(&PH(1, i) + tid, p.H + i * n3 + l);
+            cpa16(&PH(0, i) + sid, p.bh + i * n3 + lc);
+            cpa16(&PH(1, i) + sid, p.H + i * n3 + l);
         }
         if (pmy | pinfo[z - z0].pm | pmx) {
 #pragma unroll
-            for (int i = 0; i < 3; i++) cpa16(&PH(2, i) + tid, p.Ha + i * n3 + l);
+            for (int i = 0; i < 3; i++) cpa16(&PH(2, i) + sid, p.Ha + i * n3 + l);
         }
     };
     /* G3: be, E aux of plane z (its E update runs at stage z + 1) */
     auto stage_e = [&](int z) {
         const long long l = lr + pl * z, lc = l - b * bs;
 #pragma unroll
-        for (int i = 0; i < 3; i++) cpa16(&PE(0, i) + tid, p.be + i * n3 + lc);
+        for (int i = 0; i < 3; i++) cpa16(&PE(0, i) + sid, p.be + i * n3 + lc);
         if (pmy | pinfo[z - z0].pm | pmx) {
 #pragma unroll
-            for (int i = 0; i < 3; i++) cpa16(&PE(1, i) + tid, p.Ea + i * n3 + l);
+            for (int i = 0; i < 3; i++) cpa16(&PE(1, i) + sid, p.Ea + i * n3 + l);
         }
     };
 
@@ -367,28 +391,24 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
             float4 c[3], a[3];
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                c[i] = (&PH(0, i))[tid];
-                o[i] = (&PH(1, i))[tid];
-                e[i] = (&ES(s, i))[tid];
+                c[i] = (&PH(0, i))[sid];
+                o[i] = (&PH(1, i))[sid];
+                e[i] = (&ES(s, i))[sid];
             }
             if (qs) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) a[i] = (&PH(2, i))[tid];
+                for (int i = 0; i < 3; i++) a[i] = (&PH(2, i))[sid];
             }
             float4 gy0, gy2;
             if (ry == 0) {
                 gy0 = scale4((&TOP(s, 0))[xq], fy);
                 gy2 = scale4((&TOP(s, 1))[xq], fy);
             } else {
-                gy0 = scale4((&ES(s, 0))[yb * NX + xs], fy);
-                gy2 = scale4((&ES(s, 2))[yb * NX + xs], fy);
+                gy0 = scale4((&ES(s, 0))[yb * NQ + xs], fy);
+                gy2 = scale4((&ES(s, 2))[yb * NQ + xs], fy);
             }
-            /* x-1 neighbour: the lane to the left, or staged E at a warp's first lane */
-            float xn1 = __shfl_up_sync(amask, e[1].w, 1), xn2 = __shfl_up_sync(amask, e[2].w, 1);
-            if (lane == 0 || x0 == 0) {
-                xn1 = fxm * (&ES(s, 1))[ry * NX + xl].w;
-                xn2 = fxm * (&ES(s, 2))[ry * NX + xl].w;
-            }
+            /* x-1 neighbour: the staged E of the quad to the left */
+            const float xn1 = fxm * lds4(&ES(s, 1) + ry * NQ + xl).w, xn2 = fxm * lds4(&ES(s, 2) + ry * NQ + xl).w;
             const float4 gz0 = scale4(Ep[0], fzw), gz1 = scale4(Ep[1], fzw);
             th.az = zi.ah;
             th.gz = zi.gh;
@@ -423,23 +443,18 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
             const bool qse = pyze | pmx;
             float4 ce[3], ae[3];
 #pragma unroll
-            for (int i = 0; i < 3; i++) ce[i] = (&PE(0, i))[tid];
+            for (int i = 0; i < 3; i++) ce[i] = (&PE(0, i))[sid];
             if (qse) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) ae[i] = (&PE(1, i))[tid];
+                for (int i = 0; i < 3; i++) ae[i] = (&PE(1, i))[sid];
             }
             /* H_new of plane z-1 (own quad, row above, quad to the right) from
              * shared memory, of plane z from registers */
             const float4 hp[3] = {(&HS(ze, ry, 0))[xs], (&HS(ze, ry, 1))[xs], (&HS(ze, ry, 2))[xs]};
             const float4 ey0 = (&HS(ze, rown, 0))[xs], ey2 = (&HS(ze, rown, 2))[xs];
             const float4 ez0 = scale4(o[0], fzw), ez1 = scale4(o[1], fzw);
-            /* x+1 neighbour: the lane to the right, or H_new(z-1) in shared
-             * memory at a warp's last lane and at the row end */
-            float xp1 = __shfl_down_sync(amask, hp[1].x, 1), xp2 = __shfl_down_sync(amask, hp[2].x, 1);
-            if (lane == 31 || xe1) {
-                xp1 = fxp * (&HS(ze, ry, 1))[xqn].x;
-                xp2 = fxp * (&HS(ze, ry, 2))[xqn].x;
-            }
+            /* x+1 neighbour: H_new(z-1) of the quad to the right */
+            const float xp1 = fxp * lds4(&HS(ze, ry, 1) + xqn).x, xp2 = fxp * lds4(&HS(ze, ry, 2) + xqn).x;
             te.az = zi.ae;
             te.gz = zi.ge;
             row_quad<true>(p, k, b, gy, ze, x0, ze == iIb, te, ce, Ep, hp, ae, ey0, ey2, ez0, ez1, xp1, xp2, pyze);
@@ -498,13 +513,13 @@ const void *row_kernel(int threads, int mb)
 
 } // namespace
 
-int row32_threads_x(int L0) { return ((L0 / 4 + 31) / 32) * 32; }
+int row32_threads(int L0, int ty) { return ((L0 / 4 * (ty + 1) + 31) / 32) * 32; }
 
 size_t row32_smem(int L0, int ty, int zc) { return sizeof(float4) * row_smem_f4(L0, ty, zc); }
 
 int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc)
 {
-    const int threads = row32_threads_x(L0) * (ty + 1);
+    const int threads = row32_threads(L0, ty);
     const void *fn = row_kernel(threads, mb);
     if (!fn) return 0;
     const size_t sm = row32_smem(L0, ty, zc);
@@ -522,9 +537,9 @@ int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc)
 
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st)
 {
-    const int nx = row32_threads_x(r.p.g.L0);
-    const dim3 blk(nx, r.ty + 1);
-    const void *fn = row_kernel(nx * (r.ty + 1), mb);
+    const int nt = row32_threads(r.p.g.L0, r.ty);
+    const dim3 blk(nt);
+    const void *fn = row_kernel(nt, mb);
     const size_t sm = row32_smem(r.p.g.L0, r.ty, r.zc);
     void *args[] = {(void *)&r, (void *)&rel};
     cudaLaunchKernel(fn, dim3(r.nitems), blk, args, sm, st);

@@ -99,6 +99,8 @@ struct smat_fdtd_plan {
     float *d_H32b = nullptr, *d_E32b = nullptr, *d_Ha32b = nullptr, *d_Ea32b = nullptr; /* second set */
     int cur = 0;          /* FP32: which field set holds the current state */
     int *d_stable = nullptr;
+    int *d_qorder = nullptr; /* kernel 6: quads with a PML x index first (nqp of them), then the others */
+    int nqp = 0;
     int nstable = 0;
     int *d_hgen = nullptr, *d_egen = nullptr; /* record (general) cells of each sweep, in cell order */
     int nhgen = 0, negen = 0;

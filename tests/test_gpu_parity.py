@@ -385,12 +385,11 @@ ROW_CASES = [
 
 
 def _row_fits(L0, ty, mb, zc):
-    """Kernel 6 launch shape: a warp per 128 cells of a row, tile_y + 1 rows,
-    staging rings in shared memory (at most 227 KB per CTA)."""
+    """Kernel 6 launch shape: a thread per quad of tile_y + 1 rows (whole
+    warps), staging rings in shared memory (at most 227 KB per CTA)."""
     nq = L0 // 4
-    nx = ((nq + 31) // 32) * 32
-    threads = nx * (ty + 1)
-    smem = 16 * (21 * threads + 4 * nx + 6 * (ty + 1) * nq + 2 * (zc + 1))
+    threads = ((nq * (ty + 1) + 31) // 32) * 32
+    smem = 16 * (27 * nq * (ty + 1) + 4 * nq + 2 * (zc + 1))
     return threads <= {1: 1024, 2: 384, 3: 256}[mb] and smem <= 232448
 
 
