@@ -64,6 +64,8 @@ TRAFFIC_PER_LAUNCH = {
     (6, 5, 24): 2.619e9 + 2.007e9,
     (6, 5, 20): 2.617e9 + 2.007e9,
     (6, 4, 32): 2.582e9 + 2.008e9,
+    (6, 5, 0): 2.567e9 + 2.010e9,             # k_row32, persistent CTAs
+    (6, 2, 0): 2.766e9 + 2.016e9,
 }
 
 

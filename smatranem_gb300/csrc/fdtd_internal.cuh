@@ -157,8 +157,9 @@ struct Fused32T {
 struct Row32 {
     P32 p;
     float *Hn, *En, *Han, *Ean; /* new set */
-    int ty, zc;                 /* rows per tile, planes per z chunk */
-    int nyt, nzc, nitems;       /* row tiles, z chunks, work items (= CTAs) */
+    int ty, zc;                 /* rows per tile, planes per z chunk (0: persistent groups) */
+    int nyt, nzc, nitems;       /* row tiles, z chunks, CTAs */
+    int ngroups;                /* persistent: groups of one CTA per excitation */
     const int *qorder;          /* [L0/4]: quads whose x index lies in a PML, then the others */
     int nqp;                    /* how many of the first kind */
 };

@@ -140,8 +140,17 @@ Row32 make_row(const smat_fdtd_plan *p, bool xp)
     r.ty = p->ty;
     r.zc = p->zc;
     r.nyt = (p->L[1] + p->ty - 1) / p->ty;
-    r.nzc = (p->L[2] + p->zc - 1) / p->zc;
-    r.nitems = p->batch * r.nyt * r.nzc;
+    if (p->zc > 0) {
+        r.nzc = (p->L[2] + p->zc - 1) / p->zc;
+        r.nitems = p->batch * r.nyt * r.nzc;
+        r.ngroups = 0;
+    } else {
+        /* persistent: as many groups of `batch` CTAs as are resident at once */
+        const int resident = sm_count() * (p->max_ctas > 0 ? p->max_ctas : 1);
+        r.nzc = 1;
+        r.ngroups = resident / p->batch > 0 ? resident / p->batch : 1;
+        r.nitems = r.ngroups * p->batch;
+    }
     r.qorder = p->d_qorder;
     r.nqp = p->nqp;
     return r;
@@ -1242,16 +1251,18 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         /* whole-row fused step: tile_y rows per CTA, z chunks, ctas_per_sm = register bound 1..3 */
         if (p->L[0] % 4 != 0 || p->nhgen > 0 || p->negen > 0 || p->nstable > 0)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 needs L0 %% 4 == 0 and a plan without record cells");
-        if (tile_y < 1 || tile_y > 16 || z_chunk < 1 || ctas_per_sm < 1 || ctas_per_sm > 3)
-            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 takes tile_y in 1..16, z_chunk >= 1 and "
-                                          "ctas_per_sm (register bound) 1..3");
-        if (row32_max_ctas_per_sm(p->L[0], tile_y, ctas_per_sm, z_chunk < p->L[2] ? z_chunk : p->L[2]) < 1)
+        if (tile_y < 1 || tile_y > 16 || z_chunk < 0 || ctas_per_sm < 1 || ctas_per_sm > 3)
+            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 takes tile_y in 1..16, z_chunk >= 0 (0: persistent "
+                                          "CTAs) and ctas_per_sm (register bound) 1..3");
+        const int zc = z_chunk == 0 || z_chunk >= p->L[2] ? (z_chunk == 0 ? 0 : p->L[2]) : z_chunk;
+        const int occ = row32_max_ctas_per_sm(p->L[0], tile_y, ctas_per_sm, zc > 0 ? zc : p->L[2]);
+        if (occ < 1)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 with %d rows of %d cells does not fit an SM at %d "
                                           "CTAs per SM", tile_y, p->L[0], ctas_per_sm);
         p->ty = tile_y;
-        p->zc = z_chunk < p->L[2] ? z_chunk : p->L[2];
+        p->zc = zc;
         p->ctas_per_sm = ctas_per_sm;
-        p->max_ctas = ctas_per_sm;
+        p->max_ctas = occ;
         p->fused = 6;
         drop_graph(p);
         return SMAT_OK;
@@ -1355,7 +1366,7 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
     if (p->L[0] % 4 == 0 && p->nhgen == 0 && p->negen == 0 && p->nstable == 0)
         for (int ty : {2, 4, 5})
             for (int mb : {1, 2})
-                for (int zc : {L2, 40, 32, 24, 20})
+                for (int zc : {0, L2, 40, 32, 24, 20})
                     if (zc <= L2 && !(zc < 48 && zc >= L2)) cands.push_back({6, ty, zc, mb, 0});
     cands.push_back({0, 4, 0, 0, 4});
     cands.push_back({0, 8, 0, 0, 4});

@@ -229,15 +229,9 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
 #define TOP(s, c) top[((s) * 2 + (c)) * NQ]
 #define HS(z, row, c) hs[((((z) & 1) * NR + (row)) * 3 + (c)) * NQ]
 
-    /* the item: excitation fastest (the coefficient stream is shared), then
-     * the row tile, then the z chunk */
-    int t = blockIdx.x;
-    const int b = t % p.batch;
-    t /= p.batch;
-    const int yt = t % r.nyt;
-    const int zci = t / r.nyt;
-    const int Y0 = yt * TY, h = min(TY, L1 - Y0);
-    const int z0 = zci * r.zc, z1 = min(z0 + r.zc, L2);
+    /* CTAs in order of excitation fastest (the coefficient stream is shared
+     * by the CTAs of one row tile and plane range), then item group */
+    const int b = blockIdx.x % p.batch, gidx = blockIdx.x / p.batch;
 
     /* this thread's quad: the quads of the tile's rows whose x index lies in
      * a PML (split cells) take the first threads, row by row, the others the
@@ -255,32 +249,15 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
         xq = r.qorder[nqp + u % nqi];
     }
     const int sid = ry * NQ + xq; /* its staging slot */
-    /* its row: own rows 0..h-1, rows h..TY-1 idle (a partial last tile), row
-     * TY the halo row y0+h */
-    const bool halo = ry == TY;
-    const bool own = !halo && ry < h && xlive;
-    const bool act = own || (halo && xlive); /* stages and computes H_new */
-    int gy = halo ? Y0 + h : min(Y0 + ry, L1 - 1);
-    float fyw = 1.0f; /* the halo row wrapped to row 0 holds iBc_y * H_new */
-    if (gy == L1) {
-        gy = 0;
-        fyw = (float)g.bc[1];
-    }
     const int xs = xq;
     const int x0 = 4 * xs;
-    const int rown = ry + 1 == h ? TY : ry + 1; /* H_new row of the y+1 neighbour */
-    const int yb = halo ? h - 1 : ry - 1;       /* staged E row of the y-1 neighbour (ry = 0: top) */
+    const bool halo = ry == TY;
     const int k = *p.s.base + rel;
-    const long long lr = x0 + (long long)L0 * gy + b * bs;
-    const int px0 = x0 + L0 * gy;
-    const float fy = gy == 0 ? (float)g.bc[1] : 1.0f; /* y-1 neighbour wrapped with iBc_y */
-    const int gtop = Y0 == 0 ? L1 - 1 : Y0 - 1;         /* the row above the tile */
-    const float fxm = x0 == 0 ? (float)g.bc[0] : 1.0f;  /* x-1 neighbour wrapped with iBc_x */
+    const float fxm = x0 == 0 ? (float)g.bc[0] : 1.0f; /* x-1 neighbour wrapped with iBc_x */
     const int xl = x0 == 0 ? NQ - 1 : xs - 1;
     const bool xe1 = x0 + 4 == L0;
     const float fxp = xe1 ? (float)g.bc[0] : 1.0f; /* x+1 neighbour of the E update */
     const int xqn = xe1 ? 0 : xs + 1;
-    const bool pmy = p.pmask[s1 + gy];
     const int S = L0 + L1 + L2;
     QuadTab th, te; /* split-PML factors of the H and the E update */
     th.xm = 0;
@@ -294,193 +271,248 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
     }
     te.xm = th.xm;
     const bool pmx = th.xm != 0;
-    th.ay = p.tab[s1 + gy];
-    th.gy = p.tab[S + s1 + gy];
-    te.ay = p.tab[2 * S + s1 + gy];
-    te.gy = p.tab[3 * S + s1 + gy];
     const int iIb = p.s.iI[b]; /* the excitation's source plane */
 
-    /* G1: E of stage z (plane z, or 0 for z = L2) and the row above */
-    auto stage_e_old = [&](int z) {
-        const int zr = z == L2 ? 0 : z, s = z & 1;
-        const long long l = lr + pl * zr;
-#pragma unroll
-        for (int i = 0; i < 3; i++) cpa16(&ES(s, i) + sid, p.E + i * n3 + l);
-        if (ry == 0) {
-            const long long lt = x0 + (long long)L0 * gtop + b * bs + pl * zr;
-            cpa16(&TOP(s, 0) + xq, p.E + lt);
-            cpa16(&TOP(s, 1) + xq, p.E + 2 * n3 + lt);
+    /* The work of this CTA: pieces (row tile yt, planes [z0, z1)) of
+     * excitation b.  With z chunks (r.zc > 0) one piece per CTA: item gidx =
+     * row tile fastest, then z chunk.  Persistent (r.zc == 0): r.ngroups
+     * groups of one CTA per excitation; group gidx takes row tile
+     * round * ngroups + gidx, whole, in each full round (adjacent tiles run
+     * together, so their halo rows are read from L2), then an equal share of
+     * the planes of the tiles left over. */
+    const int G = r.ngroups > 0 ? r.ngroups : 1;
+    const int R = r.zc > 0 ? 0 : r.nyt / G;
+    const long long lrem = (long long)(r.nyt - R * G) * L2;
+    long long u = (long long)gidx * lrem / G;
+    const long long uhi = (long long)(gidx + 1) * lrem / G;
+    int round = 0;
+    bool first = true;
+    for (;;) {
+        int yt, z0, z1;
+        if (r.zc > 0) {
+            if (!first) break;
+            yt = gidx % r.nyt;
+            z0 = gidx / r.nyt * r.zc;
+            z1 = min(z0 + r.zc, L2);
+        } else if (round < R) {
+            yt = round * G + gidx;
+            z0 = 0;
+            z1 = L2;
+            round++;
+        } else if (u < uhi) {
+            yt = R * G + (int)(u / L2);
+            z0 = (int)(u % L2);
+            z1 = (int)min((long long)L2, z0 + (uhi - u));
+            u += z1 - z0;
+        } else {
+            break;
         }
-    };
-    /* G2: bh, H, H aux of stage z */
-    auto stage_h = [&](int z) {
-        const int zr = z == L2 ? 0 : z;
-        const long long l = lr + pl * zr, lc = l - b * bs;
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            cpa16(&PH(0, i) + sid, p.bh + i * n3 + lc);
-            cpa16(&PH(1, i) + sid, p.H + i * n3 + l);
+        first = false;
+        const int Y0 = yt * TY, h = min(TY, L1 - Y0);
+        /* this thread's row: own rows 0..h-1, rows h..TY-1 idle (a partial last
+         * tile), row TY the halo row y0+h */
+        const bool own = !halo && ry < h && xlive;
+        const bool act = own || (halo && xlive); /* stages and computes H_new */
+        int gy = halo ? Y0 + h : min(Y0 + ry, L1 - 1);
+        float fyw = 1.0f; /* the halo row wrapped to row 0 holds iBc_y * H_new */
+        if (gy == L1) {
+            gy = 0;
+            fyw = (float)g.bc[1];
         }
-        if (pmy | pinfo[z - z0].pm | pmx) {
-#pragma unroll
-            for (int i = 0; i < 3; i++) cpa16(&PH(2, i) + sid, p.Ha + i * n3 + l);
-        }
-    };
-    /* G3: be, E aux of plane z (its E update runs at stage z + 1) */
-    auto stage_e = [&](int z) {
-        const long long l = lr + pl * z, lc = l - b * bs;
-#pragma unroll
-        for (int i = 0; i < 3; i++) cpa16(&PE(0, i) + sid, p.be + i * n3 + lc);
-        if (pmy | pinfo[z - z0].pm | pmx) {
-#pragma unroll
-            for (int i = 0; i < 3; i++) cpa16(&PE(1, i) + sid, p.Ea + i * n3 + l);
-        }
-    };
+        const int rown = ry + 1 == h ? TY : ry + 1; /* H_new row of the y+1 neighbour */
+        const int yb = halo ? h - 1 : ry - 1;       /* staged E row of the y-1 neighbour (ry = 0: top) */
+        const long long lr = x0 + (long long)L0 * gy + b * bs;
+        const int px0 = x0 + L0 * gy;
+        const float fy = gy == 0 ? (float)g.bc[1] : 1.0f; /* y-1 neighbour wrapped with iBc_y */
+        const int gtop = Y0 == 0 ? L1 - 1 : Y0 - 1;         /* the row above the tile */
+        const bool pmy = p.pmask[s1 + gy];
+        th.ay = p.tab[s1 + gy];
+        th.gy = p.tab[S + s1 + gy];
+        te.ay = p.tab[2 * S + s1 + gy];
+        te.gy = p.tab[3 * S + s1 + gy];
 
-    /* the plane table of the chunk (z1 = L2 is plane 0) */
-    for (int j = tid; j <= z1 - z0; j += T) {
-        const int zz = z0 + j == L2 ? 0 : z0 + j;
-        PlaneInfo pi;
-        pi.ah = p.tab[s2 + zz];
-        pi.gh = p.tab[S + s2 + zz];
-        pi.ae = p.tab[2 * S + s2 + zz];
-        pi.ge = p.tab[3 * S + s2 + zz];
-        pi.pm = p.pmask[s2 + zz] != 0;
-        pi.q = row_monitor(p.d, zz);
-        pi.pad0 = pi.pad1 = 0;
-        pinfo[j] = pi;
-    }
-    __syncthreads();
-
-    /* E_old(z0-1), components 0 and 1 (the z-1 neighbour of H_new(z0)), and
-     * the inputs of the first stage */
-    float4 Ep[3];
-    Ep[2] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (act) {
-        int zp = z0 - 1;
-        float fz = 1.0f;
-        if (zp < 0) {
-            zp = L2 - 1;
-            fz = (float)g.bc[2];
-        }
-        const long long l = lr + pl * zp;
-        Ep[0] = scale4(ld4(p.E + l), fz);
-        Ep[1] = scale4(ld4(p.E + n3 + l), fz);
-        stage_e_old(z0);
-        stage_h(z0);
-    }
-    cpa_commit();
-    cpa_wait_all();
-    __syncthreads();
-
-    for (int z = z0; z <= z1; z++) {
-        const bool wz = z == L2; /* the closing plane wraps to 0 */
-        const int zr = wz ? 0 : z, s = z & 1;
-        const float fzw = wz ? (float)g.bc[2] : 1.0f;
-        /* G1: the next plane's E leaves now (its slot was last read before
-         * the previous barrier) */
-        if (act && z < z1) stage_e_old(z + 1);
-        cpa_commit();
-        float4 o[3], e[3];
-        if (act) {
-            /* this thread's bh, H, aux of plane z (the previous stage's G2) */
-            cpa_wait2();
-            const PlaneInfo zi = pinfo[z - z0];
-            const bool pyz = pmy | zi.pm;
-            const bool qs = pyz | pmx;
-            float4 c[3], a[3];
+        /* G1: E of stage z (plane z, or 0 for z = L2) and the row above */
+        auto stage_e_old = [&](int z) {
+            const int zr = z == L2 ? 0 : z, s = z & 1;
+            const long long l = lr + pl * zr;
+#pragma unroll
+            for (int i = 0; i < 3; i++) cpa16(&ES(s, i) + sid, p.E + i * n3 + l);
+            if (ry == 0) {
+                const long long lt = x0 + (long long)L0 * gtop + b * bs + pl * zr;
+                cpa16(&TOP(s, 0) + xq, p.E + lt);
+                cpa16(&TOP(s, 1) + xq, p.E + 2 * n3 + lt);
+            }
+        };
+        /* G2: bh, H, H aux of stage z */
+        auto stage_h = [&](int z) {
+            const int zr = z == L2 ? 0 : z;
+            const long long l = lr + pl * zr, lc = l - b * bs;
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                c[i] = (&PH(0, i))[sid];
-                o[i] = (&PH(1, i))[sid];
-                e[i] = (&ES(s, i))[sid];
+                cpa16(&PH(0, i) + sid, p.bh + i * n3 + lc);
+                cpa16(&PH(1, i) + sid, p.H + i * n3 + l);
             }
-            if (qs) {
+            if (pmy | pinfo[z - z0].pm | pmx) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) a[i] = (&PH(2, i))[sid];
+                for (int i = 0; i < 3; i++) cpa16(&PH(2, i) + sid, p.Ha + i * n3 + l);
             }
-            float4 gy0, gy2;
-            if (ry == 0) {
-                gy0 = scale4((&TOP(s, 0))[xq], fy);
-                gy2 = scale4((&TOP(s, 1))[xq], fy);
-            } else {
-                gy0 = scale4((&ES(s, 0))[yb * NQ + xs], fy);
-                gy2 = scale4((&ES(s, 2))[yb * NQ + xs], fy);
-            }
-            /* x-1 neighbour: the staged E of the quad to the left */
-            const float xn1 = fxm * lds4(&ES(s, 1) + ry * NQ + xl).w, xn2 = fxm * lds4(&ES(s, 2) + ry * NQ + xl).w;
-            const float4 gz0 = scale4(Ep[0], fzw), gz1 = scale4(Ep[1], fzw);
-            th.az = zi.ah;
-            th.gz = zi.gh;
-            row_quad<false>(p, k, b, gy, zr, x0, zr == iIb, th, c, o, e, a, gy0, gy2, gz0, gz1, xn1, xn2, pyz);
-            /* the private slot is free: plane z+1's bh, H, aux leave */
-            if (z < z1) stage_h(z + 1);
-            const long long l = lr + pl * zr;
-            if (own && z < z1) {
+        };
+        /* G3: be, E aux of plane z (its E update runs at stage z + 1) */
+        auto stage_e = [&](int z) {
+            const long long l = lr + pl * z, lc = l - b * bs;
 #pragma unroll
-                for (int i = 0; i < 3; i++) st4(r.Hn + i * n3 + l, o[i]);
+            for (int i = 0; i < 3; i++) cpa16(&PE(0, i) + sid, p.be + i * n3 + lc);
+            if (pmy | pinfo[z - z0].pm | pmx) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) cpa16(&PE(1, i) + sid, p.Ea + i * n3 + l);
+            }
+        };
+
+        /* the plane table of the chunk (z1 = L2 is plane 0) */
+        for (int j = tid; j <= z1 - z0; j += T) {
+            const int zz = z0 + j == L2 ? 0 : z0 + j;
+            PlaneInfo pi;
+            pi.ah = p.tab[s2 + zz];
+            pi.gh = p.tab[S + s2 + zz];
+            pi.ae = p.tab[2 * S + s2 + zz];
+            pi.ge = p.tab[3 * S + s2 + zz];
+            pi.pm = p.pmask[s2 + zz] != 0;
+            pi.q = row_monitor(p.d, zz);
+            pi.pad0 = pi.pad1 = 0;
+            pinfo[j] = pi;
+        }
+        __syncthreads();
+
+        /* E_old(z0-1), components 0 and 1 (the z-1 neighbour of H_new(z0)), and
+         * the inputs of the first stage */
+        float4 Ep[3];
+        Ep[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (act) {
+            int zp = z0 - 1;
+            float fz = 1.0f;
+            if (zp < 0) {
+                zp = L2 - 1;
+                fz = (float)g.bc[2];
+            }
+            const long long l = lr + pl * zp;
+            Ep[0] = scale4(ld4(p.E + l), fz);
+            Ep[1] = scale4(ld4(p.E + n3 + l), fz);
+            stage_e_old(z0);
+            stage_h(z0);
+        }
+        cpa_commit();
+        cpa_wait_all();
+        __syncthreads();
+
+        for (int z = z0; z <= z1; z++) {
+            const bool wz = z == L2; /* the closing plane wraps to 0 */
+            const int zr = wz ? 0 : z, s = z & 1;
+            const float fzw = wz ? (float)g.bc[2] : 1.0f;
+            /* G1: the next plane's E leaves now (its slot was last read before
+             * the previous barrier) */
+            if (act && z < z1) stage_e_old(z + 1);
+            cpa_commit();
+            float4 o[3], e[3];
+            if (act) {
+                /* this thread's bh, H, aux of plane z (the previous stage's G2) */
+                cpa_wait2();
+                const PlaneInfo zi = pinfo[z - z0];
+                const bool pyz = pmy | zi.pm;
+                const bool qs = pyz | pmx;
+                float4 c[3], a[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    c[i] = (&PH(0, i))[sid];
+                    o[i] = (&PH(1, i))[sid];
+                    e[i] = (&ES(s, i))[sid];
+                }
                 if (qs) {
 #pragma unroll
-                    for (int i = 0; i < 3; i++) st4(r.Han + i * n3 + l, a[i]);
+                    for (int i = 0; i < 3; i++) a[i] = (&PH(2, i))[sid];
+                }
+                float4 gy0, gy2;
+                if (ry == 0) {
+                    gy0 = scale4((&TOP(s, 0))[xq], fy);
+                    gy2 = scale4((&TOP(s, 1))[xq], fy);
+                } else {
+                    gy0 = scale4((&ES(s, 0))[yb * NQ + xs], fy);
+                    gy2 = scale4((&ES(s, 2))[yb * NQ + xs], fy);
+                }
+                /* x-1 neighbour: the staged E of the quad to the left */
+                const float xn1 = fxm * lds4(&ES(s, 1) + ry * NQ + xl).w, xn2 = fxm * lds4(&ES(s, 2) + ry * NQ + xl).w;
+                const float4 gz0 = scale4(Ep[0], fzw), gz1 = scale4(Ep[1], fzw);
+                th.az = zi.ah;
+                th.gz = zi.gh;
+                row_quad<false>(p, k, b, gy, zr, x0, zr == iIb, th, c, o, e, a, gy0, gy2, gz0, gz1, xn1, xn2, pyz);
+                /* the private slot is free: plane z+1's bh, H, aux leave */
+                if (z < z1) stage_h(z + 1);
+                const long long l = lr + pl * zr;
+                if (own && z < z1) {
+#pragma unroll
+                    for (int i = 0; i < 3; i++) st4(r.Hn + i * n3 + l, o[i]);
+                    if (qs) {
+#pragma unroll
+                        for (int i = 0; i < 3; i++) st4(r.Han + i * n3 + l, a[i]);
+                    }
+                    const int q = zi.q;
+                    if (q >= 0) {
+                        st4(row_ring(p.d, g.pl, b, k, q, 0) + px0, o[0]);
+                        st4(row_ring(p.d, g.pl, b, k, q, 1) + px0, o[1]);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 3; i++) (&HS(z, ry, i))[xs] = scale4(o[i], fyw);
+            }
+            cpa_commit(); /* G2 */
+            if (own && z > z0) {
+                /* this thread's be, E aux of plane z-1 (the previous stage's G3) */
+                cpa_wait2();
+                const int ze = z - 1;
+                const long long le = lr + pl * ze;
+                const PlaneInfo zi = pinfo[ze - z0];
+                const bool pyze = pmy | zi.pm;
+                const bool qse = pyze | pmx;
+                float4 ce[3], ae[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) ce[i] = (&PE(0, i))[sid];
+                if (qse) {
+#pragma unroll
+                    for (int i = 0; i < 3; i++) ae[i] = (&PE(1, i))[sid];
+                }
+                /* H_new of plane z-1 (own quad, row above, quad to the right) from
+                 * shared memory, of plane z from registers */
+                const float4 hp[3] = {(&HS(ze, ry, 0))[xs], (&HS(ze, ry, 1))[xs], (&HS(ze, ry, 2))[xs]};
+                const float4 ey0 = (&HS(ze, rown, 0))[xs], ey2 = (&HS(ze, rown, 2))[xs];
+                const float4 ez0 = scale4(o[0], fzw), ez1 = scale4(o[1], fzw);
+                /* x+1 neighbour: H_new(z-1) of the quad to the right */
+                const float xp1 = fxp * lds4(&HS(ze, ry, 1) + xqn).x, xp2 = fxp * lds4(&HS(ze, ry, 2) + xqn).x;
+                te.az = zi.ae;
+                te.gz = zi.ge;
+                row_quad<true>(p, k, b, gy, ze, x0, ze == iIb, te, ce, Ep, hp, ae, ey0, ey2, ez0, ez1, xp1, xp2, pyze);
+#pragma unroll
+                for (int i = 0; i < 3; i++) st4(r.En + i * n3 + le, Ep[i]);
+                if (qse) {
+#pragma unroll
+                    for (int i = 0; i < 3; i++) st4(r.Ean + i * n3 + le, ae[i]);
                 }
                 const int q = zi.q;
                 if (q >= 0) {
-                    st4(row_ring(p.d, g.pl, b, k, q, 0) + px0, o[0]);
-                    st4(row_ring(p.d, g.pl, b, k, q, 1) + px0, o[1]);
+                    st4(row_ring(p.d, g.pl, b, k, q, 2) + px0, Ep[0]);
+                    st4(row_ring(p.d, g.pl, b, k, q, 3) + px0, Ep[1]);
                 }
             }
+            /* the private slot is free: plane z's be, E aux leave (G3) */
+            if (own && z < z1) stage_e(z);
+            cpa_commit();
+            if (act) {
 #pragma unroll
-            for (int i = 0; i < 3; i++) (&HS(z, ry, i))[xs] = scale4(o[i], fyw);
-        }
-        cpa_commit(); /* G2 */
-        if (own && z > z0) {
-            /* this thread's be, E aux of plane z-1 (the previous stage's G3) */
+                for (int i = 0; i < 3; i++) Ep[i] = e[i];
+            }
+            /* the next plane's E (G1) complete, then visible to the neighbours */
             cpa_wait2();
-            const int ze = z - 1;
-            const long long le = lr + pl * ze;
-            const PlaneInfo zi = pinfo[ze - z0];
-            const bool pyze = pmy | zi.pm;
-            const bool qse = pyze | pmx;
-            float4 ce[3], ae[3];
-#pragma unroll
-            for (int i = 0; i < 3; i++) ce[i] = (&PE(0, i))[sid];
-            if (qse) {
-#pragma unroll
-                for (int i = 0; i < 3; i++) ae[i] = (&PE(1, i))[sid];
-            }
-            /* H_new of plane z-1 (own quad, row above, quad to the right) from
-             * shared memory, of plane z from registers */
-            const float4 hp[3] = {(&HS(ze, ry, 0))[xs], (&HS(ze, ry, 1))[xs], (&HS(ze, ry, 2))[xs]};
-            const float4 ey0 = (&HS(ze, rown, 0))[xs], ey2 = (&HS(ze, rown, 2))[xs];
-            const float4 ez0 = scale4(o[0], fzw), ez1 = scale4(o[1], fzw);
-            /* x+1 neighbour: H_new(z-1) of the quad to the right */
-            const float xp1 = fxp * lds4(&HS(ze, ry, 1) + xqn).x, xp2 = fxp * lds4(&HS(ze, ry, 2) + xqn).x;
-            te.az = zi.ae;
-            te.gz = zi.ge;
-            row_quad<true>(p, k, b, gy, ze, x0, ze == iIb, te, ce, Ep, hp, ae, ey0, ey2, ez0, ez1, xp1, xp2, pyze);
-#pragma unroll
-            for (int i = 0; i < 3; i++) st4(r.En + i * n3 + le, Ep[i]);
-            if (qse) {
-#pragma unroll
-                for (int i = 0; i < 3; i++) st4(r.Ean + i * n3 + le, ae[i]);
-            }
-            const int q = zi.q;
-            if (q >= 0) {
-                st4(row_ring(p.d, g.pl, b, k, q, 2) + px0, Ep[0]);
-                st4(row_ring(p.d, g.pl, b, k, q, 3) + px0, Ep[1]);
-            }
+            __syncthreads();
         }
-        /* the private slot is free: plane z's be, E aux leave (G3) */
-        if (own && z < z1) stage_e(z);
-        cpa_commit();
-        if (act) {
-#pragma unroll
-            for (int i = 0; i < 3; i++) Ep[i] = e[i];
-        }
-        /* the next plane's E (G1) complete, then visible to the neighbours */
-        cpa_wait2();
-        __syncthreads();
-    }
+    } /* pieces */
 #undef ES
 #undef PH
 #undef PE
@@ -540,7 +572,7 @@ void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st)
     const int nt = row32_threads(r.p.g.L0, r.ty);
     const dim3 blk(nt);
     const void *fn = row_kernel(nt, mb);
-    const size_t sm = row32_smem(r.p.g.L0, r.ty, r.zc);
+    const size_t sm = row32_smem(r.p.g.L0, r.ty, r.zc > 0 ? r.zc : r.p.g.L2);
     void *args[] = {(void *)&r, (void *)&rel};
     cudaLaunchKernel(fn, dim3(r.nitems), blk, args, sm, st);
 }

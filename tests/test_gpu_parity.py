@@ -397,9 +397,11 @@ def _row_fits(L0, ty, mb, zc):
 def test_row_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     """The whole-row fused step (kernel 6) reproduces the scalar FP32 sweeps
     bit for bit: partial last row tiles, z chunks of 1 plane to the whole
-    grid, every register bound, iBc = -1/0/1 wraps on each axis (the halo row
-    and closing plane hold iBc * H_new), split PML on all faces, per-excitation
-    source planes and DFT planes, across field-set swaps."""
+    grid, persistent CTAs (whole tiles in rounds, the leftover tiles' planes
+    shared out in pieces of a few planes), every register bound, iBc = -1/0/1
+    wraps on each axis (the halo row and closing plane hold iBc * H_new),
+    split PML on all faces, per-excitation source planes and DFT planes,
+    across field-set swaps."""
     from smatranem_gb300 import workloads as W
     L, seed, kw, iBTIin = ROW_CASES[case]
     s = W.random_structure(L, seed=seed, **kw)
@@ -408,8 +410,8 @@ def test_row_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
     tunings = [(6, ty, zc, mb, 0) for ty, zc, mb in
                [(1, L[2], 1), (2, 5, 2), (4, 3, 1), (3, 1, 3), (4, 7, 2), (8, 40, 1), (2, 2, 3), (5, L[2], 1),
-                (1, 4, 3), (1, 2, 2)]
-               if _row_fits(L[0], ty, mb, min(zc, L[2]))]
+                (1, 4, 3), (1, 2, 2), (1, 0, 1), (2, 0, 2), (5, 0, 1), (3, 0, 3)]
+               if _row_fits(L[0], ty, mb, min(zc, L[2]) if zc else L[2])]
     assert len(tunings) >= 5
     for tuning in tunings:
         got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
