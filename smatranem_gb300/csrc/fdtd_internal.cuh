@@ -162,6 +162,7 @@ struct Row32 {
     int ngroups;                /* persistent: groups of one CTA per excitation */
     const int *qorder;          /* [L0/4]: quads whose x index lies in a PML, then the others */
     int nqp;                    /* how many of the first kind */
+    int has_rec;                /* the plan has record cells (lossy or PEC cells; no stable-form metal) */
 };
 
 /* launchers (one translation unit per precision) */
@@ -190,10 +191,11 @@ int fused32t_max_ctas_per_sm(int ty, int ns);
 int fused32_max_ctas_per_sm(int ty, int ns);
 /* form 6: threads of a CTA (one per quad of its ty + 1 rows, rounded up to
  * whole warps), shared memory, resident CTAs of ty rows and z chunks of zc
- * planes at register bound mb (1, 2 or 3 CTAs per SM) */
+ * planes at register bound mb (1, 2 or 3 CTAs per SM; 1 for plans with record
+ * cells) */
 int row32_threads(int L0, int ty);
 size_t row32_smem(int L0, int ty, int zc);
-int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc);
+int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc, bool rec);
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st);
 void launch_bump(int *base, int by, cudaStream_t st);
 void launch_set(int *base, int value, cudaStream_t st);

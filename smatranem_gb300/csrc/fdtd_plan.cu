@@ -153,6 +153,7 @@ Row32 make_row(const smat_fdtd_plan *p, bool xp)
     }
     r.qorder = p->d_qorder;
     r.nqp = p->nqp;
+    r.has_rec = p->nhgen + p->negen > 0;
     return r;
 }
 
@@ -767,6 +768,19 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
         CK(cudaMemcpyAsync(p->d_hgen, hgen.data(), hgen.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
     if (!egen.empty())
         CK(cudaMemcpyAsync(p->d_egen, egen.data(), egen.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    /* record kinds kernel 6 can or cannot take */
+    for (int side = 0; side < 2; side++) {
+        const std::vector<float> &cf = side ? be : bh;
+        const std::vector<Rec32> &recs = side ? erec : hrec;
+        for (long long l = 0; l < n3; l++) {
+            if (!std::isnan(cf[l])) continue;
+            int idx;
+            memcpy(&idx, &cf[n3 + l], 4);
+            const int kind = recs[idx].kind;
+            if (kind == RK_STABLE || kind == RK_FROZEN) p->nrec_metal++;
+            if (kind == RK_A) p->nrec_split++;
+        }
+    }
     if (p->L[0] % 4 == 0) {
         p->fused = 2; /* default: vectorised sweeps where they apply */
         p->by32 = 2;
@@ -1249,13 +1263,15 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
     }
     if (fused == 6) {
         /* whole-row fused step: tile_y rows per CTA, z chunks, ctas_per_sm = register bound 1..3 */
-        if (p->L[0] % 4 != 0 || p->nhgen > 0 || p->negen > 0 || p->nstable > 0)
-            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 needs L0 %% 4 == 0 and a plan without record cells");
+        if (p->L[0] % 4 != 0 || p->nrec_metal > 0 || p->nrec_split > 0)
+            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 needs L0 %% 4 == 0 and a plan without stable-form "
+                                          "metal cells or lossy split cells");
         if (tile_y < 1 || tile_y > 16 || z_chunk < 0 || ctas_per_sm < 1 || ctas_per_sm > 3)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 takes tile_y in 1..16, z_chunk >= 0 (0: persistent "
                                           "CTAs) and ctas_per_sm (register bound) 1..3");
         const int zc = z_chunk == 0 || z_chunk >= p->L[2] ? (z_chunk == 0 ? 0 : p->L[2]) : z_chunk;
-        const int occ = row32_max_ctas_per_sm(p->L[0], tile_y, ctas_per_sm, zc > 0 ? zc : p->L[2]);
+        const int occ =
+            row32_max_ctas_per_sm(p->L[0], tile_y, ctas_per_sm, zc > 0 ? zc : p->L[2], p->nhgen + p->negen > 0);
         if (occ < 1)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 with %d rows of %d cells does not fit an SM at %d "
                                           "CTAs per SM", tile_y, p->L[0], ctas_per_sm);
@@ -1363,7 +1379,7 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
             for (int lag : {0, 4, 8})
                 if (rows <= p->L[1] && lag <= L2) cands.push_back({4, rows, lag, 0, 0});
     /* whole-row fused step (plans without record cells) */
-    if (p->L[0] % 4 == 0 && p->nhgen == 0 && p->negen == 0 && p->nstable == 0)
+    if (p->L[0] % 4 == 0 && p->nrec_metal == 0 && p->nrec_split == 0)
         for (int ty : {2, 4, 5})
             for (int mb : {1, 2})
                 for (int zc : {0, L2, 40, 32, 24, 20})

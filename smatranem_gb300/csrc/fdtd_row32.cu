@@ -106,7 +106,27 @@ struct QuadTab {
     unsigned xm;
 };
 
+/* A record cell of an ordinary ('n') cell -- lossy or PEC: the update of the
+ * sweeps' general-cell path (fdtd_f32.cu, general32_cell) from the same
+ * curls; t is the cell's total field, updated in place.  The host admits no
+ * other record kind to this kernel.  Out of line: record cells are rare and
+ * must not cost the quads registers. */
 template <bool EF>
+__device__ __noinline__ void row_record(const P32 &p, const int k, const int b, const bool on_src, const int px,
+                                        const int ridx, const float *pl, const float *mi, float *t)
+{
+    const Geo &g = p.g;
+    const float sg = EF ? 1.0f : -1.0f;
+    const Rec32 r = (EF ? p.erec : p.hrec)[ridx];
+    float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
+    if (on_src) {
+        W[0] += (float)(p.s.sgn[b] * row_sheet(p.s, g.pl, b, k, !EF, 1, px));
+        W[1] -= (float)(p.s.sgn[b] * row_sheet(p.s, g.pl, b, k, !EF, 0, px));
+    }
+    for (int c = 0; c < 3; c++) t[c] = fmaf(sg * r.B0[c], W[c], r.A0[c] * t[c]);
+}
+
+template <bool EF, bool REC>
 __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b, const int j1, const int j2,
                                          const int x0, const bool on_src, const QuadTab &tq, const float4 c[3],
                                          float4 out[3], const float4 gh[3], float4 aux[3], const float4 gy0,
@@ -144,7 +164,12 @@ __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b,
             mi[2] = h0 - el(gy0, i);
         }
         const float bn[3] = {el(c[0], i), el(c[1], i), el(c[2], i)};
-        if (!(((tq.xm >> i) & 1u) | pyz)) {
+        if (REC && isnan(bn[0])) { /* a record cell (marked by NaN in its first coefficient) */
+            float t[3] = {el(out[0], i), el(out[1], i), el(out[2], i)};
+            row_record<EF>(p, k, b, on_src, px0 + i, __float_as_int(bn[1]), pl, mi, t);
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) set_el(out[cc], i, t[cc]);
+        } else if (!(((tq.xm >> i) & 1u) | pyz)) {
             float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
             if (on_src) {
                 W[0] += (float)(p.s.sgn[b] * row_sheet(p.s, g.pl, b, k, !EF, 1, px0 + i));
@@ -209,7 +234,7 @@ struct PlaneInfo {
     int pm, q, pad0, pad1;
 };
 
-template <int MAXT, int MB>
+template <int MAXT, int MB, bool REC>
 __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel)
 {
     extern __shared__ float4 sm4[];
@@ -443,7 +468,7 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
                 const float4 gz0 = scale4(Ep[0], fzw), gz1 = scale4(Ep[1], fzw);
                 th.az = zi.ah;
                 th.gz = zi.gh;
-                row_quad<false>(p, k, b, gy, zr, x0, zr == iIb, th, c, o, e, a, gy0, gy2, gz0, gz1, xn1, xn2, pyz);
+                row_quad<false, REC>(p, k, b, gy, zr, x0, zr == iIb, th, c, o, e, a, gy0, gy2, gz0, gz1, xn1, xn2, pyz);
                 /* the private slot is free: plane z+1's bh, H, aux leave */
                 if (z < z1) stage_h(z + 1);
                 const long long l = lr + pl * zr;
@@ -488,7 +513,7 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
                 const float xp1 = fxp * lds4(&HS(ze, ry, 1) + xqn).x, xp2 = fxp * lds4(&HS(ze, ry, 2) + xqn).x;
                 te.az = zi.ae;
                 te.gz = zi.ge;
-                row_quad<true>(p, k, b, gy, ze, x0, ze == iIb, te, ce, Ep, hp, ae, ey0, ey2, ez0, ez1, xp1, xp2, pyze);
+                row_quad<true, REC>(p, k, b, gy, ze, x0, ze == iIb, te, ce, Ep, hp, ae, ey0, ey2, ez0, ez1, xp1, xp2, pyze);
 #pragma unroll
                 for (int i = 0; i < 3; i++) st4(r.En + i * n3 + le, Ep[i]);
                 if (qse) {
@@ -520,25 +545,33 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
 #undef HS
 }
 
-template <int MAXT, int MB> const void *row_fn() { return (const void *)k_row32<MAXT, MB>; }
+template <int MAXT, int MB, bool REC> const void *row_fn() { return (const void *)k_row32<MAXT, MB, REC>; }
 
 /* the instantiation for a block of `threads` at register bound mb (at least
- * mb resident CTAs of MAXT threads: 65536 / (MAXT * mb) registers), or null */
-const void *row_kernel(int threads, int mb)
+ * mb resident CTAs of MAXT threads: 65536 / (MAXT * mb) registers), or null;
+ * plans with record cells: one CTA per SM only */
+const void *row_kernel(int threads, int mb, bool rec)
 {
+    if (rec) {
+        if (mb != 1) return nullptr;
+        if (threads <= 384) return row_fn<384, 1, true>();
+        if (threads <= 640) return row_fn<640, 1, true>();
+        if (threads <= 1024) return row_fn<1024, 1, true>();
+        return nullptr;
+    }
     switch (mb) {
     case 1:
-        if (threads <= 384) return row_fn<384, 1>();
-        if (threads <= 448) return row_fn<448, 1>();
-        if (threads <= 512) return row_fn<512, 1>();
-        if (threads <= 640) return row_fn<640, 1>();
-        if (threads <= 1024) return row_fn<1024, 1>();
+        if (threads <= 384) return row_fn<384, 1, false>();
+        if (threads <= 448) return row_fn<448, 1, false>();
+        if (threads <= 512) return row_fn<512, 1, false>();
+        if (threads <= 640) return row_fn<640, 1, false>();
+        if (threads <= 1024) return row_fn<1024, 1, false>();
         return nullptr;
     case 2:
-        if (threads <= 192) return row_fn<192, 2>();
-        if (threads <= 384) return row_fn<384, 2>();
+        if (threads <= 192) return row_fn<192, 2, false>();
+        if (threads <= 384) return row_fn<384, 2, false>();
         return nullptr;
-    case 3: return threads <= 256 ? row_fn<256, 3>() : nullptr;
+    case 3: return threads <= 256 ? row_fn<256, 3, false>() : nullptr;
     default: return nullptr;
     }
 }
@@ -549,10 +582,10 @@ int row32_threads(int L0, int ty) { return ((L0 / 4 * (ty + 1) + 31) / 32) * 32;
 
 size_t row32_smem(int L0, int ty, int zc) { return sizeof(float4) * row_smem_f4(L0, ty, zc); }
 
-int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc)
+int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc, bool rec)
 {
     const int threads = row32_threads(L0, ty);
-    const void *fn = row_kernel(threads, mb);
+    const void *fn = row_kernel(threads, mb, rec);
     if (!fn) return 0;
     const size_t sm = row32_smem(L0, ty, zc);
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
@@ -571,7 +604,7 @@ void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st)
 {
     const int nt = row32_threads(r.p.g.L0, r.ty);
     const dim3 blk(nt);
-    const void *fn = row_kernel(nt, mb);
+    const void *fn = row_kernel(nt, mb, r.has_rec != 0);
     const size_t sm = row32_smem(r.p.g.L0, r.ty, r.zc > 0 ? r.zc : r.p.g.L2);
     void *args[] = {(void *)&r, (void *)&rel};
     cudaLaunchKernel(fn, dim3(r.nitems), blk, args, sm, st);

@@ -101,6 +101,8 @@ struct smat_fdtd_plan {
     int *d_stable = nullptr;
     int *d_qorder = nullptr; /* kernel 6: quads with a PML x index first (nqp of them), then the others */
     int nqp = 0;
+    int nrec_metal = 0;   /* records of stable-form or frozen components (metal cells) */
+    int nrec_split = 0;   /* records of split cells (lossy media in a PML) */
     int nstable = 0;
     int *d_hgen = nullptr, *d_egen = nullptr; /* record (general) cells of each sweep, in cell order */
     int nhgen = 0, negen = 0;

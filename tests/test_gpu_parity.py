@@ -420,11 +420,42 @@ def test_row_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
                 assert np.array_equal(a, b_), tuning
 
 
-def test_row_fused_refuses_record_cells(built):
-    """Kernel 6 has no record-cell path: a plan with lossy or PEC cells is refused."""
+ROW_REC_CASES = [
+    # record cells other than stable-form metal: lossy and PEC ordinary cells
+    ((40, 17, 19, 3), 41, dict(pml=(4, 4, 4), lossy=0.05, iBc=(1, 1, -1)), (5, 13, 7, -1)),
+    ((136, 13, 17, 2), 42, dict(pml=(4, 3, 3), lossy=0.05, pec=0.03, iBc=(0, 0, 0)), (4, 12, 6, 1)),
+    ((36, 9, 12, 2), 43, dict(pml=(0, 0, 3), pml_z_only=True, pec=0.05, iBc=(0, -1, 0)), (4, 8, 5, 1)),
+]
+
+
+@pytest.mark.parametrize("case", range(len(ROW_REC_CASES)))
+def test_row_fused_record_cells_bit_identical(built, case):
+    """Record cells in kernel 6 (the sweeps' general-cell update, out of
+    line): lossy and PEC ordinary cells, bit for bit as the scalar sweeps,
+    chunked and persistent."""
+    from smatranem_gb300 import workloads as W
+    L, seed, kw, iBTIin = ROW_REC_CASES[case]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    nsteps = 33
+    ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
+    # plans with record cells run kernel 6 at one CTA per SM only
+    tunings = [(6, ty, zc, 1, 0) for ty, zc in [(2, 5), (5, 0), (1, 3), (3, 0), (4, L[2])]
+               if _row_fits(L[0], ty, 1, min(zc, L[2]) if zc else L[2])]
+    assert len(tunings) >= 4
+    for tuning in tunings:
+        got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
+        for rb, gb in zip(ref, got):
+            for a, b_ in zip(rb, gb):
+                assert np.array_equal(a, b_), tuning
+
+
+def test_row_fused_refuses_metal_cells(built):
+    """Kernel 6 has no stable-form path: a plan with metal ('h', 'e', 'b')
+    cells is refused."""
     from smatranem_gb300 import workloads as W
     f = _fdtd()
-    L, seed, kw, iBTIin = FUSED_CASES[4]
+    L, seed, kw, iBTIin = FUSED_CASES[0]
     s = W.random_structure(L, seed=seed, **kw)
     pr = W.prepare(s)
     with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=f.FP32,
