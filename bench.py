@@ -549,8 +549,9 @@ def run_adjoint(args):
 def run_group(args):
     """Batched S-matrix workload: the bend with its 8 excitations plus 16 slabs of
     uneven size (128^3 .. 256x256x192, 1-6 random cuboid inclusions each, one
-    excitation each), all FP32, advanced together by one group (one launch per
-    sweep for all structures); compared with the same plans stepped one by one."""
+    excitation each), all FP32, advanced together by one group in the form its
+    autotuner picks (one sweep launch for all structures, or every member's own
+    launches in one graph); compared with the same plans stepped one by one."""
     import torch
     from smatranem_gb300 import fdtd as F
     from smatranem_gb300 import workloads as W
@@ -574,8 +575,9 @@ def run_group(args):
     g.run(0, args.warmup)
     _, t_group = _timed(lambda: g.run(args.warmup, nsteps))
     g.close()
-    for p in plans:  # the same steps again as separate plans, each on its own stream
-        p.set_tuning(2, by, 0, 0, 4)
+    if gmode != 2:  # the same steps again as separate plans, each on its own stream
+        for p in plans:  # (in form 2 every member keeps its own autotuned launch form)
+            p.set_tuning(2, by, 0, 0, 4)
 
     def one_by_one():
         for p in plans:
@@ -587,8 +589,9 @@ def run_group(args):
         "mode": "group", "config": "bend 256x192x160 x 8 excitations + 16 slabs 128^3..256x256x192, FP32, "
                                    "21-wavelength FP64 DFT on 2 planes each",
         "structures": len(plans), "cell_excitations": cells, "steps": args.steps,
-        "group_tuning": {"mode": ["one grouped launch per sweep", "members' own launches in one graph"][gmode],
-                         "block_y": by},
+        "group_tuning": {"mode": ["one grouped launch per sweep", "members' own sweep launches in one graph",
+                                  "members' own autotuned launch forms in one graph"][gmode],
+                         "block_y": by, "member_tunings": [list(p.get_tuning()) for p in plans]},
         "group_gcell_per_s": cells * args.steps / t_group / 1e9, "group_ms_per_step": 1e3 * t_group / args.steps,
         "separate_plans_gcell_per_s": cells * args.steps / t_sep / 1e9,
         "device_gb": sum(p.device_bytes for p in plans) / 1e9,

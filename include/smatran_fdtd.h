@@ -241,10 +241,10 @@ int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const doubl
  * No counterpart in the reference (it runs one structure per process, main
  * :32-187).  A group advances several FP32 plans -- structures of any size,
  * each with its own batch of excitations, schedule and DFT -- together, one
- * CUDA graph launch per 32 steps (see set_tuning for the two launch forms
- * inside it, plus the general cells and each member's DFT flush).  Members need
+ * CUDA graph launch per 32 steps (see set_tuning for the launch forms inside
+ * it, plus the general cells and each member's DFT flush).  Members need
  * L0 % 4 == 0 and stay usable on their own; results are bit-identical to
- * stepping each member alone with the vectorised sweeps.  At most 32 members;
+ * stepping each member alone.  At most 32 members;
  * the group launches on the first member's stream and waits for the others'
  * streams before each run. */
 typedef struct smat_fdtd_group smat_fdtd_group;
@@ -252,11 +252,15 @@ int smat_fdtd_group_create(smat_fdtd_plan *const *plans, int nplans, smat_fdtd_g
 int smat_fdtd_group_destroy(smat_fdtd_group *group);
 /* mode 0: one grouped sweep launch for all members (blocks find their member
  * by prefix sums); mode 1: every member's own sweep launches back to back on
- * the group's stream.  Both are captured as one graph per 32 steps.  block_y:
- * rows per block, 1..4. */
+ * the group's stream; mode 2: every member's own launch form (its
+ * smat_fdtd_set_tuning: the whole-row fused step or the sweeps) on the
+ * member's own stream, forked from the group's stream and joined back, so the
+ * members run side by side.  All are captured as one graph per 32 steps.
+ * block_y: rows per sweep block, 1..4 (modes 0, 1). */
 int smat_fdtd_group_set_tuning(smat_fdtd_group *group, int mode, int block_y);
-/* fastest {mode, block_y} over nsteps steps; members must be at the zero state
- * and are left as they were */
+/* fastest {mode, block_y} over nsteps steps, after autotuning every member
+ * (smat_fdtd_autotune: their launch form for mode 2); members must be at the
+ * zero state and are left there */
 int smat_fdtd_group_autotune(smat_fdtd_group *group, int nsteps, int best[2], double *best_ms);
 /* steps [k_begin, k_end) of every member's schedule */
 int smat_fdtd_group_run(smat_fdtd_group *group, int k_begin, int k_end);

@@ -32,8 +32,11 @@ struct smat_fdtd_group {
     std::vector<int> cur; /* members' field sets when the graph was captured */
     Group32 *h_gr = nullptr; /* pinned copy of the member table (mode 0) */
     cudaStream_t stream = nullptr;
-    int mode = 0; /* 0: one grouped launch per sweep; 1: each member's own sweep launches */
+    int mode = 0; /* 0: one grouped launch per sweep; 1: each member's own sweep launches;
+                     2: each member's own launch form, on its own stream */
     int by = 1;
+    cudaEvent_t fork = nullptr;      /* mode 2: members' streams wait for the group's stream ... */
+    std::vector<cudaEvent_t> join;   /* ... and the group's stream for each member's */
     cudaGraphExec_t graph = nullptr;
     bool graph_failed = false;
 };
@@ -77,6 +80,23 @@ void enqueue_group(smat_fdtd_group *g, int rel0, int n)
         *g->h_gr = make_group(g); /* same bytes on every call while the members stand still */
         load_group32(g->h_gr, g->stream);
         for (int i = 0; i < n; i++) launch_group32v(*g->h_gr, rel0 + i, g->stream);
+    } else if (g->mode == 2) {
+        /* each member's own (autotuned) launch form and DFT flush on its own
+         * stream, forked from the group's stream and joined back: the members
+         * run side by side (one graph launch per chunk of steps) */
+        cudaEventRecord(g->fork, g->stream);
+        for (size_t j = 0; j < g->m.size(); j++) {
+            smat_fdtd_plan *p = g->m[j];
+            const cudaStream_t st = p->stream;
+            if (st != g->stream) cudaStreamWaitEvent(st, g->fork, 0);
+            for (int i = 0; i < n; i++) enqueue_update(p, rel0 + i, st);
+            launch_flush32(make_p32(p, false), rel0 + n, n, st);
+            if (st != g->stream) {
+                cudaEventRecord(g->join[j], st);
+                cudaStreamWaitEvent(g->stream, g->join[j], 0);
+            }
+        }
+        return;
     } else {
         /* each member's own vectorised sweeps (rows g->by, whole grid), in
          * order on the group's stream: one graph launch per chunk of steps */
@@ -159,6 +179,15 @@ extern "C" int smat_fdtd_group_create(smat_fdtd_plan *const *plans, int nplans, 
     }
     g->m.assign(plans, plans + nplans);
     g->stream = plans[0]->stream;
+    g->join.assign(nplans, nullptr);
+    bool ev_ok = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < nplans && ev_ok; i++)
+        ev_ok = cudaEventCreateWithFlags(&g->join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ev_ok) {
+        cudaGetLastError();
+        smat_fdtd_group_destroy(g);
+        return smat_fail(SMAT_ECUDA, "group_create: events");
+    }
     *out = g;
     return SMAT_OK;
 }
@@ -169,6 +198,9 @@ extern "C" int smat_fdtd_group_destroy(smat_fdtd_group *g)
     if (g->stream) cudaStreamSynchronize(g->stream);
     drop_group_graph(g);
     if (g->h_gr) cudaFreeHost(g->h_gr);
+    if (g->fork) cudaEventDestroy(g->fork);
+    for (cudaEvent_t e : g->join)
+        if (e) cudaEventDestroy(e);
     delete g;
     return SMAT_OK;
 }
@@ -176,9 +208,9 @@ extern "C" int smat_fdtd_group_destroy(smat_fdtd_group *g)
 extern "C" int smat_fdtd_group_set_tuning(smat_fdtd_group *g, int mode, int block_y)
 {
     smat_clear_error();
-    if (!g || mode < 0 || mode > 1 || block_y < 1 || block_y > 4)
-        return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 0 (one launch per sweep) or 1 (members' own "
-                                      "launches), block_y in 1..4");
+    if (!g || mode < 0 || mode > 2 || block_y < 1 || block_y > 4)
+        return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 0 (one launch per sweep), 1 (members' own sweep "
+                                      "launches) or 2 (members' own tuned launch forms), block_y in 1..4");
     g->mode = mode;
     g->by = block_y;
     drop_group_graph(g);
@@ -255,6 +287,12 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best
         if (rc) return rc;
         if (mx != 0.0) return smat_fail(SMAT_ESTATE, "group_autotune: needs every member at the zero state");
     }
+    /* form 2 steps each member in its own fastest launch form: tune them
+     * (each on its own stream, sources and DFT off, back at the zero state) */
+    for (smat_fdtd_plan *p : g->m) {
+        int rc = smat_fdtd_autotune(p, nsteps, nullptr, nullptr);
+        if (rc) return rc;
+    }
     std::vector<int> nq(g->m.size());
     for (size_t i = 0; i < g->m.size(); i++) {
         smat_fdtd_plan *p = g->m[i];
@@ -269,8 +307,9 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best
     double bms = 1e30;
     int bmode = g->mode, bby = g->by;
     std::lock_guard<std::mutex> lock(g_table_mu);
-    for (int mode : {0, 1})
+    for (int mode : {0, 1, 2})
         for (int by : {1, 2, 4}) {
+            if (mode == 2 && by != 1) continue; /* rows per block: the members' own */
             g->mode = mode;
             g->by = by;
             enqueue_group(g, 0, 1);

@@ -403,6 +403,23 @@ int setup_pipe(smat_fdtd_plan *p, int by, int lag)
     return SMAT_OK;
 }
 
+/* One step's update launches of plan p on stream st, without the DFT flush:
+ * the plan's own launch form for kernel 6 and the sweeps (0, 2); the other
+ * forms step as vectorised sweeps.  Kernel 6 swaps the field sets. */
+void enqueue_update(smat_fdtd_plan *p, int rel, cudaStream_t st)
+{
+    if (p->precision != SMAT_FP32) return;
+    if (p->fused == 6) {
+        launch_row32(make_row(p, false), rel, p->ctas_per_sm, st);
+        p->cur ^= 1;
+        return;
+    }
+    const int fu = p->fused;
+    if (fu != 0 && fu != 2) p->fused = 2;
+    sweep_step(p, make_p32(p, false), rel, st);
+    p->fused = fu;
+}
+
 /* One FP32 step as two sweeps (kernels 0 and 2), in z-chunks of szc planes:
  * H on planes [z0, z1), then E on [z0-1, z1-1) -- E of a plane needs H_new of
  * the plane above, H of a plane needs E_old of the plane below, and both

@@ -152,6 +152,7 @@ P32 make_p32(const smat_fdtd_plan *p, bool xp);
 /* the launches of steps rel0 .. rel0+n-1 relative to *d_base (no bump) */
 void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp);
 void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel, cudaStream_t st);
+void enqueue_update(smat_fdtd_plan *p, int rel, cudaStream_t st);
 Pipe32 make_pipe(const smat_fdtd_plan *p);
 int setup_pipe(smat_fdtd_plan *p, int by, int lag);
 int pipe_nxw(int L0);

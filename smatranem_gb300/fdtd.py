@@ -412,7 +412,8 @@ class Group:
         self.close()
 
     def set_tuning(self, mode, block_y):
-        """mode 0: one grouped launch per sweep; 1: members' own launches."""
+        """mode 0: one grouped launch per sweep; 1: members' own sweep launches;
+        2: members' own launch forms (their set_tuning / autotune)."""
         _check(lib().smat_fdtd_group_set_tuning(self._h, mode, block_y))
 
     def autotune(self, nsteps=4):

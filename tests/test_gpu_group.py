@@ -1,7 +1,7 @@
 """Groups: structures of uneven size stepped together (smat_fdtd_group_*).
 
 Every member of a group must end bit-identical -- fields and DFT -- to the same
-plan stepped alone with the vectorised sweeps."""
+plan stepped alone with the vectorised sweeps, whatever the group's launch form."""
 import numpy as np
 import pytest
 
@@ -69,6 +69,45 @@ def test_group_members_match_plans_stepped_alone(built, mode, block_y):
             p.close()
 
 
+def test_group_members_own_launch_forms(built):
+    """Mode 2: every member in its own launch form -- the whole-row fused step
+    (kernel 6: chunked or persistent, with and without record cells) or the
+    sweeps -- gives the bits of the member stepped alone with the sweeps, over
+    run windows that leave the fused members on either field set."""
+    from smatranem_gb300 import fdtd as f
+    from smatranem_gb300 import workloads as W
+    nsteps = 60
+    windows = [(0, 20), (20, 53), (53, nsteps)]  # 33 steps: a captured 32-step chunk and one more
+    own = [(6, 2, 0, 1, 0), (6, 4, 7, 1, 0), (2, 1, 0, 0, 4), (6, 1, 0, 2, 0)]
+    structs = []
+    for L, seed, kw, iBTIin, batch in MEMBERS:
+        s = W.random_structure(L, seed=seed, **kw)
+        structs.append((s, W.prepare(s), iBTIin, batch, seed))
+    alone = []
+    for s, pr, iBTIin, batch, seed in structs:
+        with _setup(f, W, s, pr, iBTIin, batch, seed, nsteps) as p:
+            p.set_tuning(2, 1, 0, 0, 4)
+            for a, b in windows:
+                p.run(a, b)
+            alone.append(_result(p, batch))
+    plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
+    try:
+        for p, t in zip(plans, own):
+            p.set_tuning(*t)
+        with f.Group(plans) as g:
+            g.set_tuning(2, 1)
+            for a, b in windows:
+                g.run(a, b)
+        for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
+            got = _result(p, batch)
+            for rb, gb in zip(ref, got):
+                for a, b_ in zip(rb, gb):
+                    assert np.all(np.isfinite(a)) and np.array_equal(a, b_)
+    finally:
+        for p in plans:
+            p.close()
+
+
 def test_group_autotune_and_errors(built):
     from smatranem_gb300 import fdtd as f
     from smatranem_gb300 import workloads as W
@@ -83,7 +122,7 @@ def test_group_autotune_and_errors(built):
         p.set_schedule(src, planes=(iBTIin[0], iBTIin[1]), phase=ph)
         with f.Group([p]) as g:
             (mode, by), ms = g.autotune(2)
-            assert mode in (0, 1) and by in (1, 2, 4) and ms > 0
+            assert mode in (0, 1, 2) and by in (1, 2, 4) and ms > 0
             assert p.check_finite() == (True, 0.0)  # left at the zero state
             with pytest.raises(f.FdtdError):
                 g.run(0, src.shape[0] + 1)  # beyond the schedule
