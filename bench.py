@@ -17,8 +17,12 @@ of the batch.  Reported:
   fp64       the plain FP64 (bit-identical to the reference) kernel: Gcell/s
   s_cols     S-matrix columns per second of full 8000-step runs, FP32 batched
              and FP64 plain, and the max relative S-parameter error FP32 vs FP64
-  roofline   achieved HBM GB/s of the dominant kernel (the FP32 sweeps) from
-             algorithmic bytes / CUDA-event launch time, against MEASURED_PEAKS.json
+  roofline   achieved HBM GB/s of the dominant kernel (the fused FP32 step, or
+             the sweeps) from algorithmic bytes / CUDA-event launch time, against
+             MEASURED_PEAKS.json: per cell-update the 6 field components read and
+             written, the 6 per-cell coefficients and the aux slots of split cells
+             (87.6 B on this workload); beside it the compulsory traffic of the
+             batch, which reads the coefficient stream once for all excitations
   cpu_baseline  the CPU oracle (a restatement of the reference main_calc) on a
              bounded sample of the same workload on this host's cores
 
@@ -80,10 +84,18 @@ def launches_per_step(tuning, L2):
 
 
 def algorithmic_bytes_per_step(n3, n_split, batch, s_f=4, coef_bytes=24):
-    """Compulsory HBM traffic of one step: every field component read and
-    written once per excitation (12*s_f per cell), the per-cell coefficients
-    once per step (shared by the batch), the aux slot of split cells read and
-    written per excitation; sigma tables and DFT samples excluded."""
+    """Algorithmic bytes of one step, per cell-update: every field component
+    read and written (12*s_f), the per-cell coefficients (6 on a metric mesh,
+    coef_bytes), the aux slot of a split cell read and written (12*s_f, for the
+    N_split/N share of cells); sigma tables and DFT samples excluded.  Times N
+    cells and the batch's excitations."""
+    return batch * (n3 * (12 * s_f + coef_bytes) + n_split * 12 * s_f)
+
+
+def compulsory_bytes_per_step(n3, n_split, batch, s_f=4, coef_bytes=24):
+    """The same with the coefficient stream read once per step for the whole
+    batch (the excitations of a plan share it): the least traffic a step of
+    the batch can move."""
     return n3 * (12 * s_f * batch + coef_bytes) + n_split * 12 * s_f * batch
 
 
@@ -348,9 +360,11 @@ def run_ours(args):
     tuning = p32.get_tuning()
     per_step = launches_per_step(tuning, bend.s.L[2])
     bytes_step = algorithmic_bytes_per_step(n3, n_split, batch)
+    comp_step = compulsory_bytes_per_step(n3, n_split, batch)
     step_kernel_ms = kt[0] + kt[1]  # the update kernels of one step (DFT flush apart)
     launch_ms = step_kernel_ms / per_step
     achieved = bytes_step / (step_kernel_ms * 1e-3) / 1e9
+    achieved_comp = comp_step / (step_kernel_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     launches = per_step * args.steps + 2 * math.ceil(args.steps / 32) + 1
     # ---- full runs: S-matrix columns/s and the FP32-vs-FP64 S error -----
@@ -431,7 +445,12 @@ def run_ours(args):
                                 0: "k_sweep32 (H, E)"}[tuning[0]],
                      "tuning": {"kernel": tuning[0], "tile_y": tuning[1], "z_chunk": tuning[2],
                                 "ctas_per_sm": tuning[3], "slots": tuning[4]},
-                     "bytes_per_launch": bytes_step / per_step, "ms_per_launch": launch_ms,
+                     "bytes_per_launch": bytes_step / per_step,
+                     "bytes_per_cell_update": bytes_step / (n3 * batch),
+                     "compulsory": {"bytes_per_launch": comp_step / per_step, "achieved": achieved_comp,
+                                    "frac": achieved_comp / peak,
+                                    "what": "coefficient stream read once per step for all excitations"},
+                     "ms_per_launch": launch_ms,
                      "launches_per_step": per_step, "ms_per_step_kernels": step_kernel_ms,
                      "ms_dft_flush_per_step": kt[2]},
         "fp64_plain": {"value": fp64_rate, "unit": "Gcell-updates/s", "steps": args.steps64,
