@@ -25,11 +25,14 @@ def _plan(design: W.Design, eps, precision, nsteps, src, phase, mode, dt_factor)
 
 
 def objective_and_grad(design: W.Design, eps, *, precision=F.FP32, nsteps=6000, K=64, mode=None, src=None,
-                       phase=None, dt_factor=1.0 / 0.99):
-    """J = |overlap of the output-port DFT with `mode`|^2 and dJ/d eps_r (design box)."""
+                       phase=None, dt_factor=1.0 / 0.99, autotune=True):
+    """J = |overlap of the output-port DFT with `mode`|^2 and dJ/d eps_r (design box).
+    autotune: pick the FP32 forward's launch form (cached per grid and GPU)."""
     eps = np.asarray(eps, dtype=np.float64)
     p = _plan(design, eps, precision, nsteps, src, phase, mode, dt_factor)
     try:
+        if autotune and precision == F.FP32:
+            p.autotune(4)
         Hinc, Einc = mode
         t = np.concatenate([Hinc[0::2], Hinc[1::2], -Einc[1::2], Einc[0::2]])
         J, g, _ = p.adjoint_grad(nsteps, K, 0, 1, t, design.box)

@@ -1397,7 +1397,7 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
                 if (rows <= p->L[1] && lag <= L2) cands.push_back({4, rows, lag, 0, 0});
     /* whole-row fused step (plans without record cells) */
     if (p->L[0] % 4 == 0 && p->nrec_metal == 0 && p->nrec_split == 0)
-        for (int ty : {2, 4, 5})
+        for (int ty : {1, 2, 4, 5})
             for (int mb : {1, 2})
                 for (int zc : {0, L2, 40, 32, 24, 20})
                     if (zc <= L2 && !(zc < 48 && zc >= L2)) cands.push_back({6, ty, zc, mb, 0});

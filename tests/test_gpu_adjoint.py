@@ -57,10 +57,12 @@ def _objective(d, eps, precision, schedule):
     return abs(S) ** 2
 
 
-def _adjoint(d, eps, precision, schedule, K=64):
+def _adjoint(d, eps, precision, schedule, K=64, tuning=None):
     F, W = _mods()
     p, _, nsteps = _plan(d, eps, precision, schedule)
     with p:
+        if tuning:
+            p.set_tuning(*tuning)
         J, g, gc = p.adjoint_grad(nsteps, K, 0, 1, _column(W.mode_profiles(d, n_modes=1)[0]), d.box)
     return J, g / eps, gc
 
@@ -222,6 +224,19 @@ def test_vectorised_fp32_adjoint_matches_the_scalar_one(built, monkeypatch):
     Js, gs, _ = _adjoint(d, d.eps, F.FP32, "pulse")
     assert Jv == Js
     assert np.max(np.abs(gv - gs)) <= 1e-6 * np.max(np.abs(gs))
+
+
+@pytest.mark.parametrize("tuning", [(6, 2, 0, 1, 0), (6, 3, 7, 1, 0), (6, 1, 0, 2, 0)])
+def test_adjoint_with_the_fused_forward(built, tuning):
+    """The forward and the recompute from checkpoints in the whole-row fused
+    step (kernel 6: it swaps the field sets each step; persistent and chunked)
+    give the bits of the sweeps' forward: the same J and gradient."""
+    F, _ = _mods()
+    d = _design(pml_xy=True, shape=(24, 20, 28), design=(6, 5, 4), pml=6)
+    ref = _adjoint(d, d.eps, F.FP32, "pulse", K=7, tuning=(2, 1, 0, 0, 4))
+    got = _adjoint(d, d.eps, F.FP32, "pulse", K=7, tuning=tuning)
+    assert got[0] == ref[0]
+    assert np.array_equal(got[1], ref[1]) and np.array_equal(got[2], ref[2])
 
 
 def test_adjoint_with_a_column_per_excitation(built):
