@@ -5,10 +5,11 @@
  * Same update as the two FP32 sweeps of fdtd_f32.cu (the reference main_calc,
  * FDTDcalc/FDTDsplitfieldMetal.c:242-329, in total-field form), with the same
  * floating point expressions, so the results are bit-identical to them.  For
- * plans without record cells and with L0 % 4 == 0.
+ * plans with L0 % 4 == 0 and without stable-form metal or lossy split cells
+ * (lossy and PEC ordinary cells run a compile-time variant, REC).
  *
  *   - a CTA owns TY whole x rows (y0 .. y0+TY-1) of one excitation and marches
- *     along z through a chunk of planes [z0, z1).  At stage z it computes
+ *     along z through a range of planes [z0, z1).  At stage z it computes
  *     H_new(z) on its rows plus one halo row (y0+TY, recomputed, never stored),
  *     then E_new(z-1) on its rows, which needs H_new of planes z-1 and z: of
  *     plane z on its own column from registers, of plane z-1 (its own cells,
@@ -18,22 +19,23 @@
  *     march.  Each field value is read once and written once per step (48 B
  *     per cell and excitation, plus the coefficient stream and the aux slots
  *     of split cells): the compulsory traffic of a step, where the two sweeps
- *     move 72 B.
+ *     move 72 B.  Quads whose x index lies in a PML take the first threads, so
+ *     that the other warps run the ordinary update without the split branch.
  *   - the inputs of the next plane are in flight while the current one is
- *     computed: at stage z every thread issues cp.async copies of its quad's
- *     H-update inputs of plane z+1 (coefficients, H, E, H aux) and of the
- *     E-update inputs of plane z (coefficients, E aux; used at stage z+1) into
- *     double-buffered shared memory, so the stage barrier never waits on a
- *     DRAM round trip and no registers are held by loads in flight.  The y-1
- *     and x-1 neighbours of the H update come from the neighbouring threads'
- *     staged E (the first row also stages the E row above the tile).
+ *     computed: cp.async copies into shared memory of the next plane's E
+ *     (double-buffered: the neighbouring threads read it for the y-1 and x-1
+ *     terms; the first row also stages the E row above the tile), of the
+ *     thread's own bh, H, H aux of the next plane and be, E aux of this plane
+ *     (one slot each, refilled right after use), so the stage barrier does not
+ *     wait on a DRAM round trip and no registers are held by loads in flight.
  *   - whole rows: the x wrap is inside the row.
  *   - fields are double-buffered (read the current set, write the other), so
  *     the halo reads of a neighbouring CTA never see an advanced value.
- *   - the plane z1 closing a chunk: H_new(z1) is recomputed, not stored; at
+ *   - the plane z1 closing a range: H_new(z1) is recomputed, not stored; at
  *     z1 = L2 it is iBc_z * H_new(0), which is what the sweeps read through the
  *     wrapped z boundary (:334, :355); a wrapped halo row likewise holds
- *     iBc_y * H_new(row 0).
+ *     iBc_y * H_new(row 0).  Ranges are independent: fixed z chunks, one per
+ *     CTA, or persistent CTAs marching whole row tiles in rounds.
  */
 #include <cuda_runtime.h>
 
@@ -90,13 +92,6 @@ __device__ __forceinline__ float *row_ring(const Dft &d, int pl, int b, int k, i
     return d.ring + ((((long long)b * d.ringK + slot) * d.nq + q) * 4 + v) * (long long)pl;
 }
 
-/* The update of one quad -- H (EF = false) or E (EF = true) of cells x0..x0+3
- * of row j1, plane j2 -- in place in out (total field) and aux (split cells),
- * from the other field at the cells (gh), its y and z neighbours (gy0, gy2:
- * components 0 and 2 one row away; gz0, gz1: components 0 and 1 one plane
- * away, both already scaled by the boundary factor) and the outer x neighbour
- * of the quad (xn1, xn2: components 1 and 2).  The expressions of the
- * vectorised sweep (fdtd_f32.cu), element by element. */
 /* The 1-D split-PML factors A(sigma), G(sigma) of one field at a quad's four
  * x indices, its row and its plane, and the PML bits of the four x indices:
  * loaded once per thread (the plane's once per stage) instead of per element. */
@@ -126,6 +121,13 @@ __device__ __noinline__ void row_record(const P32 &p, const int k, const int b, 
     for (int c = 0; c < 3; c++) t[c] = fmaf(sg * r.B0[c], W[c], r.A0[c] * t[c]);
 }
 
+/* The update of one quad -- H (EF = false) or E (EF = true) of cells x0..x0+3
+ * of row j1, plane j2 -- in place in out (total field) and aux (split cells),
+ * from the other field at the cells (gh), its y and z neighbours (gy0, gy2:
+ * components 0 and 2 one row away; gz0, gz1: components 0 and 1 one plane
+ * away, both already scaled by the boundary factor) and the outer x neighbour
+ * of the quad (xn1, xn2: components 1 and 2).  The expressions of the
+ * vectorised sweep (fdtd_f32.cu), element by element. */
 template <bool EF, bool REC>
 __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b, const int j1, const int j2,
                                          const int x0, const bool on_src, const QuadTab &tq, const float4 c[3],
@@ -196,7 +198,6 @@ __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b,
     }
 }
 
-
 /* Shared memory (float4 units):
  *   es  [2][3][NC]       staged E of a plane (read by the neighbouring threads:
  *                        double-buffered, slot z & 1)
@@ -205,7 +206,7 @@ __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b,
  *   pe  [2][3][NC]       staged be, E aux of the plane whose E update is next
  *   top [2][2][NQ]       E components 0 and 2 of the row above the tile
  *   hs  [2][TY+1][3][NQ] H_new of the last two planes (the halo row last)
- *   the plane table of the chunk
+ *   the plane table of the plane range (PlaneInfo, 2 float4 a plane)
  * with NC = (TY+1) * NQ quads, quad q of tile row r at r * NQ + q.
  * cp.async groups, three a stage, in this order: E of plane z+1 (G1), bh/H/aux
  * of plane z+1 (G2, after the H update), be/E aux of plane z (G3, after the E
@@ -216,6 +217,8 @@ size_t row_smem_f4(int L0, int ty, int zc)
     return 21 * nc + 4 * nq + 6 * nc + 2 * (size_t)(zc + 1);
 }
 
+/* a 16-byte shared-memory load kept whole (lanes reading consecutive quads
+ * then access consecutive 16-byte words: no bank conflicts) */
 __device__ __forceinline__ float4 lds4(const float4 *a)
 {
     float4 v;
@@ -227,7 +230,7 @@ __device__ __forceinline__ float4 lds4(const float4 *a)
     return v;
 }
 
-/* per plane of a chunk: the 1-D split-PML factors of its z index (H: A, G;
+/* per plane of a range: the 1-D split-PML factors of its z index (H: A, G;
  * E: A, G), whether it lies in a PML and its monitor index (or -1) */
 struct PlaneInfo {
     float ah, gh, ae, ge;
