@@ -619,6 +619,78 @@ def run_group(args):
         p.close()
 
 
+def _cube_cpu_worker(args):
+    """One process: `nsteps` oracle main_calc steps of the 96^3 cube."""
+    nsteps, kind = args
+    import oracle
+    from smatranem_gb300 import workloads as W
+    c = W.cube_structure()
+    pr = W.prepare(c.s, dt_factor=1.0 / 0.99)
+    o = oracle.Oracle(kind)
+    Ah, Bh, Ae, Be = pr.coefficients()
+    cells = np.flatnonzero(c.s.pec)
+    for k in range(3):  # the PEC plate
+        Ae[3 * cells + k] = 0.0
+        Be[3 * cells + k] = 0.0
+    n3, pl = c.s.n3, c.s.L[0] * c.s.L[1]
+    H = np.zeros(3 * (n3 + pr.lnotn + 1))
+    E = np.zeros_like(H)
+    mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+    t0 = time.perf_counter()
+    o.time_loop(c.s.L, Ah, Bh, Ae, Be, c.s.iBc, H, E, (c.iM, c.iM, c.iI, 1), *W.point_source(c), pr.n2pi,
+                (1, 1, 3), 0, nsteps, *mons, pr.cont, pr.addr)
+    return time.perf_counter() - t0, n3 * nsteps
+
+
+def run_cube(args):
+    """The plain FP64 benchmark case: 96^3 cells in vacuum, a centred 30^3
+    block of eps 12.11, a 40x40 one-cell PEC plate 15 cells below it, 10-cell
+    split PML on all faces (grading 3, R = 1e-6), an x point source driven by a
+    Gaussian-modulated sine (1.55 um, 20 % bandwidth), 4000 steps at Courant
+    0.99/sqrt(3), running DFT at 11 wavelengths on one plane.  FP64 (bit-
+    identical to the reference loop) and FP32 (autotuned) on the GPU; the CPU
+    oracle (the reference loop restated) on a bounded sample of steps."""
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    c = W.cube_structure()
+    pr = W.prepare(c.s, dt_factor=1.0 / 0.99)
+    nsteps = args.cube_steps
+    lams = [float(x) for x in np.linspace(1.55 * 0.9, 1.55 * 1.1, 11)]
+    src, ph = W.pulse_schedule(nsteps, pr.dt, lam0_um=1.55, bandwidth=0.2, lams_um=lams)
+    Hinc, Einc = W.point_source(c)
+    res, dft = {}, {}
+    for prec, name in ((F.FP64, "fp64"), (F.FP32, "fp32")):
+        p = F.Plan.create(c.s.L, c.s.iBc, (c.iM, c.iM, c.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
+                          pr.sigma, precision=prec, batch=1, pec=c.s.pec)
+        tuning = list(p.autotune(4)[0]) if prec == F.FP32 else None
+        p.set_incident(0, Hinc, Einc)
+        p.set_schedule(src, planes=(c.iM,), phase=ph)
+        p.run(0, args.warmup)
+        _, t = _timed(lambda: p.run(args.warmup, nsteps))
+        dft[name] = np.array([p.get_dft(0, fi, 0) for fi in range(len(lams))])
+        res[name] = {"gcell_per_s": c.s.n3 * (nsteps - args.warmup) / t / 1e9,
+                     "ms_per_step": 1e3 * t / (nsteps - args.warmup), "tuning": tuning}
+        p.close()
+    err = float(np.max(np.abs(dft["fp32"] - dft["fp64"])) / np.max(np.abs(dft["fp64"])))
+    cpu = None
+    if not args.no_cpu:
+        kind = oracle_kind()
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(1) as pool:
+            t_cpu, cells = pool.map(_cube_cpu_worker, [(args.cpu_steps, kind)])[0]
+        cpu = {"value": cells / t_cpu / 1e9, "unit": "Gcell-updates/s", "cores": 1, "kind": kind,
+               "sample": f"{args.cpu_steps} main_calc steps of the 96^3 cube, {t_cpu:.1f} s on 1 core"}
+    print(json.dumps({
+        "mode": "cube", "config": "96^3 vacuum, 30^3 block eps 12.11, 40x40 PEC plate 15 cells below, 10-cell split "
+                                  "PML on 6 faces (R = 1e-6, grading 3), x point source, Gaussian-modulated sine "
+                                  "1.55 um / 20 %, Courant 0.99/sqrt(3), DFT at 11 wavelengths on one plane",
+        "cells": c.s.n3, "split_cells": pr.lnotn, "pec_cells": int(c.s.pec.sum()), "steps": nsteps,
+        "fp64": res["fp64"], "fp32": res["fp32"],
+        "dft_rel_err_fp32_vs_fp64": err, "fp64_bit_identical_to_reference": "tests/test_gpu_cube.py",
+        "cpu_baseline": cpu,
+    }))
+
+
 def run_large(args):
     """Large-domain throughput: 640x640x512 cells (~210M) in FP32, split PML,
     gently curved substrate (radius 50 um), PEC patch-array grating."""
@@ -749,10 +821,12 @@ def run_scalc(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", default="main", choices=["main", "adjoint", "group", "large", "modes", "scalc"],
+    ap.add_argument("--mode", default="main", choices=["main", "adjoint", "group", "large", "modes", "scalc",
+                                                       "cube"],
                     help="main: the contract line; the others: the adjoint, batched-structures and large-domain "
                          "workloads (one summary line each)")
     ap.add_argument("--adj-steps", type=int, default=6000)
+    ap.add_argument("--cube-steps", type=int, default=4000)
     ap.add_argument("--fd-cells", type=int, default=32)
     ap.add_argument("--group-seed", type=int, default=0)
     ap.add_argument("--gpus", type=int, default=1)
@@ -775,7 +849,7 @@ def main():
         run_profile(args)
     elif args.mode != "main":
         {"adjoint": run_adjoint, "group": run_group, "large": run_large, "modes": run_modes,
-         "scalc": run_scalc}[args.mode](args)
+         "scalc": run_scalc, "cube": run_cube}[args.mode](args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -442,6 +442,57 @@ def design_structure(shape=(160, 160, 120), design=(60, 60, 20), pml=12, seed=0,
     return d
 
 
+@dataclasses.dataclass
+class Cube:
+    s: Structure
+    iI: int          # source plane (the point source sits at pixel src_px of it)
+    iM: int          # monitor plane of the running DFT
+    src_px: int      # j0 + L0*j1 of the point source
+    pml: int
+
+
+def cube_structure(n=96, pml=10, cube=30, plate=40, gap=15, eps_cube=12.11, dx_um=0.02, lam0_um=1.55,
+                   reflection=1e-6, power=3) -> Cube:
+    """The plain FP64 benchmark case: n^3 uniform cells of dx_um in vacuum
+    (metric factor dx), a centred cube^3 dielectric block of eps_cube, a
+    one-cell-thick plate x plate PEC plate `gap` cells below the block, split
+    PML of `pml` cells on all six faces (polynomial grading `power`, normal
+    reflection `reflection`: the PML deck's squareRef is its square).  An x
+    point source (one pixel of the sheet source, driving E_x) on a plane above
+    the block; the monitor plane between the plate and the block."""
+    L0 = L1 = L2 = n
+    dx = dx_um / INV_K0_UM
+    n3 = n ** 3
+    j = np.indices((L2, L1, L0)).reshape(3, -1)[::-1]
+    c0 = (n - cube) // 2
+    in_cube = np.all([(j[a] >= c0) & (j[a] < c0 + cube) for a in range(3)], axis=0)
+    eps_r = np.where(in_cube, eps_cube, 1.0)
+    mu_r = np.full((n3, 3), dx)
+    eps3 = np.repeat(eps_r[:, None] * dx, 3, axis=1)
+    omega = 2 * math.pi * INV_K0_UM / lam0_um
+    sig = [pml_sigma(n, pml, pml, omega, pml * dx, pml * dx, reflection ** 2, power) for _ in range(3)]
+    mu_s, ep_s = stretch_media((L0, L1, L2), mu_r, eps3, sig)
+    min_dt = cfl_min_dt(mu_r, np.full((n3, 3), dx))
+    zp, p0 = c0 - gap, (n - plate) // 2
+    pec = ((j[2] == zp) & (j[0] >= p0) & (j[0] < p0 + plate) & (j[1] >= p0) & (j[1] < p0 + plate)).astype(np.uint8)
+    s = Structure(L=(L0, L1, L2, pml + 2), mu=mu_s, epsi=ep_s, omega=omega, min_dt=min_dt, iBc=(0, 0, 0), pec=pec,
+                  name=f"cube{n}")
+    iI = c0 + cube + (L2 - pml - (c0 + cube)) // 2
+    iM = zp + (c0 - zp) // 2
+    return Cube(s=s, iI=iI, iM=iM, src_px=n // 2 + L0 * (n // 2), pml=pml)
+
+
+def point_source(c: Cube):
+    """Sheet arrays (Hinc, Einc, 2*L0*L1 complex each) of the x point source:
+    the H-sheet component that drives E_x (W_0 += s * Hi_1 in the E step,
+    main_calc :293-296) is 1 at the source pixel, everything else 0."""
+    pl = c.s.L[0] * c.s.L[1]
+    Hinc = np.zeros(2 * pl, np.complex128)
+    Einc = np.zeros(2 * pl, np.complex128)
+    Hinc[1 + 2 * c.src_px] = 1.0
+    return Hinc, Einc
+
+
 def slab_structure(shape, seed=0, pml=12, slab_um=0.22, eps_slab=12.11, eps_clad=2.085,
                    eps_range=(2.085, 12.11), n_incl=(1, 6), dx_um=0.02, lam0_um=1.55, sq_ref=1e-12,
                    power=3) -> Bend:
