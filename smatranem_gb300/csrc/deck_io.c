@@ -961,7 +961,7 @@ int smat_scalc_main(int argc, char **argv)
     int rc = scalc_input(argv[1], prefix, bc, target, both, solv);
     double complex *meds = NULL, *xiB = NULL, *xiT = NULL, *S = NULL, *mu = NULL, *ep = NULL;
     if (!rc) { /* input_file1 :643-653 */
-        char name[BUF + 32], buf[BUF];
+        char name[2 * BUF + 32], buf[BUF];
         snprintf(name, sizeof name, "%s_Med%s.dat", prefix, target[0]);
         FILE *f = fopen(name, "r");
         if (!f) rc = smat_fail(SMAT_EINVAL, "open error!: open input-file1!");

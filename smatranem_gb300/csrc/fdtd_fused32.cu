@@ -787,7 +787,7 @@ __global__ void __launch_bounds__(256) k_fused32t(const __grid_constant__ Fused3
         const int X0 = tix * TX, Y0 = tiy * TY;
         const int w = min(TX, L0 - X0), h = min(TY, L1 - Y0);
         const int z0 = zci * f.zc, z1 = min(z0 + f.zc, L2);
-        const float *Eo = p.E + b * bs, *Ho = p.H + b * bs, *Hao = p.Ha + b * bs, *Eao = p.Ea + b * bs;
+        const float *Eo = p.E + b * bs, *Ho = p.H + b * bs, *Hao = p.Ha + b * bs;
         float *En = f.En + b * bs, *Hn = f.Hn + b * bs, *Han = f.Han + b * bs, *Ean = f.Ean + b * bs;
         const bool own = tx < w && ty < h;
         const int gx = X0 + tx, gy = Y0 + ty;
