@@ -333,19 +333,40 @@ __global__ void __launch_bounds__(128, 4) k_adj32v(const Geo g, const int batch,
     const long long oy = (long long)g.L0 * (EF ? (ey ? -(g.L1 - 1) : 1) : (ey ? g.L1 - 1 : -1));
     const long long oz = (long long)g.pl * (EF ? (ez ? -(g.L2 - 1) : 1) : (ez ? g.L2 - 1 : -1));
     const float fy = ey ? (float)g.bc[1] : 1.0f, fz = ez ? (float)g.bc[2] : 1.0f;
+    /* In a quad with no split cell psi equals phi: both start at zero and take
+     * the same coefficients (A- = A+, B- = B+) and the same source.  Such quads
+     * neither read nor write psi, and neighbours read their phi in its place;
+     * psi is kept (read and written) for quads with a split cell only. */
+    const bool pmx = cf.pmask[x0] | cf.pmask[x0 + 1] | cf.pmask[x0 + 2] | cf.pmask[x0 + 3];
+    const bool pmy = cf.pmask[cf.s1 + y], pmz = cf.pmask[cf.s2 + z];
+    const bool qsplit = pmx | pmy | pmz;
+    const int yn = EF ? (ey ? 0 : y + 1) : (ey ? g.L1 - 1 : y - 1);
+    const int zn = EF ? (ez ? 0 : z + 1) : (ez ? g.L2 - 1 : z - 1);
+    const bool ysplit = pmx | cf.pmask[cf.s1 + yn] | pmz, zsplit = pmx | pmy | cf.pmask[cf.s2 + zn];
     float4 cq[3], pf[3], qf[3], pg[3], qg[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         cq[c] = ldf4(cfs + c * n3 + l);
         pf[c] = ldf4(PF + c * n3 + l);
-        qf[c] = ldf4(QF + c * n3 + l);
         pg[c] = ldf4(PG + c * n3 + l);
-        qg[c] = ldf4(QG + c * n3 + l);
+    }
+    if (qsplit) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            qf[c] = ldf4(QF + c * n3 + l);
+            qg[c] = ldf4(QG + c * n3 + l);
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            qf[c] = pf[c];
+            qg[c] = pg[c];
+        }
     }
     /* y and z neighbours: EF reads psi_z, phi_x at y+1 and phi_y, psi_x at z+1;
      * the H transpose reads psi_z, phi_x at y-1 and phi_y, psi_x at z-1 */
-    float4 qyz = ldf4(QG + 2 * n3 + l + oy), pyx = ldf4(PG + 0 * n3 + l + oy);
-    float4 pzy = ldf4(PG + 1 * n3 + l + oz), qzx = ldf4(QG + 0 * n3 + l + oz);
+    float4 qyz = ldf4((ysplit ? QG : PG) + 2 * n3 + l + oy), pyx = ldf4(PG + 0 * n3 + l + oy);
+    float4 pzy = ldf4(PG + 1 * n3 + l + oz), qzx = ldf4((zsplit ? QG : PG) + 0 * n3 + l + oz);
     /* x neighbours: phi_z and psi_y at x+1 (EF) or x-1 */
     const unsigned full = 0xffffffffu;
     float xpz, xqy;
@@ -356,8 +377,10 @@ __global__ void __launch_bounds__(128, 4) k_adj32v(const Geo g, const int batch,
             const bool edge = x0 + 4 == g.L0;
             const long long ox = edge ? -(g.L0 - 4) : 4;
             const float f = edge ? (float)g.bc[0] : 1.0f;
+            const int xq = edge ? 0 : x0 + 4; /* the neighbouring quad */
+            const bool xsplit = pmy | pmz | cf.pmask[xq] | cf.pmask[xq + 1] | cf.pmask[xq + 2] | cf.pmask[xq + 3];
             xpz = f * PG[2 * n3 + l + ox];
-            xqy = f * QG[1 * n3 + l + ox];
+            xqy = f * (xsplit ? QG : PG)[1 * n3 + l + ox];
         }
     } else {
         xpz = __shfl_up_sync(full, pg[2].w, 1);
@@ -366,13 +389,15 @@ __global__ void __launch_bounds__(128, 4) k_adj32v(const Geo g, const int batch,
             const bool edge = x0 == 0;
             const long long ox = edge ? g.L0 - 1 : -1;
             const float f = edge ? (float)g.bc[0] : 1.0f;
+            const int xq = edge ? g.L0 - 4 : x0 - 4; /* the neighbouring quad */
+            const bool xsplit = pmy | pmz | cf.pmask[xq] | cf.pmask[xq + 1] | cf.pmask[xq + 2] | cf.pmask[xq + 3];
             xpz = f * PG[2 * n3 + l + ox];
-            xqy = f * QG[1 * n3 + l + ox];
+            xqy = f * (xsplit ? QG : PG)[1 * n3 + l + ox];
         }
     }
     if (!live) return;
     const float fx_in = 1.0f;
-    const bool pyzm = cf.pmask[cf.s1 + y] | cf.pmask[cf.s2 + z];
+    const bool pyzm = pmy | pmz;
     float gs[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     if (z == o.zq) {
 #pragma unroll
@@ -422,9 +447,10 @@ __global__ void __launch_bounds__(128, 4) k_adj32v(const Geo g, const int batch,
         }
     }
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        stf4(PF + c * n3 + l, pf[c]);
-        stf4(QF + c * n3 + l, qf[c]);
+    for (int c = 0; c < 3; c++) stf4(PF + c * n3 + l, pf[c]);
+    if (qsplit) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) stf4(QF + c * n3 + l, qf[c]);
     }
 }
 
