@@ -216,10 +216,10 @@ int smat_overlap(int npix, int ncols, int nvec, long long vec_stride, const doub
                  const double *dft, double *S, void *stream);
 
 /* No counterpart in the reference.  smat_overlap without any device
- * allocation, for callers that must not allocate at this point: inside a
- * stream capture that may not contain allocation nodes, under a framework that
- * owns the device's memory pool, or in a loop that must not fail on memory
- * after start-up.  The block partial sums go to a static device array of
+ * allocation, for callers that must not allocate at this point: a host
+ * process whose device memory pool belongs to a framework that forbids other
+ * code to call cudaMalloc, or a long-running loop that must not fail on
+ * memory after start-up.  The block partial sums go to a static device array of
  * SMAT_OVERLAP_NOALLOC_MAX complex doubles (1 MiB, held on every device that
  * loads the library until exit); a call needing more (ncols * nvec * blocks,
  * blocks <= 64 and about 4*npix/1024) fails with SMAT_EINVAL before launching.

@@ -170,10 +170,9 @@ extern "C" int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, 
  * Allocation-free variant of smat_overlap.
  *
  * Some callers cannot allocate device memory while they extract S parameters:
- * code that runs inside a stream capture that must not contain allocation
- * nodes, a host process whose memory pool is reserved by a framework that
- * owns the device (and forbids others to call cudaMalloc/cudaMallocAsync), or
- * a real-time loop that must not risk an allocation failure after start-up.
+ * a host process whose memory pool is reserved by a framework that owns the
+ * device (and forbids others to call cudaMalloc/cudaMallocAsync), or a
+ * real-time loop that must not risk an allocation failure after start-up.
  * smat_overlap_noalloc does the same projection with its block partial sums in
  * a fixed device array that lives in this library's module, so it never
  * allocates.  The array holds SMAT_OVERLAP_NOALLOC_MAX complex partial sums

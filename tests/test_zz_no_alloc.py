@@ -1,8 +1,8 @@
 """The allocation-free S extraction, smat_overlap_noalloc, through the C ABI.
 
 For callers that cannot allocate device memory when they extract S
-parameters (inside a stream capture, under a framework that owns the memory
-pool, in a loop that must not fail on memory after start-up).  Checked against
+parameters (under a framework that owns the device's memory pool, in a loop
+that must not fail on memory after start-up).  Checked against
 smat_overlap, the allocating entry point, on the same device inputs, on two
 calls in a row (the static scratch keeps the previous call's contents), with
 the tolerance the overlap tests use (1e-12 relative).  Runs last so that a run
