@@ -139,6 +139,19 @@ int smat_fdtd_info(const smat_fdtd_plan *plan, int L[4], int *Lnotn, int *precis
 int smat_fdtd_set_fields(smat_fdtd_plan *plan, int b, const double *H_t, const double *E_t);
 int smat_fdtd_get_fields(smat_fdtd_plan *plan, int b, double *H_t, double *E_t);
 
+/* Checkpoint and resume.  No counterpart in the reference (its FDTD state is
+ * never written).  save_state writes the plan's state -- the fields and aux
+ * slots of every excitation and the running-DFT accumulators -- to a binary
+ * file, exactly as held on the device; load_state restores it into a plan of
+ * the same grid, precision, batch, split-cell count and DFT setup (refused
+ * with SMAT_EINVAL otherwise), after which run(k, ...) continues from step k
+ * with the bits an uninterrupted run would give (FP32: with the same launch
+ * form; another form gives the same fields and DFT sums grouped differently,
+ * equal to rounding).  Call them between runs (an FP32 run leaves no DFT
+ * samples pending). */
+int smat_fdtd_save_state(smat_fdtd_plan *plan, const char *path);
+int smat_fdtd_load_state(smat_fdtd_plan *plan, const char *path);
+
 /* One step with explicit sheet sources (main_calc's Hi, Ei: 2*L0*L1 doubles,
  * shared by every excitation) and DFT phases ExpN2 (2 complex).  Accumulates
  * the reference DFT (frequency slot 0 on planes iB, iT). */

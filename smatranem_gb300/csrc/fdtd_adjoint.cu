@@ -41,6 +41,7 @@
 #include <cstring>
 #include <vector>
 
+#include "trace.cuh"
 #include "plan_internal.cuh"
 
 using namespace smat;
@@ -578,17 +579,20 @@ int adjoint_run(smat_fdtd_plan *p, const C &coef, int nsteps, int K, int f, int 
 
     /* ---- forward pass from rest, checkpoint every K steps ---- */
     if ((rc = zero_state(p))) return rc;
-    for (int j = 0; j < nseg; j++) {
-        sv = state_view(p);
-        size_t off = ck_bytes * j;
-        for (int i = 0; i < 4; i++) {
-            CK(cudaMemcpyAsync(ckpt + off, sv.ptr[i], sv.bytes[i], cudaMemcpyDeviceToDevice, p->stream));
-            off += sv.bytes[i];
+    {
+        smat::TraceRange trace_fwd("adjoint: forward with checkpoints");
+        for (int j = 0; j < nseg; j++) {
+            sv = state_view(p);
+            size_t off = ck_bytes * j;
+            for (int i = 0; i < 4; i++) {
+                CK(cudaMemcpyAsync(ckpt + off, sv.ptr[i], sv.bytes[i], cudaMemcpyDeviceToDevice, p->stream));
+                off += sv.bytes[i];
+            }
+            const int k0 = j * K, k1 = k0 + K < nsteps ? k0 + K : nsteps;
+            if ((rc = smat_fdtd_run(p, k0, k1))) return rc;
         }
-        const int k0 = j * K, k1 = k0 + K < nsteps ? k0 + K : nsteps;
-        if ((rc = smat_fdtd_run(p, k0, k1))) return rc;
+        if ((rc = smat_fdtd_sync(p))) return rc;
     }
-    if ((rc = smat_fdtd_sync(p))) return rc;
 
     /* ---- objective and its sensitivity to the DFT samples ---- */
     const int zq = p->planes[q];
@@ -623,6 +627,7 @@ int adjoint_run(smat_fdtd_plan *p, const C &coef, int nsteps, int K, int f, int 
     CK(cudaMemcpyAsync(dad, adh.data(), adh.size() * 8, cudaMemcpyHostToDevice, p->stream));
 
     /* ---- backward pass: per segment, recompute then adjoint ---- */
+    smat::TraceRange trace_bwd("adjoint: recompute and backward");
     const Geo g = make_geo(p);
     const Obj o{zq, f, p->nfreq, p->d_phase, dad};
     const AState<T> as{phiH, psiH, phiE, psiE};

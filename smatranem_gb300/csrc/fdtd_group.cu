@@ -22,6 +22,7 @@
 #include <mutex>
 #include <vector>
 
+#include "trace.cuh"
 #include "plan_internal.cuh"
 
 using namespace smat;
@@ -219,6 +220,7 @@ extern "C" int smat_fdtd_group_set_tuning(smat_fdtd_group *g, int mode, int bloc
 
 extern "C" int smat_fdtd_group_run(smat_fdtd_group *g, int k_begin, int k_end)
 {
+    smat::TraceRange trace_("smat_fdtd_group_run");
     smat_clear_error();
     if (!g || k_begin < 0 || k_end < k_begin) return smat_fail(SMAT_EINVAL, "group_run: bad step range");
     for (size_t i = 0; i < g->m.size(); i++) {

@@ -15,6 +15,7 @@
 
 #include <mutex>
 
+#include "trace.cuh"
 #include "fdtd_internal.cuh"
 #include "host_internal.h"
 #include "smatran_fdtd.h"
@@ -134,6 +135,7 @@ extern "C" int smat_fdtd_dft_device(smat_fdtd_plan *plan, int b, int f, int q, c
 extern "C" int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, const double *tilXi_host,
                                  double *S_host)
 {
+    smat::TraceRange trace_("smat_fdtd_overlap");
     smat_clear_error();
     const double *acc = nullptr;
     long long fstride = 0;

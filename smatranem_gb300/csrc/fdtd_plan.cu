@@ -18,6 +18,7 @@
 #include <cstring>
 #include <vector>
 
+#include "trace.cuh"
 #include "plan_internal.cuh"
 
 using namespace smat;
@@ -851,6 +852,7 @@ int finish_create(smat_fdtd_plan *p, int rc, smat_fdtd_plan **out)
 
 extern "C" int smat_fdtd_create(const smat_fdtd_desc *d, void *stream, smat_fdtd_plan **out)
 {
+    smat::TraceRange trace_("smat_fdtd_create");
     smat_clear_error();
     if (!d || !out || !d->mu || !d->epsi || !d->sigma) return smat_fail(SMAT_EINVAL, "create: null argument");
     *out = nullptr;
@@ -1156,6 +1158,7 @@ extern "C" int smat_fdtd_step(smat_fdtd_plan *p, const double *Hi, const double 
 
 extern "C" int smat_fdtd_run(smat_fdtd_plan *p, int k_begin, int k_end)
 {
+    smat::TraceRange trace_("smat_fdtd_run");
     smat_clear_error();
     if (!p || k_begin < 0 || k_end < k_begin) return smat_fail(SMAT_EINVAL, "run: bad step range");
     if (!p->d_sched) return smat_fail(SMAT_ESTATE, "run: no schedule (call set_cw_schedule or set_schedule)");
@@ -1357,6 +1360,7 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
  * so a plan whose fields are all zero is left exactly as it was. */
 extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], double *best_ms)
 {
+    smat::TraceRange trace_("smat_fdtd_autotune");
     smat_clear_error();
     if (!p || nsteps < 1) return smat_fail(SMAT_EINVAL, "autotune: bad arguments");
     if (p->precision != SMAT_FP32) {
@@ -1627,5 +1631,120 @@ extern "C" int smat_main_calc(const int L[4], const double *Ah, const double *Bh
     if (!rc) rc = smat_fdtd_get_fields(p, 0, H_t, E_t);
     if (!rc) rc = smat_fdtd_get_monitor(p, 0, HB, EB, HT, ET);
     smat_fdtd_destroy(p);
+    return rc;
+}
+
+/* ---- checkpoint and resume ------------------------------------------------ */
+
+namespace {
+
+struct StateHeader {
+    char magic[8];
+    int32_t version, precision, batch, L[4], lnotn, nfreq, nq;
+    int32_t cur; /* FP32: the field set that holds the state */
+    int32_t reserved[4];
+};
+
+constexpr char STATE_MAGIC[8] = {'S', 'M', 'A', 'T', 'S', 'T', 'A', 'T'};
+
+/* the device arrays that hold a plan's state, in file order */
+std::vector<std::pair<void *, size_t>> state_arrays(smat_fdtd_plan *p)
+{
+    std::vector<std::pair<void *, size_t>> a;
+    const size_t b = (size_t)p->batch, n3 = (size_t)p->n3;
+    if (p->precision == SMAT_FP64) {
+        const size_t main = b * 3 * n3 * 8, aux = b * 3 * ((size_t)p->lnotn + 1) * 8;
+        a.push_back({p->d_H64, main});
+        a.push_back({p->d_E64, main});
+        a.push_back({p->d_Ha64, aux});
+        a.push_back({p->d_Ea64, aux});
+    } else {
+        const P32 q = make_p32(p, false);
+        const size_t f = b * 3 * n3 * 4;
+        a.push_back({q.H, f});
+        a.push_back({q.E, f});
+        a.push_back({q.Ha, f});
+        a.push_back({q.Ea, f});
+    }
+    if (p->d_acc && p->nq > 0 && p->nfreq > 0)
+        a.push_back({p->d_acc, b * (size_t)p->nfreq * p->nq * 4 * (size_t)p->pl * 16});
+    return a;
+}
+
+void fill_header(const smat_fdtd_plan *p, StateHeader &h)
+{
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, STATE_MAGIC, 8);
+    h.version = 1;
+    h.precision = p->precision;
+    h.batch = p->batch;
+    for (int i = 0; i < 4; i++) h.L[i] = p->L[i];
+    h.lnotn = p->lnotn;
+    h.nfreq = p->d_acc ? p->nfreq : 0;
+    h.nq = p->d_acc ? p->nq : 0;
+    h.cur = p->precision == SMAT_FP32 ? p->cur : 0;
+}
+
+} // namespace
+
+extern "C" int smat_fdtd_save_state(smat_fdtd_plan *p, const char *path)
+{
+    smat_clear_error();
+    if (!p || !path) return smat_fail(SMAT_EINVAL, "save_state: bad arguments");
+    CK(cudaStreamSynchronize(p->stream));
+    StateHeader h;
+    fill_header(p, h);
+    FILE *f = fopen(path, "wb");
+    if (!f) return smat_fail(SMAT_EINVAL, "save_state: cannot open %s", path);
+    int rc = fwrite(&h, sizeof h, 1, f) == 1 ? SMAT_OK : smat_fail(SMAT_EINVAL, "save_state: write error");
+    std::vector<char> buf;
+    for (const auto &a : state_arrays(p)) {
+        if (rc) break;
+        buf.resize(a.second);
+        if (cudaMemcpy(buf.data(), a.first, a.second, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = cuda_fail(cudaGetLastError(), "save_state: copy");
+            break;
+        }
+        if (fwrite(buf.data(), 1, a.second, f) != a.second) rc = smat_fail(SMAT_EINVAL, "save_state: write error");
+    }
+    if (fclose(f) != 0 && !rc) rc = smat_fail(SMAT_EINVAL, "save_state: write error");
+    return rc;
+}
+
+extern "C" int smat_fdtd_load_state(smat_fdtd_plan *p, const char *path)
+{
+    smat_clear_error();
+    if (!p || !path) return smat_fail(SMAT_EINVAL, "load_state: bad arguments");
+    CK(cudaStreamSynchronize(p->stream));
+    FILE *f = fopen(path, "rb");
+    if (!f) return smat_fail(SMAT_EINVAL, "load_state: cannot open %s", path);
+    StateHeader h, want;
+    fill_header(p, want);
+    int rc = SMAT_OK;
+    if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, STATE_MAGIC, 8) != 0 || h.version != 1)
+        rc = smat_fail(SMAT_EINVAL, "load_state: %s is not a state file", path);
+    else if (h.precision != want.precision || h.batch != want.batch || memcmp(h.L, want.L, sizeof h.L) != 0 ||
+             h.lnotn != want.lnotn || h.nfreq != want.nfreq || h.nq != want.nq)
+        rc = smat_fail(SMAT_EINVAL, "load_state: %s holds another plan's state (grid, precision, batch, split "
+                                    "cells or DFT setup differ)", path);
+    else if (h.cur != 0 && h.cur != 1)
+        rc = smat_fail(SMAT_EINVAL, "load_state: %s is not a state file", path);
+    /* FP32: into the field set it was saved from, so that a run continues with
+     * the same set parity (and so the same grouping of the DFT ring's sums) */
+    if (!rc && p->precision == SMAT_FP32) p->cur = h.cur;
+    std::vector<char> buf;
+    for (const auto &a : state_arrays(p)) {
+        if (rc) break;
+        buf.resize(a.second);
+        if (fread(buf.data(), 1, a.second, f) != a.second) {
+            rc = smat_fail(SMAT_EINVAL, "load_state: %s is truncated", path);
+            break;
+        }
+        if (cudaMemcpy(a.first, buf.data(), a.second, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = cuda_fail(cudaGetLastError(), "load_state: copy");
+    }
+    if (!rc && fgetc(f) != EOF) rc = smat_fail(SMAT_EINVAL, "load_state: %s has trailing data", path);
+    fclose(f);
+    if (!rc) drop_graph(p);
     return rc;
 }

@@ -48,6 +48,7 @@
 
 #include "host_internal.h"
 #include "smatran_fdtd.h"
+#include "trace.cuh"
 
 namespace {
 
@@ -848,6 +849,7 @@ extern "C" int smat_mode_apply(int L0, int L1, const int BoundC[2], double omega
 extern "C" int smat_mode_solve(int L0, int L1, const int BoundC[2], double omega, const double *med, int nmodes,
                                const smat_mode_opts *opts, double *theta, double *Xi, smat_mode_info *info)
 {
+    smat::TraceRange trace_("smat_mode_solve");
     const auto t_start = std::chrono::steady_clock::now();
     std::vector<double> V;
     int rc = check_media(L0, L1, BoundC, omega, med, V);

@@ -26,6 +26,7 @@
 #include "dense_z.cuh"
 #include "host_internal.h"
 #include "smatran_fdtd.h"
+#include "trace.cuh"
 
 namespace {
 
@@ -321,6 +322,7 @@ extern "C" int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int
                           const double *XiB, int nB, const double *XiT, int nT, int both_ways, double *S,
                           smat_scalc_info *info)
 {
+    smat::TraceRange trace_("smat_scalc");
     const auto t0 = std::chrono::steady_clock::now();
     if (L0 <= 0 || L1 <= 0 || (long long)L0 * L1 > 8192)
         return smat_fail(SMAT_EINVAL, "smat_scalc: lattice %d x %d (dense transfer: 2*L0*L1 <= 16384)", L0, L1);

@@ -56,6 +56,8 @@ def lib():
         L.smat_fdtd_create.argtypes = [_P, _P, _P]
         L.smat_fdtd_create_from_coeffs.argtypes = [_P] * 8 + [C.c_int, _P, C.c_int, _P, _P]
         L.smat_fdtd_set_fields.argtypes = [_P, C.c_int, _P, _P]
+        L.smat_fdtd_save_state.argtypes = [_P, C.c_char_p]
+        L.smat_fdtd_load_state.argtypes = [_P, C.c_char_p]
         L.smat_fdtd_get_fields.argtypes = [_P, C.c_int, _P, _P]
         L.smat_fdtd_set_incident.argtypes = [_P, C.c_int, _P, _P]
         L.smat_fdtd_set_cw_schedule.argtypes = [_P, C.c_int, _P]
@@ -317,6 +319,15 @@ class Plan:
         ms = np.zeros(3)
         _check(lib().smat_fdtd_time_kernels(self._h, k_begin, nsteps, _ptr(ms)))
         return ms
+
+    def save_state(self, path):
+        """Fields, aux slots and DFT accumulators to a file (smat_fdtd_save_state)."""
+        _check(lib().smat_fdtd_save_state(self._h, os.fsencode(path)))
+
+    def load_state(self, path):
+        """Restore a state saved from a plan of the same setup (smat_fdtd_load_state);
+        run(k, ...) then continues from step k."""
+        _check(lib().smat_fdtd_load_state(self._h, os.fsencode(path)))
 
     def set_tuning(self, fused=1, tile_y=8, z_chunk=40, ctas_per_sm=0, slots=5):
         _check(lib().smat_fdtd_set_tuning(self._h, fused, tile_y, z_chunk, ctas_per_sm, slots))

@@ -601,3 +601,51 @@ def test_degenerate_grids(built, port, case):
         for rb, gb in zip(ref, got):
             for a, b_ in zip(rb, gb):
                 assert np.array_equal(a, b_), tuning
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32"])
+def test_checkpoint_and_resume(built, tmp_path, precision):
+    """save_state after a run, then a new plan of the same setup (and FP32
+    launch form) that loads it continues with the bits of the uninterrupted
+    run (fields, aux slots and the DFT); a plan of another setup refuses the
+    file."""
+    from smatranem_gb300 import workloads as W
+    f = _fdtd()
+    L, seed, kw, iBTIin = FUSED_CASES[1]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    prec = getattr(f, precision)
+    n3, pl = s.n3, L[0] * L[1]
+    src, ph = f.cw_schedule(pr.n2pi, (1, 1, 3))
+
+    def plan(batch=2):
+        p = f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=prec,
+                          batch=batch, pec=s.pec)
+        for b in range(batch):
+            p.set_incident(b, *W.random_incident(pl, seed=50 + b))
+            p.set_source_plane(b, iBTIin[2] + b, 1 - 2 * b)
+        p.set_schedule(src, planes=(iBTIin[0], iBTIin[1], 0), phase=ph)
+        return p
+
+    path = str(tmp_path / "state.bin")
+    with plan() as p:
+        if prec == f.FP32:
+            p.set_tuning(6, 2, 0, 1, 0)  # the fused step, which swaps field sets every step
+        for b in range(2):
+            p.set_fields(b, *W.random_fields(n3, pr.lnotn, seed=60 + b, scale=1e-2))
+        p.run(0, 25)
+        p.save_state(path)
+        p.run(25, 60)
+        ref = [(*p.get_fields(b), *[p.get_dft(b, 0, q) for q in range(3)]) for b in range(2)]
+    with plan() as p:
+        if prec == f.FP32:
+            p.set_tuning(6, 2, 0, 1, 0)  # the same launch form: the same DFT sum grouping
+        p.load_state(path)
+        p.run(25, 60)
+        got = [(*p.get_fields(b), *[p.get_dft(b, 0, q) for q in range(3)]) for b in range(2)]
+    for rb, gb in zip(ref, got):
+        for a, b_ in zip(rb, gb):
+            assert np.array_equal(a, b_)
+    with plan(batch=1) as p:
+        with pytest.raises(f.FdtdError):
+            p.load_state(path)
