@@ -361,10 +361,12 @@ int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double
  *   kernel 5: one fused launch per step on 128 x 4 tiles with a TMA producer
  *             warp (L0 % 4 == 0, iBc = 0 on every axis); z_chunk planes per item.
  *   kernel 6: one fused launch per step; a CTA marches tile_y whole x rows
- *             along z through z_chunk planes, four cells a thread, the next
- *             plane's inputs staged by cp.async; ctas_per_sm is its register
- *             bound (1..3 resident CTAs per SM); for plans with L0 % 4 == 0
- *             and no record cells (no lossy, PEC or stable-form metal cells).
+ *             along z through z_chunk planes (0: persistent CTAs), four cells
+ *             a thread, the next plane's inputs staged by cp.async;
+ *             ctas_per_sm is its register bound (1..3 resident CTAs per SM);
+ *             slots is not used; for plans with L0 % 4 == 0 and no
+ *             stable-form metal or lossy split cells (lossy and PEC ordinary
+ *             cells run an out-of-line record update).
  * Results are bit-identical across configurations. */
 int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int kernel, int tile_y, int z_chunk, int ctas_per_sm,
                          int slots);

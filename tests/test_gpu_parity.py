@@ -464,6 +464,25 @@ def test_row_fused_refuses_metal_cells(built):
             p.set_tuning(6, 2, 4, 1, 0)
 
 
+def test_row_fused_refuses_bad_tunings(built):
+    """Kernel 6's arguments out of range are refused and leave the plan's
+    launch form as it was."""
+    from smatranem_gb300 import workloads as W
+    f = _fdtd()
+    L, seed, kw, iBTIin = ROW_CASES[0]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                       precision=f.FP32) as p:
+        p.set_tuning(6, 2, 0, 1, 0)
+        assert tuple(p.get_tuning())[:4] == (6, 2, 0, 1)
+        for bad in [(6, 0, 0, 1, 0), (6, 17, 0, 1, 0), (6, 2, -1, 1, 0), (6, 2, 0, 0, 0), (6, 2, 0, 4, 0),
+                    (6, 200, 0, 1, 0), (7, 2, 0, 1, 0), (-1, 2, 0, 1, 0)]:
+            with pytest.raises(f.FdtdError):
+                p.set_tuning(*bad)
+            assert tuple(p.get_tuning())[:4] == (6, 2, 0, 1)
+
+
 def test_fused_fp32_within_tolerance_of_fp64_long_run(built):
     """A 300-step run with PML on all faces: FP32 (fused) vs the FP64 plan."""
     f = _fdtd()
