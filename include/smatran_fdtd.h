@@ -380,6 +380,16 @@ int smat_fdtd_get_tuning(const smat_fdtd_plan *plan, int out[5]);
  * plan is left unchanged apart from its configuration.  FP64: no-op. */
 int smat_fdtd_autotune(smat_fdtd_plan *plan, int nsteps, int best[5], double *best_ms);
 
+/* The work partition of launch form 6, run on the host: the pieces {row
+ * tile, z0, z1} (planes [z0, z1) of rows tile*tile_y ..) that CTA group gidx
+ * of every excitation marches on an L1 x L2 (rows x planes) grid, with
+ * z_chunk planes per item (gidx = item, row tile fastest) or persistent
+ * groups (z_chunk = 0, ngroups groups).  Up to max_pieces triples into out,
+ * their count in *n.  Needs no GPU: a check that the pieces of all groups
+ * cover every cell exactly once (no two CTAs write one cell). */
+int smat_row32_pieces(int L1, int L2, int tile_y, int z_chunk, int ngroups, int gidx, int *out, int max_pieces,
+                      int *n);
+
 /* Name, SM count and compute capability (major*10+minor) of the current device. */
 int smat_device_info(char *name, int name_len, int *sm_count, int *cc);
 

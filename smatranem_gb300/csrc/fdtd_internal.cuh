@@ -154,6 +154,51 @@ struct Fused32T {
 
 /* launch form 6: the fused step over whole x rows (fdtd_row32.cu); reads the
  * field set in p, writes the other set */
+/* The work of one CTA of launch form 6 (excitation aside): pieces (row tile yt,
+ * planes [z0, z1)).  With z chunks (zc > 0) one piece, item gidx = row tile
+ * fastest, then z chunk.  Persistent (zc == 0): ngroups groups of one CTA per
+ * excitation; group gidx takes row tile round * ngroups + gidx, whole, in each
+ * full round (adjacent tiles run together, so their halo rows are read from
+ * L2), then an equal share of the planes of the tiles left over.  Shared by the
+ * kernel and the host's check of the partition (smat_row32_pieces). */
+struct RowPieces {
+    int G, R; /* groups, full rounds */
+    long long u, uhi;
+    int round;
+    bool first;
+    __host__ __device__ RowPieces(int nyt, int L2, int zc, int ngroups, int gidx)
+        : G(ngroups > 0 ? ngroups : 1), R(zc > 0 ? 0 : nyt / (ngroups > 0 ? ngroups : 1)), round(0), first(true)
+    {
+        const long long lrem = (long long)(nyt - R * G) * L2;
+        u = (long long)gidx * lrem / G;
+        uhi = (long long)(gidx + 1) * lrem / G;
+    }
+    /* the next piece, or false; nyt, L2, zc and gidx as given to the constructor */
+    __host__ __device__ bool next(int nyt, int L2, int zc, int gidx, int &yt, int &z0, int &z1)
+    {
+        if (zc > 0) {
+            if (!first) return false;
+            yt = gidx % nyt;
+            z0 = gidx / nyt * zc;
+            z1 = z0 + zc < L2 ? z0 + zc : L2;
+        } else if (round < R) {
+            yt = round * G + gidx;
+            z0 = 0;
+            z1 = L2;
+            round++;
+        } else if (u < uhi) {
+            yt = R * G + (int)(u / L2);
+            z0 = (int)(u % L2);
+            z1 = (int)(L2 < z0 + (uhi - u) ? L2 : z0 + (uhi - u));
+            u += z1 - z0;
+        } else {
+            return false;
+        }
+        first = false;
+        return true;
+    }
+};
+
 struct Row32 {
     P32 p;
     float *Hn, *En, *Han, *Ean; /* new set */

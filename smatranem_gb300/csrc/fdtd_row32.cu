@@ -40,6 +40,8 @@
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.cuh"
+#include "host_internal.h"
+#include "smatran_fdtd.h"
 
 namespace smat {
 namespace {
@@ -301,41 +303,11 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
     const bool pmx = th.xm != 0;
     const int iIb = p.s.iI[b]; /* the excitation's source plane */
 
-    /* The work of this CTA: pieces (row tile yt, planes [z0, z1)) of
-     * excitation b.  With z chunks (r.zc > 0) one piece per CTA: item gidx =
-     * row tile fastest, then z chunk.  Persistent (r.zc == 0): r.ngroups
-     * groups of one CTA per excitation; group gidx takes row tile
-     * round * ngroups + gidx, whole, in each full round (adjacent tiles run
-     * together, so their halo rows are read from L2), then an equal share of
-     * the planes of the tiles left over. */
-    const int G = r.ngroups > 0 ? r.ngroups : 1;
-    const int R = r.zc > 0 ? 0 : r.nyt / G;
-    const long long lrem = (long long)(r.nyt - R * G) * L2;
-    long long u = (long long)gidx * lrem / G;
-    const long long uhi = (long long)(gidx + 1) * lrem / G;
-    int round = 0;
-    bool first = true;
+    /* the pieces (row tile yt, planes [z0, z1)) of excitation b this CTA marches */
+    RowPieces work(r.nyt, L2, r.zc, r.ngroups, gidx);
     for (;;) {
         int yt, z0, z1;
-        if (r.zc > 0) {
-            if (!first) break;
-            yt = gidx % r.nyt;
-            z0 = gidx / r.nyt * r.zc;
-            z1 = min(z0 + r.zc, L2);
-        } else if (round < R) {
-            yt = round * G + gidx;
-            z0 = 0;
-            z1 = L2;
-            round++;
-        } else if (u < uhi) {
-            yt = R * G + (int)(u / L2);
-            z0 = (int)(u % L2);
-            z1 = (int)min((long long)L2, z0 + (uhi - u));
-            u += z1 - z0;
-        } else {
-            break;
-        }
-        first = false;
+        if (!work.next(r.nyt, L2, r.zc, gidx, yt, z0, z1)) break;
         const int Y0 = yt * TY, h = min(TY, L1 - Y0);
         /* this thread's row: own rows 0..h-1, rows h..TY-1 idle (a partial last
          * tile), row TY the halo row y0+h */
@@ -582,6 +554,39 @@ const void *row_kernel(int threads, int mb, bool rec)
 } // namespace
 
 int row32_threads(int L0, int ty) { return ((L0 / 4 * (ty + 1) + 31) / 32) * 32; }
+
+} // namespace smat
+
+/* The pieces CTA group gidx of launch form 6 marches (the kernel's own
+ * schedule, run on the host): {row tile, z0, z1} triples into out (room for
+ * max_pieces), their count in *n.  For checking that the pieces of all groups
+ * partition the grid. */
+extern "C" int smat_row32_pieces(int L1, int L2, int tile_y, int z_chunk, int ngroups, int gidx, int *out,
+                                 int max_pieces, int *n)
+{
+    if (L1 < 1 || L2 < 1 || tile_y < 1 || z_chunk < 0 || ngroups < 0 || gidx < 0 || !out || !n || max_pieces < 0)
+        return smat_fail(SMAT_EINVAL, "row32_pieces: bad arguments");
+    const int nyt = (L1 + tile_y - 1) / tile_y;
+    const int zc = z_chunk >= L2 ? L2 : z_chunk;
+    if (zc > 0 && gidx >= nyt * ((L2 + zc - 1) / zc))
+        return smat_fail(SMAT_EINVAL, "row32_pieces: item %d beyond the %d chunked items", gidx,
+                         nyt * ((L2 + zc - 1) / zc));
+    if (zc == 0 && gidx >= (ngroups > 0 ? ngroups : 1))
+        return smat_fail(SMAT_EINVAL, "row32_pieces: group %d beyond the %d groups", gidx, ngroups);
+    smat::RowPieces w(nyt, L2, zc, ngroups, gidx);
+    int yt, z0, z1, k = 0;
+    while (w.next(nyt, L2, zc, gidx, yt, z0, z1)) {
+        if (k >= max_pieces) return smat_fail(SMAT_EINVAL, "row32_pieces: more than %d pieces", max_pieces);
+        out[3 * k] = yt;
+        out[3 * k + 1] = z0;
+        out[3 * k + 2] = z1;
+        k++;
+    }
+    *n = k;
+    return SMAT_OK;
+}
+
+namespace smat {
 
 size_t row32_smem(int L0, int ty, int zc) { return sizeof(float4) * row_smem_f4(L0, ty, zc); }
 

@@ -89,6 +89,7 @@ def lib():
         L.smat_fdtd_group_autotune.argtypes = [_P, C.c_int, _P, _P]
         L.smat_fdtd_group_run.argtypes = [_P, C.c_int, C.c_int]
         L.smat_fdtd_group_sync.argtypes = [_P]
+        L.smat_row32_pieces.argtypes = [C.c_int] * 6 + [_P, C.c_int, _P]
         _lib = L
     return _lib
 
@@ -195,6 +196,17 @@ def device_info():
     sms, cc = C.c_int(0), C.c_int(0)
     _check(lib().smat_device_info(name, 128, C.byref(sms), C.byref(cc)))
     return name.value.decode(), sms.value, cc.value
+
+
+def row32_pieces(L1, L2, tile_y, z_chunk, ngroups, gidx):
+    """The pieces (row tile, z0, z1) that CTA group (or item) gidx of the
+    whole-row fused step marches: the kernel's own schedule, run on the host
+    (smat_row32_pieces; no GPU needed)."""
+    cap = 4 * (L1 + 4) + 16
+    out = np.zeros(3 * cap, np.int32)
+    n = C.c_int(0)
+    _check(lib().smat_row32_pieces(L1, L2, tile_y, z_chunk, ngroups, gidx, _ptr(out), cap, C.byref(n)))
+    return [tuple(int(v) for v in out[3 * i:3 * i + 3]) for i in range(n.value)]
 
 
 class Plan:
