@@ -569,8 +569,10 @@ def run_group(args):
     """Batched S-matrix workload: the bend with its 8 excitations plus 16 slabs of
     uneven size (128^3 .. 256x256x192, 1-6 random cuboid inclusions each, one
     excitation each), all FP32, advanced together by one group in the form its
-    autotuner picks (one sweep launch for all structures, or every member's own
-    launches in one graph); compared with the same plans stepped one by one."""
+    autotuner picks (one sweep launch for all structures, every member's own
+    launches in one graph, or one persistent fused launch per step for all
+    members); the one-launch form timed as well, and the same plans stepped
+    one by one."""
     import torch
     from smatranem_gb300 import fdtd as F
     from smatranem_gb300 import workloads as W
@@ -593,6 +595,12 @@ def run_group(args):
     (gmode, by), _ = g.autotune(4)
     g.run(0, args.warmup)
     _, t_group = _timed(lambda: g.run(args.warmup, nsteps))
+    # the one-launch form (3) timed over the same steps whatever the autotuner chose
+    t_one = t_group
+    if gmode != 3:
+        g.set_tuning(3, 1)
+        g.run(0, args.warmup)
+        _, t_one = _timed(lambda: g.run(args.warmup, nsteps))
     g.close()
     if gmode != 2:  # the same steps again as separate plans, each on its own stream
         for p in plans:  # (in form 2 every member keeps its own autotuned launch form)
@@ -609,9 +617,12 @@ def run_group(args):
                                    "21-wavelength FP64 DFT on 2 planes each",
         "structures": len(plans), "cell_excitations": cells, "steps": args.steps,
         "group_tuning": {"mode": ["one grouped launch per sweep", "members' own sweep launches in one graph",
-                                  "members' own autotuned launch forms in one graph"][gmode],
+                                  "members' own autotuned launch forms in one graph",
+                                  "one persistent fused launch per step for every member"][gmode],
                          "block_y": by, "member_tunings": [list(p.get_tuning()) for p in plans]},
         "group_gcell_per_s": cells * args.steps / t_group / 1e9, "group_ms_per_step": 1e3 * t_group / args.steps,
+        "one_launch_gcell_per_s": cells * args.steps / t_one / 1e9,
+        "one_launch_form": "mode 3: the resident CTAs shared out among the members, each member's own schedule",
         "separate_plans_gcell_per_s": cells * args.steps / t_sep / 1e9,
         "device_gb": sum(p.device_bytes for p in plans) / 1e9,
     }))

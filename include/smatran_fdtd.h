@@ -268,8 +268,12 @@ int smat_fdtd_group_destroy(smat_fdtd_group *group);
  * the group's stream; mode 2: every member's own launch form (its
  * smat_fdtd_set_tuning: the whole-row fused step or the sweeps) on the
  * member's own stream, forked from the group's stream and joined back, so the
- * members run side by side.  All are captured as one graph per 32 steps.
- * block_y: rows per sweep block, 1..4 (modes 0, 1). */
+ * members run side by side; mode 3: one persistent launch of the whole-row
+ * fused step per step for every member (members without stable-form metal or
+ * lossy split cells, at most one excitation per resident CTA in all): the
+ * resident CTAs are shared out in groups of one CTA per excitation, each
+ * member's groups marching its own persistent schedule.  All are captured as
+ * one graph per 32 steps.  block_y: rows per sweep block, 1..4 (modes 0, 1). */
 int smat_fdtd_group_set_tuning(smat_fdtd_group *group, int mode, int block_y);
 /* fastest {mode, block_y} over nsteps steps, after autotuning every member
  * (smat_fdtd_autotune: their launch form for mode 2); members must be at the

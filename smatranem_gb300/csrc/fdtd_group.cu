@@ -12,12 +12,19 @@
  *      group_run holds a lock and completes before returning in this mode);
  *   1: each member's own vectorised-sweep launches, back to back on the
  *      group's stream;
- * either way captured as one CUDA graph per 32 steps, with each member's DFT
+ *   2: each member's own tuned launch form on its own stream (forked from the
+ *      group's stream and joined back);
+ *   3: one persistent launch of the whole-row fused step per step over every
+ *      member (k_row32g): the resident CTAs are shared out among the members
+ *      in groups of one CTA per excitation, each member's groups marching its
+ *      own persistent schedule;
+ * always captured as one CUDA graph per 32 steps, with each member's DFT
  * ring flushed in it.  Member results are bit-identical to stepping each
- * plan alone with the vectorised sweeps.
+ * plan alone.
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -34,8 +41,14 @@ struct smat_fdtd_group {
     Group32 *h_gr = nullptr; /* pinned copy of the member table (mode 0) */
     cudaStream_t stream = nullptr;
     int mode = 0; /* 0: one grouped launch per sweep; 1: each member's own sweep launches;
-                     2: each member's own launch form, on its own stream */
-    int by = 1;
+                     2: each member's own launch form, on its own stream;
+                     3: one persistent fused launch over every member */
+    int by = 1;   /* modes 0, 1: rows per block (unused by modes 2 and 3) */
+    /* mode 3: members' rows per tile and CTA groups, the launch's shape */
+    std::vector<int> ty3, groups3;
+    int grid3 = 0;
+    size_t smem3 = 0;
+    bool rec3 = false;
     cudaEvent_t fork = nullptr;      /* mode 2: members' streams wait for the group's stream ... */
     std::vector<cudaEvent_t> join;   /* ... and the group's stream for each member's */
     cudaGraphExec_t graph = nullptr;
@@ -74,10 +87,110 @@ Group32 make_group(const smat_fdtd_group *g)
     return gr;
 }
 
+/* Mode 3's shape.  Each member's tile is the most whole rows (up to 16)
+ * whose quads fit the 384 threads of a CTA and whose staging fits shared
+ * memory.  The resident CTAs are shared out in groups of one CTA per
+ * excitation: every member gets one group, then each further group goes to
+ * the member with the most cells per CTA while CTAs are left. */
+int setup_persistent(smat_fdtd_group *g)
+{
+    const int n = (int)g->m.size();
+    std::vector<int> ty(n), groups(n, 1);
+    size_t smem = 0;
+    bool rec = false;
+    int used = 0;
+    for (int i = 0; i < n; i++) {
+        const smat_fdtd_plan *p = g->m[i];
+        if (p->nrec_metal > 0 || p->nrec_split > 0)
+            return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 needs members without stable-form metal or "
+                                          "lossy split cells (member %d has them)", i);
+        const int nq = p->L[0] / 4;
+        int t = 0;
+        for (int c = 16; c >= 1 && !t; c--)
+            if (nq * (c + 1) <= ROW_GROUP_THREADS && row32_smem(p->L[0], c, p->L[2]) <= 232448) t = c;
+        if (!t)
+            return smat_fail(SMAT_EINVAL, "group_set_tuning: member %d's rows of %d cells do not fit mode 3's CTA",
+                             i, p->L[0]);
+        ty[i] = t;
+        smem = std::max(smem, row32_smem(p->L[0], t, p->L[2]));
+        rec |= p->nhgen + p->negen > 0;
+        used += p->batch;
+    }
+    const int occ = row32_group_max_ctas_per_sm(smem, rec);
+    if (occ < 1) return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 does not fit an SM");
+    const int total = sm_count() * occ;
+    if (used > total)
+        return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 needs a CTA per excitation (%d) within the %d "
+                                      "resident CTAs", used, total);
+    std::vector<double> cells(n);
+    for (int i = 0; i < n; i++) {
+        const smat_fdtd_plan *p = g->m[i];
+        cells[i] = (double)p->L[0] * p->L[1] * p->L[2];
+    }
+    for (;;) {
+        int best = -1;
+        double load = 0;
+        for (int i = 0; i < n; i++) {
+            const double l = cells[i] / groups[i]; /* per CTA of the member */
+            if (used + g->m[i]->batch <= total && l > load) {
+                load = l;
+                best = i;
+            }
+        }
+        if (best < 0) break;
+        groups[best]++;
+        used += g->m[best]->batch;
+    }
+    g->ty3 = ty;
+    g->groups3 = groups;
+    g->smem3 = smem;
+    g->rec3 = rec;
+    g->grid3 = used;
+    return SMAT_OK;
+}
+
+/* the mode and block_y of set_tuning (mode 3 builds its piece list) */
+int configure(smat_fdtd_group *g, int mode, int by)
+{
+    if (mode == 3) {
+        int rc = setup_persistent(g);
+        if (rc) return rc;
+    }
+    g->mode = mode;
+    g->by = by;
+    return SMAT_OK;
+}
+
 /* steps rel0 .. rel0+n-1 of every member (relative to each member's d_base) */
 void enqueue_group(smat_fdtd_group *g, int rel0, int n)
 {
-    if (g->mode == 0) {
+    if (g->mode == 3) {
+        /* one persistent launch a step: each member's groups of CTAs */
+        RowGroup32 G;
+        memset(&G, 0, sizeof G);
+        G.n = (int)g->m.size();
+        int first = 0;
+        for (int j = 0; j < G.n; j++) {
+            G.first[j] = first;
+            first += g->groups3[j] * g->m[j]->batch;
+        }
+        G.first[G.n] = first;
+        for (int i = 0; i < n; i++) {
+            for (int j = 0; j < G.n; j++) {
+                const smat_fdtd_plan *p = g->m[j];
+                Row32 &r = G.r[j];
+                r = make_row(p, false);
+                r.ty = g->ty3[j];
+                r.zc = 0;
+                r.nyt = (p->L[1] + g->ty3[j] - 1) / g->ty3[j];
+                r.nzc = 1;
+                r.ngroups = g->groups3[j];
+                r.nitems = g->groups3[j] * p->batch;
+            }
+            launch_row32_group(G, rel0 + i, g->grid3, g->smem3, g->rec3, g->stream);
+            for (smat_fdtd_plan *p : g->m) p->cur ^= 1;
+        }
+    } else if (g->mode == 0) {
         *g->h_gr = make_group(g); /* same bytes on every call while the members stand still */
         load_group32(g->h_gr, g->stream);
         for (int i = 0; i < n; i++) launch_group32v(*g->h_gr, rel0 + i, g->stream);
@@ -209,13 +322,14 @@ extern "C" int smat_fdtd_group_destroy(smat_fdtd_group *g)
 extern "C" int smat_fdtd_group_set_tuning(smat_fdtd_group *g, int mode, int block_y)
 {
     smat_clear_error();
-    if (!g || mode < 0 || mode > 2 || block_y < 1 || block_y > 4)
+    if (!g || mode < 0 || mode > 3 || block_y < 1 || block_y > 4)
         return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 0 (one launch per sweep), 1 (members' own sweep "
-                                      "launches) or 2 (members' own tuned launch forms), block_y in 1..4");
-    g->mode = mode;
-    g->by = block_y;
+                                      "launches), 2 (members' own tuned launch forms) or 3 (one persistent fused "
+                                      "launch), block_y in 1..4");
+    if (g->stream) CK(cudaStreamSynchronize(g->stream));
+    int rc = configure(g, mode, block_y);
     drop_group_graph(g);
-    return SMAT_OK;
+    return rc;
 }
 
 extern "C" int smat_fdtd_group_run(smat_fdtd_group *g, int k_begin, int k_end)
@@ -309,11 +423,13 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best
     double bms = 1e30;
     int bmode = g->mode, bby = g->by;
     std::lock_guard<std::mutex> lock(g_table_mu);
-    for (int mode : {0, 1, 2})
+    for (int mode : {0, 1, 2, 3})
         for (int by : {1, 2, 4}) {
-            if (mode == 2 && by != 1) continue; /* rows per block: the members' own */
-            g->mode = mode;
-            g->by = by;
+            if (mode >= 2 && by != 1) continue; /* rows per block: the members' own */
+            if (configure(g, mode, by) != SMAT_OK) {
+                smat_clear_error();
+                continue;
+            }
             enqueue_group(g, 0, 1);
             CK(cudaEventRecord(e0, g->stream));
             enqueue_group(g, 0, nsteps);
@@ -321,6 +437,7 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best
             CK(cudaEventSynchronize(e1));
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (cudaGetLastError() != cudaSuccess) continue; /* a form whose launches were refused */
             if (ms < bms) {
                 bms = ms;
                 bmode = mode;
@@ -335,8 +452,8 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best
         CK(cudaMemcpyAsync(p->d_iI, p->h_iI.data(), sizeof(int) * p->batch, cudaMemcpyHostToDevice, g->stream));
     }
     CK(cudaStreamSynchronize(g->stream));
-    g->mode = bmode;
-    g->by = bby;
+    int rc = configure(g, bmode, bby);
+    if (rc) return rc;
     drop_group_graph(g);
     if (best) {
         best[0] = bmode;

@@ -152,8 +152,6 @@ struct Fused32T {
     int *err;
 };
 
-/* launch form 6: the fused step over whole x rows (fdtd_row32.cu); reads the
- * field set in p, writes the other set */
 /* The work of one CTA of launch form 6 (excitation aside): pieces (row tile yt,
  * planes [z0, z1)).  With z chunks (zc > 0) one piece, item gidx = row tile
  * fastest, then z chunk.  Persistent (zc == 0): ngroups groups of one CTA per
@@ -199,6 +197,8 @@ struct RowPieces {
     }
 };
 
+/* launch form 6: the fused step over whole x rows (fdtd_row32.cu); reads the
+ * field set in p, writes the other set */
 struct Row32 {
     P32 p;
     float *Hn, *En, *Han, *Ean; /* new set */
@@ -209,6 +209,18 @@ struct Row32 {
     int nqp;                    /* how many of the first kind */
     int has_rec;                /* the plan has record cells (lossy or PEC cells; no stable-form metal) */
 };
+
+/* Several plans in one persistent launch of form 6 (a group's form 3): CTAs
+ * first[m] .. first[m+1]-1 belong to member m, in groups of one CTA per
+ * excitation that march the member's own persistent schedule (RowPieces with
+ * r[m].ngroups groups, r[m].ty rows per tile).  Passed whole as a kernel
+ * parameter (under 12 KB). */
+struct RowGroup32 {
+    int n;
+    int first[MAX_GROUP + 1];
+    Row32 r[MAX_GROUP];
+};
+
 
 /* launchers (one translation unit per precision) */
 void launch_h64(const P64 &p, int rel, cudaStream_t st);
@@ -242,6 +254,11 @@ int row32_threads(int L0, int ty);
 size_t row32_smem(int L0, int ty, int zc);
 int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc, bool rec);
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st);
+/* the grouped launch (384 threads a CTA): its resident CTAs per SM at smem
+ * bytes of shared memory (0: does not fit), and the launch itself */
+constexpr int ROW_GROUP_THREADS = 384;
+int row32_group_max_ctas_per_sm(size_t smem, bool rec);
+void launch_row32_group(const RowGroup32 &g, int rel, int grid, size_t smem, bool rec, cudaStream_t st);
 void launch_bump(int *base, int by, cudaStream_t st);
 void launch_set(int *base, int value, cudaStream_t st);
 void launch_maxabs(const void *x, long long n, int is_double, double *out, cudaStream_t st);

@@ -1437,6 +1437,7 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
         CK(cudaEventSynchronize(e1));
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (cudaGetLastError() != cudaSuccess) continue; /* a form whose launches were refused */
         if (verbose)
             fprintf(stderr, "autotune: kernel %d tile_y %d z_chunk %d ctas_per_sm %d slots %d: %.4f ms/step\n",
                     c.fused, c.ty, c.zc, c.ctas, c.ns, ms / nsteps);

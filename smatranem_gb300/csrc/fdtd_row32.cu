@@ -239,8 +239,14 @@ struct PlaneInfo {
     int pm, q, pad0, pad1;
 };
 
-template <int MAXT, int MB, bool REC>
-__global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel)
+/* The march of one CTA through the pieces next(yt, z0, z1) gives -- rows
+ * yt*TY .. of excitation b through planes [z0, z1) -- by the whole CTA (every
+ * thread sees the same pieces).  The per-thread setup (quad, split factors)
+ * is done once.  At the end of each piece every shared-memory read of it has
+ * passed a barrier, so the next piece (of this plan or, in a group, of
+ * another) may restage at once. */
+template <bool REC, class Next>
+__device__ __forceinline__ void row_march(const Row32 &r, const int rel, const int b, Next &&next)
 {
     extern __shared__ float4 sm4[];
     const P32 &p = r.p;
@@ -258,10 +264,6 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
 #define PE(f, c) pe[((f) * 3 + (c)) * NC]
 #define TOP(s, c) top[((s) * 2 + (c)) * NQ]
 #define HS(z, row, c) hs[((((z) & 1) * NR + (row)) * 3 + (c)) * NQ]
-
-    /* CTAs in order of excitation fastest (the coefficient stream is shared
-     * by the CTAs of one row tile and plane range), then item group */
-    const int b = blockIdx.x % p.batch, gidx = blockIdx.x / p.batch;
 
     /* this thread's quad: the quads of the tile's rows whose x index lies in
      * a PML (split cells) take the first threads, row by row, the others the
@@ -303,11 +305,9 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
     const bool pmx = th.xm != 0;
     const int iIb = p.s.iI[b]; /* the excitation's source plane */
 
-    /* the pieces (row tile yt, planes [z0, z1)) of excitation b this CTA marches */
-    RowPieces work(r.nyt, L2, r.zc, r.ngroups, gidx);
     for (;;) {
         int yt, z0, z1;
-        if (!work.next(r.nyt, L2, r.zc, gidx, yt, z0, z1)) break;
+        if (!next(yt, z0, z1)) break;
         const int Y0 = yt * TY, h = min(TY, L1 - Y0);
         /* this thread's row: own rows 0..h-1, rows h..TY-1 idle (a partial last
          * tile), row TY the halo row y0+h */
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
             cpa_wait2();
             __syncthreads();
         }
-    } /* pieces */
+    }
 #undef ES
 #undef PH
 #undef PE
@@ -520,7 +520,44 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel
 #undef HS
 }
 
+template <int MAXT, int MB, bool REC>
+__global__ void __launch_bounds__(MAXT, MB) k_row32(const Row32 r, const int rel)
+{
+    /* CTAs in order of excitation fastest (the coefficient stream is shared
+     * by the CTAs of one row tile and plane range), then item group; the
+     * pieces (row tile, planes [z0, z1)) of excitation b this CTA marches */
+    const int b = blockIdx.x % r.p.batch, gidx = blockIdx.x / r.p.batch;
+    RowPieces work(r.nyt, r.p.g.L2, r.zc, r.ngroups, gidx);
+    row_march<REC>(r, rel, b, [&](int &yt, int &z0, int &z1) { return work.next(r.nyt, r.p.g.L2, r.zc, gidx, yt, z0, z1); });
+}
+
+/* A group of plans in one persistent launch: CTA blockIdx.x belongs to the
+ * member whose CTA range holds it and runs that member's own persistent
+ * schedule there (a group of one CTA per excitation marching the same pieces,
+ * so that the excitations of a tile share the coefficient stream through L2).
+ * The member's parameters are read in place from the parameter space at an
+ * offset that is uniform over the CTA (derived from blockIdx only), so they
+ * stay in uniform registers: a copy in shared memory, or an index loaded from
+ * memory, cost a quarter of the step's speed. */
+template <int MAXT, int MB, bool REC>
+__global__ void __launch_bounds__(MAXT, MB) k_row32g(const __grid_constant__ RowGroup32 G, const int rel)
+{
+    int m = 0;
+    while (m + 1 < G.n && (int)blockIdx.x >= G.first[m + 1]) m++;
+    const Row32 &r = G.r[m];
+    const int c = (int)blockIdx.x - G.first[m];
+    const int b = c % r.p.batch, gidx = c / r.p.batch;
+    RowPieces work(r.nyt, r.p.g.L2, 0, r.ngroups, gidx);
+    row_march<REC>(r, rel, b, [&](int &yt, int &z0, int &z1) { return work.next(r.nyt, r.p.g.L2, 0, gidx, yt, z0, z1); });
+}
+
 template <int MAXT, int MB, bool REC> const void *row_fn() { return (const void *)k_row32<MAXT, MB, REC>; }
+
+/* the grouped launch: ROW_GROUP_THREADS threads, one CTA per SM */
+const void *row_group_kernel(bool rec)
+{
+    return rec ? (const void *)k_row32g<ROW_GROUP_THREADS, 1, true> : (const void *)k_row32g<ROW_GROUP_THREADS, 1, false>;
+}
 
 /* the instantiation for a block of `threads` at register bound mb (at least
  * mb resident CTAs of MAXT threads: 65536 / (MAXT * mb) registers), or null;
@@ -590,22 +627,60 @@ namespace smat {
 
 size_t row32_smem(int L0, int ty, int zc) { return sizeof(float4) * row_smem_f4(L0, ty, zc); }
 
+/* Lets fn take up to the device's opt-in maximum of dynamic shared memory.
+ * One limit for every launch of a kernel: several plans (a group's members)
+ * share one instantiation with different staging sizes, so a limit lowered
+ * for one plan must not refuse another's launch. */
+bool allow_max_smem(const void *fn, size_t need)
+{
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const long long room = (long long)optin - (long long)fa.sharedSizeBytes;
+    if (room < (long long)need) return false;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
 int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc, bool rec)
 {
     const int threads = row32_threads(L0, ty);
     const void *fn = row_kernel(threads, mb, rec);
     if (!fn) return 0;
     const size_t sm = row32_smem(L0, ty, zc);
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
+    if (!allow_max_smem(fn, sm)) return 0;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, sm) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     return n;
+}
+
+int row32_group_max_ctas_per_sm(size_t smem, bool rec)
+{
+    const void *fn = row_group_kernel(rec);
+    if (!allow_max_smem(fn, smem)) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, ROW_GROUP_THREADS, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+void launch_row32_group(const RowGroup32 &g, int rel, int grid, size_t smem, bool rec, cudaStream_t st)
+{
+    void *args[] = {(void *)&g, (void *)&rel};
+    cudaLaunchKernel(row_group_kernel(rec), dim3(grid), dim3(ROW_GROUP_THREADS), args, smem, st);
 }
 
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st)

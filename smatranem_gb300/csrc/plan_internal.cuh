@@ -149,6 +149,7 @@ namespace plan {
 Geo make_geo(const smat_fdtd_plan *p);
 P64 make_p64(const smat_fdtd_plan *p, bool xp);
 P32 make_p32(const smat_fdtd_plan *p, bool xp);
+Row32 make_row(const smat_fdtd_plan *p, bool xp);
 /* the launches of steps rel0 .. rel0+n-1 relative to *d_base (no bump) */
 void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp);
 void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel, cudaStream_t st);

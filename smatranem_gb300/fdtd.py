@@ -436,7 +436,10 @@ class Group:
 
     def set_tuning(self, mode, block_y):
         """mode 0: one grouped launch per sweep; 1: members' own sweep launches;
-        2: members' own launch forms (their set_tuning / autotune)."""
+        2: members' own launch forms (their set_tuning / autotune); 3: one
+        persistent whole-row fused launch per step for every member (the
+        resident CTAs shared out among the members).  block_y: rows per sweep
+        block (modes 0, 1)."""
         _check(lib().smat_fdtd_group_set_tuning(self._h, mode, block_y))
 
     def autotune(self, nsteps=4):

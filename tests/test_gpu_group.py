@@ -108,6 +108,67 @@ def test_group_members_own_launch_forms(built):
             p.close()
 
 
+@pytest.mark.parametrize("order", [(0, 1, 2, 3), (3, 2, 1, 0), (2,), (1, 3)])
+def test_group_one_persistent_launch(built, order):
+    """Mode 3: one persistent launch of the whole-row fused step per step over
+    every member (tiles of up to 16 whole rows per member, the resident CTAs
+    shared out among the members, each marching its member's own schedule;
+    members with lossy and PEC record cells) gives each member the bits of the
+    member stepped alone with the sweeps, over run windows that leave the
+    members on either field set and across re-captured graphs."""
+    from smatranem_gb300 import fdtd as f
+    from smatranem_gb300 import workloads as W
+    nsteps = 60
+    windows = [(0, 20), (20, 53), (53, nsteps)]
+    structs = []
+    for L, seed, kw, iBTIin, batch in [MEMBERS[i] for i in order]:
+        s = W.random_structure(L, seed=seed, **kw)
+        structs.append((s, W.prepare(s), iBTIin, batch, seed))
+    alone = []
+    for s, pr, iBTIin, batch, seed in structs:
+        with _setup(f, W, s, pr, iBTIin, batch, seed, nsteps) as p:
+            p.set_tuning(2, 1, 0, 0, 4)
+            for a, b in windows:
+                p.run(a, b)
+            alone.append(_result(p, batch))
+    plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
+    try:
+        with f.Group(plans) as g:
+            g.set_tuning(3, 1)
+            for a, b in windows:
+                g.run(a, b)
+        for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
+            got = _result(p, batch)
+            for rb, gb in zip(ref, got):
+                for a, b_ in zip(rb, gb):
+                    assert np.all(np.isfinite(a)) and np.array_equal(a, b_)
+    finally:
+        for p in plans:
+            p.close()
+
+
+def test_group_persistent_launch_refuses_metal(built):
+    """Mode 3 has no stable-form path: a member with metal cells is refused
+    and the group keeps its form."""
+    from smatranem_gb300 import fdtd as f
+    from smatranem_gb300 import workloads as W
+    L, seed, kw, iBTIin, batch = MEMBERS[3]
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    sm = W.random_structure((40, 17, 19, 3), seed=7, pml=(4, 4, 4), metals=0.02)
+    prm = W.prepare(sm)
+    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
+                       precision=f.FP32) as p, \
+            f.Plan.create(sm.L, sm.iBc, (5, 13, 7, 1), prm.invtau_R, prm.invtau_I, prm.mu, prm.epsi, prm.sigma,
+                          precision=f.FP32, pec=sm.pec) as pm:
+        with f.Group([p]) as g:
+            g.set_tuning(3, 2)
+        with f.Group([p, pm]) as g:
+            with pytest.raises(f.FdtdError):
+                g.set_tuning(3, 1)
+            g.set_tuning(1, 1)
+
+
 def test_group_autotune_and_errors(built):
     from smatranem_gb300 import fdtd as f
     from smatranem_gb300 import workloads as W
@@ -122,7 +183,7 @@ def test_group_autotune_and_errors(built):
         p.set_schedule(src, planes=(iBTIin[0], iBTIin[1]), phase=ph)
         with f.Group([p]) as g:
             (mode, by), ms = g.autotune(2)
-            assert mode in (0, 1, 2) and by in (1, 2, 4) and ms > 0
+            assert mode in (0, 1, 2, 3) and by in (1, 2, 4) and ms > 0
             assert p.check_finite() == (True, 0.0)  # left at the zero state
             with pytest.raises(f.FdtdError):
                 g.run(0, src.shape[0] + 1)  # beyond the schedule
