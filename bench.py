@@ -220,6 +220,12 @@ def mode_columns(modes):
     return np.array(cols)
 
 
+def dft_fields(p, b):
+    """The running DFT of excitation b: [wavelength][port plane][Hx, Hy, Ex, Ey][pixel]."""
+    nf, nq = p.dft_count()
+    return np.array([[p.get_dft(b, fi, q) for q in range(nq)] for fi in range(nf)])
+
+
 def s_parameters(p, bend, modes, b):
     """Mode overlaps on the GPU (FP64): [port plane][lambda][mode column]."""
     return np.stack([p.overlap(b, q, modes["cols"]) for q in range(2)])
@@ -375,6 +381,7 @@ def run_ours(args):
     p32b.run(0, full)
     t_full32 = time.perf_counter() - t0
     S32 = s_parameters(p32b, bend, modes, 0)
+    D32 = dft_fields(p32b, 0)
     finite32 = p32b.check_finite()[0]
     p32b.close()
     p32.close()
@@ -394,11 +401,19 @@ def run_ours(args):
     p64.run(0, full)
     t_full64 = time.perf_counter() - t0
     S64 = s_parameters(p64, bend, modes, 0)
+    D64 = dft_fields(p64, 0)
     p64.close()
     clocks.stop()
     big = np.abs(S64) > 1e-3 * np.abs(S64).max()
     s_rel = float(np.max(np.abs(S32 - S64)[big] / np.abs(S64)[big]))
     s_abs = float(np.max(np.abs(S32 - S64)) / np.abs(S64).max())
+    # the DFT fields themselves: per (wavelength, port plane) slice, the
+    # relative L2 error and the largest deviation over the slice's largest value
+    dd = (D32 - D64).reshape(D64.shape[0], D64.shape[1], -1)
+    dr = D64.reshape(dd.shape)
+    d_l2 = float(np.max(np.linalg.norm(dd, axis=2) / np.linalg.norm(dr, axis=2)))
+    d_max = float(np.max(np.abs(dd).max(axis=2) / np.abs(dr).max(axis=2)))
+    del D32, D64, dd, dr
     # ---- e2e through the C ABI from host buffers --------------------------
     t0 = time.perf_counter()
     pe = make_plan(bend, pr, modes, F.FP32, batch, full, tuning=tuning)
@@ -461,6 +476,9 @@ def run_ours(args):
         "s_param_rel_err_fp32_vs_fp64": {"max_rel": s_rel, "max_abs_over_max": s_abs,
                                          "over": "2 ports x 21 wavelengths x 4 modes x (+,-), excitation 0, "
                                                  "|S| > 1e-3 max"},
+        "dft_field_rel_err_fp32_vs_fp64": {"max_rel_l2": d_l2, "max_abs_over_max": d_max,
+                                           "over": "Hx, Hy, Ex, Ey on both port planes x 21 wavelengths, "
+                                                   "excitation 0, per (wavelength, plane) slice"},
         "port_modes": {"theta": modes["theta"], "solver": modes["solver"]},
         "gpu_launches": launches,
         "clocks": clocks.summary(),

@@ -376,6 +376,12 @@ class Plan:
         _check(lib().smat_fdtd_get_tuning(self._h, out))
         return tuple(out)
 
+    def dft_count(self):
+        """(DFT frequencies, DFT planes) of the schedule."""
+        nf, nq = C.c_int(0), C.c_int(0)
+        _check(lib().smat_fdtd_dft_count(self._h, C.byref(nf), C.byref(nq)))
+        return nf.value, nq.value
+
     def overlap(self, b, q, tilxi_cols):
         """S for every DFT frequency of plane q: (nfreq, ncols) complex (GPU, FP64)."""
         t = _c128(tilxi_cols)
