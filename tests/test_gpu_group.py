@@ -147,6 +147,47 @@ def test_group_one_persistent_launch(built, order):
             p.close()
 
 
+def test_group_one_persistent_launch_mixed_tiles(built):
+    """Mode 3 with members whose tiles differ: 256-cell rows (5-row tiles) and
+    128-cell rows (11-row tiles), batches 2 and 3, a PML-free member with
+    wrapped boundaries -- each member ends with the bits of the member stepped
+    alone."""
+    from smatranem_gb300 import fdtd as f
+    from smatranem_gb300 import workloads as W
+    members = [
+        ((256, 13, 10, 2), 41, dict(pml=(4, 3, 3)), (3, 7, 5, 1), 2),
+        ((128, 24, 12, 2), 42, dict(pml=(5, 5, 3), lossy=0.03), (4, 8, 6, -1), 3),
+        ((64, 7, 9, 1), 43, dict(pml=(0, 0, 0), iBc=(1, -1, 1)), (2, 6, 4, 1), 1),
+    ]
+    nsteps = 45
+    windows = [(0, 7), (7, 45)]
+    structs = []
+    for L, seed, kw, iBTIin, batch in members:
+        s = W.random_structure(L, seed=seed, **kw)
+        structs.append((s, W.prepare(s), iBTIin, batch, seed))
+    alone = []
+    for s, pr, iBTIin, batch, seed in structs:
+        with _setup(f, W, s, pr, iBTIin, batch, seed, nsteps) as p:
+            p.set_tuning(2, 1, 0, 0, 4)
+            for a, b in windows:
+                p.run(a, b)
+            alone.append(_result(p, batch))
+    plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
+    try:
+        with f.Group(plans) as g:
+            g.set_tuning(3, 1)
+            for a, b in windows:
+                g.run(a, b)
+        for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
+            got = _result(p, batch)
+            for rb, gb in zip(ref, got):
+                for a, b_ in zip(rb, gb):
+                    assert np.all(np.isfinite(a)) and np.array_equal(a, b_)
+    finally:
+        for p in plans:
+            p.close()
+
+
 def test_group_persistent_launch_refuses_metal(built):
     """Mode 3 has no stable-form path: a member with metal cells is refused
     and the group keeps its form."""
