@@ -614,14 +614,18 @@ def run_group(args):
     g.run(0, args.warmup)
     _, t_group = _timed(lambda: g.run(args.warmup, nsteps))
     # the one-launch form (3) timed over the same steps whatever the autotuner chose
-    t_one = t_group
+    t_one, shape_one = t_group, by
     if gmode != 3:
-        g.set_tuning(3, 1)
-        g.run(0, args.warmup)
-        _, t_one = _timed(lambda: g.run(args.warmup, nsteps))
+        t_one = float("inf")
+        for shape in (1, 2):
+            g.set_tuning(3, shape)
+            g.run(0, args.warmup)
+            _, t = _timed(lambda: g.run(args.warmup, nsteps))
+            if t < t_one:
+                t_one, shape_one = t, shape
     g.close()
-    if gmode != 2:  # the same steps again as separate plans, each on its own stream
-        for p in plans:  # (in form 2 every member keeps its own autotuned launch form)
+    if gmode in (0, 1):  # the same steps again as separate plans, each on its own stream
+        for p in plans:  # (after forms 2 and 3 every member keeps its own autotuned launch form)
             p.set_tuning(2, by, 0, 0, 4)
 
     def one_by_one():
@@ -640,7 +644,8 @@ def run_group(args):
                          "block_y": by, "member_tunings": [list(p.get_tuning()) for p in plans]},
         "group_gcell_per_s": cells * args.steps / t_group / 1e9, "group_ms_per_step": 1e3 * t_group / args.steps,
         "one_launch_gcell_per_s": cells * args.steps / t_one / 1e9,
-        "one_launch_form": "mode 3: the resident CTAs shared out among the members, each member's own schedule",
+        "one_launch_form": "mode 3: the resident CTAs shared out among the members, each member's own schedule; "
+                           + ("CTAs of 384 threads, one per SM" if shape_one == 1 else "CTAs of 192 threads, two per SM"),
         "separate_plans_gcell_per_s": cells * args.steps / t_sep / 1e9,
         "device_gb": sum(p.device_bytes for p in plans) / 1e9,
     }))

@@ -273,7 +273,9 @@ int smat_fdtd_group_destroy(smat_fdtd_group *group);
  * lossy split cells, at most one excitation per resident CTA in all): the
  * resident CTAs are shared out in groups of one CTA per excitation, each
  * member's groups marching its own persistent schedule.  All are captured as
- * one graph per 32 steps.  block_y: rows per sweep block, 1..4 (modes 0, 1). */
+ * one graph per 32 steps.  block_y: rows per sweep block, 1..4 (modes 0, 1);
+ * mode 3: CTAs of 384 threads, one per SM (1), or of 192, two per SM (2),
+ * each member's tile the most whole rows that fit. */
 int smat_fdtd_group_set_tuning(smat_fdtd_group *group, int mode, int block_y);
 /* fastest {mode, block_y} over nsteps steps, after autotuning every member
  * (smat_fdtd_autotune: their launch form for mode 2); members must be at the

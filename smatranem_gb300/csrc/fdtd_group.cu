@@ -43,10 +43,10 @@ struct smat_fdtd_group {
     int mode = 0; /* 0: one grouped launch per sweep; 1: each member's own sweep launches;
                      2: each member's own launch form, on its own stream;
                      3: one persistent fused launch over every member */
-    int by = 1;   /* modes 0, 1: rows per block (unused by modes 2 and 3) */
+    int by = 1;   /* modes 0, 1: rows per block; mode 3: 1 = CTAs of 384 threads, 2 = of 192 */
     /* mode 3: members' rows per tile and CTA groups, the launch's shape */
     std::vector<int> ty3, groups3;
-    int grid3 = 0;
+    int grid3 = 0, threads3 = 384;
     size_t smem3 = 0;
     bool rec3 = false;
     cudaEvent_t fork = nullptr;      /* mode 2: members' streams wait for the group's stream ... */
@@ -87,13 +87,15 @@ Group32 make_group(const smat_fdtd_group *g)
     return gr;
 }
 
-/* Mode 3's shape.  Each member's tile is the most whole rows (up to 16)
- * whose quads fit the 384 threads of a CTA and whose staging fits shared
- * memory.  The resident CTAs are shared out in groups of one CTA per
- * excitation: every member gets one group, then each further group goes to
- * the member with the most cells per CTA while CTAs are left. */
-int setup_persistent(smat_fdtd_group *g)
+/* Mode 3's shape for CTAs of `threads` threads (384: one per SM, 192: two).
+ * Each member's tile is the most whole rows (up to 16) whose quads fit the
+ * CTA and whose staging fits the CTA's share of shared memory.  The resident
+ * CTAs are shared out in groups of one CTA per excitation: every member gets
+ * one group, then each further group goes to the member with the most cells
+ * per CTA while CTAs are left. */
+int setup_persistent(smat_fdtd_group *g, int threads)
 {
+    const size_t room = threads == 384 ? 232448 : 232448 / 2 - 1024;
     const int n = (int)g->m.size();
     std::vector<int> ty(n), groups(n, 1);
     size_t smem = 0;
@@ -107,7 +109,7 @@ int setup_persistent(smat_fdtd_group *g)
         const int nq = p->L[0] / 4;
         int t = 0;
         for (int c = 16; c >= 1 && !t; c--)
-            if (nq * (c + 1) <= ROW_GROUP_THREADS && row32_smem(p->L[0], c, p->L[2]) <= 232448) t = c;
+            if (nq * (c + 1) <= threads && row32_smem(p->L[0], c, p->L[2]) <= room) t = c;
         if (!t)
             return smat_fail(SMAT_EINVAL, "group_set_tuning: member %d's rows of %d cells do not fit mode 3's CTA",
                              i, p->L[0]);
@@ -116,7 +118,7 @@ int setup_persistent(smat_fdtd_group *g)
         rec |= p->nhgen + p->negen > 0;
         used += p->batch;
     }
-    const int occ = row32_group_max_ctas_per_sm(smem, rec);
+    const int occ = row32_group_max_ctas_per_sm(threads, smem, rec);
     if (occ < 1) return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 does not fit an SM");
     const int total = sm_count() * occ;
     if (used > total)
@@ -146,6 +148,7 @@ int setup_persistent(smat_fdtd_group *g)
     g->smem3 = smem;
     g->rec3 = rec;
     g->grid3 = used;
+    g->threads3 = threads;
     return SMAT_OK;
 }
 
@@ -153,7 +156,8 @@ int setup_persistent(smat_fdtd_group *g)
 int configure(smat_fdtd_group *g, int mode, int by)
 {
     if (mode == 3) {
-        int rc = setup_persistent(g);
+        if (by != 1 && by != 2) return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 takes block_y 1 or 2");
+        int rc = setup_persistent(g, by == 1 ? 384 : 192);
         if (rc) return rc;
     }
     g->mode = mode;
@@ -187,7 +191,7 @@ void enqueue_group(smat_fdtd_group *g, int rel0, int n)
                 r.ngroups = g->groups3[j];
                 r.nitems = g->groups3[j] * p->batch;
             }
-            launch_row32_group(G, rel0 + i, g->grid3, g->smem3, g->rec3, g->stream);
+            launch_row32_group(G, rel0 + i, g->threads3, g->grid3, g->smem3, g->rec3, g->stream);
             for (smat_fdtd_plan *p : g->m) p->cur ^= 1;
         }
     } else if (g->mode == 0) {
@@ -425,7 +429,7 @@ extern "C" int smat_fdtd_group_autotune(smat_fdtd_group *g, int nsteps, int best
     std::lock_guard<std::mutex> lock(g_table_mu);
     for (int mode : {0, 1, 2, 3})
         for (int by : {1, 2, 4}) {
-            if (mode >= 2 && by != 1) continue; /* rows per block: the members' own */
+            if ((mode == 2 && by != 1) || (mode == 3 && by > 2)) continue; /* mode 2: the members' own */
             if (configure(g, mode, by) != SMAT_OK) {
                 smat_clear_error();
                 continue;

@@ -254,11 +254,11 @@ int row32_threads(int L0, int ty);
 size_t row32_smem(int L0, int ty, int zc);
 int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc, bool rec);
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st);
-/* the grouped launch (384 threads a CTA): its resident CTAs per SM at smem
- * bytes of shared memory (0: does not fit), and the launch itself */
-constexpr int ROW_GROUP_THREADS = 384;
-int row32_group_max_ctas_per_sm(size_t smem, bool rec);
-void launch_row32_group(const RowGroup32 &g, int rel, int grid, size_t smem, bool rec, cudaStream_t st);
+/* the grouped launch, CTAs of `threads` = 384 (one per SM) or 192 (two per
+ * SM): its resident CTAs per SM at smem bytes of shared memory (0: does not
+ * fit), and the launch itself */
+int row32_group_max_ctas_per_sm(int threads, size_t smem, bool rec);
+void launch_row32_group(const RowGroup32 &g, int rel, int threads, int grid, size_t smem, bool rec, cudaStream_t st);
 void launch_bump(int *base, int by, cudaStream_t st);
 void launch_set(int *base, int value, cudaStream_t st);
 void launch_maxabs(const void *x, long long n, int is_double, double *out, cudaStream_t st);

@@ -553,10 +553,13 @@ __global__ void __launch_bounds__(MAXT, MB) k_row32g(const __grid_constant__ Row
 
 template <int MAXT, int MB, bool REC> const void *row_fn() { return (const void *)k_row32<MAXT, MB, REC>; }
 
-/* the grouped launch: ROW_GROUP_THREADS threads, one CTA per SM */
-const void *row_group_kernel(bool rec)
+/* the grouped launch: 384 threads at one CTA per SM or 192 at two (the
+ * register bound of the single-plan instantiations of those shapes) */
+const void *row_group_kernel(int threads, bool rec)
 {
-    return rec ? (const void *)k_row32g<ROW_GROUP_THREADS, 1, true> : (const void *)k_row32g<ROW_GROUP_THREADS, 1, false>;
+    if (threads == 384) return rec ? (const void *)k_row32g<384, 1, true> : (const void *)k_row32g<384, 1, false>;
+    if (threads == 192) return rec ? (const void *)k_row32g<192, 2, true> : (const void *)k_row32g<192, 2, false>;
+    return nullptr;
 }
 
 /* the instantiation for a block of `threads` at register bound mb (at least
@@ -665,22 +668,23 @@ int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc, bool rec)
     return n;
 }
 
-int row32_group_max_ctas_per_sm(size_t smem, bool rec)
+int row32_group_max_ctas_per_sm(int threads, size_t smem, bool rec)
 {
-    const void *fn = row_group_kernel(rec);
+    const void *fn = row_group_kernel(threads, rec);
+    if (!fn) return 0;
     if (!allow_max_smem(fn, smem)) return 0;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, ROW_GROUP_THREADS, smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     return n;
 }
 
-void launch_row32_group(const RowGroup32 &g, int rel, int grid, size_t smem, bool rec, cudaStream_t st)
+void launch_row32_group(const RowGroup32 &g, int rel, int threads, int grid, size_t smem, bool rec, cudaStream_t st)
 {
     void *args[] = {(void *)&g, (void *)&rel};
-    cudaLaunchKernel(row_group_kernel(rec), dim3(grid), dim3(ROW_GROUP_THREADS), args, smem, st);
+    cudaLaunchKernel(row_group_kernel(threads, rec), dim3(grid), dim3(threads), args, smem, st);
 }
 
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st)

@@ -445,7 +445,8 @@ class Group:
         2: members' own launch forms (their set_tuning / autotune); 3: one
         persistent whole-row fused launch per step for every member (the
         resident CTAs shared out among the members).  block_y: rows per sweep
-        block (modes 0, 1)."""
+        block (modes 0, 1); mode 3: 1 = CTAs of 384 threads, 2 = of 192 (two
+        per SM, smaller tiles)."""
         _check(lib().smat_fdtd_group_set_tuning(self._h, mode, block_y))
 
     def autotune(self, nsteps=4):

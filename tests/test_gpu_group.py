@@ -108,8 +108,9 @@ def test_group_members_own_launch_forms(built):
             p.close()
 
 
-@pytest.mark.parametrize("order", [(0, 1, 2, 3), (3, 2, 1, 0), (2,), (1, 3)])
-def test_group_one_persistent_launch(built, order):
+@pytest.mark.parametrize("order,shape", [((0, 1, 2, 3), 1), ((3, 2, 1, 0), 2), ((2,), 1), ((1, 3), 2),
+                                         ((0, 1, 2, 3), 2)])
+def test_group_one_persistent_launch(built, order, shape):
     """Mode 3: one persistent launch of the whole-row fused step per step over
     every member (tiles of up to 16 whole rows per member, the resident CTAs
     shared out among the members, each marching its member's own schedule;
@@ -134,7 +135,7 @@ def test_group_one_persistent_launch(built, order):
     plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
     try:
         with f.Group(plans) as g:
-            g.set_tuning(3, 1)
+            g.set_tuning(3, shape)
             for a, b in windows:
                 g.run(a, b)
         for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
@@ -147,7 +148,8 @@ def test_group_one_persistent_launch(built, order):
             p.close()
 
 
-def test_group_one_persistent_launch_mixed_tiles(built):
+@pytest.mark.parametrize("shape", [1, 2])
+def test_group_one_persistent_launch_mixed_tiles(built, shape):
     """Mode 3 with members whose tiles differ: 256-cell rows (5-row tiles) and
     128-cell rows (11-row tiles), batches 2 and 3, a PML-free member with
     wrapped boundaries -- each member ends with the bits of the member stepped
@@ -175,7 +177,7 @@ def test_group_one_persistent_launch_mixed_tiles(built):
     plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
     try:
         with f.Group(plans) as g:
-            g.set_tuning(3, 1)
+            g.set_tuning(3, shape)
             for a, b in windows:
                 g.run(a, b)
         for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
@@ -204,6 +206,8 @@ def test_group_persistent_launch_refuses_metal(built):
                           precision=f.FP32, pec=sm.pec) as pm:
         with f.Group([p]) as g:
             g.set_tuning(3, 2)
+            with pytest.raises(f.FdtdError):
+                g.set_tuning(3, 3)
         with f.Group([p, pm]) as g:
             with pytest.raises(f.FdtdError):
                 g.set_tuning(3, 1)
