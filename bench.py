@@ -610,7 +610,11 @@ def run_group(args):
         plans.append(p)
         cells += sl.s.n3
     g = F.Group(plans)
-    (gmode, by), _ = g.autotune(4)
+    if args.group_form == 3:  # the one-launch form as it is, without the autotuner's survey
+        gmode, by = 3, 1
+        g.set_tuning(gmode, by)
+    else:
+        (gmode, by), _ = g.autotune(4)
     g.run(0, args.warmup)
     _, t_group = _timed(lambda: g.run(args.warmup, nsteps))
     # the one-launch form (3) timed over the same steps whatever the autotuner chose
@@ -863,6 +867,8 @@ def main():
     ap.add_argument("--cube-steps", type=int, default=4000)
     ap.add_argument("--fd-cells", type=int, default=32)
     ap.add_argument("--group-seed", type=int, default=0)
+    ap.add_argument("--group-form", type=int, default=-1, choices=[-1, 3],
+                    help="--mode group: -1 = the group autotuner's pick, 3 = the one-launch form directly")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
