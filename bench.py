@@ -610,7 +610,7 @@ def run_group(args):
         plans.append(p)
         cells += sl.s.n3
     g = F.Group(plans)
-    if args.group_form == 3:  # the one-launch form as it is, without the autotuner's survey
+    if args.group_form == 3:  # the one-launch form directly, without timing the other forms
         gmode, by = 3, 1
         g.set_tuning(gmode, by)
     else:
