@@ -638,6 +638,11 @@ def run_group(args):
         for p in plans:
             p.sync()
     _, t_sep = _timed(one_by_one)
+    tunings = [list(p.get_tuning()) for p in plans]
+    device_gb = sum(p.device_bytes for p in plans) / 1e9
+    for p in plans:
+        p.close()
+    acc = _group_accuracy(bend, pr, modes, W.slab_shapes(16, seed=args.group_seed)[0], 100)
     print(json.dumps({
         "mode": "group", "config": "bend 256x192x160 x 8 excitations + 16 slabs 128^3..256x256x192, FP32, "
                                    "21-wavelength FP64 DFT on 2 planes each",
@@ -645,16 +650,57 @@ def run_group(args):
         "group_tuning": {"mode": ["one grouped launch per sweep", "members' own sweep launches in one graph",
                                   "members' own autotuned launch forms in one graph",
                                   "one persistent fused launch per step for every member"][gmode],
-                         "block_y": by, "member_tunings": [list(p.get_tuning()) for p in plans]},
+                         "block_y": by, "member_tunings": tunings},
         "group_gcell_per_s": cells * args.steps / t_group / 1e9, "group_ms_per_step": 1e3 * t_group / args.steps,
         "one_launch_gcell_per_s": cells * args.steps / t_one / 1e9,
         "one_launch_form": "mode 3: the resident CTAs shared out among the members, each member's own schedule; "
                            + ("CTAs of 384 threads, one per SM" if shape_one == 1 else "CTAs of 192 threads, two per SM"),
         "separate_plans_gcell_per_s": cells * args.steps / t_sep / 1e9,
-        "device_gb": sum(p.device_bytes for p in plans) / 1e9,
+        "device_gb": device_gb,
+        "fp32_vs_fp64": acc,
     }))
-    for p in plans:
+
+
+def _group_accuracy(bend, pr, modes, slab_shape, slab_seed, nsteps=300):
+    """A fresh one-launch group (form 3) of the bend (its 8 excitations) and one
+    slab, nsteps steps of the pulse; each member's DFT against the FP64 plan of
+    the same structure and source: per (wavelength, plane) slice the relative
+    L2 error, the largest over the slices (the bend's excitation 0)."""
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    sl = W.slab_structure(slab_shape, seed=slab_seed)
+    prs = W.prepare(sl.s, dt_factor=1.0 / 0.99)
+
+    def slab_plan(prec):
+        p = F.Plan.create(sl.s.L, sl.s.iBc, (sl.iB, sl.iT, sl.iI, 1), prs.invtau_R, prs.invtau_I, prs.mu,
+                          prs.epsi, prs.sigma, precision=prec, batch=1)
+        p.set_incident(0, *W.mode_profiles(sl, n_modes=1)[0])
+        src, ph = W.pulse_schedule(nsteps, prs.dt, lams_um=LAMS)
+        p.set_schedule(src, planes=(sl.iB, sl.iT), phase=ph)
+        return p
+
+    def rel(a, b):
+        d = (a - b).reshape(a.shape[0], a.shape[1], -1)
+        r = b.reshape(d.shape)
+        return float(np.max(np.linalg.norm(d, axis=2) / np.linalg.norm(r, axis=2)))
+
+    g32 = [make_plan(bend, pr, modes, F.FP32, BATCH, nsteps, tuning=None), slab_plan(F.FP32)]
+    g = F.Group(g32)
+    g.set_tuning(3, 1)
+    g.run(0, nsteps)
+    g.close()
+    d32 = [dft_fields(g32[0], 0), dft_fields(g32[1], 0)]
+    for p in g32:
         p.close()
+    out = {}
+    for name, mk, d in (("bend", lambda: make_plan(bend, pr, modes, F.FP64, 1, nsteps, tuning=None), d32[0]),
+                        ("slab", lambda: slab_plan(F.FP64), d32[1])):
+        p = mk()
+        p.run(0, nsteps)
+        out[name] = rel(d, dft_fields(p, 0))
+        p.close()
+    return {"dft_max_rel_l2": out, "steps": nsteps, "slab": list(slab_shape),
+            "over": "Hx, Hy, Ex, Ey on both planes x 21 wavelengths, per (wavelength, plane) slice; bend: excitation 0"}
 
 
 def _cube_cpu_worker(args):
