@@ -786,21 +786,53 @@ def run_large(args):
     p = F.Plan.create(st.s.L, st.s.iBc, (st.iB, st.iT, st.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
                       pr.sigma, precision=F.FP32, batch=1, pec=st.s.pec)
     nsteps = args.warmup + args.steps
-    p.set_incident(0, *W.mode_profiles(st, n_modes=1)[0])
-    src, ph = W.pulse_schedule(nsteps, pr.dt, lams_um=[1.55])
-    p.set_schedule(src, planes=(st.iB, st.iT), phase=ph)
+    lams = list(np.linspace(1.50, 1.60, 5))
+    sheets = W.mode_profiles(st, n_modes=1)[0]
+
+    def plan(prec, n):
+        q = F.Plan.create(st.s.L, st.s.iBc, (st.iB, st.iT, st.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
+                          pr.sigma, precision=prec, batch=1, pec=st.s.pec)
+        q.set_incident(0, *sheets)
+        src, ph = W.pulse_schedule(n, pr.dt, lams_um=lams)
+        q.set_schedule(src, planes=(st.iB, st.iT), phase=ph)
+        return q
+
+    p = plan(F.FP32, nsteps)
     t_setup = time.perf_counter() - t0
     best, _ = p.autotune(2)
     p.run(0, args.warmup)
     _, t = _timed(lambda: p.run(args.warmup, nsteps))
     ok, mx = p.check_finite()
+    dev_gb = p.device_bytes / 1e9
+    p.close()
+    # the DFT fields of fresh FP32 and FP64 plans after a bounded pulse run:
+    # per (wavelength, plane) slice the relative L2 error, the largest
+    check = None
+    if args.large_check_steps > 0:
+        n = args.large_check_steps
+        d = {}
+        for prec in (F.FP32, F.FP64):
+            q = plan(prec, n)
+            if prec == F.FP32:
+                q.set_tuning(*best)
+            q.run(0, n)
+            d[prec] = dft_fields(q, 0)
+            q.close()
+        dd = (d[F.FP32] - d[F.FP64]).reshape(len(lams), 2, -1)
+        rr = d[F.FP64].reshape(dd.shape)
+        nd, nr = np.linalg.norm(dd, axis=2), np.linalg.norm(rr, axis=2)
+        live = nr > 1e-9 * nr.max()  # a plane the pulse has not reached yet holds no field
+        check = {"steps": n, "dft_max_rel_l2": float(np.max(nd[live] / nr[live])),
+                 "slices": int(live.sum()), "of": int(live.size),
+                 "over": "Hx, Hy, Ex, Ey on both planes x 5 wavelengths, per (wavelength, plane) slice holding "
+                         "field"}
     print(json.dumps({
-        "mode": "large", "config": "640x640x512 FP32, 12-cell split PML, curved substrate R=50um, PEC patch array",
+        "mode": "large", "config": "640x640x512 FP32, 12-cell split PML, curved substrate R=50um, PEC patch array, "
+                                   "DFT at 5 wavelengths (1.50-1.60 um) on 2 planes",
         "cells": st.s.n3, "split_cells": pr.lnotn, "steps": args.steps, "tuning": list(best),
         "gcell_per_s": st.s.n3 * args.steps / t / 1e9, "ms_per_step": 1e3 * t / args.steps,
-        "device_gb": p.device_bytes / 1e9, "setup_s": t_setup, "finite": ok,
+        "device_gb": dev_gb, "setup_s": t_setup, "finite": ok, "fp32_vs_fp64": check,
     }))
-    p.close()
 
 
 def run_modes(args):
@@ -913,6 +945,8 @@ def main():
     ap.add_argument("--cube-steps", type=int, default=4000)
     ap.add_argument("--fd-cells", type=int, default=32)
     ap.add_argument("--group-seed", type=int, default=0)
+    ap.add_argument("--large-check-steps", type=int, default=600,
+                    help="--mode large: steps of the FP32-vs-FP64 DFT check (0: none)")
     ap.add_argument("--group-form", type=int, default=-1, choices=[-1, 3],
                     help="--mode group: -1 = the group autotuner's pick, 3 = the one-launch form directly")
     ap.add_argument("--gpus", type=int, default=1)
