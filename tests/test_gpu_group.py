@@ -190,6 +190,37 @@ def test_group_one_persistent_launch_mixed_tiles(built, shape):
             p.close()
 
 
+def test_group_persistent_launch_needs_a_cta_per_excitation(built):
+    """Mode 3 gives every excitation its own CTA: 160 excitations exceed the
+    152 resident CTAs of 384 threads (refused, the group keeps its form) but
+    fit the 304 of 192 threads, where the members still end with the bits of
+    the plans stepped alone."""
+    from smatranem_gb300 import fdtd as f
+    from smatranem_gb300 import workloads as W
+    _, sms, _ = f.device_info()
+    L, seed, kw, iBTIin = (16, 6, 8, 1), 51, dict(pml=(2, 2, 2)), (2, 5, 3, 1)
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    batch = sms + 8
+    nsteps = 12
+    with _setup(f, W, s, pr, iBTIin, batch, seed, nsteps) as ref:
+        ref.set_tuning(2, 1, 0, 0, 4)
+        ref.run(0, nsteps)
+        picks = (0, 1, sms - 1, batch - 1)  # CTAs at both ends of the member's range
+        want = [(*ref.get_fields(b), *[ref.get_dft(b, 0, q) for q in range(3)]) for b in picks]
+    with _setup(f, W, s, pr, iBTIin, batch, seed, nsteps) as p:
+        with f.Group([p]) as g:
+            g.set_tuning(1, 1)
+            with pytest.raises(f.FdtdError):
+                g.set_tuning(3, 1)
+            g.set_tuning(3, 2)
+            g.run(0, nsteps)
+        got = [(*p.get_fields(b), *[p.get_dft(b, 0, q) for q in range(3)]) for b in picks]
+    for rb, gb in zip(want, got):
+        for a, b_ in zip(rb, gb):
+            assert np.array_equal(a, b_)
+
+
 def test_group_persistent_launch_refuses_metal(built):
     """Mode 3 has no stable-form path: a member with metal cells is refused
     and the group keeps its form."""
