@@ -32,6 +32,7 @@ oracle; all host cores as independent processes, one excitation each).
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import math
 import multiprocessing as mp
@@ -74,10 +75,9 @@ TRAFFIC_PER_LAUNCH = {
 
 
 def launches_per_step(tuning, L2):
-    """Update-kernel launches of one step: one fused launch (kernels 1, 3, 5,
-    6), or an H and an E sweep per z-chunk (kernels 0, 2; z_chunk 0 = one
-    chunk)."""
-    if tuning[0] in (1, 3, 5, 6):
+    """Update-kernel launches of one step: one fused launch (kernel 6), or an
+    H and an E sweep per z-chunk (kernels 0, 2; z_chunk 0 = one chunk)."""
+    if tuning[0] == 6:
         return 1
     zc = tuning[2]
     return 2 * (1 if zc <= 0 or zc >= L2 else math.ceil(L2 / zc))
@@ -235,37 +235,72 @@ def s_parameters(p, bend, modes, b):
 # CPU baseline (oracle) -- bounded samples
 # ---------------------------------------------------------------------------
 
-def _cpu_worker(args):
-    """One process: `nsteps` oracle main_calc steps of the full bend, one excitation."""
-    shape, nsteps, kind = args
-    import oracle
-    bend, pr, modes = make_workload(shape, solve_modes=False)  # no GPU in this process
-    o = oracle.Oracle(kind)
-    Ah, Bh, Ae, Be = pr.coefficients()
-    s = bend.s
-    n3 = s.n3
-    pl = s.L[0] * s.L[1]
-    H = np.zeros(3 * (n3 + pr.lnotn + 1))
-    E = np.zeros_like(H)
-    Hinc, Einc = modes["fwd"][0]
-    rng = np.random.default_rng(0)
-    H[:3 * n3] = rng.standard_normal(3 * n3) * 1e-3
-    mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
-    t0 = time.perf_counter()
-    o.time_loop(s.L, Ah, Bh, Ae, Be, s.iBc, H, E, (bend.iB, bend.iT, bend.iI, 1), Hinc, Einc, pr.n2pi, (1, 1, 3),
-                0, nsteps, *mons, pr.cont, pr.addr)
-    return time.perf_counter() - t0, n3 * nsteps
-
-
-def cpu_rate(nproc, shape, nsteps, kind):
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(nproc) as pool:
+def _cpu_worker(shape, warmup, nsteps, kind, idx, barrier, queue):
+    """One process: `warmup` untimed then `nsteps` timed main_calc steps of the
+    full bend, one excitation, on the CPU oracle.  Loads only the oracle's
+    libraries: the structure is numpy (workloads' generators), the
+    precompute is the oracle port's (oracle.prepare), the sheet is a Gaussian
+    stand-in (the update rate does not depend on the sheet)."""
+    try:
+        import oracle
+        from smatranem_gb300 import workloads as W
+        bend = W.bend_structure(shape=shape)
+        s = bend.s
+        pr = oracle.prepare(s.L, s.mu, s.epsi, s.omega, s.min_dt, dt_factor=1.0 / 0.99)
+        bend.s = s = dataclasses.replace(s, mu=None, epsi=None)  # the media are no longer needed
+        o = oracle.Oracle(kind)
+        n3 = s.L[0] * s.L[1] * s.L[2]
+        pl = s.L[0] * s.L[1]
+        H = np.zeros(3 * (n3 + pr["lnotn"] + 1))
+        E = np.zeros_like(H)
+        Hinc, Einc = W.mode_profiles(bend, n_modes=N_MODES)[idx % N_MODES]
+        rng = np.random.default_rng(idx)
+        H[:3 * n3] = rng.standard_normal(3 * n3) * 1e-3
+        mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
+        args = (s.L, pr["Ah"], pr["Bh"], pr["Ae"], pr["Be"], s.iBc, H, E, (bend.iB, bend.iT, bend.iI, 1), Hinc, Einc,
+                pr["n2pi"], (1, 1, 3))
+        o.time_loop(*args, 0, warmup, *mons, pr["cont"], pr["addr"])
+        barrier.wait(timeout=1800)
         t0 = time.perf_counter()
-        res = pool.map(_cpu_worker, [(shape, nsteps, kind)] * nproc)
-        wall = time.perf_counter() - t0
-    cells = sum(r[1] for r in res)
-    tmax = max(r[0] for r in res)
-    return cells / tmax, tmax, wall
+        o.time_loop(*args, warmup, warmup + nsteps, *mons, pr["cont"], pr["addr"])
+        queue.put((idx, time.perf_counter() - t0, n3, pr["lnotn"], None))
+    except Exception as e:  # reported by the parent
+        barrier.abort()
+        queue.put((idx, None, None, None, repr(e)))
+
+
+def cpu_rate(nproc, shape, warmup, nsteps, kind):
+    """nproc independent oracle processes (spawned, no CUDA in any of them),
+    their timed regions started together behind a barrier.  Returns
+    (cell-updates/s over all processes, the slowest process's timed seconds,
+    cells, split cells)."""
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(nproc)
+    queue = ctx.Queue()
+    procs = [ctx.Process(target=_cpu_worker, args=(shape, warmup, nsteps, kind, i, barrier, queue))
+             for i in range(nproc)]
+    for pr in procs:
+        pr.start()
+    res = []
+    try:
+        while len(res) < nproc:
+            try:
+                res.append(queue.get(timeout=5))
+            except Exception:
+                dead = [pr.exitcode for pr in procs if pr.exitcode not in (None, 0)]
+                if dead:
+                    raise RuntimeError(f"CPU oracle worker died (exit {dead[0]})")
+    finally:
+        for pr in procs:
+            pr.join(timeout=60)
+            if pr.is_alive():
+                pr.kill()
+    bad = [r[4] for r in res if r[4]]
+    if bad:
+        raise RuntimeError("CPU oracle worker failed: " + bad[0])
+    tmax = max(r[1] for r in res)
+    n3, lnotn = res[0][2], res[0][3]
+    return nproc * n3 * nsteps / tmax, tmax, n3, lnotn
 
 
 def oracle_kind():
@@ -310,27 +345,41 @@ def dist_barrier(ws):
         dist.barrier()
 
 
+def bench_config(n3, n_split, batch, ws):
+    """The `config` of the contract line (the same for both arms)."""
+    return {"workload": WORKLOAD, "cells": n3, "split_cells": n_split, "batch": batch,
+            "l2": "inputs larger than L2 (fields of %d excitations: %.1f GB)" % (batch, batch * 4 * 3 * n3 * 4 / 1e9),
+            "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"}
+
+
 def run_reference(args):
+    """The reference arm: the reference's CPU implementation of the step (the
+    oracle: the reference compiled from its own source where it was built
+    here, else the restatement) on every host core, as independent
+    single-threaded processes (the reference has no threads; S columns are
+    independent), each stepping one excitation of the full bend: --warmup
+    untimed steps, then exactly --steps timed steps, started together.  No
+    process loads the CUDA library."""
     ws, rank, local = dist_setup()
     if rank != 0:
         return
     kind = oracle_kind()
     nproc = os.cpu_count() or 1
     shape = (256, 192, 160)
-    nsteps = args.ref_steps
     t_all = time.perf_counter()
-    rate, tmax, wall = cpu_rate(nproc, shape, nsteps, kind)
+    rate, tmax, n3, lnotn = cpu_rate(nproc, shape, args.warmup, args.steps, kind)
     g = rate / 1e9
-    sample = (f"{nproc} independent processes (one excitation each, the reference is single-threaded), "
-              f"{nsteps} main_calc steps of the full bend each; {tmax:.1f} s timed per process")
+    sample = (f"{nproc} independent single-threaded processes, one excitation of the full bend each (Gaussian "
+              f"stand-in sheet), {args.warmup} untimed + {args.steps} timed main_calc steps each, timed regions "
+              f"started together; slowest process {tmax:.2f} s")
     line = {"impl": "reference", "metric": METRIC, "value": g, "unit": "Gcell-updates/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmax / nsteps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmax / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": sample},
+            "config": bench_config(n3, lnotn, args.batch, args.gpus),
             "cpu_baseline": {"value": g, "unit": "Gcell-updates/s", "cores": nproc, "kind": kind,
                              "sample": sample},
             "e2e": {"value": g, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": time.perf_counter() - t_all}
+            "gpu_launches": 0, "wall_s": time.perf_counter() - t_all}
     print(json.dumps(line))
 
 
@@ -429,9 +478,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         kind = oracle_kind()
-        rate, tmax, wall = cpu_rate(1, (256, 192, 160), args.cpu_steps, kind)
+        rate, tmax, _, _ = cpu_rate(1, (256, 192, 160), 1, args.cpu_steps, kind)
         cpu = {"value": rate / 1e9, "unit": "Gcell-updates/s", "cores": 1, "kind": kind,
-               "sample": f"{args.cpu_steps} main_calc steps of the full bend, one excitation, "
+               "sample": f"{args.cpu_steps} main_calc steps of the full bend after 1 untimed, one excitation, "
                          f"{tmax:.1f} s on 1 core"}
     if rank != 0:
         return
@@ -439,9 +488,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": n3, "split_cells": n_split, "batch": batch,
-                   "l2": "inputs larger than L2 (fields of 8 excitations: %.1f GB)" % (batch * 4 * 3 * n3 * 4 / 1e9),
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+        "config": bench_config(n3, n_split, batch, ws),
         "e2e": {"value": e2e, "unit": "Gcell-updates/s", "h2d_bytes_per_step": h2d / full,
                 "d2h_bytes_per_step": d2h / full, "what": f"create+incident+schedule+{full} steps+DFT read-back, "
                                                           f"{t_e2e:.2f} s"},
@@ -449,12 +496,8 @@ def run_ours(args):
                      "peak_kind": peak_kind,
                      "traffic": TRAFFIC_PER_LAUNCH.get(tuple(tuning[:3])) if batch == BATCH else None,
                      "traffic_per": "launch (ncu, dram read + write)",
-                     "kernel": {1: "k_fused32 (one fused H+E launch per step)",
-                                2: "k_sweep32v (H, E; float4)" + (f", z-chunks of {tuning[2]} planes"
+                     "kernel": {2: "k_sweep32v (H, E; float4)" + (f", z-chunks of {tuning[2]} planes"
                                                                    if 0 < tuning[2] < bend.s.L[2] else ""),
-                                3: "k_fused32t (one fused H+E launch per step, TMA-staged planes)",
-                                4: "k_pipe32v (pipelined H/E sweeps in one cooperative launch)",
-                                5: "k_zm32 (one fused H+E launch per step: 128x4 tiles, TMA producer warp)",
                                 6: f"k_row32 (one fused H+E launch per step: z-march of {tuning[1]} whole x rows"
                                    f" per CTA, float4 quads)",
                                 0: "k_sweep32 (H, E)"}[tuning[0]],
@@ -704,25 +747,27 @@ def _group_accuracy(bend, pr, modes, slab_shape, slab_seed, nsteps=300):
 
 
 def _cube_cpu_worker(args):
-    """One process: `nsteps` oracle main_calc steps of the 96^3 cube."""
+    """One process: `nsteps` oracle main_calc steps of the 96^3 cube (precompute
+    by the oracle port; no CUDA library in this process)."""
     nsteps, kind = args
     import oracle
     from smatranem_gb300 import workloads as W
     c = W.cube_structure()
-    pr = W.prepare(c.s, dt_factor=1.0 / 0.99)
+    s = c.s
+    pr = oracle.prepare(s.L, s.mu, s.epsi, s.omega, s.min_dt, dt_factor=1.0 / 0.99)
     o = oracle.Oracle(kind)
-    Ah, Bh, Ae, Be = pr.coefficients()
-    cells = np.flatnonzero(c.s.pec)
+    Ah, Bh, Ae, Be = pr["Ah"], pr["Bh"], pr["Ae"], pr["Be"]
+    cells = np.flatnonzero(s.pec)
     for k in range(3):  # the PEC plate
         Ae[3 * cells + k] = 0.0
         Be[3 * cells + k] = 0.0
-    n3, pl = c.s.n3, c.s.L[0] * c.s.L[1]
-    H = np.zeros(3 * (n3 + pr.lnotn + 1))
+    n3, pl = s.n3, s.L[0] * s.L[1]
+    H = np.zeros(3 * (n3 + pr["lnotn"] + 1))
     E = np.zeros_like(H)
     mons = [np.zeros(2 * pl, np.complex128) for _ in range(4)]
     t0 = time.perf_counter()
-    o.time_loop(c.s.L, Ah, Bh, Ae, Be, c.s.iBc, H, E, (c.iM, c.iM, c.iI, 1), *W.point_source(c), pr.n2pi,
-                (1, 1, 3), 0, nsteps, *mons, pr.cont, pr.addr)
+    o.time_loop(s.L, Ah, Bh, Ae, Be, s.iBc, H, E, (c.iM, c.iM, c.iI, 1), *W.point_source(c), pr["n2pi"],
+                (1, 1, 3), 0, nsteps, *mons, pr["cont"], pr["addr"])
     return time.perf_counter() - t0, n3 * nsteps
 
 
@@ -957,7 +1002,6 @@ def main():
     ap.add_argument("--full-steps", type=int, default=FULL_STEPS)
     ap.add_argument("--steps64", type=int, default=40)
     ap.add_argument("--cpu-steps", type=int, default=8)
-    ap.add_argument("--ref-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", choices=["fp32", "fp64"], help="small case for ncu captures")
     ap.add_argument("--shape", default="256,192,48")

@@ -237,7 +237,8 @@ int smat_overlap(int npix, int ncols, int nvec, long long vec_stride, const doub
  * loads the library until exit); a call needing more (ncols * nvec * blocks,
  * blocks <= 64 and about 4*npix/1024) fails with SMAT_EINVAL before launching.
  * The first call on a device looks up the array's device address (no
- * allocation); make that first call outside any stream capture.  All calls on
+ * allocation), and so does the first call after the device's context was
+ * re-created (cudaDeviceReset); make such a call outside any stream capture.  All calls on
  * a device share the array: calls that overlap on the GPU (different streams,
  * no ordering) race and corrupt each other's results; calls ordered on one
  * stream are safe.  Results equal smat_overlap's bit for bit. */
@@ -356,16 +357,6 @@ int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double
  *             tile_y 1..4; the default where it applies); z_chunk as for 0;
  *             ctas_per_sm = register bound as minimum resident blocks (0 or 5:
  *             96 registers, 6, 8), or -3 for two z-planes per thread (168).
- *   kernel 1: one fused z-marching launch per step with tiles of 32 x tile_y
- *             cells (2..8), z chunks of z_chunk planes, ctas_per_sm resident
- *             CTAs (0: as many as fit) and `slots` shared-memory plane slots
- *             (4..6: planes staged 1..3 ahead).
- *   kernel 3: kernel 1 with TMA plane staging (L0 % 4 == 0).
- *   kernel 4: H and E sweeps pipelined in one cooperative launch; tile_y rows
- *             per item, z_chunk = how many planes H may run ahead of E (0: no
- *             limit, else >= 2).
- *   kernel 5: one fused launch per step on 128 x 4 tiles with a TMA producer
- *             warp (L0 % 4 == 0, iBc = 0 on every axis); z_chunk planes per item.
  *   kernel 6: one fused launch per step; a CTA marches tile_y whole x rows
  *             along z through z_chunk planes (0: persistent CTAs), four cells
  *             a thread, the next plane's inputs staged by cp.async;
@@ -373,13 +364,14 @@ int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double
  *             slots is not used; for plans with L0 % 4 == 0 and no
  *             stable-form metal or lossy split cells (lossy and PEC ordinary
  *             cells run an out-of-line record update).
- * Results are bit-identical across configurations. */
+ * Other kernel codes are refused (SMAT_EINVAL).  Results are bit-identical
+ * across configurations. */
 int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int kernel, int tile_y, int z_chunk, int ctas_per_sm,
                          int slots);
 /* {kernel, tile_y, z_chunk, ctas_per_sm, slots} of the plan. */
 int smat_fdtd_get_tuning(const smat_fdtd_plan *plan, int out[5]);
-/* Autotuner: times the candidate FP32 configurations (tile rows, staged
- * slots, z chunk; fused and two-sweep) for nsteps steps each on this plan's
+/* Autotuner: times the candidate FP32 configurations (tile rows, z chunk,
+ * register bound; the fused step and the two sweeps) for nsteps steps each on this plan's
  * structure and batch, and keeps the fastest (returned in best, its time per
  * step in *best_ms; either may be NULL).  Needs the zero state (call it before
  * set_fields / run); sources and DFT sampling are off while it runs, so the

@@ -26,7 +26,16 @@ REF_LIB = os.path.join(HERE, "_ref", "libref_fdtd.so")
 REF_BIN = os.path.join(HERE, "_ref", "FDTD_ref")
 MCALC_BIN = os.path.join(HERE, "_ref", "Mcalc_ref")
 SCALC_BIN = os.path.join(HERE, "_ref", "Scalc_ref")
-REF_DIR_DEFAULT = "/root/reference"
+
+
+def reference_dir() -> str:
+    """Where the reference sources are read from: $SMATRAN_REFERENCE_DIR, else
+    the directory named ``reference`` beside this repository's directory."""
+    env = os.environ.get("SMATRAN_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
 
 _P = C.c_void_p
 
@@ -44,15 +53,15 @@ def _newer(target, deps):
 def build(with_reference: bool | None = None) -> None:
     """Compile the port (always) and the reference (when its sources exist).
 
-    The reference is compiled from its own file under SMATRAN_REFERENCE_DIR
-    (default /root/reference): a shared object with main renamed and exit()
+    The reference is compiled from its own file under reference_dir(): a
+    shared object with main renamed and exit()
     made non-fatal (ref_prelude.h), and the stock command-line binary.
     Nothing from the reference tree is copied; outputs go to _ref/ only."""
     os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
     src = os.path.join(HERE, "fdtd_oracle.c")
     if _newer(PORT_LIB, [src, os.path.join(HERE, "fdtd_oracle.h")]):
         subprocess.run(["gcc", *CFLAGS, "-Wall", "-shared", src, "-o", PORT_LIB, "-lm"], check=True)
-    ref_dir = os.environ.get("SMATRAN_REFERENCE_DIR", REF_DIR_DEFAULT)
+    ref_dir = reference_dir()
     ref_src = os.path.join(ref_dir, "FDTDcalc", "FDTDsplitfieldMetal.c")
     if with_reference is None:
         with_reference = os.path.isfile(ref_src)
@@ -259,6 +268,26 @@ class Oracle:
         S = np.zeros(ncol, dtype=np.complex128)
         self.lib.orc_overlap(_ptr(L), ncol, _ptr(t), _ptr(HB), _ptr(EB), _ptr(S))
         return S
+
+
+def prepare(L, mu, epsi, omega, min_dt, dt_factor=1.0):
+    """The reference precompute of main :62-143 through the port alone, for a
+    process that must not load the CUDA library (the CPU timing workers):
+    set_sigma, remove_sigma, set_address, set_tau (with min_Dt divided by
+    dt_factor, as main :92 divides it by Dt_factor) and the coefficient arrays.
+    mu, epsi: the stretched media as the Med files hold them, complex (n3*3,).
+    Returns a dict of sigma, mu, epsi, cont, addr, lnotn, n2pi, invtau_R,
+    invtau_I, Ah, Bh, Ae, Be."""
+    o = Oracle("port")
+    mu = np.ascontiguousarray(np.asarray(mu, np.complex128).reshape(-1))
+    epsi = np.ascontiguousarray(np.asarray(epsi, np.complex128).reshape(-1))
+    sigma = o.set_sigma(L, mu, epsi)
+    mu2, ep2 = o.remove_sigma(L, mu, epsi, sigma)
+    cont, addr, lnotn = o.set_address(L, sigma, mu2, ep2)
+    n2pi, inv_r, inv_i = o.set_tau(omega, min_dt / dt_factor)
+    Ah, Bh, Ae, Be = o.coefficients(L, lnotn, sigma, mu2, ep2, cont, addr, inv_r, inv_i)
+    return {"sigma": sigma, "mu": mu2, "epsi": ep2, "cont": cont, "addr": addr, "lnotn": lnotn, "n2pi": n2pi,
+            "invtau_R": inv_r, "invtau_I": inv_i, "Ah": Ah, "Bh": Bh, "Ae": Ae, "Be": Be}
 
 
 def expn_table(n2pi: int) -> np.ndarray:

@@ -38,7 +38,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" 
 NV_EXTRA = {"fdtd_f64.cu": ["-fmad=false"]}
 
 C_SOURCES = ["host_precompute.c", "errors.c", "deck_io.c"]
-CU_SOURCES = ["fdtd_f64.cu", "fdtd_f32.cu", "fdtd_fused32.cu", "fdtd_plan.cu", "fdtd_overlap.cu", "fdtd_adjoint.cu",
+CU_SOURCES = ["fdtd_f64.cu", "fdtd_f32.cu", "fdtd_plan.cu", "fdtd_overlap.cu", "fdtd_adjoint.cu",
               "fdtd_group.cu", "mode_solver.cu", "dense_z.cu", "scalc.cu", "fdtd_row32.cu"]
 
 

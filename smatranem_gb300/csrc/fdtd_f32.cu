@@ -764,174 +764,6 @@ __global__ void k_general32(const P32 p, const int rel, const int *cells, int nc
 }
 
 /* ---------------------------------------------------------------------------
- * Pipelined sweeps (kernel 4).  The same quad and general-cell updates as
- * k_sweep32v / k_general32 (so the same bits), but H and E of one step run in
- * one launch, ordered plane by plane: the E sweep of plane z runs right after
- * the H sweep of plane z+1, while the old E of plane z (read by both H sweeps
- * around it) and the new H of planes z, z+1 are still in L2.  HBM then sees
- * each field read once and written once per step, as in a fused kernel, with
- * the sweeps' access pattern and occupancy.
- *
- * The E sweep of plane z runs D planes behind the H sweep (after H(z+D)), so
- * that what it waits for was issued a group or more earlier.
- *
- * Items are assigned statically (item i to CTA i mod grid, in increasing i)
- * and every wait is on an H item of an earlier group, so with all CTAs
- * resident (a cooperative launch) the earliest unfinished item can always
- * proceed.  Waits are bounded: after ~2^22 polls the CTA records error 2 and
- * goes on (results are then invalid, the launch still ends).
- * ------------------------------------------------------------------------- */
-__device__ __forceinline__ int ld_acquire_gpu(const int *p)
-{
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release_gpu(int *p, int v)
-{
-    asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ void red_add_release_gpu(int *p, int v)
-{
-    asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
-}
-
-/* E-plane progress counters count finished items and are never reset: launch
- * `ep` has finished plane z when the counter reaches ep * per_plane */
-__device__ __forceinline__ bool wait_epoch_count(const int *ctr, int ep, int per_plane)
-{
-    const int want = ep * per_plane;
-    for (int it = 0; it < (1 << 22); it++) {
-        if (ld_acquire_gpu(ctr) - want >= 0) return true;
-        __nanosleep(64);
-    }
-    return false;
-}
-
-__device__ __forceinline__ bool wait_epoch(const int *flag, int ep)
-{
-    for (int it = 0; it < (1 << 22); it++) {
-        if (ld_acquire_gpu(flag) - ep >= 0) return true;
-        __nanosleep(64);
-    }
-    return false;
-}
-
-/* out of line: general cells are rare and must not cost the quads registers */
-__device__ __noinline__ void pipe_general(const P32 &p, int rel, int b, long long l, bool efield)
-{
-    if (efield) general32_cell<true, true>(p, rel, b, l);
-    else general32_cell<false, false>(p, rel, b, l);
-}
-
-/* the items of one sweep (H: EF = false, E: EF = true) taken by `ncta` CTAs,
- * this one being number `cta`: plane-major order, (row block, excitation)
- * inside a plane */
-template <bool EF>
-__device__ __forceinline__ void pipe_loop(const P32 &p, const int rel, const Pipe32 &pp, const int ep, const int cta,
-                                          const int ncta)
-{
-    const Geo &g = p.g;
-    const int per_plane = pp.nyb * p.batch;
-    const int nitems = g.L2 * per_plane;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-    const int L2 = g.L2;
-    auto hflag = [&](int z, int yb, int b) { return pp.hflag + ((long long)z * pp.nyb + yb) * p.batch + b; };
-    for (int item = cta; item < nitems; item += ncta) {
-        const int z = item / per_plane, r = item % per_plane;
-        const int b = r % p.batch, yb = r / p.batch;
-        if (EF) {
-            /* lanes 0..4 of warp 0 each wait on one H item, in parallel */
-            if (tid < 5) {
-                const int zn = z + 1 == L2 ? 0 : z + 1, yn = yb + 1 == pp.nyb ? 0 : yb + 1;
-                const int yp = yb == 0 ? pp.nyb - 1 : yb - 1;
-                /* stable-form E cells read the new H of their backward
-                 * neighbours (waits 3, 4); plans that wrap z with such cells
-                 * are not pipelined, so plane 0 has no z-1 dependence */
-                const int *f = tid == 0 ? hflag(z, yb, b) : tid == 1 ? hflag(z, yn, b) : tid == 2 ? hflag(zn, yb, b)
-                             : tid == 3 ? (pp.wait_back && z > 0 ? hflag(z - 1, yb, b) : nullptr)
-                                        : (pp.wait_back ? hflag(z, yp, b) : nullptr);
-                if (f && !wait_epoch(f, ep)) atomicExch(pp.err, 2);
-            }
-            __syncthreads();
-        } else if (pp.lag > 0 && z >= pp.lag) {
-            /* keep the H sweep at most `lag` planes ahead of the E sweep, so
-             * that what E re-reads is still in L2 */
-            if (tid == 0 && !wait_epoch_count(pp.eplane + (z - pp.lag), ep, per_plane)) atomicExch(pp.err, 2);
-            __syncthreads();
-        }
-        /* rows [yb*R, yb*R + R) of plane z, blockDim.y rows at a time */
-        const int R = pp.by, yend = min(g.L1, yb * R + R);
-        for (int j1 = yb * R + threadIdx.y; j1 < yend; j1 += blockDim.y) { /* uniform per warp: one row each */
-            for (int xb = 0; xb * 4 * (int)blockDim.x < g.L0; xb++)
-                sweep32v_quad<EF, EF>(p, rel, b, j1, z, (xb * blockDim.x + threadIdx.x) * 4);
-        }
-        const int *grow = EF ? pp.egen_row : pp.hgen_row;
-        const int g0 = grow[z * pp.nyb + yb], g1 = grow[z * pp.nyb + yb + 1];
-        if (g1 > g0) {
-            __syncthreads(); /* the quads stored placeholders for these cells */
-            const int *gl = EF ? pp.egen : pp.hgen;
-            for (int i = g0 + tid; i < g1; i += nthr) pipe_general(p, rel, b, gl[i], EF);
-        }
-        __syncthreads();
-        /* release at gpu scope after the barrier: cumulative over the CTA's writes */
-        if (tid == 0) {
-            if (!EF) st_release_gpu(hflag(z, yb, b), ep);
-            else if (pp.lag > 0) red_add_release_gpu(pp.eplane + z, 1);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(128, 5) k_pipe32v(const P32 p, const int rel, const Pipe32 pp)
-{
-    const int ep = ld_acquire_gpu(&pp.ctl[0]) + 1;
-    /* CTAs [0, nh) run the H sweep, the rest the E sweep: H CTAs wait only on
-     * finished E planes `lag` behind, E CTAs on H items of their own and the
-     * next plane; with every CTA resident (a cooperative launch) both ends
-     * always have a runnable item */
-    const int nh = gridDim.x / 2;
-    if ((int)blockIdx.x < nh) pipe_loop<false>(p, rel, pp, ep, blockIdx.x, nh);
-    else pipe_loop<true>(p, rel, pp, ep, blockIdx.x - nh, gridDim.x - nh);
-    /* the last CTA out publishes the epoch for the next launch */
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        __threadfence();
-        const int n = atomicAdd(&pp.ctl[1], 1);
-        if (n == (int)gridDim.x - 1) {
-            pp.ctl[1] = 0;
-            __threadfence();
-            atomicAdd(&pp.ctl[0], 1);
-        }
-    }
-}
-
-int pipe32v_max_ctas_per_sm(int threads)
-{
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pipe32v, threads, 0) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    return n;
-}
-
-void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStream_t st)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(pp.nxw, 128 / pp.nxw); /* rows of an item are walked blockDim.y at a time */
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_pipe32v, p, rel, pp);
-}
-
-/* ---------------------------------------------------------------------------
  * Groups: the vectorised H (E) sweep of every member plan in one launch.
  * Block i belongs to the member m with blk[m] <= i < blk[m+1]; inside it the
  * block decodes exactly as a k_sweep32v block (x block fastest, then row

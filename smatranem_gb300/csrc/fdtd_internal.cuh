@@ -27,7 +27,7 @@
 #define SMATRAN_FDTD_INTERNAL_CUH
 
 #include <cstdint>
-#include <cuda.h>
+#include <cuda_runtime.h>
 
 namespace smat {
 
@@ -101,25 +101,6 @@ struct P32 {
     Dft d;
 };
 
-/* Pipelined sweeps (kernel 4): one cooperative launch per step.  Items are
- * (plane z, block of `by` rows, excitation b); half of the CTAs take the H
- * items, half the E items, each in plane order.  An E item waits until the H
- * items it reads (and whose E inputs it overwrites) have finished, through
- * per-item flags stamped with a launch epoch; an H item waits until the E
- * sweep is at most `lag` planes behind. */
-struct Pipe32 {
-    int by, nyb, nitems;            /* rows per item, row blocks per plane, items per step */
-    int nxw;                        /* threads along x (a multiple of 32): four cells each */
-    int lag;                        /* H may run at most `lag` planes ahead of E (0: no limit, else >= 2) */
-    int *eplane;                    /* [L2]: finished E items per plane, cumulative over launches */
-    int *hflag;                     /* [L2][nyb][batch]: epoch of the finished H item */
-    int *ctl;                       /* [0] epoch of the last finished launch, [1] exit count */
-    int *err;                       /* set to 2 when a wait gives up */
-    const int *hgen, *egen;         /* general (record) cells, cell order */
-    const int *hgen_row, *egen_row; /* [L2*nyb + 1]: first general cell of item (z, yb) */
-    int wait_back;                  /* E items also wait for H(z-1), H(z, yb-1) (stable-form E cells) */
-};
-
 /* Several FP32 plans stepped together (a group): one vectorised-sweep launch
  * covers the cells of every member; block ranges and general-cell ranges per
  * member are prefix sums.  Loaded into a constant-memory table before the
@@ -132,24 +113,6 @@ struct Group32 {
     const int *hgen[MAX_GROUP], *egen[MAX_GROUP];
     int nhgen[MAX_GROUP], negen[MAX_GROUP];
     P32 p[MAX_GROUP];
-};
-
-/* the fused FP32 step: reads the field set in p, writes the other set */
-struct Fused32 {
-    P32 p;
-    float *Hn, *En, *Han, *Ean; /* new set */
-    int ty, zc, ns;             /* tile rows, z-chunk length, staged plane slots (4..6) */
-    int ntx, nty, nzc, nitems;  /* work items: batch x tiles x z-chunks */
-    const int *stable;          /* cells whose E update is the stable form */
-    int nstable;
-};
-
-/* the fused step with TMA staging: tensor maps of the current ("old") field set
- * and of the coefficient streams, and the pipeline error flag */
-struct Fused32T {
-    Fused32 f;
-    CUtensorMap mE, mH, mEa, mHa, mBh, mBe;
-    int *err;
 };
 
 /* The work of one CTA of launch form 6 (excitation aside): pieces (row tile yt,
@@ -232,20 +195,8 @@ void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st);
 /* mb: register bound of the vectorised sweep (minimum resident blocks: 5, 6 or 8) */
 void launch_h32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int ngh, cudaStream_t st);
 void launch_e32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const int *gcells, int nge, cudaStream_t st);
-void launch_pipe32v(const P32 &p, int rel, const Pipe32 &pp, int grid, cudaStream_t st);
 void load_group32(const Group32 *host_pinned, cudaStream_t st);
 void launch_group32v(const Group32 &gr, int rel, cudaStream_t st);
-int pipe32v_max_ctas_per_sm(int threads);
-void launch_fused32(const Fused32 &f, int rel, int grid, cudaStream_t st);
-size_t fused32_smem(int ty, int ns);
-void launch_fused32t(const Fused32T &f, int rel, int grid, cudaStream_t st);
-/* kernel 5: 128 x 4 tiles, TMA producer warp (plans with iBc = 0 only) */
-void launch_zm32(const Fused32T &f, int rel, int grid, cudaStream_t st);
-size_t zm32_smem();
-int zm32_max_ctas_per_sm();
-size_t fused32t_smem(int ty, int ns);
-int fused32t_max_ctas_per_sm(int ty, int ns);
-int fused32_max_ctas_per_sm(int ty, int ns);
 /* form 6: threads of a CTA (one per quad of its ty + 1 rows, rounded up to
  * whole warps), shared memory, resident CTAs of ty rows and z chunks of zc
  * planes at register bound mb (1, 2 or 3 CTAs per SM; 1 for plans with record

@@ -11,6 +11,7 @@
  * values), then one thread per (v, c) adds the partials in block order.  The
  * grid is a function of npix only, so a result is the same bits on every call.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -185,8 +186,31 @@ static __device__ __align__(256) double2 g_overlap_scratch[SMAT_OVERLAP_NOALLOC_
 namespace {
 constexpr int MAX_DEVICES = 64;
 std::mutex g_noalloc_mu;
+/* the array's device address per device, and the context it was taken in: a
+ * context destroyed and re-created (cudaDeviceReset, a primary context
+ * released by its last user) reloads the module, so the address is looked up
+ * again when the current context is not the one it was taken in */
 double2 *g_noalloc_addr[MAX_DEVICES];
+CUcontext g_noalloc_ctx[MAX_DEVICES];
+
+typedef CUresult (*ctx_get_current_fn)(CUcontext *);
+ctx_get_current_fn ctx_get_current()
+{
+    static ctx_get_current_fn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &ptr, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (ctx_get_current_fn)ptr;
+        else
+            cudaGetLastError();
+    }
+    return fn;
 }
+} // namespace
 
 extern "C" int smat_overlap_noalloc(int npix, int ncols, int nvec, long long vec_stride, const double *tilXi,
                                     const double *dft, double *S, void *stream)
@@ -206,15 +230,20 @@ extern "C" int smat_overlap_noalloc(int npix, int ncols, int nvec, long long vec
     if (dev < 0 || dev >= MAX_DEVICES) return smat_fail(SMAT_EINVAL, "overlap_noalloc: device %d out of range", dev);
     double2 *scratch = nullptr;
     {
-        /* once per device, with that device current: the device address of the
-         * static array (the host-side symbol is not a device address) */
+        /* once per device (and context), with that device current: the device
+         * address of the static array (the host-side symbol is not a device
+         * address) */
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
+        CUcontext ctx = nullptr;
+        ctx_get_current_fn get = ctx_get_current();
+        const bool known_ctx = get && get(&ctx) == CUDA_SUCCESS && ctx;
+        if (!g_noalloc_addr[dev] || !known_ctx || ctx != g_noalloc_ctx[dev]) {
             void *ptr = nullptr;
             e = cudaGetSymbolAddress(&ptr, g_overlap_scratch);
             if (e != cudaSuccess || !ptr)
                 return smat_fail(SMAT_ECUDA, "overlap_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
             g_noalloc_addr[dev] = (double2 *)ptr;
+            g_noalloc_ctx[dev] = known_ctx ? ctx : nullptr;
         }
         scratch = g_noalloc_addr[dev];
     }

@@ -7,8 +7,6 @@
  * main :146-167) and its per-step main_calc (:242-329); the host precompute
  * in host_precompute.c replaces main :62-143.
  */
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -109,26 +107,6 @@ P32 make_p32(const smat_fdtd_plan *p, bool xp)
     return q;
 }
 
-Fused32 make_fused(const smat_fdtd_plan *p, bool xp)
-{
-    Fused32 f;
-    f.p = make_p32(p, xp);
-    f.Hn = p->cur ? p->d_H32 : p->d_H32b;
-    f.En = p->cur ? p->d_E32 : p->d_E32b;
-    f.Han = p->cur ? p->d_Ha32 : p->d_Ha32b;
-    f.Ean = p->cur ? p->d_Ea32 : p->d_Ea32b;
-    f.ty = p->ty;
-    f.zc = p->zc;
-    f.ns = p->ns;
-    f.ntx = (p->L[0] + 31) / 32;
-    f.nty = (p->L[1] + p->ty - 1) / p->ty;
-    f.nzc = (p->L[2] + p->zc - 1) / p->zc;
-    f.nitems = p->batch * f.ntx * f.nty * f.nzc;
-    f.stable = p->d_stable;
-    f.nstable = p->nstable;
-    return f;
-}
-
 /* launch form 6: whole-row tiles of ty rows, z chunks of zc planes */
 Row32 make_row(const smat_fdtd_plan *p, bool xp)
 {
@@ -169,121 +147,6 @@ int sm_count()
     return n;
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 tma_encoder()
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *ptr = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
-        else
-            cudaGetLastError();
-    }
-    return fn;
-}
-
-/* a 4-D map (x, y, z, component-block) of one [w][L2][L1][L0] float array */
-int encode_map(CUtensorMap *m, const float *base, const int L[4], int nw, int bx, int by)
-{
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
-    if (!enc) return smat_fail(SMAT_ECUDA, "cuTensorMapEncodeTiled is not available");
-    const cuuint64_t dims[4] = {(cuuint64_t)L[0], (cuuint64_t)L[1], (cuuint64_t)L[2], (cuuint64_t)nw};
-    const cuuint64_t strides[3] = {(cuuint64_t)L[0] * 4, (cuuint64_t)L[0] * L[1] * 4,
-                                   (cuuint64_t)L[0] * L[1] * L[2] * 4};
-    const cuuint32_t box[4] = {(cuuint32_t)bx, (cuuint32_t)by, 1, 3};
-    const cuuint32_t es[4] = {1, 1, 1, 1};
-    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void *)base, dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return smat_fail(SMAT_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-    return SMAT_OK;
-}
-
-int build_tmaps(smat_fdtd_plan *p)
-{
-    if (p->tma_ty == p->ty) return SMAT_OK;
-    const int ty = p->ty, nw = 3 * p->batch;
-    float *sets[2][4] = {{p->d_E32, p->d_H32, p->d_Ea32, p->d_Ha32}, {p->d_E32b, p->d_H32b, p->d_Ea32b, p->d_Ha32b}};
-    int rc = SMAT_OK;
-    for (int st = 0; st < 2 && !rc; st++) {
-        rc = encode_map(&p->tmap[st][0], sets[st][0], p->L, nw, 40, ty + 2);          /* E tile + halo */
-        if (!rc) rc = encode_map(&p->tmap[st][1], sets[st][1], p->L, nw, 36, ty + 1); /* H + halo col/row */
-        if (!rc) rc = encode_map(&p->tmap[st][2], sets[st][2], p->L, nw, 32, ty);     /* E aux, tile */
-        if (!rc) rc = encode_map(&p->tmap[st][3], sets[st][3], p->L, nw, 36, ty + 1); /* H aux + halo */
-    }
-    if (!rc) rc = encode_map(&p->tmap_bh, p->d_bh, p->L, 3, 36, ty + 1);
-    if (!rc) rc = encode_map(&p->tmap_be, p->d_be, p->L, 3, 32, ty);
-    if (!rc) p->tma_ty = ty;
-    return rc;
-}
-
-Fused32T make_fused_t(const smat_fdtd_plan *p, bool xp)
-{
-    Fused32T ft;
-    ft.f = make_fused(p, xp);
-    const int st = p->cur;
-    ft.mE = p->tmap[st][0];
-    ft.mH = p->tmap[st][1];
-    ft.mEa = p->tmap[st][2];
-    ft.mHa = p->tmap[st][3];
-    ft.mBh = p->tmap_bh;
-    ft.mBe = p->tmap_be;
-    ft.err = p->d_err;
-    return ft;
-}
-
-/* kernel 5: tile 128 x 4, tensor maps with its box sizes */
-int build_zmaps(smat_fdtd_plan *p)
-{
-    if (p->zmaps) return SMAT_OK;
-    const int nw = 3 * p->batch;
-    float *sets[2][4] = {{p->d_E32, p->d_H32, p->d_Ea32, p->d_Ha32}, {p->d_E32b, p->d_H32b, p->d_Ea32b, p->d_Ha32b}};
-    int rc = SMAT_OK;
-    for (int st = 0; st < 2 && !rc; st++) {
-        rc = encode_map(&p->zmap[st][0], sets[st][0], p->L, nw, 136, 6);
-        if (!rc) rc = encode_map(&p->zmap[st][1], sets[st][1], p->L, nw, 132, 5);
-        if (!rc) rc = encode_map(&p->zmap[st][2], sets[st][2], p->L, nw, 128, 4);
-        if (!rc) rc = encode_map(&p->zmap[st][3], sets[st][3], p->L, nw, 132, 5);
-    }
-    if (!rc) rc = encode_map(&p->zmap_bh, p->d_bh, p->L, 3, 132, 5);
-    if (!rc) rc = encode_map(&p->zmap_be, p->d_be, p->L, 3, 128, 4);
-    if (!rc) p->zmaps = true;
-    return rc;
-}
-
-Fused32T make_zm(const smat_fdtd_plan *p, bool xp)
-{
-    Fused32T ft;
-    ft.f = make_fused(p, xp);
-    ft.f.ty = 4;
-    ft.f.ntx = (p->L[0] + 127) / 128;
-    ft.f.nty = (p->L[1] + 3) / 4;
-    ft.f.nitems = p->batch * ft.f.ntx * ft.f.nty * ft.f.nzc;
-    const int st = p->cur;
-    ft.mE = p->zmap[st][0];
-    ft.mH = p->zmap[st][1];
-    ft.mEa = p->zmap[st][2];
-    ft.mHa = p->zmap[st][3];
-    ft.mBh = p->zmap_bh;
-    ft.mBe = p->zmap_be;
-    ft.err = p->d_err;
-    return ft;
-}
-
-int fused_grid(smat_fdtd_plan *p, const Fused32 &f)
-{
-    if (p->max_ctas < 0)
-        p->max_ctas = p->fused == 5   ? zm32_max_ctas_per_sm()
-                      : p->fused == 3 ? fused32t_max_ctas_per_sm(p->ty, p->ns)
-                                      : fused32_max_ctas_per_sm(p->ty, p->ns);
-    const int per_sm = p->ctas_per_sm > 0 ? p->ctas_per_sm : (p->max_ctas > 0 ? p->max_ctas : 1);
-    const long long g = (long long)per_sm * sm_count();
-    return (int)(g < f.nitems ? g : f.nitems);
-}
-
 /* the launches of steps rel0 .. rel0+n-1 relative to *d_base (no bump) */
 void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
 {
@@ -294,38 +157,12 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
             launch_e64(q, rel0 + i, p->stream);
             launch_dft64(q, rel0 + i, p->stream);
         }
-    } else if (p->fused == 1) {
-        for (int i = 0; i < n; i++) {
-            const Fused32 f = make_fused(p, xp);
-            launch_fused32(f, rel0 + i, fused_grid(p, f), p->stream);
-            p->cur ^= 1;
-        }
-        launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
-    } else if (p->fused == 3) {
-        for (int i = 0; i < n; i++) {
-            const Fused32T ft = make_fused_t(p, xp);
-            launch_fused32t(ft, rel0 + i, fused_grid(p, ft.f), p->stream);
-            p->cur ^= 1;
-        }
-        launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
-    } else if (p->fused == 5) {
-        for (int i = 0; i < n; i++) {
-            const Fused32T ft = make_zm(p, xp);
-            launch_zm32(ft, rel0 + i, fused_grid(p, ft.f), p->stream);
-            p->cur ^= 1;
-        }
-        launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
     } else if (p->fused == 6) {
         for (int i = 0; i < n; i++) {
             launch_row32(make_row(p, xp), rel0 + i, p->ctas_per_sm, p->stream);
             p->cur ^= 1;
         }
         launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
-    } else if (p->fused == 4) {
-        const P32 q = make_p32(p, xp);
-        const Pipe32 pp = make_pipe(p);
-        for (int i = 0; i < n; i++) launch_pipe32v(q, rel0 + i, pp, p->pipe_grid, p->stream);
-        launch_flush32(q, rel0 + n, n, p->stream);
     } else {
         const P32 q = make_p32(p, xp);
         for (int i = 0; i < n; i++) sweep_step(p, q, rel0 + i, p->stream);
@@ -333,80 +170,9 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
     }
 }
 
-Pipe32 make_pipe(const smat_fdtd_plan *p)
-{
-    Pipe32 pp;
-    pp.by = p->pipe_by;
-    pp.nyb = (p->L[1] + p->pipe_by - 1) / p->pipe_by;
-    pp.nitems = 2 * p->L[2] * pp.nyb * p->batch;
-    pp.hflag = p->d_hflag;
-    pp.ctl = p->d_pipe_ctl;
-    pp.err = p->d_err;
-    pp.hgen = p->d_hgen;
-    pp.egen = p->d_egen;
-    pp.hgen_row = p->d_hgen_row;
-    pp.egen_row = p->d_egen_row;
-    pp.wait_back = p->nstable > 0;
-    pp.nxw = p->pipe_nxw;
-    pp.lag = p->pipe_lag;
-    pp.eplane = p->d_eplane;
-    return pp;
-}
-
-/* x-threads of a pipelined item: the whole row at four cells a thread, up to 128 */
-int pipe_nxw(int L0)
-{
-    const int t = ((L0 / 4 + 31) / 32) * 32;
-    return t < 128 ? t : 128;
-}
-
-/* kernel 4 for `by` rows per item: flags, per-item general-cell offsets, grid */
-int setup_pipe(smat_fdtd_plan *p, int by, int lag)
-{
-    int rc;
-    const int L1 = p->L[1], L2 = p->L[2];
-    if (!p->d_hflag) {
-        if ((rc = p->alloc(&p->d_hflag, (size_t)L2 * L1 * p->batch))) return rc;
-        if ((rc = p->alloc(&p->d_pipe_ctl, 2))) return rc;
-        if ((rc = p->alloc(&p->d_hgen_row, (size_t)L2 * L1 + 1))) return rc;
-        if ((rc = p->alloc(&p->d_egen_row, (size_t)L2 * L1 + 1))) return rc;
-        if ((rc = p->alloc(&p->d_eplane, (size_t)L2))) return rc;
-    }
-    /* flags and counters are relative to the epoch: restart both */
-    drop_graph(p);
-    CK(cudaMemsetAsync(p->d_hflag, 0, sizeof(int) * (size_t)L2 * L1 * p->batch, p->stream));
-    CK(cudaMemsetAsync(p->d_eplane, 0, sizeof(int) * (size_t)L2, p->stream));
-    CK(cudaMemsetAsync(p->d_pipe_ctl, 0, sizeof(int) * 2, p->stream));
-    const int nyb = (L1 + by - 1) / by;
-    for (int side = 0; side < 2; side++) {
-        const std::vector<int> &gl = side ? p->egen_host : p->hgen_host;
-        std::vector<int> rows((size_t)L2 * nyb + 1);
-        for (int z = 0; z < L2; z++)
-            for (int yb = 0; yb < nyb; yb++) {
-                const long long first = (long long)z * p->pl + (long long)yb * by * p->L[0];
-                rows[(size_t)z * nyb + yb] = (int)(std::lower_bound(gl.begin(), gl.end(), first) - gl.begin());
-            }
-        rows[(size_t)L2 * nyb] = (int)gl.size();
-        CK(cudaMemcpyAsync(side ? p->d_egen_row : p->d_hgen_row, rows.data(), rows.size() * sizeof(int),
-                           cudaMemcpyHostToDevice, p->stream));
-    }
-    CK(cudaStreamSynchronize(p->stream));
-    const int nxw = pipe_nxw(p->L[0]);
-    const int per_sm = pipe32v_max_ctas_per_sm(128);
-    if (per_sm < 1) return smat_fail(SMAT_ECUDA, "pipelined sweeps: no resident CTA of %d x %d threads", nxw, by);
-    const int want = p->ctas_per_sm > 0 && p->ctas_per_sm < per_sm ? p->ctas_per_sm : per_sm;
-    const long long nitems = 2LL * L2 * nyb * p->batch;
-    const long long grid = (long long)want * sm_count();
-    p->pipe_grid = (int)(grid < nitems ? grid : nitems);
-    p->pipe_by = by;
-    p->pipe_lag = lag;
-    p->pipe_nxw = nxw;
-    return SMAT_OK;
-}
-
 /* One step's update launches of plan p on stream st, without the DFT flush:
- * the plan's own launch form for kernel 6 and the sweeps (0, 2); the other
- * forms step as vectorised sweeps.  Kernel 6 swaps the field sets. */
+ * the plan's own launch form (the whole-row fused step 6, which swaps the
+ * field sets, or the sweeps 0 and 2). */
 void enqueue_update(smat_fdtd_plan *p, int rel, cudaStream_t st)
 {
     if (p->precision != SMAT_FP32) return;
@@ -415,10 +181,7 @@ void enqueue_update(smat_fdtd_plan *p, int rel, cudaStream_t st)
         p->cur ^= 1;
         return;
     }
-    const int fu = p->fused;
-    if (fu != 0 && fu != 2) p->fused = 2;
     sweep_step(p, make_p32(p, false), rel, st);
-    p->fused = fu;
 }
 
 /* One FP32 step as two sweeps (kernels 0 and 2), in z-chunks of szc planes:
@@ -814,10 +577,6 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
         if ((rc = p->alloc(&p->d_qorder, (size_t)nq))) return rc;
         CK(cudaMemcpyAsync(p->d_qorder, qorder.data(), nq * sizeof(int), cudaMemcpyHostToDevice, p->stream));
     }
-    if ((rc = p->alloc(&p->d_stable, stable.size() + 1))) return rc;
-    if (!stable.empty())
-        CK(cudaMemcpyAsync(p->d_stable, stable.data(), stable.size() * sizeof(int), cudaMemcpyHostToDevice,
-                           p->stream));
     CK(cudaMemcpyAsync(p->d_bh, bh.data(), bh.size() * 4, cudaMemcpyHostToDevice, p->stream));
     CK(cudaMemcpyAsync(p->d_be, be.data(), be.size() * 4, cudaMemcpyHostToDevice, p->stream));
     CK(cudaMemcpyAsync(p->d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, p->stream));
@@ -1165,8 +924,7 @@ extern "C" int smat_fdtd_run(smat_fdtd_plan *p, int k_begin, int k_end)
     if (k_end > p->nsched) return smat_fail(SMAT_EINVAL, "run: k_end %d beyond the %d-step schedule", k_end, p->nsched);
     launch_set(p->d_base, k_begin, p->stream);
     int n = k_end - k_begin;
-    if (p->precision == SMAT_FP32 && (p->fused == 1 || p->fused == 3 || p->fused == 5 || p->fused == 6) && p->cur != 0 &&
-        n >= GRAPH_STEPS + 1) {
+    if (p->precision == SMAT_FP32 && p->fused == 6 && p->cur != 0 && n >= GRAPH_STEPS + 1) {
         /* graphs are captured from field set 0: take one step to get there */
         enqueue_steps(p, 0, 1, false);
         launch_bump(p->d_base, 1, p->stream);
@@ -1207,23 +965,9 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
         const P32 q32 = make_p32(p, false);
         CK(cudaEventRecord(ev[0], p->stream));
         if (p->precision == SMAT_FP64) launch_h64(q64, i, p->stream);
-        else if (p->fused == 1) {
-            const Fused32 f = make_fused(p, false);
-            launch_fused32(f, i, fused_grid(p, f), p->stream);
-            p->cur ^= 1;
-        } else if (p->fused == 3) {
-            const Fused32T ft = make_fused_t(p, false);
-            launch_fused32t(ft, i, fused_grid(p, ft.f), p->stream);
-            p->cur ^= 1;
-        } else if (p->fused == 5) {
-            const Fused32T ft = make_zm(p, false);
-            launch_zm32(ft, i, fused_grid(p, ft.f), p->stream);
-            p->cur ^= 1;
-        } else if (p->fused == 6) {
+        else if (p->fused == 6) {
             launch_row32(make_row(p, false), i, p->ctas_per_sm, p->stream);
             p->cur ^= 1;
-        } else if (p->fused == 4) {
-            launch_pipe32v(q32, i, make_pipe(p), p->pipe_grid, p->stream);
         } else if (p->szc > 0 && p->szc < p->L[2]) {
             sweep_step(p, q32, i, p->stream); /* chunked sweeps: the whole step in ms[0] */
         } else if (p->fused == 2) {
@@ -1233,7 +977,7 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
         }
         CK(cudaEventRecord(ev[1], p->stream));
         if (p->precision == SMAT_FP64) launch_e64(q64, i, p->stream);
-        else if (p->fused == 4 || (p->szc > 0 && p->szc < p->L[2])) {
+        else if (p->fused == 6 || (p->szc > 0 && p->szc < p->L[2])) {
         } else if (p->fused == 2)
             launch_e32v(q32, i, p->by32, p->sweep_mb, 0, p->L[2], p->d_egen, p->negen, p->stream);
         else if (p->fused == 0) launch_e32(q32, i, p->by32, 0, p->L[2], p->stream);
@@ -1264,23 +1008,9 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
 {
     smat_clear_error();
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
-    if (fused < 0 || fused > 6)
-        return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 1 (fused), 2 (vector sweeps), 3 (fused, TMA), "
-                                      "4 (pipelined vector sweeps), 5 (fused, 128x4 tiles, TMA producer warp), "
-                                      "6 (fused, whole rows)");
-    if (fused == 5) {
-        if (p->L[0] % 4 != 0 || p->iBc[0] != 0 || p->iBc[1] != 0 || p->iBc[2] != 0 || z_chunk < 1)
-            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 5 needs L0 %% 4 == 0, iBc = (0,0,0) and z_chunk >= 1");
-        if (zm32_max_ctas_per_sm() < 1) return smat_fail(SMAT_ECUDA, "set_tuning: kernel 5 does not fit an SM");
-        int rc = build_zmaps(p);
-        if (rc) return rc;
-        p->zc = z_chunk;
-        p->ctas_per_sm = 1;
-        p->max_ctas = 1;
-        p->fused = 5;
-        drop_graph(p);
-        return SMAT_OK;
-    }
+    if (fused != 0 && fused != 2 && fused != 6)
+        return smat_fail(SMAT_EINVAL, "set_tuning: kernel 0 (sweeps), 2 (vector sweeps) or 6 (fused step, whole "
+                                      "rows)");
     if (fused == 6) {
         /* whole-row fused step: tile_y rows per CTA, z chunks, ctas_per_sm = register bound 1..3 */
         if (p->L[0] % 4 != 0 || p->nrec_metal > 0 || p->nrec_split > 0)
@@ -1303,53 +1033,17 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         drop_graph(p);
         return SMAT_OK;
     }
-    if (fused == 4) {
-        const int lag = z_chunk;
-        if (p->L[0] % 4 != 0 || tile_y < 1 || tile_y > p->L[1] || ctas_per_sm < 0 || lag < 0 || lag == 1 ||
-            lag > p->L[2])
-            return smat_fail(SMAT_EINVAL, "set_tuning: pipelined sweeps need L0 %% 4 == 0, tile_y (rows per item) "
-                                          "in 1..L1 and a lag (z_chunk) of 0 (none) or 2..L2");
-        if (p->nstable > 0 && p->iBc[2] != 0)
-            return smat_fail(SMAT_EINVAL, "set_tuning: pipelined sweeps cannot order stable-form E cells across a "
-                                          "wrapped z boundary");
-        p->ctas_per_sm = ctas_per_sm;
-        int rc = setup_pipe(p, tile_y, lag);
-        if (rc) return rc;
-        p->fused = 4;
-        drop_graph(p);
-        return SMAT_OK;
-    }
-    if (fused == 3 && p->L[0] % 4 != 0) return smat_fail(SMAT_EINVAL, "set_tuning: the TMA kernel needs L0 %% 4 == 0");
     if (fused == 2 && (p->L[0] % 4 != 0 || tile_y < 1 || tile_y > 4))
         return smat_fail(SMAT_EINVAL, "set_tuning: vector sweeps need L0 %% 4 == 0 and tile_y in 1..4");
-    if (fused == 1 || fused == 3) {
-        if (tile_y < 2 || tile_y > 8 || z_chunk < 1 || ctas_per_sm < 0 || slots < 4 || slots > 6)
-            return smat_fail(SMAT_EINVAL,
-                             "set_tuning: tile_y in 2..8, z_chunk >= 1, ctas_per_sm >= 0, slots in 4..6");
-        const int mx = fused == 3 ? fused32t_max_ctas_per_sm(tile_y, slots) : fused32_max_ctas_per_sm(tile_y, slots);
-        if (mx < 1 || ctas_per_sm > mx)
-            return smat_fail(SMAT_EINVAL, "set_tuning: %d CTAs per SM do not fit (max %d)", ctas_per_sm, mx);
-        p->ty = tile_y;
-        p->zc = z_chunk;
-        p->ns = slots;
-        p->ctas_per_sm = ctas_per_sm;
-        p->max_ctas = mx;
-        if (fused == 3) {
-            p->fused = 3;
-            int rc = build_tmaps(p);
-            if (rc) return rc;
-        }
-    } else {
-        if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
-        if (z_chunk < 0) return smat_fail(SMAT_EINVAL, "set_tuning: z_chunk >= 0 (0: whole grid per sweep)");
-        if (ctas_per_sm != 0 && ctas_per_sm != 5 && ctas_per_sm != 6 && ctas_per_sm != 8 &&
-            !(fused == 2 && ctas_per_sm == -3))
-            return smat_fail(SMAT_EINVAL, "set_tuning: sweeps take ctas_per_sm 0 (= 5), 5, 6 or 8 (register bound), "
-                                          "or -3 (vector sweeps, two planes per thread)");
-        p->by32 = tile_y;
-        p->szc = z_chunk >= p->L[2] ? 0 : z_chunk;
-        p->sweep_mb = ctas_per_sm == 0 ? 5 : ctas_per_sm;
-    }
+    if (tile_y < 1 || tile_y > 8) return smat_fail(SMAT_EINVAL, "set_tuning: block_y in 1..8");
+    if (z_chunk < 0) return smat_fail(SMAT_EINVAL, "set_tuning: z_chunk >= 0 (0: whole grid per sweep)");
+    if (ctas_per_sm != 0 && ctas_per_sm != 5 && ctas_per_sm != 6 && ctas_per_sm != 8 &&
+        !(fused == 2 && ctas_per_sm == -3))
+        return smat_fail(SMAT_EINVAL, "set_tuning: sweeps take ctas_per_sm 0 (= 5), 5, 6 or 8 (register bound), "
+                                      "or -3 (vector sweeps, two planes per thread)");
+    p->by32 = tile_y;
+    p->szc = z_chunk >= p->L[2] ? 0 : z_chunk;
+    p->sweep_mb = ctas_per_sm == 0 ? 5 : ctas_per_sm;
     p->fused = fused;
     drop_graph(p);
     return SMAT_OK;
@@ -1388,17 +1082,6 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
                 if (zc > 0 && zc < L2) cands.push_back({2, by, zc, 5, 4});
         cands.push_back({2, 4, 0, 5, 4});
     }
-    if (p->L[0] % 4 == 0 && p->iBc[0] == 0 && p->iBc[1] == 0 && p->iBc[2] == 0)
-        for (int zc : {20, 40, 80, 1 << 20}) {
-            const int z = zc > L2 ? L2 : zc;
-            bool dup = false;
-            for (auto &c : cands) dup |= c.fused == 5 && c.zc == z;
-            if (!dup) cands.push_back({5, 4, z, 1, 4});
-        }
-    if (p->L[0] % 4 == 0 && !(p->nstable > 0 && p->iBc[2] != 0))
-        for (int rows : {2, 4, 8})
-            for (int lag : {0, 4, 8})
-                if (rows <= p->L[1] && lag <= L2) cands.push_back({4, rows, lag, 0, 0});
     /* whole-row fused step (plans without record cells) */
     if (p->L[0] % 4 == 0 && p->nrec_metal == 0 && p->nrec_split == 0)
         for (int ty : {1, 2, 4, 5})
@@ -1408,12 +1091,6 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
     cands.push_back({0, 4, 0, 0, 4});
     cands.push_back({0, 8, 0, 0, 4});
     cands.push_back({0, 4, 4 < L2 ? 4 : 0, 0, 4});
-    /* fused z-march: a few representative shapes */
-    for (int ns : {4, 5}) {
-        const int z = 32 > L2 ? L2 : 32;
-        if (fused32_max_ctas_per_sm(8, ns) >= 1) cands.push_back({1, 8, z, 0, ns});
-        if (p->L[0] % 4 == 0 && fused32t_max_ctas_per_sm(8, ns) >= 1) cands.push_back({3, 8, z, 0, ns});
-    }
     const int nq = p->nq;
     p->nq = 0;
     CK(cudaMemsetAsync(p->d_iI, 0xff, sizeof(int) * p->batch, p->stream));
@@ -1477,14 +1154,9 @@ extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
 {
     if (!p || !out) return smat_fail(SMAT_EINVAL, "get_tuning: bad arguments");
     out[0] = p->fused;
-    out[1] = (p->fused == 1 || p->fused == 3 || p->fused == 6) ? p->ty
-             : p->fused == 4                                    ? p->pipe_by
-             : p->fused == 5                                    ? 4
-                                                                : p->by32;
-    out[2] = (p->fused == 1 || p->fused == 3 || p->fused == 5 || p->fused == 6) ? p->zc
-             : p->fused == 4                                                    ? p->pipe_lag
-                                                                                : p->szc;
-    out[3] = (p->fused == 0 || p->fused == 2) ? p->sweep_mb : p->ctas_per_sm;
+    out[1] = p->fused == 6 ? p->ty : p->by32;
+    out[2] = p->fused == 6 ? p->zc : p->szc;
+    out[3] = p->fused == 6 ? p->ctas_per_sm : p->sweep_mb;
     out[4] = p->ns;
     return SMAT_OK;
 }

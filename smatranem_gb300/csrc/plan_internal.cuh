@@ -7,8 +7,6 @@
 #ifndef SMATRAN_PLAN_INTERNAL_CUH
 #define SMATRAN_PLAN_INTERNAL_CUH
 
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -98,7 +96,6 @@ struct smat_fdtd_plan {
     float *d_H32 = nullptr, *d_E32 = nullptr, *d_Ha32 = nullptr, *d_Ea32 = nullptr;
     float *d_H32b = nullptr, *d_E32b = nullptr, *d_Ha32b = nullptr, *d_Ea32b = nullptr; /* second set */
     int cur = 0;          /* FP32: which field set holds the current state */
-    int *d_stable = nullptr;
     int *d_qorder = nullptr; /* kernel 6: quads with a PML x index first (nqp of them), then the others */
     int nqp = 0;
     int nrec_metal = 0;   /* records of stable-form or frozen components (metal cells) */
@@ -111,20 +108,12 @@ struct smat_fdtd_plan {
     int sweep_mb = 5; /* vectorised sweep register bound: minimum resident blocks 5, 6 or 8 */
     bool adj_scalar = false; /* FP32 adjoint: scalar kernels even where the vectorised ones apply */
     std::vector<int> hgen_host, egen_host; /* host copies of the general-cell lists */
-    /* pipelined sweeps (kernel 4) */
-    int pipe_by = 0, pipe_grid = 0, pipe_lag = 1, pipe_nxw = 32;
-    int *d_hflag = nullptr, *d_pipe_ctl = nullptr, *d_hgen_row = nullptr, *d_egen_row = nullptr;
-    int *d_eplane = nullptr;
-    /* FP32 launch configuration (autotuned): fused z-march (1), two sweeps (0),
-     * two vectorised sweeps (2, needs L0 % 4 == 0) */
-    int fused = 1, ty = 8, zc = 40, ns = 5, ctas_per_sm = 0;
+    /* FP32 launch configuration (autotuned): two sweeps (0), two vectorised
+     * sweeps (2, needs L0 % 4 == 0), the whole-row fused step (6); ns is the
+     * fifth tuning value, unused by these forms */
+    int fused = 0, ty = 8, zc = 40, ns = 4, ctas_per_sm = 0;
     int max_ctas = -1; /* cached occupancy of the current configuration */
-    /* TMA tensor maps (kernel 3), built for tile rows tma_ty: [set][E, H, Ea, Ha], bh, be */
-    CUtensorMap tmap[2][4], tmap_bh, tmap_be;
-    CUtensorMap zmap[2][4], zmap_bh, zmap_be; /* kernel 5: boxes 136x6 (E), 132x5 (H side), 128x4 (E side) */
-    bool zmaps = false;
-    int tma_ty = -1;
-    int *d_err = nullptr; /* device pipeline error flag */
+    int *d_err = nullptr; /* device error flag */
     int by32 = 8;
 
     /* graphs: a chunk of GRAPH_STEPS steps, position independent via d_base */
@@ -154,9 +143,6 @@ Row32 make_row(const smat_fdtd_plan *p, bool xp);
 void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp);
 void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel, cudaStream_t st);
 void enqueue_update(smat_fdtd_plan *p, int rel, cudaStream_t st);
-Pipe32 make_pipe(const smat_fdtd_plan *p);
-int setup_pipe(smat_fdtd_plan *p, int by, int lag);
-int pipe_nxw(int L0);
 int sm_count();
 void drop_graph(smat_fdtd_plan *p);
 } // namespace plan

@@ -10,7 +10,11 @@ sigma_max * |depth/thickness|^p, sigma_max = -(p+1) ln(sqRef) / (4 omega d)
 sqrt(min over cells of e00 e11 e22 m00 m11 m22 / ((e00+e11+e22)(m00+m11+m22)))
 (PMLset/PMLcalc.c:279-313); the FDTD takes min_Dt as its square root.
 
-Everything here is seeded numpy; no dataset is involved.
+Everything here is seeded numpy; no dataset is involved.  The generators
+are plain numpy and load no native code: only prepare(), Prepared.coefficients()
+and port_modes() call into the CUDA library (imported where they run), so a
+process that must not load it (a CPU-only timing worker) can still build the
+structures.
 """
 from __future__ import annotations
 
@@ -18,8 +22,6 @@ import dataclasses
 import math
 
 import numpy as np
-
-from . import fdtd
 
 
 @dataclasses.dataclass
@@ -53,6 +55,7 @@ class Prepared:
     invtau_I: float
 
     def coefficients(self):
+        from . import fdtd
         return fdtd.coefficients(self.s.L, self.lnotn, self.sigma, self.mu, self.epsi, self.cont, self.addr,
                                  self.invtau_R, self.invtau_I)
 
@@ -188,6 +191,7 @@ def random_structure(L, seed=0, pml=(2, 2, 2), pml_z_only=False, metals=0.0, los
 
 def prepare(s: Structure, dt_factor: float = 1.0) -> Prepared:
     """The reference precompute through the library (set_sigma .. set_tau)."""
+    from . import fdtd
     mu = np.ascontiguousarray(s.mu.reshape(-1))
     ep = np.ascontiguousarray(s.epsi.reshape(-1))
     sigma = fdtd.set_sigma(s.L, mu, ep)

@@ -308,7 +308,7 @@ def test_finite_check_and_errors(built):
         assert not ok
 
 
-# ---- the fused FP32 kernel ----------------------------------------------------
+# ---- FP32 launch forms ---------------------------------------------------------
 
 FUSED_CASES = [
     # (L, seed, structure kwargs, iBTIin)
@@ -316,10 +316,9 @@ FUSED_CASES = [
     ((40, 17, 19, 3), 22, dict(pml=(4, 4, 4), lossy=0.05, iBc=(1, 1, -1)), (5, 13, 7, -1)),
     ((33, 9, 12, 2), 23, dict(pml=(0, 0, 2), pml_z_only=True, iBc=(0, -1, 0)), (3, 8, 5, 1)),
     ((64, 24, 20, 3), 24, dict(pml=(5, 5, 4), metals=0.02, iBc=(0, 0, 0)), (5, 14, 7, 1)),
-    # partial 128 x 4 tiles in x and y (kernel 5), lossy and PEC records
+    # rows of 34 quads, lossy and PEC records
     ((136, 13, 17, 2), 25, dict(pml=(4, 3, 3), lossy=0.05, pec=0.03, iBc=(0, 0, 0)), (4, 12, 6, 1)),
 ]
-TUNINGS = [(1, 8, 40, 0, 5), (1, 4, 5, 0, 4), (1, 2, 3, 1, 6), (1, 8, 7, 1, 6), (1, 3, 1, 0, 5), (1, 2, 2, 0, 4)]
 
 
 def _run_fp32(s, pr, iBTIin, tuning, nsteps, batch=2, seed=0):
@@ -343,12 +342,11 @@ def _run_fp32(s, pr, iBTIin, tuning, nsteps, batch=2, seed=0):
 
 
 @pytest.mark.parametrize("case", range(len(FUSED_CASES)))
-def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
-    """The fused z-marching launches and the z-chunked sweeps reproduce the
-    two-sweep FP32 kernels bit for bit, for every tile shape, z chunk and grid
-    size, across field-set swaps,
-    iBc = -1/0/1 wraps, PML on all faces, lossy/PEC/metal cells and per-excitation
-    source planes."""
+def test_sweep_forms_fp32_are_bit_identical(built, case):
+    """The vectorised and z-chunked sweeps reproduce the scalar two-sweep FP32
+    kernels bit for bit, for every block shape, z chunk, register bound and
+    grid size, across field-set swaps, iBc = -1/0/1 wraps, PML on all faces,
+    lossy/PEC/metal cells and per-excitation source planes."""
     from smatranem_gb300 import workloads as W
     L, seed, kw, iBTIin = FUSED_CASES[case]
     s = W.random_structure(L, seed=seed, **kw)
@@ -356,16 +354,10 @@ def test_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     nsteps = 9 if kw.get("metals") else 37
     ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
     # z_chunk of the sweeps (kernels 0, 2): planes per H/E chunk, 0 = whole grid
-    tunings = TUNINGS + [(0, 4, 1, 0, 4), (0, 2, 3, 0, 4)]
+    tunings = [(0, 4, 1, 0, 4), (0, 2, 3, 0, 4), (0, 8, 0, 6, 4), (0, 1, 5, 8, 4)]
     if L[0] % 4 == 0:
         tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (2, 4, 3, 0, 4), (2, 1, 5, 0, 4), (2, 2, 16, 0, 4),
-                    (2, 1, 0, 6, 4), (2, 2, 0, 8, 4), (2, 1, 0, -3, 4), (2, 2, 3, -3, 4),
-                    (3, 8, 40, 0, 5), (3, 4, 5, 0, 4), (3, 2, 3, 1, 6), (3, 4, 1, 0, 5), (3, 8, 7, 1, 6)]
-        if tuple(kw["iBc"]) == (0, 0, 0):  # 128 x 4 tiles with a TMA producer warp (kernel 5)
-            tunings += [(5, 4, 40, 1, 4), (5, 4, 5, 1, 4), (5, 4, 1, 1, 4), (5, 4, 7, 1, 4)]
-        if not (kw.get("metals") and kw["iBc"][2] != 0):  # pipelined sweeps (kernel 4)
-            # (4, rows per item, lag (0: none), ctas_per_sm, -)
-            tunings += [(4, 1, 0, 0, 0), (4, 2, 2, 0, 0), (4, 5, 3, 1, 0), (4, 3, L[2], 0, 0), (4, L[1], 0, 0, 0)]
+                    (2, 1, 0, 6, 4), (2, 2, 0, 8, 4), (2, 1, 0, -3, 4), (2, 2, 3, -3, 4)]
     for tuning in tunings:
         got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
         for rb, gb in zip(ref, got):
@@ -477,7 +469,8 @@ def test_row_fused_refuses_bad_tunings(built):
         p.set_tuning(6, 2, 0, 1, 0)
         assert tuple(p.get_tuning())[:4] == (6, 2, 0, 1)
         for bad in [(6, 0, 0, 1, 0), (6, 17, 0, 1, 0), (6, 2, -1, 1, 0), (6, 2, 0, 0, 0), (6, 2, 0, 4, 0),
-                    (6, 200, 0, 1, 0), (7, 2, 0, 1, 0), (-1, 2, 0, 1, 0)]:
+                    (6, 200, 0, 1, 0), (7, 2, 0, 1, 0), (-1, 2, 0, 1, 0), (1, 8, 40, 0, 5), (3, 8, 40, 0, 5),
+                    (4, 2, 2, 0, 0), (5, 4, 40, 1, 4)]:
             with pytest.raises(f.FdtdError):
                 p.set_tuning(*bad)
             assert tuple(p.get_tuning())[:4] == (6, 2, 0, 1)
