@@ -220,6 +220,35 @@ def mode_columns(modes):
     return np.array(cols)
 
 
+S_FLOOR = 1e-3
+
+
+def s_parameter_errors(S32, S64, floor=S_FLOOR):
+    """Per excitation, over all its S parameters (2 port planes x 21
+    wavelengths x 8 mode columns): the largest |S32 - S64| / max(|S64|,
+    floor * m) with m the excitation's largest |S64| (relative error, entries
+    under the floor judged against floor * m), the largest relative error of
+    the entries at or above the floor, and the largest |S32 - S64| / m."""
+    floored, rel_above, abs_over = [], [], []
+    below = 0
+    for a, r in zip(S32, S64):
+        m = float(np.abs(r).max())
+        d = np.abs(a - r)
+        big = np.abs(r) >= floor * m
+        floored.append(float(np.max(d / np.maximum(np.abs(r), floor * m))))
+        rel_above.append(float(np.max(d[big] / np.abs(r)[big])))
+        abs_over.append(float(d.max() / m))
+        below += int((~big).sum())
+    return {"per_excitation_max_rel": floored, "max_rel": max(floored),
+            "per_excitation_max_rel_above_floor": rel_above,
+            "per_excitation_max_abs_over_max": abs_over, "max_abs_over_max": max(abs_over),
+            "floor": f"{floor:g} x the excitation's largest |S|", "entries_below_floor": below,
+            "entries": int(sum(r.size for r in S64)),
+            "over": "every excitation: 2 port planes x 21 wavelengths x 8 mode columns (4 port modes, forward and "
+                    "backward dual columns); FP64 side: the plain FP64 plan (bit-identical to the reference loop) "
+                    "on the same batch"}
+
+
 def dft_fields(p, b):
     """The running DFT of excitation b: [wavelength][port plane][Hx, Hy, Ex, Ey][pixel]."""
     nf, nq = p.dft_count()
@@ -422,58 +451,55 @@ def run_ours(args):
     achieved_comp = comp_step / (step_kernel_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     launches = per_step * args.steps + 2 * math.ceil(args.steps / 32) + 1
-    # ---- full runs: S-matrix columns/s and the FP32-vs-FP64 S error -----
+    # ---- full runs: S-matrix columns/s and the FP32-vs-FP64 errors --------
     full = args.full_steps
     p32b = make_plan(bend, pr, modes, F.FP32, batch, full, stream=stream.cuda_stream, tuning=tuning)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     p32b.run(0, full)
     t_full32 = time.perf_counter() - t0
-    S32 = s_parameters(p32b, bend, modes, 0)
-    D32 = dft_fields(p32b, 0)
+    S32 = [s_parameters(p32b, bend, modes, b) for b in range(batch)]
+    D32 = [dft_fields(p32b, b) for b in range(batch)]
     finite32 = p32b.check_finite()[0]
     p32b.close()
     p32.close()
-    p64 = make_plan(bend, pr, modes, F.FP64, 1, full, stream=stream.cuda_stream)
-    p64.run(0, 3)
+    # the plain FP64 kernel (bit-identical to the reference loop) on the same
+    # batch of excitations: its S-cols/s and the FP64 side of every error
+    p64 = make_plan(bend, pr, modes, F.FP64, batch, full, stream=stream.cuda_stream)
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
     ev0.record(stream)
-    p64.run(3, 3 + args.steps64, sync=False)
+    p64.run(0, full, sync=False)
     ev1.record(stream)
-    torch.cuda.synchronize()
-    t64_ms = ev0.elapsed_time(ev1)
-    fp64_rate = n3 * args.steps64 / (t64_ms * 1e-3) / 1e9
-    p64.close()
-    p64 = make_plan(bend, pr, modes, F.FP64, 1, full, stream=stream.cuda_stream)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    p64.run(0, full)
+    p64.sync()
     t_full64 = time.perf_counter() - t0
-    S64 = s_parameters(p64, bend, modes, 0)
-    D64 = dft_fields(p64, 0)
+    t64_ms = ev0.elapsed_time(ev1)
+    fp64_rate = batch * n3 * full / (t64_ms * 1e-3) / 1e9
+    S64 = [s_parameters(p64, bend, modes, b) for b in range(batch)]
+    d_l2, d_max = [], []
+    for b in range(batch):
+        D64 = dft_fields(p64, b)
+        dd = (D32[b] - D64).reshape(D64.shape[0], D64.shape[1], -1)
+        dr = D64.reshape(dd.shape)
+        d_l2.append(float(np.max(np.linalg.norm(dd, axis=2) / np.linalg.norm(dr, axis=2))))
+        d_max.append(float(np.max(np.abs(dd).max(axis=2) / np.abs(dr).max(axis=2))))
     p64.close()
+    del D32
     clocks.stop()
-    big = np.abs(S64) > 1e-3 * np.abs(S64).max()
-    s_rel = float(np.max(np.abs(S32 - S64)[big] / np.abs(S64)[big]))
-    s_abs = float(np.max(np.abs(S32 - S64)) / np.abs(S64).max())
-    # the DFT fields themselves: per (wavelength, port plane) slice, the
-    # relative L2 error and the largest deviation over the slice's largest value
-    dd = (D32 - D64).reshape(D64.shape[0], D64.shape[1], -1)
-    dr = D64.reshape(dd.shape)
-    d_l2 = float(np.max(np.linalg.norm(dd, axis=2) / np.linalg.norm(dr, axis=2)))
-    d_max = float(np.max(np.abs(dd).max(axis=2) / np.abs(dr).max(axis=2)))
-    del D32, D64, dd, dr
+    s_err = s_parameter_errors(S32, S64)
     # ---- e2e through the C ABI from host buffers --------------------------
+    # plan creation from host arrays (precompute, uploads), the tuning (the
+    # autotuner's cached pick for this grid, batch and GPU), sheets, schedule,
+    # the full run and every excitation's S parameters read back
     t0 = time.perf_counter()
-    pe = make_plan(bend, pr, modes, F.FP32, batch, full, tuning=tuning)
+    pe = make_plan(bend, pr, modes, F.FP32, batch, full, tuning="auto")
     pe.run(0, full)
     Se = [s_parameters(pe, bend, modes, b) for b in range(batch)]
+    h2d, d2h = pe.copy_bytes()
     pe.close()
     t_e2e = time.perf_counter() - t0
-    pl = bend.s.L[0] * bend.s.L[1]
-    h2d = (8 * 3 * n3 * 4 + 2 * 3 * n3 * 4 + batch * 8 * pl * 8 + full * (6 + 4 * len(LAMS)) * 8 * 1.5)
-    d2h = batch * 2 * len(LAMS) * 4 * pl * 16
     e2e = ws * batch * n3 * full / t_e2e / 1e9
+    del Se
     # ---- CPU baseline (bounded sample, oracle) -----------------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -482,6 +508,26 @@ def run_ours(args):
         cpu = {"value": rate / 1e9, "unit": "Gcell-updates/s", "cores": 1, "kind": kind,
                "sample": f"{args.cpu_steps} main_calc steps of the full bend after 1 untimed, one excitation, "
                          f"{tmax:.1f} s on 1 core"}
+    # ---- the other workloads, bounded: one summary each ---------------------
+    extras = {}
+    if rank == 0 and args.extras:
+        t_start = time.perf_counter()
+        todo = [x for x in args.extras.split(",") if x]
+        # (key, estimated seconds, call)
+        runs = {"cube": ("config_cube_96_fp64", 20, lambda: config_cube(4000, args.warmup)),
+                "adjoint": ("config_adjoint_160x160x120", 70, lambda: config_adjoint(6000, args.extra_fd_cells)),
+                "group": ("config_group_bend8_slabs16", 120,
+                          lambda: config_group(args.warmup, 40, 0, 300, bend_workload=(bend, pr, modes))),
+                "large": ("config_large_640x640x512", 150, lambda: config_large(args.warmup, 20, 300))}
+        for name in todo:
+            key, est, fn = runs[name]
+            left = args.extras_budget - (time.perf_counter() - t_start)
+            if left < est:
+                extras[key] = {"skipped": f"time budget: {left:.0f} s left of --extras-budget {args.extras_budget} s, "
+                                          f"about {est} s needed"}
+                continue
+            t0 = time.perf_counter()
+            extras[key] = dict(fn(), wall_s=time.perf_counter() - t0)
     if rank != 0:
         return
     line = {
@@ -490,8 +536,10 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": bench_config(n3, n_split, batch, ws),
         "e2e": {"value": e2e, "unit": "Gcell-updates/s", "h2d_bytes_per_step": h2d / full,
-                "d2h_bytes_per_step": d2h / full, "what": f"create+incident+schedule+{full} steps+DFT read-back, "
-                                                          f"{t_e2e:.2f} s"},
+                "d2h_bytes_per_step": d2h / full,
+                "what": f"through the C ABI from host arrays: plan creation (precompute + uploads), the autotuner's "
+                        f"cached tuning, sheets, schedule, {full} steps, S of all {batch} excitations read back; "
+                        f"{t_e2e:.2f} s; copies counted by the library (smat_fdtd_copy_bytes)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
                      "traffic": TRAFFIC_PER_LAUNCH.get(tuple(tuning[:3])) if batch == BATCH else None,
@@ -511,22 +559,24 @@ def run_ours(args):
                      "ms_per_launch": launch_ms,
                      "launches_per_step": per_step, "ms_per_step_kernels": step_kernel_ms,
                      "ms_dft_flush_per_step": kt[2]},
-        "fp64_plain": {"value": fp64_rate, "unit": "Gcell-updates/s", "steps": args.steps64,
-                       "s_cols_per_s": 1.0 / t_full64, "full_run_s": t_full64},
+        "fp64_plain": {"value": fp64_rate, "unit": "Gcell-updates/s", "steps": full, "batch": batch,
+                       "s_cols_per_s": batch / t_full64, "full_run_s": t_full64},
         "fp32_batched": {"s_cols_per_s": batch / t_full32, "full_run_s": t_full32, "full_steps": full,
                          "finite": finite32},
-        "s_cols_speedup_fp32_vs_fp64": (batch / t_full32) / (1.0 / t_full64),
-        "s_param_rel_err_fp32_vs_fp64": {"max_rel": s_rel, "max_abs_over_max": s_abs,
-                                         "over": "2 ports x 21 wavelengths x 4 modes x (+,-), excitation 0, "
-                                                 "|S| > 1e-3 max"},
-        "dft_field_rel_err_fp32_vs_fp64": {"max_rel_l2": d_l2, "max_abs_over_max": d_max,
-                                           "over": "Hx, Hy, Ex, Ey on both port planes x 21 wavelengths, "
-                                                   "excitation 0, per (wavelength, plane) slice"},
+        "s_cols_speedup_fp32_vs_fp64": (batch / t_full32) / (batch / t_full64),
+        "s_param_rel_err_fp32_vs_fp64": s_err,
+        "dft_field_rel_err_fp32_vs_fp64": {
+            "per_excitation_max_rel_l2": d_l2, "max_rel_l2": max(d_l2),
+            "per_excitation_max_abs_over_max": d_max, "max_abs_over_max": max(d_max),
+            "over": "per excitation: Hx, Hy, Ex, Ey on both port planes, relative L2 (and largest deviation over "
+                    "the slice's largest value) of each (wavelength, plane) slice, the worst of the 21 x 2 slices; "
+                    "FP64 side: the plain FP64 plan (bit-identical to the reference loop) on the same batch"},
         "port_modes": {"theta": modes["theta"], "solver": modes["solver"]},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }
+    line.update(extras)
     print(json.dumps(line))
 
 
@@ -562,26 +612,34 @@ def _timed(fn):
     return out, time.perf_counter() - t0
 
 
-def run_adjoint(args):
+def config_adjoint(nsteps=6000, fd_cells=32, K=64):
     """Adjoint gradient workload: 160x160x120 cells, a 60x60x20 design region of
     seeded eps_r in [2.085, 12.11] between two strip-waveguide ports, objective
     |overlap of the output-port DFT at 1.55 um with TE0|^2, FP32 with a
-    checkpoint every 64 steps.  Checked against central differences (delta
-    eps_r = 1e-3) of the FP64 forward -- bit-identical to the reference loop --
-    on seeded cells, and against the FP64 adjoint."""
+    checkpoint every K steps, through the torch.autograd wrapper.  Checked
+    against central differences (delta eps_r = 1e-3) of the FP64 forward --
+    bit-identical to the reference loop -- on fd_cells seeded cells, and against
+    the FP64 adjoint over the whole design box."""
+    import torch
     from smatranem_gb300 import fdtd as F
     from smatranem_gb300 import workloads as W
-    from smatranem_gb300.autograd import objective_and_grad
+    from smatranem_gb300.autograd import PortOverlap, objective_and_grad
     d = W.design_structure(shape=(160, 160, 120), design=(60, 60, 20), pml=12, seed=0)
     pr = W.prepare(d.s, dt_factor=1.0 / 0.99)
-    nsteps, K = args.adj_steps, 64
     src, ph = W.pulse_schedule(nsteps, pr.dt, lams_um=[1.55])
     mode = W.mode_profiles(d, n_modes=1)[0]
     kw = dict(nsteps=nsteps, K=K, mode=mode, src=src, phase=ph)
-    (J32, g32), t32 = _timed(lambda: objective_and_grad(d, d.eps, precision=F.FP32, **kw))
+    objective_and_grad(d, d.eps, precision=F.FP32, **dict(kw, nsteps=min(nsteps, 2 * K)))  # warm-up, tuning
+    eps_t = torch.tensor(d.eps, dtype=torch.float64, requires_grad=True)
+
+    def fp32():
+        J = PortOverlap.apply(eps_t, d, dict(kw, precision=F.FP32))
+        J.backward()
+        return float(J.detach()), eps_t.grad.numpy().copy()
+    (J32, g32), t32 = _timed(fp32)
     (J64, g64), t64 = _timed(lambda: objective_and_grad(d, d.eps, precision=F.FP64, **kw))
     rng = np.random.default_rng(7)
-    flat = rng.choice(d.eps.size, size=args.fd_cells, replace=False)
+    flat = rng.choice(d.eps.size, size=fd_cells, replace=False)
     cells = [np.unravel_index(i, d.eps.shape) for i in flat]
 
     def objective(eps):
@@ -610,140 +668,141 @@ def run_adjoint(args):
     fs = float(np.max(np.abs(fd))) if len(cells) else float("nan")
     cells_total = d.s.n3 * nsteps
     nan = float("nan")
-    print(json.dumps({
-        "mode": "adjoint", "config": "design 160x160x120, 60x60x20 design cells, 12-cell PML on 6 faces, TE0 "
-                                     "output-port overlap at 1.55 um, Gaussian pulse",
+    return {
+        "config": "design 160x160x120, 60x60x20 design cells (eps_r ~ U[2.085, 12.11], seed 0), 12-cell split PML "
+                  "on 6 faces, TE0 output-port overlap at 1.55 um, Gaussian pulse, FP32, checkpoints every "
+                  f"{K} steps, through the torch.autograd wrapper",
         "steps": nsteps, "checkpoint_every": K, "J_fp32": J32, "J_fp64": J64,
-        "adjoint_fp32_s": t32, "adjoint_fp64_s": t64,
-        "adjoint_fp32_gcell_per_s": 3 * cells_total / t32 / 1e9,
-        "fd_cells": int(args.fd_cells), "fd_s": t_fd,
+        "gradient_fp32_s": t32, "gradient_fp64_s": t64,
+        "gradient_fp32_gcell_per_s": 3 * cells_total / t32 / 1e9,
+        "gcell_what": "forward + recompute + adjoint cell-updates (3 x cells x steps) per second",
+        "design_cells": int(d.eps.size), "fd_cells": int(fd_cells), "fd_s": t_fd,
         "err_fp32_adjoint_vs_fd": float(np.max(np.abs(a32 - fd)) / fs) if len(cells) else nan,
         "err_fp64_adjoint_vs_fd": float(np.max(np.abs(a64 - fd)) / fs) if len(cells) else nan,
-        "median_rel_err_fp32_vs_fd": (float(np.median(np.abs(a32 - fd) / np.maximum(np.abs(fd), 1e-300)))
-                                      if len(cells) else nan),
         "err_fp32_vs_fp64_adjoint_whole_box": float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64))),
-        "errors_are": "max |g - g_fd| / max |g_fd| over the checked cells (and over the whole box for fp32 vs fp64)",
-    }))
+        "errors_are": "max |g - g_fd| / max |g_fd| over the FD cells (central differences, delta eps_r = 1e-3, of "
+                      "the FP64 forward); whole box: max |g32 - g64| / max |g64|",
+    }
+
+
+def run_adjoint(args):
+    print(json.dumps(dict({"mode": "adjoint"}, **config_adjoint(args.adj_steps, args.fd_cells))))
+
+
+def _slab_plan(sl, prec, nsteps, lams=LAMS):
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    prs = W.prepare(sl.s, dt_factor=1.0 / 0.99)
+    p = F.Plan.create(sl.s.L, sl.s.iBc, (sl.iB, sl.iT, sl.iI, 1), prs.invtau_R, prs.invtau_I, prs.mu,
+                      prs.epsi, prs.sigma, precision=prec, batch=1)
+    p.set_incident(0, *W.mode_profiles(sl, n_modes=1)[0])
+    src, ph = W.pulse_schedule(nsteps, prs.dt, lams_um=lams)
+    p.set_schedule(src, planes=(sl.iB, sl.iT), phase=ph)
+    return p, prs
+
+
+def _rel_l2_slices(a, b):
+    """Largest relative L2 error over the (wavelength, plane) slices of DFT
+    arrays [nfreq][nplanes][4][pl]."""
+    d = (a - b).reshape(a.shape[0], a.shape[1], -1)
+    r = b.reshape(d.shape)
+    return float(np.max(np.linalg.norm(d, axis=2) / np.linalg.norm(r, axis=2)))
+
+
+def config_group(warmup=5, steps=40, seed=0, acc_steps=300, bend_workload=None, autotune=False):
+    """Batched S-matrix workload: the bend with its 8 excitations plus 16 slabs
+    of uneven size (128^3 .. 256x256x192, 1-6 random cuboid inclusions each,
+    one excitation each), FP32, 21-wavelength FP64 DFT on 2 planes each, all
+    advanced by one group: by default in one persistent fused launch per step
+    for every member (form 3; autotune=True lets the group autotuner choose
+    among its forms).  Roofline on the group's compulsory bytes (every
+    member's fields and aux slots read and written, its coefficient stream
+    read once).  Accuracy: a fresh one-launch group run for acc_steps steps of
+    the pulse against the FP64 plan of every member (the bend: all 8
+    excitations, DFT and S)."""
+    from smatranem_gb300 import fdtd as F
+    from smatranem_gb300 import workloads as W
+    bend, pr, modes = bend_workload or make_workload()
+    nsteps = warmup + steps
+    shapes = W.slab_shapes(16, seed=seed)
+    slabs = [W.slab_structure(shp, seed=100 + i) for i, shp in enumerate(shapes)]
+
+    def members(n):
+        ps = [make_plan(bend, pr, modes, F.FP32, BATCH, n, tuning=None)]
+        splits = [pr.lnotn]
+        for sl in slabs:
+            p, prs = _slab_plan(sl, F.FP32, n)
+            ps.append(p)
+            splits.append(prs.lnotn)
+        return ps, splits
+    plans, splits = members(nsteps)
+    cells = bend.s.n3 * BATCH + sum(sl.s.n3 for sl in slabs)
+    comp = compulsory_bytes_per_step(bend.s.n3, pr.lnotn, BATCH) + sum(
+        compulsory_bytes_per_step(sl.s.n3, sp, 1) for sl, sp in zip(slabs, splits[1:]))
+    g = F.Group(plans)
+    if autotune:
+        (gmode, by), _ = g.autotune(4)
+    else:
+        gmode, by = 3, 1
+        g.set_tuning(gmode, by)
+    g.run(0, warmup)
+    _, t = _timed(lambda: g.run(warmup, nsteps))
+    device_gb = sum(p.device_bytes for p in plans) / 1e9
+    g.close()
+    for p in plans:
+        p.close()
+    peak, peak_kind = measured_peak()
+    achieved = comp * steps / t / 1e9
+    # accuracy: a fresh group of every member, FP32 against each member's FP64 plan
+    plans, _ = members(acc_steps)
+    g = F.Group(plans)
+    g.set_tuning(gmode, by)
+    g.run(0, acc_steps)
+    g.close()
+    d32 = [[dft_fields(plans[0], b) for b in range(BATCH)]] + [[dft_fields(p, 0)] for p in plans[1:]]
+    s32 = [s_parameters(plans[0], bend, modes, b) for b in range(BATCH)]
+    for p in plans:
+        p.close()
+    p64 = make_plan(bend, pr, modes, F.FP64, BATCH, acc_steps, tuning=None)
+    p64.run(0, acc_steps)
+    bend_err = [_rel_l2_slices(d32[0][b], dft_fields(p64, b)) for b in range(BATCH)]
+    s64 = [s_parameters(p64, bend, modes, b) for b in range(BATCH)]
+    p64.close()
+    slab_err = []
+    for sl, d in zip(slabs, d32[1:]):
+        p, _ = _slab_plan(sl, F.FP64, acc_steps)
+        p.run(0, acc_steps)
+        slab_err.append(_rel_l2_slices(d[0], dft_fields(p, 0)))
+        p.close()
+    serr = s_parameter_errors(s32, s64)
+    return {
+        "config": "bend 256x192x160 x 8 excitations + 16 slabs 128^3..256x256x192 (1-6 seeded inclusions), FP32, "
+                  "21-wavelength FP64 DFT on 2 planes each",
+        "structures": 17, "cell_excitations": cells, "steps": steps,
+        "form": ["one grouped launch per sweep", "members' own sweep launches in one graph",
+                 "members' own autotuned launch forms in one graph",
+                 "one persistent fused launch per step for every member"][gmode] + (
+                     ", CTAs of 384 threads" if gmode == 3 and by == 1 else
+                     ", CTAs of 192 threads" if gmode == 3 else ""),
+        "gcell_per_s": cells * steps / t / 1e9, "ms_per_step": 1e3 * t / steps, "device_gb": device_gb,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "bytes_per_step": comp,
+                     "what": "the group's compulsory bytes (fields and aux slots of every excitation read and "
+                             "written, each member's coefficient stream once) per step / step time"},
+        "fp32_vs_fp64": {"steps": acc_steps,
+                         "bend_dft_max_rel_l2_per_excitation": bend_err,
+                         "slab_dft_max_rel_l2": slab_err,
+                         "bend_s_max_rel_per_excitation": serr["per_excitation_max_rel"],
+                         "bend_s_max_abs_over_max_per_excitation": serr["per_excitation_max_abs_over_max"],
+                         "s_floor": serr["floor"],
+                         "over": "fresh group (same form) vs every member's FP64 plan: DFT relative L2 of the worst "
+                                 "(wavelength, plane) slice; bend S over 2 planes x 21 wavelengths x 8 mode columns"},
+    }
 
 
 def run_group(args):
-    """Batched S-matrix workload: the bend with its 8 excitations plus 16 slabs of
-    uneven size (128^3 .. 256x256x192, 1-6 random cuboid inclusions each, one
-    excitation each), all FP32, advanced together by one group in the form its
-    autotuner picks (one sweep launch for all structures, every member's own
-    launches in one graph, or one persistent fused launch per step for all
-    members); the one-launch form timed as well, and the same plans stepped
-    one by one."""
-    import torch
-    from smatranem_gb300 import fdtd as F
-    from smatranem_gb300 import workloads as W
-    bend, pr, modes = make_workload()
-    nsteps = args.warmup + args.steps
-    plans = [make_plan(bend, pr, modes, F.FP32, BATCH, nsteps, tuning=(2, 1, 0, 0, 4))]
-    cells = bend.s.n3 * BATCH
-    for i, shp in enumerate(W.slab_shapes(16, seed=args.group_seed)):
-        sl = W.slab_structure(shp, seed=100 + i)
-        prs = W.prepare(sl.s, dt_factor=1.0 / 0.99)
-        p = F.Plan.create(sl.s.L, sl.s.iBc, (sl.iB, sl.iT, sl.iI, 1), prs.invtau_R, prs.invtau_I, prs.mu,
-                          prs.epsi, prs.sigma, precision=F.FP32, batch=1)
-        p.set_tuning(2, 1, 0, 0, 4)
-        p.set_incident(0, *W.mode_profiles(sl, n_modes=1)[0])
-        src, ph = W.pulse_schedule(nsteps, prs.dt, lams_um=LAMS)
-        p.set_schedule(src, planes=(sl.iB, sl.iT), phase=ph)
-        plans.append(p)
-        cells += sl.s.n3
-    g = F.Group(plans)
-    if args.group_form == 3:  # the one-launch form directly, without timing the other forms
-        gmode, by = 3, 1
-        g.set_tuning(gmode, by)
-    else:
-        (gmode, by), _ = g.autotune(4)
-    g.run(0, args.warmup)
-    _, t_group = _timed(lambda: g.run(args.warmup, nsteps))
-    # the one-launch form (3) timed over the same steps whatever the autotuner chose
-    t_one, shape_one = t_group, by
-    if gmode != 3:
-        t_one = float("inf")
-        for shape in (1, 2):
-            g.set_tuning(3, shape)
-            g.run(0, args.warmup)
-            _, t = _timed(lambda: g.run(args.warmup, nsteps))
-            if t < t_one:
-                t_one, shape_one = t, shape
-    g.close()
-    if gmode in (0, 1):  # the same steps again as separate plans, each on its own stream
-        for p in plans:  # (after forms 2 and 3 every member keeps its own autotuned launch form)
-            p.set_tuning(2, by, 0, 0, 4)
-
-    def one_by_one():
-        for p in plans:
-            p.run(args.warmup, nsteps, sync=False)
-        for p in plans:
-            p.sync()
-    _, t_sep = _timed(one_by_one)
-    tunings = [list(p.get_tuning()) for p in plans]
-    device_gb = sum(p.device_bytes for p in plans) / 1e9
-    for p in plans:
-        p.close()
-    acc = _group_accuracy(bend, pr, modes, W.slab_shapes(16, seed=args.group_seed)[0], 100)
-    print(json.dumps({
-        "mode": "group", "config": "bend 256x192x160 x 8 excitations + 16 slabs 128^3..256x256x192, FP32, "
-                                   "21-wavelength FP64 DFT on 2 planes each",
-        "structures": len(plans), "cell_excitations": cells, "steps": args.steps,
-        "group_tuning": {"mode": ["one grouped launch per sweep", "members' own sweep launches in one graph",
-                                  "members' own autotuned launch forms in one graph",
-                                  "one persistent fused launch per step for every member"][gmode],
-                         "block_y": by, "member_tunings": tunings},
-        "group_gcell_per_s": cells * args.steps / t_group / 1e9, "group_ms_per_step": 1e3 * t_group / args.steps,
-        "one_launch_gcell_per_s": cells * args.steps / t_one / 1e9,
-        "one_launch_form": "mode 3: the resident CTAs shared out among the members, each member's own schedule; "
-                           + ("CTAs of 384 threads, one per SM" if shape_one == 1 else "CTAs of 192 threads, two per SM"),
-        "separate_plans_gcell_per_s": cells * args.steps / t_sep / 1e9,
-        "device_gb": device_gb,
-        "fp32_vs_fp64": acc,
-    }))
-
-
-def _group_accuracy(bend, pr, modes, slab_shape, slab_seed, nsteps=300):
-    """A fresh one-launch group (form 3) of the bend (its 8 excitations) and one
-    slab, nsteps steps of the pulse; each member's DFT against the FP64 plan of
-    the same structure and source: per (wavelength, plane) slice the relative
-    L2 error, the largest over the slices (the bend's excitation 0)."""
-    from smatranem_gb300 import fdtd as F
-    from smatranem_gb300 import workloads as W
-    sl = W.slab_structure(slab_shape, seed=slab_seed)
-    prs = W.prepare(sl.s, dt_factor=1.0 / 0.99)
-
-    def slab_plan(prec):
-        p = F.Plan.create(sl.s.L, sl.s.iBc, (sl.iB, sl.iT, sl.iI, 1), prs.invtau_R, prs.invtau_I, prs.mu,
-                          prs.epsi, prs.sigma, precision=prec, batch=1)
-        p.set_incident(0, *W.mode_profiles(sl, n_modes=1)[0])
-        src, ph = W.pulse_schedule(nsteps, prs.dt, lams_um=LAMS)
-        p.set_schedule(src, planes=(sl.iB, sl.iT), phase=ph)
-        return p
-
-    def rel(a, b):
-        d = (a - b).reshape(a.shape[0], a.shape[1], -1)
-        r = b.reshape(d.shape)
-        return float(np.max(np.linalg.norm(d, axis=2) / np.linalg.norm(r, axis=2)))
-
-    g32 = [make_plan(bend, pr, modes, F.FP32, BATCH, nsteps, tuning=None), slab_plan(F.FP32)]
-    g = F.Group(g32)
-    g.set_tuning(3, 1)
-    g.run(0, nsteps)
-    g.close()
-    d32 = [dft_fields(g32[0], 0), dft_fields(g32[1], 0)]
-    for p in g32:
-        p.close()
-    out = {}
-    for name, mk, d in (("bend", lambda: make_plan(bend, pr, modes, F.FP64, 1, nsteps, tuning=None), d32[0]),
-                        ("slab", lambda: slab_plan(F.FP64), d32[1])):
-        p = mk()
-        p.run(0, nsteps)
-        out[name] = rel(d, dft_fields(p, 0))
-        p.close()
-    return {"dft_max_rel_l2": out, "steps": nsteps, "slab": list(slab_shape),
-            "over": "Hx, Hy, Ex, Ey on both planes x 21 wavelengths, per (wavelength, plane) slice; bend: excitation 0"}
+    print(json.dumps(dict({"mode": "group"}, **config_group(args.warmup, args.steps, args.group_seed,
+                                                             autotune=args.group_form != 3))))
 
 
 def _cube_cpu_worker(args):
@@ -771,66 +830,94 @@ def _cube_cpu_worker(args):
     return time.perf_counter() - t0, n3 * nsteps
 
 
-def run_cube(args):
+def config_cube(nsteps=4000, warmup=5, cpu_steps=0):
     """The plain FP64 benchmark case: 96^3 cells in vacuum, a centred 30^3
     block of eps 12.11, a 40x40 one-cell PEC plate 15 cells below it, 10-cell
     split PML on all faces (grading 3, R = 1e-6), an x point source driven by a
-    Gaussian-modulated sine (1.55 um, 20 % bandwidth), 4000 steps at Courant
+    Gaussian-modulated sine (1.55 um, 20 % bandwidth), nsteps steps at Courant
     0.99/sqrt(3), running DFT at 11 wavelengths on one plane.  FP64 (bit-
-    identical to the reference loop) and FP32 (autotuned) on the GPU; the CPU
-    oracle (the reference loop restated) on a bounded sample of steps."""
+    identical to the reference loop) and FP32 (autotuned) on the GPU, timed
+    with CUDA events over the steps after warmup; roofline of the FP64 step on
+    145.4 B per cell-update (fields and aux slots read and written, a material
+    index per cell); the CPU oracle on cpu_steps steps (0: none)."""
+    import torch
     from smatranem_gb300 import fdtd as F
     from smatranem_gb300 import workloads as W
     c = W.cube_structure()
     pr = W.prepare(c.s, dt_factor=1.0 / 0.99)
-    nsteps = args.cube_steps
     lams = [float(x) for x in np.linspace(1.55 * 0.9, 1.55 * 1.1, 11)]
     src, ph = W.pulse_schedule(nsteps, pr.dt, lam0_um=1.55, bandwidth=0.2, lams_um=lams)
     Hinc, Einc = W.point_source(c)
     res, dft = {}, {}
+    n3, ns = c.s.n3, pr.lnotn
+    peak, peak_kind = measured_peak()
+    st = torch.cuda.Stream()
     for prec, name in ((F.FP64, "fp64"), (F.FP32, "fp32")):
         p = F.Plan.create(c.s.L, c.s.iBc, (c.iM, c.iM, c.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
-                          pr.sigma, precision=prec, batch=1, pec=c.s.pec)
+                          pr.sigma, precision=prec, batch=1, pec=c.s.pec, stream=st.cuda_stream)
         tuning = list(p.autotune(4)[0]) if prec == F.FP32 else None
         p.set_incident(0, Hinc, Einc)
         p.set_schedule(src, planes=(c.iM,), phase=ph)
-        p.run(0, args.warmup)
-        _, t = _timed(lambda: p.run(args.warmup, nsteps))
+        p.run(0, warmup)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(st)
+        p.run(warmup, nsteps, sync=False)
+        ev1.record(st)
+        torch.cuda.synchronize()
+        t = ev0.elapsed_time(ev1) * 1e-3
         dft[name] = np.array([p.get_dft(0, fi, 0) for fi in range(len(lams))])
-        res[name] = {"gcell_per_s": c.s.n3 * (nsteps - args.warmup) / t / 1e9,
-                     "ms_per_step": 1e3 * t / (nsteps - args.warmup), "tuning": tuning}
+        res[name] = {"gcell_per_s": n3 * (nsteps - warmup) / t / 1e9, "ms_per_step": 1e3 * t / (nsteps - warmup),
+                     "tuning": tuning}
+        if prec == F.FP64:
+            bpc = (n3 * (12 * 8 + 1) + ns * 12 * 8) / n3
+            ach = bpc * n3 * (nsteps - warmup) / t / 1e9
+            res[name]["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                                     "frac": ach / peak, "peak_kind": peak_kind, "bytes_per_cell_update": bpc,
+                                     "note": "the FP64 state and coefficients (about 0.2 GB) stay largely in "
+                                             "the 126 MB L2 between steps"}
         p.close()
-    err = float(np.max(np.abs(dft["fp32"] - dft["fp64"])) / np.max(np.abs(dft["fp64"])))
+    rel = np.abs(dft["fp32"] - dft["fp64"]).reshape(len(lams), -1)
+    err = float(np.max(np.linalg.norm(rel, axis=1) / np.linalg.norm(dft["fp64"].reshape(len(lams), -1), axis=1)))
     cpu = None
-    if not args.no_cpu:
+    if cpu_steps > 0:
         kind = oracle_kind()
         ctx = mp.get_context("spawn")
         with ctx.Pool(1) as pool:
-            t_cpu, cells = pool.map(_cube_cpu_worker, [(args.cpu_steps, kind)])[0]
+            t_cpu, cells = pool.map(_cube_cpu_worker, [(cpu_steps, kind)])[0]
         cpu = {"value": cells / t_cpu / 1e9, "unit": "Gcell-updates/s", "cores": 1, "kind": kind,
-               "sample": f"{args.cpu_steps} main_calc steps of the 96^3 cube, {t_cpu:.1f} s on 1 core"}
-    print(json.dumps({
-        "mode": "cube", "config": "96^3 vacuum, 30^3 block eps 12.11, 40x40 PEC plate 15 cells below, 10-cell split "
-                                  "PML on 6 faces (R = 1e-6, grading 3), x point source, Gaussian-modulated sine "
-                                  "1.55 um / 20 %, Courant 0.99/sqrt(3), DFT at 11 wavelengths on one plane",
-        "cells": c.s.n3, "split_cells": pr.lnotn, "pec_cells": int(c.s.pec.sum()), "steps": nsteps,
+               "sample": f"{cpu_steps} main_calc steps of the 96^3 cube, {t_cpu:.1f} s on 1 core"}
+    return {
+        "config": "96^3 vacuum, 30^3 block eps 12.11, 40x40 PEC plate 15 cells below, 10-cell split PML on 6 faces "
+                  "(R = 1e-6, grading 3), x point source, Gaussian-modulated sine 1.55 um / 20 %, Courant "
+                  "0.99/sqrt(3), DFT at 11 wavelengths on one plane",
+        "cells": n3, "split_cells": ns, "pec_cells": int(c.s.pec.sum()), "steps": nsteps,
         "fp64": res["fp64"], "fp32": res["fp32"],
-        "dft_rel_err_fp32_vs_fp64": err, "fp64_bit_identical_to_reference": "tests/test_gpu_cube.py",
+        "dft_rel_l2_fp32_vs_fp64": err,
+        "dft_err_over": "per wavelength, relative L2 over the plane's Hx, Hy, Ex, Ey; the worst of 11",
+        "fp64_bit_identical_to_reference": "tests/test_gpu_cube.py",
         "cpu_baseline": cpu,
-    }))
+    }
 
 
-def run_large(args):
+def run_cube(args):
+    print(json.dumps(dict({"mode": "cube"}, **config_cube(args.cube_steps, args.warmup,
+                                                           0 if args.no_cpu else args.cpu_steps))))
+
+
+def config_large(warmup=5, steps=20, check_steps=600):
     """Large-domain throughput: 640x640x512 cells (~210M) in FP32, split PML,
-    gently curved substrate (radius 50 um), PEC patch-array grating."""
+    gently curved substrate (radius 50 um), PEC patch-array grating, DFT at 5
+    wavelengths on 2 planes; the autotuner's launch form timed over `steps`
+    steps; roofline on the algorithmic bytes (fields and aux slots read and
+    written, 6 coefficients per cell); fresh FP32 and FP64 plans after
+    check_steps pulse steps compared (0: no check)."""
     from smatranem_gb300 import fdtd as F
     from smatranem_gb300 import workloads as W
     t0 = time.perf_counter()
     st = W.large_structure()
     pr = W.prepare(st.s, dt_factor=1.0 / 0.99)
-    p = F.Plan.create(st.s.L, st.s.iBc, (st.iB, st.iT, st.iI, 1), pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi,
-                      pr.sigma, precision=F.FP32, batch=1, pec=st.s.pec)
-    nsteps = args.warmup + args.steps
+    nsteps = warmup + steps
     lams = list(np.linspace(1.50, 1.60, 5))
     sheets = W.mode_profiles(st, n_modes=1)[0]
 
@@ -845,16 +932,18 @@ def run_large(args):
     p = plan(F.FP32, nsteps)
     t_setup = time.perf_counter() - t0
     best, _ = p.autotune(2)
-    p.run(0, args.warmup)
-    _, t = _timed(lambda: p.run(args.warmup, nsteps))
+    p.run(0, warmup)
+    _, t = _timed(lambda: p.run(warmup, nsteps))
     ok, mx = p.check_finite()
     dev_gb = p.device_bytes / 1e9
     p.close()
-    # the DFT fields of fresh FP32 and FP64 plans after a bounded pulse run:
-    # per (wavelength, plane) slice the relative L2 error, the largest
+    n3, ns = st.s.n3, pr.lnotn
+    peak, peak_kind = measured_peak()
+    bstep = algorithmic_bytes_per_step(n3, ns, 1)
+    achieved = bstep * steps / t / 1e9
     check = None
-    if args.large_check_steps > 0:
-        n = args.large_check_steps
+    if check_steps > 0:
+        n = check_steps
         d = {}
         for prec in (F.FP32, F.FP64):
             q = plan(prec, n)
@@ -871,13 +960,19 @@ def run_large(args):
                  "slices": int(live.sum()), "of": int(live.size),
                  "over": "Hx, Hy, Ex, Ey on both planes x 5 wavelengths, per (wavelength, plane) slice holding "
                          "field"}
-    print(json.dumps({
-        "mode": "large", "config": "640x640x512 FP32, 12-cell split PML, curved substrate R=50um, PEC patch array, "
-                                   "DFT at 5 wavelengths (1.50-1.60 um) on 2 planes",
-        "cells": st.s.n3, "split_cells": pr.lnotn, "steps": args.steps, "tuning": list(best),
-        "gcell_per_s": st.s.n3 * args.steps / t / 1e9, "ms_per_step": 1e3 * t / args.steps,
+    return {
+        "config": "640x640x512 FP32, 12-cell split PML, curved substrate R=50um, PEC patch array (16x16 patches, "
+                  "period 40, 20x20x2 cells) over an eps 2.085 slab, DFT at 5 wavelengths (1.50-1.60 um) on 2 planes",
+        "cells": n3, "split_cells": ns, "steps": steps, "tuning": list(best),
+        "gcell_per_s": n3 * steps / t / 1e9, "ms_per_step": 1e3 * t / steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "bytes_per_cell_update": bstep / n3},
         "device_gb": dev_gb, "setup_s": t_setup, "finite": ok, "fp32_vs_fp64": check,
-    }))
+    }
+
+
+def run_large(args):
+    print(json.dumps(dict({"mode": "large"}, **config_large(args.warmup, args.steps, args.large_check_steps))))
 
 
 def run_modes(args):
@@ -1000,9 +1095,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--full-steps", type=int, default=FULL_STEPS)
-    ap.add_argument("--steps64", type=int, default=40)
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--extras", default="cube,adjoint,group,large",
+                    help="main mode: the other workloads summarised in the contract line (comma list of cube, "
+                         "adjoint, group, large; empty: none)")
+    ap.add_argument("--extras-budget", type=float, default=420.0,
+                    help="seconds the extras may take together; one that would not fit is reported as skipped")
+    ap.add_argument("--extra-fd-cells", type=int, default=4,
+                    help="finite-difference cells of the adjoint summary in the main mode (--mode adjoint: --fd-cells)")
     ap.add_argument("--profile", choices=["fp32", "fp64"], help="small case for ncu captures")
     ap.add_argument("--shape", default="256,192,48")
     ap.add_argument("--tuning", default="", help="kernel,tile_y,z_chunk,ctas_per_sm,slots (default: autotuned)")

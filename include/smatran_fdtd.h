@@ -340,6 +340,12 @@ int smat_deck_smatrix(const smat_deck *deck, int which, const double *HB, const 
  * of :182-185) to stderr; returns the process exit status. */
 int smat_fdtd_main(int argc, char **argv);
 
+/* Bytes copied host -> device and device -> host for this plan since it was
+ * created: the uploads of creation, sources, schedules and states, and every
+ * read-back (fields, monitors, DFT planes, overlaps, states, status words).
+ * No counterpart in the reference (it has no device). */
+int smat_fdtd_copy_bytes(const smat_fdtd_plan *plan, long long *h2d, long long *d2h);
+
 /* Largest |field| over every excitation (a NaN/Inf check); *finite = 0 when a
  * non-finite value is present. */
 int smat_fdtd_check_finite(smat_fdtd_plan *plan, int *finite, double *max_abs);

@@ -821,42 +821,78 @@ void launch_group32v(const Group32 &gr, int rel, cudaStream_t st)
 }
 
 /* Fold `count` ring slots ending at step *base + rel_end into the FP64 DFT
- * accumulators: acc += sum_k phase_k * x_k with an FP32 sum over the slots. */
+ * accumulators (the reference's running DFT, FDTDsplitfieldMetal.c:318-328,
+ * here on FP32 field samples): for each pixel, monitor plane, component and
+ * frequency, acc += sum over the window of x_k * e^{i phi_k}, in compensated
+ * FP32.
+ *   - each phase (FP64 in the schedule) is carried as a float pair hi + lo,
+ *     hi = fl(phi), lo = fl(phi - hi): together exact to about 2^-48;
+ *   - each product x*hi is split exactly into p = fl(x*hi) and its rounding
+ *     error e = fma(x, hi, -p); x*lo joins e (its own rounding is ~2^-48 of
+ *     the term);
+ *   - the window's p are summed by Kahan summation whose compensation also
+ *     carries the low parts e + x*lo, so the window sum s - c is good to a
+ *     few units of 2^-24 of sum |x| whatever the window length, and is added
+ *     to the FP64 accumulator as (double)s - (double)c.
+ * A thread takes one pixel and the two components of one half (H: Hx, Hy, or
+ * E: Ex, Ey) of one plane and excitation, so each phase pair, read from
+ * shared memory as one 16-byte broadcast, serves four products. */
 constexpr int RING_MAX = 32;
 
-__global__ void k_flush32(const P32 p, const int rel_end, const int count)
+/* one term of the compensated sum; the _rn intrinsics keep every operation a
+ * separately rounded one (no multiply-add contraction may merge them) */
+__device__ __forceinline__ void kahan_term(float x, float hi, float lo, float &s, float &c)
 {
-    extern __shared__ float sph[]; /* [count][nfreq][4] phases of the window */
+    const float p = __fmul_rn(x, hi);
+    float e = fmaf(x, hi, -p);
+    e = fmaf(x, lo, e);
+    const float y = __fsub_rn(p, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(__fsub_rn(t, s), y), e);
+    s = t;
+}
+
+__global__ void __launch_bounds__(128) k_flush32(const P32 p, const int rel_end, const int count)
+{
+    extern __shared__ float4 sph4[]; /* [count][nfreq] {hi re, hi im, lo re, lo im} of this half */
     const Dft &d = p.d;
     const int k0 = *p.s.base + rel_end - count;
-    const int nph = count * d.nfreq * 4;
+    const int qh = blockIdx.y, b = blockIdx.z;
+    const int q = qh >> 1, half = qh & 1, po = 2 * half;
+    const int nph = count * d.nfreq;
     for (int i = threadIdx.x; i < nph; i += blockDim.x) {
-        const int s = i / (d.nfreq * 4), r = i % (d.nfreq * 4);
-        sph[i] = d.xphase32 ? d.xphase32[r & 3] : d.phase32[4 * (long long)(k0 + s) * d.nfreq + r];
+        const int s = i / d.nfreq, f = i % d.nfreq;
+        const double *ph = d.xphase ? d.xphase + po : d.phase + 4 * ((long long)(k0 + s) * d.nfreq + f) + po;
+        const float hr = (float)ph[0], hi = (float)ph[1];
+        sph4[i] = make_float4(hr, hi, (float)(ph[0] - (double)hr), (float)(ph[1] - (double)hi));
     }
     __syncthreads();
     const int px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int qv = blockIdx.y, b = blockIdx.z;
-    const int q = qv >> 2, v = qv & 3;
     if (px >= p.g.pl) return;
-    float x[RING_MAX];
+    float x0[RING_MAX], x1[RING_MAX];
 #pragma unroll
-    for (int s = 0; s < RING_MAX; s++)
-        x[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, v)[px] : 0.0f;
-    const int po = v < 2 ? 0 : 2;
+    for (int s = 0; s < RING_MAX; s++) {
+        x0[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, po)[px] : 0.0f;
+        x1[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, po + 1)[px] : 0.0f;
+    }
     for (int f = 0; f < d.nfreq; f++) {
-        float sr = 0.0f, si = 0.0f;
+        float s0r = 0.f, c0r = 0.f, s0i = 0.f, c0i = 0.f, s1r = 0.f, c1r = 0.f, s1i = 0.f, c1i = 0.f;
 #pragma unroll
         for (int s = 0; s < RING_MAX; s++) {
             if (s < count) {
-                const float *ph = sph + (s * d.nfreq + f) * 4 + po;
-                sr = fmaf(ph[0], x[s], sr);
-                si = fmaf(ph[1], x[s], si);
+                const float4 ph = sph4[s * d.nfreq + f];
+                kahan_term(x0[s], ph.x, ph.z, s0r, c0r);
+                kahan_term(x0[s], ph.y, ph.w, s0i, c0i);
+                kahan_term(x1[s], ph.x, ph.z, s1r, c1r);
+                kahan_term(x1[s], ph.y, ph.w, s1i, c1i);
             }
         }
-        double *acc = d.acc + 2 * (((((long long)b * d.nfreq + f) * d.nq + q) * 4 + v) * p.g.pl + px);
-        acc[0] += (double)sr;
-        acc[1] += (double)si;
+        double *a0 = d.acc + 2 * (((((long long)b * d.nfreq + f) * d.nq + q) * 4 + po) * p.g.pl + px);
+        double *a1 = a0 + 2 * (long long)p.g.pl;
+        a0[0] += (double)s0r - (double)c0r;
+        a0[1] += (double)s0i - (double)c0i;
+        a1[0] += (double)s1r - (double)c1r;
+        a1[1] += (double)s1i - (double)c1i;
     }
 }
 
@@ -925,8 +961,8 @@ void launch_e32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const in
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st)
 {
     if (p.d.nfreq <= 0 || p.d.nq <= 0 || count <= 0) return;
-    dim3 blk(256), grd((p.g.pl + 255) / 256, p.d.nq * 4, p.batch);
-    const size_t sm = sizeof(float) * 4 * (size_t)count * p.d.nfreq;
+    dim3 blk(128), grd((p.g.pl + 127) / 128, p.d.nq * 2, p.batch);
+    const size_t sm = sizeof(float4) * (size_t)count * p.d.nfreq;
     if (sm > 48 * 1024) cudaFuncSetAttribute(k_flush32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_flush32<<<grd, blk, sm, st>>>(p, rel_end, count);
 }

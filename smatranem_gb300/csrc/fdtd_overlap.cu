@@ -18,6 +18,7 @@
 
 #include "trace.cuh"
 #include "fdtd_internal.cuh"
+#include "plan_internal.cuh"
 #include "host_internal.h"
 #include "smatran_fdtd.h"
 
@@ -158,10 +159,12 @@ extern "C" int smat_fdtd_overlap(smat_fdtd_plan *plan, int b, int q, int ncols, 
         return smat_fail(SMAT_ENOMEM, "fdtd_overlap: device buffers");
     }
     rc = SMAT_OK;
+    plan->h2d_bytes += (long long)tn * 8;
     if (cudaMemcpy(dt, tilXi_host, tn * 8, cudaMemcpyHostToDevice) != cudaSuccess)
         rc = smat_fail(SMAT_ECUDA, "fdtd_overlap: upload");
     if (!rc) rc = smat_fdtd_sync(plan);
     if (!rc) rc = smat_overlap(npix, ncols, nfreq, fstride, dt, acc, dS, nullptr);
+    if (!rc) plan->d2h_bytes += (long long)sn * 8;
     if (!rc && cudaMemcpy(S_host, dS, sn * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
         rc = smat_fail(SMAT_ECUDA, "fdtd_overlap: download");
     cudaFree(dt);

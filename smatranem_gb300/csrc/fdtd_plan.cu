@@ -343,8 +343,8 @@ int common_alloc(smat_fdtd_plan *p)
         std::vector<int> ii(p->batch, p->iBTIin[2]);
         p->h_iI = ii;
         std::vector<double> sg(p->batch, (double)(m / (m < 0 ? -m : m)));
-        CK(cudaMemcpyAsync(p->d_iI, ii.data(), ii.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
-        CK(cudaMemcpyAsync(p->d_isgn, sg.data(), sg.size() * 8, cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_iI, ii.data(), ii.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CK(p->cpy(p->d_isgn, sg.data(), sg.size() * 8, cudaMemcpyHostToDevice));
         CK(cudaStreamSynchronize(p->stream));
     }
     /* the reference DFT: one frequency on planes iB and iT */
@@ -421,10 +421,10 @@ int upload_f64(smat_fdtd_plan *p, const double *Ah, const double *Bh, const doub
             for (long long l = 0; l < n3; l++) cm[((size_t)w * 3 + c) * n3 + l] = src[w][c + 3 * l];
             for (int a = 0; a < ln; a++) ca[((size_t)w * 3 + c) * ln + a] = src[w][c + 3 * (n3 + a)];
         }
-    CK(cudaMemcpyAsync(p->d_flags, fl.data(), n3, cudaMemcpyHostToDevice, p->stream));
-    CK(cudaMemcpyAsync(p->d_addr, p->addr.data(), n3 * sizeof(int), cudaMemcpyHostToDevice, p->stream));
-    CK(cudaMemcpyAsync(p->d_cm, cm.data(), cm.size() * 8, cudaMemcpyHostToDevice, p->stream));
-    if (ln) CK(cudaMemcpyAsync(p->d_ca, ca.data(), ca.size() * 8, cudaMemcpyHostToDevice, p->stream));
+    CK(p->cpy(p->d_flags, fl.data(), n3, cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_addr, p->addr.data(), n3 * sizeof(int), cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_cm, cm.data(), cm.size() * 8, cudaMemcpyHostToDevice));
+    if (ln) CK(p->cpy(p->d_ca, ca.data(), ca.size() * 8, cudaMemcpyHostToDevice));
     CK(cudaStreamSynchronize(p->stream));
     return SMAT_OK;
 }
@@ -546,9 +546,9 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
     }
     if ((rc = p->alloc(&p->d_hgen, hgen.size() + 1)) || (rc = p->alloc(&p->d_egen, egen.size() + 1))) return rc;
     if (!hgen.empty())
-        CK(cudaMemcpyAsync(p->d_hgen, hgen.data(), hgen.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_hgen, hgen.data(), hgen.size() * sizeof(int), cudaMemcpyHostToDevice));
     if (!egen.empty())
-        CK(cudaMemcpyAsync(p->d_egen, egen.data(), egen.size() * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_egen, egen.data(), egen.size() * sizeof(int), cudaMemcpyHostToDevice));
     /* record kinds kernel 6 can or cannot take */
     for (int side = 0; side < 2; side++) {
         const std::vector<float> &cf = side ? be : bh;
@@ -575,16 +575,16 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
                 if (pass == 0 && px) p->nqp++;
             }
         if ((rc = p->alloc(&p->d_qorder, (size_t)nq))) return rc;
-        CK(cudaMemcpyAsync(p->d_qorder, qorder.data(), nq * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_qorder, qorder.data(), nq * sizeof(int), cudaMemcpyHostToDevice));
     }
-    CK(cudaMemcpyAsync(p->d_bh, bh.data(), bh.size() * 4, cudaMemcpyHostToDevice, p->stream));
-    CK(cudaMemcpyAsync(p->d_be, be.data(), be.size() * 4, cudaMemcpyHostToDevice, p->stream));
-    CK(cudaMemcpyAsync(p->d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, p->stream));
-    CK(cudaMemcpyAsync(p->d_pmask, pmask.data(), pmask.size(), cudaMemcpyHostToDevice, p->stream));
+    CK(p->cpy(p->d_bh, bh.data(), bh.size() * 4, cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_be, be.data(), be.size() * 4, cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_pmask, pmask.data(), pmask.size(), cudaMemcpyHostToDevice));
     if (!hrec.empty())
-        CK(cudaMemcpyAsync(p->d_hrec, hrec.data(), hrec.size() * sizeof(Rec32), cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_hrec, hrec.data(), hrec.size() * sizeof(Rec32), cudaMemcpyHostToDevice));
     if (!erec.empty())
-        CK(cudaMemcpyAsync(p->d_erec, erec.data(), erec.size() * sizeof(Rec32), cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_erec, erec.data(), erec.size() * sizeof(Rec32), cudaMemcpyHostToDevice));
     CK(cudaStreamSynchronize(p->stream));
     return SMAT_OK;
 }
@@ -739,8 +739,8 @@ extern "C" int smat_fdtd_set_fields(smat_fdtd_plan *p, int b, const double *H_t,
             }
             double *dm = (w ? p->d_E64 : p->d_H64) + (size_t)b * 3 * n3;
             double *da = (w ? p->d_Ea64 : p->d_Ha64) + (size_t)b * 3 * (ln + 1);
-            CK(cudaMemcpyAsync(dm, m.data(), m.size() * 8, cudaMemcpyHostToDevice, p->stream));
-            CK(cudaMemcpyAsync(da, a.data(), a.size() * 8, cudaMemcpyHostToDevice, p->stream));
+            CK(p->cpy(dm, m.data(), m.size() * 8, cudaMemcpyHostToDevice));
+            CK(p->cpy(da, a.data(), a.size() * 8, cudaMemcpyHostToDevice));
             CK(cudaStreamSynchronize(p->stream));
         } else {
             std::vector<float> t(3 * n3), a(3 * n3, 0.0f);
@@ -754,8 +754,8 @@ extern "C" int smat_fdtd_set_fields(smat_fdtd_plan *p, int b, const double *H_t,
             const P32 q = make_p32(p, false);
             float *dt = (w ? q.E : q.H) + (size_t)b * 3 * n3;
             float *da = (w ? q.Ea : q.Ha) + (size_t)b * 3 * n3;
-            CK(cudaMemcpyAsync(dt, t.data(), t.size() * 4, cudaMemcpyHostToDevice, p->stream));
-            CK(cudaMemcpyAsync(da, a.data(), a.size() * 4, cudaMemcpyHostToDevice, p->stream));
+            CK(p->cpy(dt, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+            CK(p->cpy(da, a.data(), a.size() * 4, cudaMemcpyHostToDevice));
             CK(cudaStreamSynchronize(p->stream));
         }
     }
@@ -775,8 +775,8 @@ extern "C" int smat_fdtd_get_fields(smat_fdtd_plan *p, int b, double *H_t, doubl
             std::vector<double> m(3 * n3), a(3 * (size_t)(ln + 1));
             const double *dm = (w ? p->d_E64 : p->d_H64) + (size_t)b * 3 * n3;
             const double *da = (w ? p->d_Ea64 : p->d_Ha64) + (size_t)b * 3 * (ln + 1);
-            CK(cudaMemcpyAsync(m.data(), dm, m.size() * 8, cudaMemcpyDeviceToHost, p->stream));
-            CK(cudaMemcpyAsync(a.data(), da, a.size() * 8, cudaMemcpyDeviceToHost, p->stream));
+            CK(p->cpy(m.data(), dm, m.size() * 8, cudaMemcpyDeviceToHost));
+            CK(p->cpy(a.data(), da, a.size() * 8, cudaMemcpyDeviceToHost));
             CK(cudaStreamSynchronize(p->stream));
             for (int c = 0; c < 3; c++) {
                 for (long long l = 0; l < n3; l++) dst[c + 3 * l] = m[c * n3 + l];
@@ -787,8 +787,8 @@ extern "C" int smat_fdtd_get_fields(smat_fdtd_plan *p, int b, double *H_t, doubl
             const P32 q = make_p32(p, false);
             const float *dt = (w ? q.E : q.H) + (size_t)b * 3 * n3;
             const float *da = (w ? q.Ea : q.Ha) + (size_t)b * 3 * n3;
-            CK(cudaMemcpyAsync(t.data(), dt, t.size() * 4, cudaMemcpyDeviceToHost, p->stream));
-            CK(cudaMemcpyAsync(a.data(), da, a.size() * 4, cudaMemcpyDeviceToHost, p->stream));
+            CK(p->cpy(t.data(), dt, t.size() * 4, cudaMemcpyDeviceToHost));
+            CK(p->cpy(a.data(), da, a.size() * 4, cudaMemcpyDeviceToHost));
             CK(cudaStreamSynchronize(p->stream));
             memset(dst, 0, sizeof(double) * 3 * (size_t)(n3 + ln + 1));
             for (int c = 0; c < 3; c++)
@@ -811,8 +811,8 @@ extern "C" int smat_fdtd_set_incident(smat_fdtd_plan *p, int b, const double *Hi
     smat_clear_error();
     if (!p || !Hinc || !Einc || b < 0 || b >= p->batch) return smat_fail(SMAT_EINVAL, "set_incident: bad arguments");
     const size_t n = 4 * (size_t)p->pl;
-    CK(cudaMemcpyAsync(p->d_inc + (size_t)b * 8 * p->pl, Hinc, n * 8, cudaMemcpyHostToDevice, p->stream));
-    CK(cudaMemcpyAsync(p->d_inc + (size_t)b * 8 * p->pl + n, Einc, n * 8, cudaMemcpyHostToDevice, p->stream));
+    CK(p->cpy(p->d_inc + (size_t)b * 8 * p->pl, Hinc, n * 8, cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_inc + (size_t)b * 8 * p->pl + n, Einc, n * 8, cudaMemcpyHostToDevice));
     CK(cudaStreamSynchronize(p->stream));
     return SMAT_OK;
 }
@@ -824,8 +824,8 @@ extern "C" int smat_fdtd_set_source_plane(smat_fdtd_plan *p, int b, int iI, int 
         return smat_fail(SMAT_EINVAL, "set_source_plane: bad arguments");
     const double sg = (double)(inci_mode / (inci_mode < 0 ? -inci_mode : inci_mode));
     p->h_iI[b] = iI;
-    CK(cudaMemcpyAsync(p->d_iI + b, &iI, sizeof(int), cudaMemcpyHostToDevice, p->stream));
-    CK(cudaMemcpyAsync(p->d_isgn + b, &sg, 8, cudaMemcpyHostToDevice, p->stream));
+    CK(p->cpy(p->d_iI + b, &iI, sizeof(int), cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_isgn + b, &sg, 8, cudaMemcpyHostToDevice));
     CK(cudaStreamSynchronize(p->stream));
     return SMAT_OK;
 }
@@ -843,16 +843,16 @@ extern "C" int smat_fdtd_set_schedule(smat_fdtd_plan *p, int nsteps, const doubl
     if (p->d_phase) cudaFree(p->d_phase), p->d_phase = nullptr;
     if (p->d_phase32) cudaFree(p->d_phase32), p->d_phase32 = nullptr;
     if ((rc = dalloc(&p->d_sched, 6 * (size_t)nsteps, p->stream))) return rc;
-    CK(cudaMemcpyAsync(p->d_sched, src, 6 * (size_t)nsteps * 8, cudaMemcpyHostToDevice, p->stream));
+    CK(p->cpy(p->d_sched, src, 6 * (size_t)nsteps * 8, cudaMemcpyHostToDevice));
     if (nfreq > 0) {
         const size_t np = 4 * (size_t)nsteps * nfreq;
         if ((rc = dalloc(&p->d_phase, np, p->stream))) return rc;
-        CK(cudaMemcpyAsync(p->d_phase, phase, np * 8, cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_phase, phase, np * 8, cudaMemcpyHostToDevice));
         if (p->precision == SMAT_FP32) {
             std::vector<float> ph32(np);
             for (size_t i = 0; i < np; i++) ph32[i] = (float)phase[i];
             if ((rc = dalloc(&p->d_phase32, np, p->stream))) return rc;
-            CK(cudaMemcpyAsync(p->d_phase32, ph32.data(), np * 4, cudaMemcpyHostToDevice, p->stream));
+            CK(p->cpy(p->d_phase32, ph32.data(), np * 4, cudaMemcpyHostToDevice));
         }
     }
     p->nsched = nsteps;
@@ -901,10 +901,10 @@ extern "C" int smat_fdtd_step(smat_fdtd_plan *p, const double *Hi, const double 
     p->nfreq = 1; /* explicit phases drive frequency slot 0 only */
     const size_t n = 2 * (size_t)p->pl;
     float x32[4] = {(float)ExpN2[0], (float)ExpN2[1], (float)ExpN2[2], (float)ExpN2[3]};
-    cudaError_t e = cudaMemcpyAsync(p->d_xsrc, Hi, n * 8, cudaMemcpyHostToDevice, p->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_xsrc + n, Ei, n * 8, cudaMemcpyHostToDevice, p->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_xphase, ExpN2, 4 * 8, cudaMemcpyHostToDevice, p->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_xphase32, x32, 4 * 4, cudaMemcpyHostToDevice, p->stream);
+    cudaError_t e = p->cpy(p->d_xsrc, Hi, n * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = p->cpy(p->d_xsrc + n, Ei, n * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = p->cpy(p->d_xphase, ExpN2, 4 * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = p->cpy(p->d_xphase32, x32, 4 * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         launch_set(p->d_base, 0, p->stream);
         enqueue_steps(p, 0, 1, true);
@@ -1126,7 +1126,7 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     p->nq = nq;
-    CK(cudaMemcpyAsync(p->d_iI, p->h_iI.data(), sizeof(int) * p->batch, cudaMemcpyHostToDevice, p->stream));
+    CK(p->cpy(p->d_iI, p->h_iI.data(), sizeof(int) * p->batch, cudaMemcpyHostToDevice));
     CK(cudaStreamSynchronize(p->stream));
     rc = smat_fdtd_set_tuning(p, bc.fused, bc.ty, bc.zc, bc.ctas, bc.ns);
     if (rc) return rc;
@@ -1161,6 +1161,14 @@ extern "C" int smat_fdtd_get_tuning(const smat_fdtd_plan *p, int out[5])
     return SMAT_OK;
 }
 
+extern "C" int smat_fdtd_copy_bytes(const smat_fdtd_plan *p, long long *h2d, long long *d2h)
+{
+    if (!p) return smat_fail(SMAT_EINVAL, "null plan");
+    if (h2d) *h2d = p->h2d_bytes;
+    if (d2h) *d2h = p->d2h_bytes;
+    return SMAT_OK;
+}
+
 extern "C" int smat_fdtd_sync(smat_fdtd_plan *p)
 {
     if (!p) return smat_fail(SMAT_EINVAL, "null plan");
@@ -1168,6 +1176,7 @@ extern "C" int smat_fdtd_sync(smat_fdtd_plan *p)
     if (p->d_err) {
         int err = 0;
         CK(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        p->d2h_bytes += sizeof(int);
         if (err) {
             CK(cudaMemset(p->d_err, 0, sizeof(int)));
             return smat_fail(SMAT_ECUDA, err == 2 ? "pipelined sweeps: a wait for an H item timed out"
@@ -1182,7 +1191,7 @@ static int read_acc(smat_fdtd_plan *p, int b, int f, int q, std::vector<double> 
     const size_t n = 4 * (size_t)p->pl * 2;
     out.resize(n);
     const double *src = p->d_acc + (((size_t)b * p->nfreq + f) * p->nq + q) * n;
-    CK(cudaMemcpyAsync(out.data(), src, n * 8, cudaMemcpyDeviceToHost, p->stream));
+    CK(p->cpy(out.data(), src, n * 8, cudaMemcpyDeviceToHost));
     CK(cudaStreamSynchronize(p->stream));
     return SMAT_OK;
 }
@@ -1227,7 +1236,7 @@ static int set_monitor(smat_fdtd_plan *p, const double *HB, const double *EB, co
                 a[2 * ((2 + v) * p->pl + px)] = Es[2 * (v + 2 * px)];
                 a[2 * ((2 + v) * p->pl + px) + 1] = Es[2 * (v + 2 * px) + 1];
             }
-        CK(cudaMemcpyAsync(p->d_acc + q * n, a.data(), n * 8, cudaMemcpyHostToDevice, p->stream));
+        CK(p->cpy(p->d_acc + q * n, a.data(), n * 8, cudaMemcpyHostToDevice));
         CK(cudaStreamSynchronize(p->stream));
     }
     return SMAT_OK;
@@ -1275,7 +1284,7 @@ extern "C" int smat_fdtd_check_finite(smat_fdtd_plan *p, int *finite, double *ma
                           d ? (void *)p->d_Ha64 : (void *)q.Ha, d ? (void *)p->d_Ea64 : (void *)q.Ea};
     for (int i = 0; i < 4; i++) launch_maxabs(arr[i], i < 2 ? nf : na, d, p->d_scratch, p->stream);
     unsigned long long bits = 0;
-    CK(cudaMemcpyAsync(&bits, p->d_scratch, 8, cudaMemcpyDeviceToHost, p->stream));
+    CK(p->cpy(&bits, p->d_scratch, 8, cudaMemcpyDeviceToHost));
     CK(cudaStreamSynchronize(p->stream));
     double m;
     memcpy(&m, &bits, 8);
@@ -1374,6 +1383,7 @@ extern "C" int smat_fdtd_save_state(smat_fdtd_plan *p, const char *path)
     for (const auto &a : state_arrays(p)) {
         if (rc) break;
         buf.resize(a.second);
+        p->d2h_bytes += (long long)a.second;
         if (cudaMemcpy(buf.data(), a.first, a.second, cudaMemcpyDeviceToHost) != cudaSuccess) {
             rc = cuda_fail(cudaGetLastError(), "save_state: copy");
             break;
@@ -1413,6 +1423,7 @@ extern "C" int smat_fdtd_load_state(smat_fdtd_plan *p, const char *path)
             rc = smat_fail(SMAT_EINVAL, "load_state: %s is truncated", path);
             break;
         }
+        p->h2d_bytes += (long long)a.second;
         if (cudaMemcpy(a.first, buf.data(), a.second, cudaMemcpyHostToDevice) != cudaSuccess)
             rc = cuda_fail(cudaGetLastError(), "load_state: copy");
     }

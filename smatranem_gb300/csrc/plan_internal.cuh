@@ -122,6 +122,16 @@ struct smat_fdtd_plan {
 
     std::vector<void *> allocations;
 
+    /* bytes copied between host and device on behalf of this plan (uploads
+     * at creation, sources, schedules, read-backs), for smat_fdtd_copy_bytes */
+    long long h2d_bytes = 0, d2h_bytes = 0;
+    cudaError_t cpy(void *dst, const void *src, size_t n, cudaMemcpyKind kind)
+    {
+        if (kind == cudaMemcpyHostToDevice) h2d_bytes += (long long)n;
+        else if (kind == cudaMemcpyDeviceToHost) d2h_bytes += (long long)n;
+        return cudaMemcpyAsync(dst, src, n, kind, stream);
+    }
+
     template <class T> int alloc(T **p, size_t n)
     {
         int rc = smat::plan::dalloc(p, n, stream);

@@ -72,6 +72,7 @@ def lib():
         L.smat_fdtd_device_bytes.argtypes = [_P]
         L.smat_fdtd_destroy.argtypes = [_P]
         L.smat_fdtd_sync.argtypes = [_P]
+        L.smat_fdtd_copy_bytes.argtypes = [_P, _P, _P]
         L.smat_fdtd_info.argtypes = [_P, _P, _P, _P, _P]
         L.smat_fdtd_time_kernels.argtypes = [_P, C.c_int, C.c_int, _P]
         L.smat_fdtd_set_tuning.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
@@ -317,6 +318,13 @@ class Plan:
     def sync(self):
         _check(lib().smat_fdtd_sync(self._h))
 
+    def copy_bytes(self):
+        """(host->device, device->host) bytes copied for this plan so far
+        (smat_fdtd_copy_bytes)."""
+        h, d = C.c_longlong(0), C.c_longlong(0)
+        _check(lib().smat_fdtd_copy_bytes(self._h, C.byref(h), C.byref(d)))
+        return h.value, d.value
+
     def get_monitor(self, b=0):
         out = [np.zeros(2 * self.pl, dtype=np.complex128) for _ in range(4)]
         _check(lib().smat_fdtd_get_monitor(self._h, b, *[_ptr(a) for a in out]))
@@ -341,7 +349,7 @@ class Plan:
         run(k, ...) then continues from step k."""
         _check(lib().smat_fdtd_load_state(self._h, os.fsencode(path)))
 
-    def set_tuning(self, fused=1, tile_y=8, z_chunk=40, ctas_per_sm=0, slots=5):
+    def set_tuning(self, fused=2, tile_y=1, z_chunk=0, ctas_per_sm=0, slots=4):
         _check(lib().smat_fdtd_set_tuning(self._h, fused, tile_y, z_chunk, ctas_per_sm, slots))
 
     def autotune(self, nsteps=4, cache=True):

@@ -262,3 +262,60 @@ def test_adjoint_with_a_column_per_excitation(built):
             p.adjoint_grad(nsteps, 32, 0, 1, np.stack([col, col, col]), d.box)
     assert J2 == pytest.approx(5 * J1, rel=1e-13)
     assert np.allclose(g2 / d.eps, 5 * g1, rtol=1e-12, atol=1e-12 * np.max(np.abs(g1)))
+
+
+def test_adjoint_at_the_design_workload_shape(built):
+    """The adjoint workload's own shape: 160 x 160 x 120 cells, a 60 x 60 x 20
+    design box of seeded eps_r ~ U[2.085, 12.11] between two single-mode strip
+    ports, 12-cell split PML on all six faces, objective |TE0 overlap of the
+    output-port DFT at 1.55 um|^2, FP32 forward and adjoint with a checkpoint
+    every 64 steps, through the torch.autograd wrapper.  A Gaussian pulse of
+    50 % bandwidth over 1600 steps (the workload runs 6000; the pulse has
+    crossed the design box by 1600) keeps the finite differences affordable.
+    Against central differences (delta eps_r = 1e-3) of the FP64 forward --
+    bit-identical to the reference loop -- on 8 seeded design cells: within
+    1e-3 of the largest difference quotient; against the FP64 adjoint over
+    all 72,000 design cells: within 1e-3 of its largest entry."""
+    torch = pytest.importorskip("torch")
+    F, W = _mods()
+    from smatranem_gb300 import autograd as A
+    d = W.design_structure(shape=(160, 160, 120), design=(60, 60, 20), pml=12, seed=0)
+    assert d.eps.shape == (20, 60, 60)
+    pr = W.prepare(d.s, dt_factor=1.0 / 0.99)
+    nsteps = 1600
+    src, ph = W.pulse_schedule(nsteps, pr.dt, bandwidth=0.5, lams_um=[1.55])
+    mode = W.mode_profiles(d, n_modes=1)[0]
+    kw = dict(nsteps=nsteps, K=64, mode=mode, src=src, phase=ph)
+    eps = torch.tensor(d.eps, dtype=torch.float64, requires_grad=True)
+    J32 = A.PortOverlap.apply(eps, d, dict(kw, precision=F.FP32))
+    J32.backward()
+    g32 = eps.grad.numpy()
+    J64, g64 = A.objective_and_grad(d, d.eps, precision=F.FP64, **kw)
+    assert float(J32.detach()) == pytest.approx(J64, rel=1e-4)
+    assert np.max(np.abs(g32 - g64)) <= 1e-3 * np.max(np.abs(g64))
+
+    def objective(e):
+        s = d.with_eps(e)
+        prx = W.prepare(s, dt_factor=1.0 / 0.99)
+        with F.Plan.create(s.L, s.iBc, (d.iB, d.iT, d.iI, 1), prx.invtau_R, prx.invtau_I, prx.mu, prx.epsi,
+                           prx.sigma, precision=F.FP64, batch=1) as p:
+            p.set_incident(0, *mode)
+            p.set_schedule(src, planes=(d.iB, d.iT), phase=ph)
+            p.run(0, nsteps)
+            return abs(W.overlap(p.get_dft(0, 0, 1), *mode)) ** 2
+
+    cells = _fd_cells(d, 8, seed=7)
+    fd = []
+    for c in cells:
+        e = d.eps.copy()
+        e[c] += 1e-3
+        jp = objective(e)
+        e[c] -= 2e-3
+        fd.append((jp - objective(e)) / 2e-3)
+    fd = np.array(fd)
+    a32 = np.array([g32[c] for c in cells])
+    a64 = np.array([g64[c] for c in cells])
+    fscale = np.max(np.abs(fd))
+    assert fscale > 0
+    assert np.max(np.abs(a64 - fd)) <= 1e-5 * fscale, (a64, fd)
+    assert np.max(np.abs(a32 - fd)) <= 1e-3 * fscale, (a32, fd)

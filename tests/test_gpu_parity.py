@@ -600,14 +600,10 @@ def test_degenerate_grids(built, port, case):
     # FP32: all tunings that apply give the scalar sweeps' bits
     fp32_planes = (iBTIin[0], iBTIin[1], 0, 1)
     ref = _run_fp32(s, pr, fp32_planes, (0, 4, 0, 0, 4), 20, batch=1)
-    tunings = [(0, 1, 0, 0, 4), (0, 2, 1, 0, 4), (1, 2, 1, 0, 4), (1, 8, 3, 0, 5)]
+    tunings = [(0, 1, 0, 0, 4), (0, 2, 1, 0, 4), (0, 8, 3, 0, 4)]
     if L[0] % 4 == 0:
-        tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (3, 2, 2, 0, 4), (4, 1, 0, 0, 0)]
-        if tuple(iBc) == (0, 0, 0):
-            tunings += [(5, 4, 2, 1, 4)]
-
-    if L[0] % 4 == 0:
-        tunings += [(6, 1, 1, 1, 0), (6, 2, 2, 2, 0), (6, 1, L[2], 3, 0)]
+        tunings += [(2, 1, 0, 0, 4), (2, 2, 1, 0, 4), (2, 1, 0, -3, 4), (6, 1, 1, 1, 0), (6, 2, 2, 2, 0),
+                    (6, 1, L[2], 3, 0)]
     for tuning in tunings:
         got = _run_fp32(s, pr, fp32_planes, tuning, 20, batch=1)
         for rb, gb in zip(ref, got):
@@ -661,3 +657,73 @@ def test_checkpoint_and_resume(built, tmp_path, precision):
     with plan(batch=1) as p:
         with pytest.raises(f.FdtdError):
             p.load_state(path)
+
+
+def test_fp32_dft_flush_is_compensated(built):
+    """The FP32 running DFT (ring of field samples folded into FP64
+    accumulators, the reference's DFT of :318-328 on FP32 samples) is summed
+    in compensated FP32: against the exact FP64 sum of the same samples with
+    the same FP64 phases, its error is a few units of 2^-24 of the summed
+    magnitudes and far below that of a plain FP32 sum of the window (FP32
+    phases, one fused multiply-add per sample, as an uncompensated flush would
+    do).  The samples come from a twin plan stepped one step per run (the
+    field updates do not depend on how steps are grouped); its monitor planes
+    hold no split cell, so a sample is the cell's field itself."""
+    from smatranem_gb300 import workloads as W
+    f = _fdtd()
+    L = (16, 12, 24, 2)
+    s = W.random_structure(L, seed=5, pml=(0, 0, 3), pml_z_only=True, iBc=(1, 1, 0))
+    pr = W.prepare(s)
+    planes = (7, 15)
+    iBTIin = (7, 15, 10, 1)
+    nsteps = 70  # flush windows of 32, 32 and 6 steps
+    src, ph = W.pulse_schedule(nsteps, pr.dt, lams_um=[1.3, 1.55, 1.9])
+    H0, E0 = W.random_fields(s.n3, pr.lnotn, seed=3, scale=1e-2)
+    Hinc, Einc = W.random_incident(L[0] * L[1], seed=4)
+
+    def plan():
+        p = f.Plan.create(L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=f.FP32)
+        p.set_tuning(2, 1, 0, 0, 4)
+        p.set_fields(0, H0, E0)
+        p.set_incident(0, Hinc, Einc)
+        p.set_schedule(src, planes=planes, phase=ph)
+        return p
+
+    pl = L[0] * L[1]
+    with plan() as a, plan() as b:
+        a.run(0, nsteps)
+        got = np.array([[a.get_dft(0, fi, q) for q in range(2)] for fi in range(3)])  # [f][q][Hx,Hy,Ex,Ey][px]
+        samples = np.zeros((nsteps, 2, 4, pl))
+        for k in range(nsteps):
+            b.run(k, k + 1)
+            H, E = b.get_fields(0)
+            for qi, z in enumerate(planes):
+                cells = np.arange(pl) + pl * z
+                for c in range(2):
+                    samples[k, qi, c] = H[c + 3 * cells]
+                    samples[k, qi, 2 + c] = E[c + 3 * cells]
+    # phases: H samples at [0] + i[1], E samples at [2] + i[3]
+    phz = np.stack([ph[:, :, 0] + 1j * ph[:, :, 1], ph[:, :, 2] + 1j * ph[:, :, 3]], axis=-1)  # [k][f][half]
+    exact = np.zeros((3, 2, 4, pl), np.complex128)
+    plain = np.zeros_like(exact)
+    scale = np.zeros((3, 2, 4, pl))
+    for w0, w1 in ((0, 32), (32, 64), (64, 70)):
+        for fi in range(3):
+            for v in range(4):
+                z = phz[w0:w1, fi, v // 2]
+                x = samples[w0:w1, :, v, :]                                   # [k][q][px]
+                exact[fi, :, v] += np.einsum("k,kqp->qp", z, x)
+                scale[fi, :, v] += np.abs(x).sum(axis=0)
+                zr = z.real.astype(np.float32).astype(np.float64)
+                zi = z.imag.astype(np.float32).astype(np.float64)
+                sr = np.zeros((2, pl), np.float32)
+                si = np.zeros((2, pl), np.float32)
+                for k in range(w1 - w0):  # fl(ph*x + s): one rounding per fused multiply-add
+                    sr = (zr[k] * x[k] + sr.astype(np.float64)).astype(np.float32)
+                    si = (zi[k] * x[k] + si.astype(np.float64)).astype(np.float32)
+                plain[fi, :, v] += sr.astype(np.float64) + 1j * si.astype(np.float64)
+    err = np.abs(got - exact)
+    err_plain = np.abs(plain - exact)
+    u = 2.0 ** -24
+    assert np.max(err / scale) < 4 * u
+    assert np.sqrt(np.mean(err ** 2)) < 0.25 * np.sqrt(np.mean(err_plain ** 2))
