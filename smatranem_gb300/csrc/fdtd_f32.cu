@@ -823,76 +823,109 @@ void launch_group32v(const Group32 &gr, int rel, cudaStream_t st)
 /* Fold `count` ring slots ending at step *base + rel_end into the FP64 DFT
  * accumulators (the reference's running DFT, FDTDsplitfieldMetal.c:318-328,
  * here on FP32 field samples): for each pixel, monitor plane, component and
- * frequency, acc += sum over the window of x_k * e^{i phi_k}, in compensated
- * FP32.
+ * frequency, acc += sum over the window of x_k * e^{i phi_k}, by compensated
+ * (Kahan) summation in FP32.
  *   - each phase (FP64 in the schedule) is carried as a float pair hi + lo,
  *     hi = fl(phi), lo = fl(phi - hi): together exact to about 2^-48;
- *   - each product x*hi is split exactly into p = fl(x*hi) and its rounding
- *     error e = fma(x, hi, -p); x*lo joins e (its own rounding is ~2^-48 of
- *     the term);
- *   - the window's p are summed by Kahan summation whose compensation also
- *     carries the low parts e + x*lo, so the window sum s - c is good to a
- *     few units of 2^-24 of sum |x| whatever the window length, and is added
- *     to the FP64 accumulator as (double)s - (double)c.
- * A thread takes one pixel and the two components of one half (H: Hx, Hy, or
- * E: Ex, Ey) of one plane and excitation, so each phase pair, read from
- * shared memory as one 16-byte broadcast, serves four products. */
+ *   - a term enters as y = fl(x*hi + (x*lo - c)), one rounding of the term
+ *     less the running compensation c; then t = s + y, c = (t - s) - y, s = t.
+ *     The window's error is then within about 3 units of 2^-24 of the sum of
+ *     |terms| whatever the window length (a plain FP32 sum's bound grows with
+ *     the number of terms);
+ *   - the window's fl(s - c) is added to the FP64 accumulator.
+ * A thread takes one pixel and one component of one plane and excitation,
+ * its window's samples in registers, two frequencies at a time (independent
+ * chains); the phases sit in shared memory frequency-major, so that a
+ * frequency's samples are at fixed offsets.  Float to double goes by the IEEE
+ * bit layout on the integer pipes (the FP64 pipe of this GPU is narrow; one
+ * add per value is its only work here). */
 constexpr int RING_MAX = 32;
 
-/* one term of the compensated sum; the _rn intrinsics keep every operation a
- * separately rounded one (no multiply-add contraction may merge them) */
-__device__ __forceinline__ void kahan_term(float x, float hi, float lo, float &s, float &c)
+/* one Kahan step: s the sum, n the negated compensation, term x * (hi + lo);
+ * the _rn intrinsics keep every operation separately rounded (no contraction
+ * may merge or reorder them) */
+__device__ __forceinline__ void kahan_term(float x, float hi, float lo, float &s, float &n)
 {
-    const float p = __fmul_rn(x, hi);
-    float e = fmaf(x, hi, -p);
-    e = fmaf(x, lo, e);
-    const float y = __fsub_rn(p, c);
+    const float y = __fmaf_rn(x, hi, __fmaf_rn(x, lo, n));
     const float t = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(__fsub_rn(t, s), y), e);
+    n = __fsub_rn(y, __fsub_rn(t, s));
     s = t;
 }
 
-__global__ void __launch_bounds__(128) k_flush32(const P32 p, const int rel_end, const int count)
+/* float -> double by the bit layout: sign, exponent rebiased (127 -> 1023),
+ * mantissa shifted into place; zero and subnormal floats (below 2^-126) give
+ * zero, infinities and NaNs keep their class */
+__device__ __forceinline__ double widen(float f)
 {
-    extern __shared__ float4 sph4[]; /* [count][nfreq] {hi re, hi im, lo re, lo im} of this half */
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned ed = e == 0xffu ? 0x7ffu : e + 896u;
+    const unsigned hi = (u & 0x80000000u) | (ed << 20) | ((u & 0x7fffffu) >> 3);
+    const unsigned lo = u << 29;
+    return e == 0u ? 0.0 : __hiloint2double((int)hi, (int)lo);
+}
+
+/* COUNT: the window length when it is the full ring (the common case, no
+ * per-sample predicate), 0 for a shorter window at the end of a run */
+template <int COUNT>
+__global__ void __launch_bounds__(128, 6) k_flush32(const P32 p, const int rel_end, const int count_rt)
+{
+    /* [nfreq][count] {hi re, hi im, lo re, lo im} of this block's half (H or E
+     * phases) */
+    extern __shared__ float4 sph[];
+    const int count = COUNT > 0 ? COUNT : count_rt;
     const Dft &d = p.d;
     const int k0 = *p.s.base + rel_end - count;
-    const int qh = blockIdx.y, b = blockIdx.z;
-    const int q = qh >> 1, half = qh & 1, po = 2 * half;
+    const int qv = blockIdx.y, b = blockIdx.z;
+    const int q = qv >> 2, v = qv & 3, half = v >> 1;
     const int nph = count * d.nfreq;
+    const float4 *ph4 = reinterpret_cast<const float4 *>(d.xphase32 ? d.xphase32 : d.phase32);
     for (int i = threadIdx.x; i < nph; i += blockDim.x) {
-        const int s = i / d.nfreq, f = i % d.nfreq;
-        const double *ph = d.xphase ? d.xphase + po : d.phase + 4 * ((long long)(k0 + s) * d.nfreq + f) + po;
-        const float hr = (float)ph[0], hi = (float)ph[1];
-        sph4[i] = make_float4(hr, hi, (float)(ph[0] - (double)hr), (float)(ph[1] - (double)hi));
+        const int f = i / count, s = i % count;
+        sph[i] = d.xphase32 ? ph4[half] : ph4[((long long)(k0 + s) * d.nfreq + f) * 2 + half];
     }
     __syncthreads();
     const int px = blockIdx.x * blockDim.x + threadIdx.x;
     if (px >= p.g.pl) return;
-    float x0[RING_MAX], x1[RING_MAX];
+    float x[RING_MAX];
 #pragma unroll
-    for (int s = 0; s < RING_MAX; s++) {
-        x0[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, po)[px] : 0.0f;
-        x1[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, po + 1)[px] : 0.0f;
-    }
-    for (int f = 0; f < d.nfreq; f++) {
-        float s0r = 0.f, c0r = 0.f, s0i = 0.f, c0i = 0.f, s1r = 0.f, c1r = 0.f, s1i = 0.f, c1i = 0.f;
+    for (int s = 0; s < RING_MAX; s++) x[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, v)[px] : 0.0f;
+    double *acc = d.acc + 2 * (((((long long)b * d.nfreq) * d.nq + q) * 4 + v) * p.g.pl + px);
+    const long long fstride = 2 * (long long)d.nq * 4 * p.g.pl; /* doubles from one frequency to the next */
+    int f = 0;
+    for (; f + 1 < d.nfreq; f += 2) {
+        const float4 *pa = sph + f * count, *pb = pa + count;
+        float sa = 0.f, na = 0.f, sai = 0.f, nai = 0.f, sb = 0.f, nb = 0.f, sbi = 0.f, nbi = 0.f;
 #pragma unroll
         for (int s = 0; s < RING_MAX; s++) {
-            if (s < count) {
-                const float4 ph = sph4[s * d.nfreq + f];
-                kahan_term(x0[s], ph.x, ph.z, s0r, c0r);
-                kahan_term(x0[s], ph.y, ph.w, s0i, c0i);
-                kahan_term(x1[s], ph.x, ph.z, s1r, c1r);
-                kahan_term(x1[s], ph.y, ph.w, s1i, c1i);
+            if (COUNT > 0 || s < count) {
+                const float4 ha = pa[s], hb = pb[s];
+                kahan_term(x[s], ha.x, ha.z, sa, na);
+                kahan_term(x[s], ha.y, ha.w, sai, nai);
+                kahan_term(x[s], hb.x, hb.z, sb, nb);
+                kahan_term(x[s], hb.y, hb.w, sbi, nbi);
             }
         }
-        double *a0 = d.acc + 2 * (((((long long)b * d.nfreq + f) * d.nq + q) * 4 + po) * p.g.pl + px);
-        double *a1 = a0 + 2 * (long long)p.g.pl;
-        a0[0] += (double)s0r - (double)c0r;
-        a0[1] += (double)s0i - (double)c0i;
-        a1[0] += (double)s1r - (double)c1r;
-        a1[1] += (double)s1i - (double)c1i;
+        double *a = acc + f * fstride;
+        a[0] += widen(__fadd_rn(sa, na));
+        a[1] += widen(__fadd_rn(sai, nai));
+        a[fstride] += widen(__fadd_rn(sb, nb));
+        a[fstride + 1] += widen(__fadd_rn(sbi, nbi));
+    }
+    if (f < d.nfreq) {
+        const float4 *pa = sph + f * count;
+        float sa = 0.f, na = 0.f, sai = 0.f, nai = 0.f;
+#pragma unroll
+        for (int s = 0; s < RING_MAX; s++) {
+            if (COUNT > 0 || s < count) {
+                const float4 ha = pa[s];
+                kahan_term(x[s], ha.x, ha.z, sa, na);
+                kahan_term(x[s], ha.y, ha.w, sai, nai);
+            }
+        }
+        double *a = acc + f * fstride;
+        a[0] += widen(__fadd_rn(sa, na));
+        a[1] += widen(__fadd_rn(sai, nai));
     }
 }
 
@@ -961,10 +994,12 @@ void launch_e32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const in
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st)
 {
     if (p.d.nfreq <= 0 || p.d.nq <= 0 || count <= 0) return;
-    dim3 blk(128), grd((p.g.pl + 127) / 128, p.d.nq * 2, p.batch);
+    dim3 blk(128), grd((p.g.pl + 127) / 128, p.d.nq * 4, p.batch);
     const size_t sm = sizeof(float4) * (size_t)count * p.d.nfreq;
-    if (sm > 48 * 1024) cudaFuncSetAttribute(k_flush32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_flush32<<<grd, blk, sm, st>>>(p, rel_end, count);
+    const void *fn = count == RING_MAX ? (const void *)k_flush32<RING_MAX> : (const void *)k_flush32<0>;
+    if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (count == RING_MAX) k_flush32<RING_MAX><<<grd, blk, sm, st>>>(p, rel_end, count);
+    else k_flush32<0><<<grd, blk, sm, st>>>(p, rel_end, count);
 }
 
 } // namespace smat

@@ -59,9 +59,10 @@ struct Dft {
     int nfreq, nq;
     int planes[MAX_PLANES];
     const double *phase;  /* [nsched][nfreq][4] {pH re, im, pE re, im} */
-    const float *phase32; /* same in FP32 (for the deferred FP32 flush) */
+    const float *phase32; /* FP32 flush: [nsched][nfreq][H, E]{hi re, hi im, lo re, lo im},
+                           * hi = fl(phase), lo = fl(phase - hi) */
     const double *xphase; /* explicit {pH, pE} for smat_fdtd_step, or null */
-    const float *xphase32; /* the same in FP32 */
+    const float *xphase32; /* the same pairs of the explicit phases, [H, E][4] */
     double *acc;          /* [batch][nfreq][nq][4][pl] complex */
     int ringK;            /* FP32: samples kept per flush */
     float *ring;          /* FP32: [batch][ringK][nq][4][pl] */

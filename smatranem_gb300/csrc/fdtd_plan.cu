@@ -334,7 +334,7 @@ int common_alloc(smat_fdtd_plan *p)
     if ((rc = p->alloc(&p->d_inc, (size_t)p->batch * 8 * p->pl))) return rc;
     if ((rc = p->alloc(&p->d_xsrc, (size_t)4 * p->pl))) return rc;
     if ((rc = p->alloc(&p->d_xphase, 4))) return rc;
-    if ((rc = p->alloc(&p->d_xphase32, 4))) return rc;
+    if ((rc = p->alloc(&p->d_xphase32, 8))) return rc;
     if ((rc = p->alloc(&p->d_scratch, 4))) return rc;
     if ((rc = p->alloc(&p->d_iI, p->batch)) || (rc = p->alloc(&p->d_isgn, p->batch))) return rc;
     if ((rc = p->alloc(&p->d_err, 1))) return rc;
@@ -849,10 +849,20 @@ extern "C" int smat_fdtd_set_schedule(smat_fdtd_plan *p, int nsteps, const doubl
         if ((rc = dalloc(&p->d_phase, np, p->stream))) return rc;
         CK(p->cpy(p->d_phase, phase, np * 8, cudaMemcpyHostToDevice));
         if (p->precision == SMAT_FP32) {
-            std::vector<float> ph32(np);
-            for (size_t i = 0; i < np; i++) ph32[i] = (float)phase[i];
-            if ((rc = dalloc(&p->d_phase32, np, p->stream))) return rc;
-            CK(p->cpy(p->d_phase32, ph32.data(), np * 4, cudaMemcpyHostToDevice));
+            /* the FP32 flush's phase pairs: per step and frequency, for H then
+             * E, {hi re, hi im, lo re, lo im} with hi = fl(phase), lo =
+             * fl(phase - hi) */
+            std::vector<float> ph32(2 * np);
+            for (size_t i = 0; i < np / 4; i++)
+                for (int h = 0; h < 2; h++)
+                    for (int c = 0; c < 2; c++) {
+                        const double v = phase[4 * i + 2 * h + c];
+                        const float hi = (float)v;
+                        ph32[8 * i + 4 * h + c] = hi;
+                        ph32[8 * i + 4 * h + 2 + c] = (float)(v - (double)hi);
+                    }
+            if ((rc = dalloc(&p->d_phase32, 2 * np, p->stream))) return rc;
+            CK(p->cpy(p->d_phase32, ph32.data(), 2 * np * 4, cudaMemcpyHostToDevice));
         }
     }
     p->nsched = nsteps;
@@ -900,11 +910,17 @@ extern "C" int smat_fdtd_step(smat_fdtd_plan *p, const double *Hi, const double 
     const int nf = p->nfreq;
     p->nfreq = 1; /* explicit phases drive frequency slot 0 only */
     const size_t n = 2 * (size_t)p->pl;
-    float x32[4] = {(float)ExpN2[0], (float)ExpN2[1], (float)ExpN2[2], (float)ExpN2[3]};
+    float x32[8]; /* the phase pairs of the FP32 flush: H then E, {hi re, hi im, lo re, lo im} */
+    for (int h = 0; h < 2; h++)
+        for (int c = 0; c < 2; c++) {
+            const float hi = (float)ExpN2[2 * h + c];
+            x32[4 * h + c] = hi;
+            x32[4 * h + 2 + c] = (float)(ExpN2[2 * h + c] - (double)hi);
+        }
     cudaError_t e = p->cpy(p->d_xsrc, Hi, n * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = p->cpy(p->d_xsrc + n, Ei, n * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = p->cpy(p->d_xphase, ExpN2, 4 * 8, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = p->cpy(p->d_xphase32, x32, 4 * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = p->cpy(p->d_xphase32, x32, 8 * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         launch_set(p->d_base, 0, p->stream);
         enqueue_steps(p, 0, 1, true);

@@ -663,10 +663,10 @@ def test_fp32_dft_flush_is_compensated(built):
     """The FP32 running DFT (ring of field samples folded into FP64
     accumulators, the reference's DFT of :318-328 on FP32 samples) is summed
     in compensated FP32: against the exact FP64 sum of the same samples with
-    the same FP64 phases, its error is a few units of 2^-24 of the summed
-    magnitudes and far below that of a plain FP32 sum of the window (FP32
-    phases, one fused multiply-add per sample, as an uncompensated flush would
-    do).  The samples come from a twin plan stepped one step per run (the
+    the same FP64 phases, its error stays under 2 units of 2^-24 of the
+    summed magnitudes and its RMS under half that of a plain FP32 sum of the
+    window (FP32 phases, one fused multiply-add per sample, as an
+    uncompensated flush would do).  The samples come from a twin plan stepped one step per run (the
     field updates do not depend on how steps are grouped); its monitor planes
     hold no split cell, so a sample is the cell's field itself."""
     from smatranem_gb300 import workloads as W
@@ -725,5 +725,5 @@ def test_fp32_dft_flush_is_compensated(built):
     err = np.abs(got - exact)
     err_plain = np.abs(plain - exact)
     u = 2.0 ** -24
-    assert np.max(err / scale) < 4 * u
-    assert np.sqrt(np.mean(err ** 2)) < 0.25 * np.sqrt(np.mean(err_plain ** 2))
+    assert np.max(err / scale) < 2 * u
+    assert np.sqrt(np.mean(err ** 2)) < 0.5 * np.sqrt(np.mean(err_plain ** 2))
