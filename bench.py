@@ -1038,15 +1038,29 @@ def run_scalc(args):
     meds = W.grating_layers(L0, L1, nl, seed=7)
     t_setup = time.perf_counter() - t0
     NA = 2 * L0 * L1
-    SC.smatrix(meds[:2], om, L0, L1, (1, 1), Xi, nr, Xi, nr)  # warm-up (allocations, module load)
-    torch.cuda.synchronize()
-    times = []
-    for _ in range(max(1, args.steps)):
-        t0 = time.perf_counter()
-        S, info = SC.smatrix(meds, om, L0, L1, (1, 1), Xi, nr, Xi, nr)
-        times.append(time.perf_counter() - t0)
+    res = {}
+    modes = [(1, "tensor_cores"), (0, "fp64_kernel")]
+    if args.dense != "both":
+        modes = [m for m in modes if m[1].startswith(args.dense[:2])]
+    for mode, name in modes:
+        SC.dense_mode(mode)
+        SC.smatrix(meds[:2], om, L0, L1, (1, 1), Xi, nr, Xi, nr)  # warm-up (allocations, module load)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            S, info = SC.smatrix(meds, om, L0, L1, (1, 1), Xi, nr, Xi, nr)
+            times.append(time.perf_counter() - t0)
+        res[name] = (float(min(times)), S, info, len(times))
+    SC.dense_mode(1)
+    best, S, info, nruns = res["tensor_cores"] if "tensor_cores" in res else res["fp64_kernel"]
+    best64, S64, info64, _ = res["fp64_kernel"] if "fp64_kernel" in res else (None, None, None, None)
     solves = info["solves"]
-    flops = solves * (8.0 / 3.0 * 4 * NA ** 3 + 8.0 * NA ** 2 * (NA + nr)) + 2 * 8.0 * (2 * NA) ** 2 * (NA + nr)
+    # complex LU of order NA (8/3 NA^3 real flops), the solve with NA + N_real
+    # right-hand sides (8 NA^2 per column), the elimination's zgemm, and the
+    # two projections on the dual modes ((2NA)^2 x (NA + N_real))
+    flops = solves * (8.0 / 3.0 * NA ** 3 + 8.0 * NA ** 2 * (NA + nr) + 8.0 * (NA + nr) * nr * NA) \
+        + 2 * 8.0 * (2 * NA) ** 2 * (NA + nr)
     cpu = None
     if not args.no_cpu:
         import scipy.linalg as sl
@@ -1066,13 +1080,18 @@ def run_scalc(args):
                "cores": os.cpu_count(), "kind": "port",
                "sample": f"one zgesv of order {NA} with {NA + nr} right-hand sides: {t_solve:.2f} s (x {solves}); "
                          f"one {2 * NA}^2 x {NA + nr} zgemm: {t_mm:.2f} s (x 2); threads of the host BLAS"}
-    best = float(min(times))
     print(json.dumps({
         "mode": "scalc", "config": f"periodic grating {L0}x{L1}, {nl} layers, uniform ports eps 2.085, "
                                    f"NA = {NA}, N_real = {nr} per port, both directions",
-        "s_per_smatrix": best, "runs": len(times), "solves": solves,
-        "fp64_tflops": flops / best / 1e12, "unitarity": info["unitarity"], "transpose": info["transpose"],
-        "setup_s": t_setup, "cpu_baseline": cpu}))
+        "s_per_smatrix": best, "runs": nruns, "solves": solves,
+        "fp64_tflops": flops / best / 1e12,
+        "products": "FP64-accurate complex products on the tensor cores (7 bf16 slices per operand, Ozaki scheme, "
+                    "tcgen05.mma); LU panels and triangle blocks in FP64",
+        "fp64_kernel": None if best64 is None else {"s_per_smatrix": best64, "fp64_tflops": flops / best64 / 1e12,
+                                                    "speedup_tensor_cores": best64 / best},
+        "s_max_abs_diff_vs_fp64_kernel": None if S64 is None else float(np.abs(S - S64).max()),
+        "unitarity": info["unitarity"], "unitarity_fp64_kernel": None if info64 is None else info64["unitarity"],
+        "transpose": info["transpose"], "setup_s": t_setup, "cpu_baseline": cpu}))
 
 
 def main():
@@ -1097,6 +1116,8 @@ def main():
     ap.add_argument("--full-steps", type=int, default=FULL_STEPS)
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--dense", default="both", choices=["both", "tensor_cores", "fp64_kernel"],
+                    help="--mode scalc: the dense products timed (tensor cores, the FP64 kernel, or both)")
     ap.add_argument("--extras", default="cube,adjoint,group,large",
                     help="main mode: the other workloads summarised in the contract line (comma list of cube, "
                          "adjoint, group, large; empty: none)")

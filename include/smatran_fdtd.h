@@ -493,6 +493,26 @@ int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int nlayers, c
  * complex column-major; *info = first zero pivot (1-based) or 0. */
 int smat_zgesv(int n, int nrhs, const double *A, const double *B, double *X, int *info);
 
+/* Replaces the zgemm_ calls of Scalc's inv_process (Smat/Scalc.c:316-400) as
+ * smat_scalc runs them: C += alpha * A * B on the GPU, on host arrays, for
+ * testing.  A: m x k (lda), B: k x n (ldb), C: m x n (ldc), complex
+ * column-major; alpha: one complex (re, im).  mode 1: FP64-accurate products
+ * on the tensor cores (bf16 slices of the operands, Ozaki scheme, 7 slices);
+ * mode 0: the FP64 multiply-add kernel. */
+int smat_zgemm(int mode, int m, int n, int k, const double *alpha, const double *A, int lda, const double *B, int ldb,
+               double *C, int ldc);
+
+/* No counterpart in the reference: the device time of one smat_zgemm product
+ * of these sizes (operands seeded on the device, CUDA events around reps
+ * calls after a warm-up), in *ms per call. */
+int smat_zgemm_time(int mode, int m, int n, int k, int reps, double *ms);
+
+/* No counterpart in the reference: how smat_scalc and smat_zgesv multiply
+ * (process-wide): 1 (the default) the tensor-core products of smat_zgemm
+ * mode 1, where the device gives them their shared memory; 0 the FP64
+ * multiply-add kernel. */
+int smat_dense_mode(int mode);
+
 /* The drop-in S-matrix program: `Scalc input.txt` reads the keys, Med layers,
  * Mode and Xi files Scalc reads (Smat/Scalc.c main :27-96) and writes
  * <prefix>_Smatrix.dat in Out_Smat's format (:113-140); returns the exit status. */

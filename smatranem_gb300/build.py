@@ -39,7 +39,7 @@ NV_EXTRA = {"fdtd_f64.cu": ["-fmad=false"]}
 
 C_SOURCES = ["host_precompute.c", "errors.c", "deck_io.c"]
 CU_SOURCES = ["fdtd_f64.cu", "fdtd_f32.cu", "fdtd_plan.cu", "fdtd_overlap.cu", "fdtd_adjoint.cu",
-              "fdtd_group.cu", "mode_solver.cu", "dense_z.cu", "scalc.cu", "fdtd_row32.cu"]
+              "fdtd_group.cu", "mode_solver.cu", "dense_z.cu", "zgemm_tc.cu", "scalc.cu", "fdtd_row32.cu"]
 
 
 def _nvcc() -> str:

@@ -169,10 +169,12 @@ struct Transfer {
     double2 *Xi = nullptr, *P = nullptr, *PH = nullptr, *FB = nullptr, *Cm = nullptr, *V = nullptr;
     int *ipiv = nullptr, *dinfo = nullptr;
     int solves = 0;
+    smat::dense::GemmCtx gm{0, nullptr, 0, nullptr}; /* how the multiply-adds run */
 
     ~Transfer()
     {
         if (st) cudaStreamSynchronize(st);
+        smat::dense::gemm_ctx_release(gm);
         for (double2 *b : {F01, B01, F2, B2, W1, W2, Xi, P, PH, FB, Cm, V}) cudaFree(b);
         cudaFree(ipiv);
         cudaFree(dinfo);
@@ -196,10 +198,10 @@ struct Transfer {
     {
         RC(transpose(NA, NA, B2, NA, W1, NA, false, st));
         RC(transpose(No + NA, NA, B01, ldF, W2, NA, false, st));
-        RC(getrf(NA, W1, NA, ipiv, dinfo, st));
-        RC(getrs(NA, No + NA, W1, NA, ipiv, W2, NA, st));
+        RC(getrf(NA, W1, NA, ipiv, dinfo, &gm, st));
+        RC(getrs(NA, No + NA, W1, NA, ipiv, W2, NA, &gm, st));
         RC(transpose(NA, No + NA, W2, NA, B01, ldF, false, st));
-        RC(zgemm_acc(No + NA, No, NA, make_double2(-1.0, 0.0), B01, ldF, F2, NA, F01, ldF, st));
+        RC(zgemm_acc(No + NA, No, NA, make_double2(-1.0, 0.0), B01, ldF, F2, NA, F01, ldF, &gm, st));
         RC(set2d(NA, No, F2, NA, 0.0));
         RC(set2d(NA, NA, B2, NA, 1.0));
         solves++;
@@ -296,7 +298,7 @@ int one_way(Transfer &T, int iway, int nlayers, const double *const *meds, doubl
     RC(T.copy2d(NA, NA, T.B01 + No, T.ldF, T.FB + (long long)N2 * No, N2));
     RC(T.copy2d(NA, NA, T.B2, NA, T.FB + NA + (long long)N2 * No, N2));
     RC(T.set2d(N2, nc, T.Cm, N2, 0.0));
-    RC(zgemm_acc(N2, nc, N2, make_double2(1.0, 0.0), T.PH, N2, T.FB, N2, T.Cm, N2, T.st));
+    RC(zgemm_acc(N2, nc, N2, make_double2(1.0, 0.0), T.PH, N2, T.FB, N2, T.Cm, N2, &T.gm, T.st));
     RC(T.copy2d(NA, No, T.Cm, N2, T.F01 + No, T.ldF));
     RC(T.copy2d(NA, No, T.Cm + NA, N2, T.F2, NA));
     RC(T.copy2d(NA, NA, T.Cm + (long long)N2 * No, N2, T.B01 + No, T.ldF));
@@ -366,6 +368,8 @@ extern "C" int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int
     SCK(cudaMalloc(&T.ipiv, sizeof(int) * NA));
     SCK(cudaMalloc(&T.dinfo, sizeof(int)));
     SCK(cudaMemsetAsync(T.dinfo, 0, sizeof(int), T.st));
+    /* products up to 2NA x (Nmax + NA) (the projection on the dual modes) */
+    RC(smat::dense::gemm_ctx_alloc(T.gm, N2, (int)ldF, T.st));
     const size_t lstride = (size_t)2 * 6 * NA1;
     std::vector<const double *> up(nlayers), down(nlayers);
     for (int l = 0; l < nlayers; l++) {
@@ -389,6 +393,7 @@ extern "C" int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int
     int hinfo = 0;
     SCK(cudaMemcpyAsync(&hinfo, T.dinfo, sizeof(int), cudaMemcpyDeviceToHost, T.st));
     SCK(cudaStreamSynchronize(T.st));
+    RC(smat::dense::gemm_ctx_check(T.gm));
     if (hinfo != 0) return smat_fail(SMAT_ENUMERIC, "smat_scalc: singular matrix in the layer transfer (zgesv info)");
     std::memcpy(S, Sm.data(), sizeof(double2) * Sm.size());
     if (info) {

@@ -27,6 +27,8 @@ def _lib():
         L.smat_scalc.argtypes = [C.c_int, C.c_int, _P, C.c_double, C.c_int, _P, _P, C.c_int, _P, C.c_int, C.c_int,
                                  _P, _P]
         L.smat_zgesv.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P]
+        L.smat_zgemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, C.c_int, _P, C.c_int, _P, C.c_int]
+        L.smat_dense_mode.argtypes = [C.c_int]
         L._scalc_bound = True
     return L
 
@@ -58,6 +60,28 @@ def zgesv(A, B):
     fdtd._check(_lib().smat_zgesv(A.shape[0], B.shape[1], A.ctypes.data_as(_P), B.ctypes.data_as(_P),
                                   X.ctypes.data_as(_P), C.byref(info)))
     return (X[:, 0] if one else np.array(X)), info.value
+
+
+def dense_mode(mode):
+    """How smatrix and zgesv multiply: 1 (the default) FP64-accurate products
+    on the tensor cores, 0 the FP64 multiply-add kernel."""
+    fdtd._check(_lib().smat_dense_mode(int(mode)))
+
+
+def zgemm(A, B, C=None, alpha=1.0, mode=1):
+    """C + alpha * A @ B on the GPU (the products of smatrix): mode 1 on the
+    tensor cores, 0 with the FP64 kernel."""
+    A = np.asfortranarray(np.asarray(A, np.complex128))
+    B = np.asfortranarray(np.asarray(B, np.complex128))
+    m, k = A.shape
+    n = B.shape[1]
+    if B.shape[0] != k:
+        raise ValueError(f"zgemm: A is {m} x {k}, B has {B.shape[0]} rows")
+    out = np.zeros((m, n), np.complex128, order="F") if C is None else np.array(C, np.complex128, order="F")
+    al = np.array([complex(alpha).real, complex(alpha).imag])
+    fdtd._check(_lib().smat_zgemm(int(mode), m, n, k, al.ctypes.data_as(_P), A.ctypes.data_as(_P), m,
+                                  B.ctypes.data_as(_P), k, out.ctypes.data_as(_P), m))
+    return out
 
 
 def read_xi(path, NA=None):

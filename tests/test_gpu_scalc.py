@@ -6,6 +6,10 @@ program (Smat/Scalc.c).
 * the S matrix against the stock Scalc's own output on its fixtures
   (tests/golden/scalc_*.npz) and against the oracle restatement on larger
   seeded structures (lossy inner layers, every BoundC);
+* the tensor-core product (smat_zgemm mode 1: FP64-accurate complex products
+  from bf16 slices, Ozaki scheme) against an extended-precision product, per
+  entry within its error bound, on ragged sizes, wide dynamic ranges, zero
+  rows and columns; the stock-Scalc comparisons in both dense modes;
 * the argument checks.
 Tolerance: 1e-10 absolute on S entries (|S| <= 1); the reference's own
 unitarity residual is 2e-14 on these cases.
@@ -25,7 +29,7 @@ FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "scalc_*.npz")))
 
 
 @pytest.mark.parametrize("n,nrhs", [(1, 1), (5, 3), (31, 7), (32, 32), (33, 40), (100, 64), (257, 300)])
-def test_zgesv_matches_numpy(built, n, nrhs):
+def test_zgesv_matches_numpy(dense, n, nrhs):
     rng = np.random.default_rng(n)
     A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
     A[np.arange(n), np.arange(n)] *= 1e-3  # small diagonal: every column pivots
@@ -44,8 +48,54 @@ def test_zgesv_reports_a_zero_pivot(built):
     assert info == 4  # 1-based, as LAPACK's INFO
 
 
+def _zgemm_case(rng, m, n, k, spread):
+    A = (rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))) * 10.0 ** rng.uniform(-spread, spread, (m, 1))
+    B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))) * 10.0 ** rng.uniform(-spread, spread, (1, n))
+    if spread:  # entries far below their row's / column's largest, zero rows and columns
+        A *= 10.0 ** rng.uniform(-6, 0, (m, k))
+        A[m // 3, :] = 0
+        B[:, n // 2] = 0
+    return A, B
+
+
+@pytest.mark.parametrize("m,n,k,spread", [(1, 1, 1, 0), (128, 32, 32, 0), (129, 33, 31, 0), (300, 70, 17, 3),
+                                          (500, 260, 100, 0), (77, 500, 64, 8), (300, 40, 2048, 0)])
+def test_zgemm_tensor_cores_within_bound(built, m, n, k, spread):
+    """Per entry: |C - exact| <= 2e-15 k max|A row| max|B col| + 4 ulp of |C0| + |C|
+    (the slices keep 55 bits of each scaled entry; the dropped slice pairs and
+    the FP64 sums stay below that), the FP64 kernel on the same inputs."""
+    rng = np.random.default_rng(m + 7 * n + 13 * k)
+    A, B = _zgemm_case(rng, m, n, k, spread)
+    C0 = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+    alpha = 0.3 - 0.7j
+    exact = C0.astype(np.clongdouble) + alpha * (A.astype(np.clongdouble) @ B.astype(np.clongdouble))
+    rm = np.abs(np.concatenate([A.real, A.imag], axis=1)).max(axis=1, keepdims=True)
+    cm = np.abs(np.concatenate([B.real, B.imag], axis=0)).max(axis=0, keepdims=True)
+    for mode in (1, 0):
+        got = scalc.zgemm(A, B, C0, alpha, mode=mode)
+        err = np.abs(got - exact).astype(np.float64)
+        bound = 2e-15 * k * abs(alpha) * rm * cm + 9e-16 * (np.abs(C0) + np.abs(got))
+        assert np.all(err <= bound), (mode, float((err / bound).max()))
+
+
+def test_zgemm_argument_checks(built):
+    with pytest.raises(ValueError):
+        scalc.zgemm(np.ones((3, 2)), np.ones((3, 2)))  # inner sizes differ
+    with pytest.raises(fdtd.FdtdError):
+        scalc.zgemm(np.ones((3, 2)), np.ones((2, 2)), mode=2)
+    with pytest.raises(fdtd.FdtdError):
+        scalc.dense_mode(5)
+
+
+@pytest.fixture(params=[1, 0], ids=["tensor_cores", "fp64_kernel"])
+def dense(request, built):
+    scalc.dense_mode(request.param)
+    yield request.param
+    scalc.dense_mode(1)
+
+
 @pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[:-4] for p in FIXTURES])
-def test_smatrix_matches_stock_scalc(built, path):
+def test_smatrix_matches_stock_scalc(dense, path):
     g = np.load(path)
     L = g["L"]
     nB, nT = (int(x) for x in g["nreal"])
@@ -76,7 +126,7 @@ def _case(L0, L1, nl, bc, seed, lossy):
 
 @pytest.mark.parametrize("L0,L1,nl,bc,lossy", [(8, 6, 6, (0, 0), False), (7, 7, 5, (1, -1), True),
                                                (9, 5, 4, (-1, 1), False), (6, 6, 2, (1, 1), False)])
-def test_smatrix_matches_oracle(built, L0, L1, nl, bc, lossy):
+def test_smatrix_matches_oracle(dense, L0, L1, nl, bc, lossy):
     om, meds, Xi, nr = _case(L0, L1, nl, bc, L0 + 10 * L1, lossy)
     ref = SO.smatrix(list(meds), om, L0, L1, bc, Xi, nr, Xi, nr)
     S, info = scalc.smatrix(meds, om, L0, L1, bc, Xi, nr, Xi, nr)
