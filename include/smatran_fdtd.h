@@ -507,6 +507,14 @@ int smat_zgemm(int mode, int m, int n, int k, const double *alpha, const double 
  * calls after a warm-up), in *ms per call. */
 int smat_zgemm_time(int mode, int m, int n, int k, int reps, double *ms);
 
+/* No counterpart in the reference: the failure path of the tensor-core
+ * product's bounded waits, for testing.  Runs one small product (128 x 32,
+ * inner 32) in which one slice pair is never loaded and the waits give up
+ * after a few thousand polls; *flag receives the error code the kernel
+ * records (1: gave up waiting for its operands), the device stays usable.
+ * Returns 0 when the call itself completed. */
+int smat_zgemm_wait_test(int *flag);
+
 /* No counterpart in the reference: how smat_scalc and smat_zgesv multiply
  * (process-wide): 1 (the default) the tensor-core products of smat_zgemm
  * mode 1, where the device gives them their shared memory; 0 the FP64

@@ -613,7 +613,7 @@ int dense_mode() { return g_mode; }
  * release) */
 int gemm_ctx_alloc(GemmCtx &g, int m, int n, cudaStream_t st)
 {
-    g = GemmCtx{0, nullptr, 0, nullptr};
+    g = GemmCtx{0, nullptr, 0, nullptr, 0, -1};
     if (dense_mode() != 1 || !tc_available()) return SMAT_OK;
     g.ws_bytes = tc_workspace_bytes(m, n);
     if (cudaMalloc(&g.ws, g.ws_bytes) != cudaSuccess || cudaMalloc(&g.err, sizeof(int)) != cudaSuccess ||
@@ -640,7 +640,7 @@ void gemm_ctx_release(GemmCtx &g)
 {
     cudaFree(g.ws);
     cudaFree(g.err);
-    g = GemmCtx{0, nullptr, 0, nullptr};
+    g = GemmCtx{0, nullptr, 0, nullptr, 0, -1};
 }
 
 } // namespace dense
@@ -661,7 +661,7 @@ extern "C" int smat_zgesv(int n, int nrhs, const double *A, const double *B, dou
     double2 *dA = nullptr, *dB = nullptr;
     int *dp = nullptr, *dinfo = nullptr;
     int rc = SMAT_OK, info = 0;
-    GemmCtx g{0, nullptr, 0, nullptr};
+    GemmCtx g{0, nullptr, 0, nullptr, 0, -1};
     const size_t an = (size_t)n * n, bn = (size_t)n * nrhs;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&dA, an * sizeof(double2)) != cudaSuccess || cudaMalloc(&dB, bn * sizeof(double2)) != cudaSuccess ||
@@ -700,7 +700,7 @@ extern "C" int smat_zgemm(int mode, int m, int n, int k, const double *alpha, co
                                                        "more shared memory than this device gives a block");
     cudaStream_t st = nullptr;
     double2 *dA = nullptr, *dB = nullptr, *dC = nullptr;
-    GemmCtx g{0, nullptr, 0, nullptr};
+    GemmCtx g{0, nullptr, 0, nullptr, 0, -1};
     int rc = SMAT_OK;
     const size_t an = (size_t)lda * k, bn = (size_t)ldb * n, cn = (size_t)ldc * n;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
@@ -755,7 +755,7 @@ extern "C" int smat_zgemm_time(int mode, int m, int n, int k, int reps, double *
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     double2 *dA = nullptr, *dB = nullptr, *dC = nullptr;
-    GemmCtx g{0, nullptr, 0, nullptr};
+    GemmCtx g{0, nullptr, 0, nullptr, 0, -1};
     int rc = SMAT_OK;
     const long long an = (long long)m * k, bn = (long long)k * n, cn = (long long)m * n;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
@@ -791,6 +791,42 @@ extern "C" int smat_zgemm_time(int mode, int m, int n, int k, int reps, double *
     cudaFree(dC);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    return rc;
+}
+
+extern "C" int smat_zgemm_wait_test(int *flag)
+{
+    using namespace smat::dense;
+    if (!flag) return smat_fail(SMAT_EINVAL, "smat_zgemm_wait_test: null flag");
+    if (!tc_available()) return smat_fail(SMAT_ECUDA, "smat_zgemm_wait_test: no tensor-core form here");
+    const int m = 128, n = 32, k = 32;
+    cudaStream_t st = nullptr;
+    double2 *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    GemmCtx g{1, nullptr, 0, nullptr, 4096, 3};
+    int rc = SMAT_OK;
+    *flag = 0;
+    g.ws_bytes = tc_workspace_bytes(m, n);
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&dA, sizeof(double2) * m * k) != cudaSuccess || cudaMalloc(&dB, sizeof(double2) * k * n) != cudaSuccess ||
+        cudaMalloc(&dC, sizeof(double2) * m * n) != cudaSuccess || cudaMalloc(&g.ws, g.ws_bytes) != cudaSuccess ||
+        cudaMalloc(&g.err, sizeof(int)) != cudaSuccess)
+        rc = smat_fail(SMAT_ENOMEM, "smat_zgemm_wait_test: device allocation");
+    if (!rc && (cudaMemsetAsync(dA, 0, sizeof(double2) * m * k, st) != cudaSuccess ||
+                cudaMemsetAsync(dB, 0, sizeof(double2) * k * n, st) != cudaSuccess ||
+                cudaMemsetAsync(dC, 0, sizeof(double2) * m * n, st) != cudaSuccess ||
+                cudaMemsetAsync(g.err, 0, sizeof(int), st) != cudaSuccess))
+        rc = smat_fail(SMAT_ECUDA, "smat_zgemm_wait_test: clear");
+    if (!rc) rc = zgemm_acc_tc(m, n, k, make_double2(1.0, 0.0), dA, m, dB, k, dC, m, g, st);
+    if (!rc && (cudaMemcpyAsync(flag, g.err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess))
+        rc = smat_fail(SMAT_ECUDA, "smat_zgemm_wait_test: %s", cudaGetErrorString(cudaGetLastError()));
+    if (st) cudaStreamSynchronize(st);
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    cudaFree(g.ws);
+    cudaFree(g.err);
     if (st) cudaStreamDestroy(st);
     return rc;
 }

@@ -18,6 +18,8 @@ struct GemmCtx {
     void *ws;
     size_t ws_bytes;
     int *err;
+    unsigned wait_limit = 0; /* polls of a bounded wait (0: the default) */
+    int skip_pair = -1;      /* >= 0: the timeout test leaves that slice pair unloaded */
 };
 
 /* C += alpha * A * B, A m x k, B k x n (g null: the FP64 kernel) */

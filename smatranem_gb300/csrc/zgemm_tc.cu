@@ -234,9 +234,9 @@ __device__ __forceinline__ double fixed_to_double(long long xt, unsigned xb, int
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, unsigned limit)
 {
-    for (unsigned it = 0; it < WAIT_LIMIT; it++) {
+    for (unsigned it = 0; it < limit; it++) {
         unsigned ok;
         asm volatile("{\n\t.reg .pred p;\n\t"
                      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -297,7 +297,8 @@ constexpr int MMA_THREADS = 512; /* 16 warps: four per TMEM lane quarter in the 
  * lanes of quarter w % 4 and the complex columns 8 (w / 4) .. + 7. */
 __global__ void __launch_bounds__(MMA_THREADS, 1)
     k_oz_mma(int m, int n, double2 alpha, const unsigned char *__restrict__ aimg, const unsigned char *__restrict__ bimg,
-             const int *__restrict__ ea, const int *__restrict__ eb, int ntr, int ntc, double2 *C, int ldc, int *err)
+             const int *__restrict__ ea, const int *__restrict__ eb, int ntr, int ntc, double2 *C, int ldc, int *err,
+             unsigned wait_limit, int skip_pair)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     unsigned char *sA = sm, *sB = sm + S * AIMG;
@@ -325,6 +326,7 @@ __global__ void __launch_bounds__(MMA_THREADS, 1)
         for (int i = 0; i < S; i++) {
             const unsigned b = smem_u32(bar + i);
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(AIMG + BIMG) : "memory");
+            if (i == skip_pair) continue; /* the timeout test: a pair that never arrives */
             asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                              smem_u32(sA + i * AIMG)),
                          "l"(aimg + (size_t)(i * ntr + tr) * AIMG), "r"(AIMG), "r"(b)
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(MMA_THREADS, 1)
         }
         bool ok = true;
         for (int d = 0; d < S && ok; d++) {
-            if (!mbar_wait(smem_u32(bar + d), 0)) {
+            if (!mbar_wait(smem_u32(bar + d), 0, wait_limit)) {
                 ok = false;
                 break;
             }
@@ -353,14 +355,14 @@ __global__ void __launch_bounds__(MMA_THREADS, 1)
             /* a slice that never landed: record it, and let the copies still
              * in flight finish (bounded) before the CTA exits */
             atomicExch(err, 1);
-            for (int i = 0; i < S; i++) mbar_wait(smem_u32(bar + i), 0);
+            for (int i = 0; i < S; i++) mbar_wait(smem_u32(bar + i), 0, wait_limit);
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_u32(bar + S))
                      : "memory");
     }
     __syncwarp();
-    const bool done = mbar_wait(smem_u32(bar + S), 0);
+    const bool done = mbar_wait(smem_u32(bar + S), 0, wait_limit);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!done) {
         if (lane == 0) atomicExch(err, 2);
@@ -472,8 +474,9 @@ int zgemm_acc_tc(int m, int n, int k, double2 alpha, const double2 *A, int lda, 
         const int kp = k - k0 < KC ? k - k0 : KC;
         k_cut_rows<<<(ntr * BM + 7) / 8, 256, 0, st>>>(m, kp, A + (long long)lda * k0, lda, aimg, ea, ntr);
         k_cut_cols<<<(ntc * BNC + 7) / 8, 256, 0, st>>>(kp, n, B + k0, ldb, bimg, eb, ntc);
-        k_oz_mma<<<dim3((unsigned)ntr, (unsigned)ntc), MMA_THREADS, SMEM, st>>>(m, n, alpha, aimg, bimg, ea, eb, ntr, ntc, C,
-                                                                        ldc, g.err);
+        k_oz_mma<<<dim3((unsigned)ntr, (unsigned)ntc), MMA_THREADS, SMEM, st>>>(
+            m, n, alpha, aimg, bimg, ea, eb, ntr, ntc, C, ldc, g.err, g.wait_limit ? g.wait_limit : WAIT_LIMIT,
+            g.skip_pair);
         if (cudaPeekAtLastError() != cudaSuccess)
             return smat_fail(SMAT_ECUDA, "zgemm (tensor cores) launch: %s", cudaGetErrorString(cudaGetLastError()));
     }

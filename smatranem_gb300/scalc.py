@@ -29,6 +29,8 @@ def _lib():
         L.smat_zgesv.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P]
         L.smat_zgemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, C.c_int, _P, C.c_int, _P, C.c_int]
         L.smat_dense_mode.argtypes = [C.c_int]
+        L.smat_zgemm_wait_test.argtypes = [_P]
+        L.smat_zgemm_time.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]
         L._scalc_bound = True
     return L
 
@@ -82,6 +84,22 @@ def zgemm(A, B, C=None, alpha=1.0, mode=1):
     fdtd._check(_lib().smat_zgemm(int(mode), m, n, k, al.ctypes.data_as(_P), A.ctypes.data_as(_P), m,
                                   B.ctypes.data_as(_P), k, out.ctypes.data_as(_P), m))
     return out
+
+
+def zgemm_time(mode, m, n, k, reps=10):
+    """Device milliseconds of one C += A B product of these sizes (operands
+    seeded on the device; mode 1 tensor cores, 0 the FP64 kernel)."""
+    ms = C.c_double()
+    fdtd._check(_lib().smat_zgemm_time(int(mode), int(m), int(n), int(k), int(reps), C.byref(ms)))
+    return ms.value
+
+
+def zgemm_wait_test():
+    """The error code the tensor-core product records when one of its operand
+    loads never arrives (its bounded waits give up): 1 expected."""
+    flag = C.c_int(-1)
+    fdtd._check(_lib().smat_zgemm_wait_test(C.byref(flag)))
+    return flag.value
 
 
 def read_xi(path, NA=None):

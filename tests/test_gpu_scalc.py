@@ -78,6 +78,18 @@ def test_zgemm_tensor_cores_within_bound(built, m, n, k, spread):
         assert np.all(err <= bound), (mode, float((err / bound).max()))
 
 
+def test_zgemm_bounded_wait_gives_up(built):
+    """A tensor-core product whose slice pair never arrives: its waits run out,
+    it records error 1 and returns (no hang, no fault), and the next product
+    on the device is right."""
+    assert scalc.zgemm_wait_test() == 1
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((130, 20)) + 1j * rng.standard_normal((130, 20))
+    B = rng.standard_normal((20, 40)) + 1j * rng.standard_normal((20, 40))
+    got = scalc.zgemm(A, B, mode=1)
+    assert np.abs(got - A @ B).max() <= 1e-13 * np.abs(A).max() * np.abs(B).max() * 20
+
+
 def test_zgemm_argument_checks(built):
     with pytest.raises(ValueError):
         scalc.zgemm(np.ones((3, 2)), np.ones((3, 2)))  # inner sizes differ
