@@ -28,16 +28,22 @@
  *   max| per entry: 2^-47 relative for S = 7 at 2k = 64, the size of the
  *   FP64 product's own rounding bound over that inner size.
  *
- * GB300 form.  One CTA of 128 threads per output tile of 128 rows x 32
- * complex columns.  The slices are written by the two cutting kernels as
- * images of the shared-memory operand tiles (K-major, no swizzle: core
- * matrices of 8 rows x 16 bytes), so one thread loads every slice of the
- * tile with bulk async copies (cp.async.bulk, completion on mbarriers) and
- * issues the tcgen05.mma (kind::f16, bf16 x bf16 -> f32, M = 128, N = 64,
- * K = 16) of slice i as soon as it has landed; the S accumulators (64 TMEM
- * columns each) are read back by all four warps (tcgen05.ld, one row per
- * thread) for the FP64 epilogue.  Inner sizes above 32 are cut into passes
- * of 32 complex terms, each adding into C.
+ * GB300 form.  Output tiles of 128 rows x 16 complex columns, two CTAs of
+ * 256 threads per SM (224 TMEM columns each), so that one CTA's epilogue runs
+ * beside the other's products.  The slices are written by the two cutting
+ * kernels (integer digit extraction: one FP64 multiply and one conversion per
+ * value) as images of the shared-memory operand tiles (K-major, no swizzle:
+ * core matrices of 8 rows x 16 bytes), so one thread loads them with bulk
+ * async copies (cp.async.bulk, completion on mbarriers: every B slice at
+ * once, the A slices through a ring of three buffers) and issues the
+ * tcgen05.mma (kind::f16, bf16 x bf16 -> f32, M = 128, N = 32, K = 16) of
+ * slice i as soon as it has landed; the S accumulators (32 TMEM columns each)
+ * are read back by all eight warps (tcgen05.ld, one row per thread) for an
+ * integer epilogue (exact int64 sum of the digit levels, the double assembled
+ * from its bits) with one FP64 multiply-add per output: GB300's FP64 pipe
+ * runs a few operations per clock per SM, so FP64 arithmetic is kept off every
+ * per-element path.  Inner sizes above 32 are cut into passes of 32 complex
+ * terms, each adding into C.
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -55,14 +61,15 @@ namespace {
 
 constexpr int S = 7;                 /* slices per operand */
 constexpr int BM = 128;              /* tile rows (TMEM lanes) */
-constexpr int BNC = 32;              /* complex columns per tile */
+constexpr int BNC = 16;              /* complex columns per tile */
 constexpr int BN = 2 * BNC;          /* real MMA columns: Pr then Pi */
 constexpr int KI = 64;               /* bf16 inner size of an image: [re (32) | im (32)] */
 constexpr int KC = KI / 2;           /* complex inner terms per pass */
 constexpr int AIMG = BM * KI * 2;    /* bytes of an A slice image (16 KB) */
-constexpr int BIMG = BN * KI * 2;    /* bytes of a B slice image (8 KB) */
-constexpr int TMEM_COLS = 512;       /* S * BN = 448 columns used */
-constexpr int SMEM = S * (AIMG + BIMG) + 8 * (S + 1) + 16;
+constexpr int BIMG = BN * KI * 2;    /* bytes of a B slice image (4 KB) */
+constexpr int RING = 3;              /* A slice buffers */
+constexpr int TMEM_COLS = 256;       /* S * BN = 224 columns used: two CTAs per SM fit TMEM */
+constexpr int SMEM = RING * AIMG + S * BIMG + 8 * (2 * RING + 2) + 16;
 constexpr unsigned WAIT_LIMIT = 1u << 24;
 
 static_assert(S * BN <= TMEM_COLS, "accumulators exceed the TMEM allocation");
@@ -288,27 +295,34 @@ __device__ __forceinline__ void tmem_ld8(unsigned taddr, float v[8])
     for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
 }
 
-constexpr int MMA_THREADS = 512; /* 16 warps: four per TMEM lane quarter in the epilogue */
+constexpr int MMA_THREADS = 256; /* 8 warps: two per TMEM lane quarter in the epilogue */
 
-/* One tile: rows 128 tr.., complex columns 32 tc.. of C.  Thread 0 loads the
- * slice pairs (A_i, B_i) in order, one mbarrier each, and issues the products
- * of accumulator d as soon as pair d has landed (d-major: (A_i, B_(d-i)),
- * i = 0 .. d); then all 16 warps read the accumulators back, warp w the TMEM
- * lanes of quarter w % 4 and the complex columns 8 (w / 4) .. + 7. */
-__global__ void __launch_bounds__(MMA_THREADS, 1)
+/* One tile: rows 128 tr.., complex columns 16 tc.. of C; two CTAs per SM, so
+ * that one's epilogue runs beside the other's products.  Thread 0 loads every
+ * B slice (one mbarrier) and streams the A slices through a ring of three
+ * buffers (full / empty mbarriers per buffer; a buffer is refilled once the
+ * products that read it have completed, tcgen05.commit); slice i is multiplied
+ * with B_l, l = 0 .. S-1-i, into accumulator i + l.  Then the 8 warps read
+ * the accumulators back, warp w the TMEM lanes of quarter w % 4 and the
+ * complex columns 8 (w / 4) .. + 7.  Every wait is bounded: on a timeout the
+ * CTA records error 1, lets its copies in flight land (bounded) and returns
+ * through the same epilogue. */
+__global__ void __launch_bounds__(MMA_THREADS, 2)
     k_oz_mma(int m, int n, double2 alpha, const unsigned char *__restrict__ aimg, const unsigned char *__restrict__ bimg,
              const int *__restrict__ ea, const int *__restrict__ eb, int ntr, int ntc, double2 *C, int ldc, int *err,
-             unsigned wait_limit, int skip_pair)
+             unsigned wait_limit, int skip_slice)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char *sA = sm, *sB = sm + S * AIMG;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sB + S * BIMG); /* [0, S): pair i landed; S: MMAs done */
-    unsigned *tslot = reinterpret_cast<unsigned *>(bar + S + 1);
+    unsigned char *ring = sm, *sB = sm + RING * AIMG;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sB + S * BIMG);
+    uint64_t *a_full = bar, *a_empty = bar + RING, *b_full = bar + 2 * RING, *acc_full = bar + 2 * RING + 1;
+    unsigned *tslot = reinterpret_cast<unsigned *>(bar + 2 * RING + 2);
     const int tr = blockIdx.x, tc = blockIdx.y;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        for (int b = 0; b <= S; b++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + b)));
+        for (int b = 0; b < 2 * RING + 2; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + b)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -323,46 +337,73 @@ __global__ void __launch_bounds__(MMA_THREADS, 1)
     const unsigned tmem = *tslot;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < S; i++) {
-            const unsigned b = smem_u32(bar + i);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(AIMG + BIMG) : "memory");
-            if (i == skip_pair) continue; /* the timeout test: a pair that never arrives */
+        int last[RING]; /* the slice last loaded into each buffer (-1: none) */
+#pragma unroll
+        for (int r = 0; r < RING; r++) last[r] = -1;
+        auto load_a = [&](int i) {
+            const int slot = i % RING;
+            const unsigned b = smem_u32(a_full + slot);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(AIMG) : "memory");
+            last[slot] = i;
+            if (i == skip_slice) return; /* the timeout test: a slice that never arrives */
             asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                             smem_u32(sA + i * AIMG)),
+                             smem_u32(ring + slot * AIMG)),
                          "l"(aimg + (size_t)(i * ntr + tr) * AIMG), "r"(AIMG), "r"(b)
                          : "memory");
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                             smem_u32(sB + i * BIMG)),
-                         "l"(bimg + (size_t)(i * ntc + tc) * BIMG), "r"(BIMG), "r"(b)
-                         : "memory");
+        };
+        {
+            const unsigned b = smem_u32(b_full);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(S * BIMG) : "memory");
+            for (int l = 0; l < S; l++)
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(sB + l * BIMG)),
+                    "l"(bimg + (size_t)(l * ntc + tc) * BIMG), "r"(BIMG), "r"(b)
+                    : "memory");
         }
-        bool ok = true;
-        for (int d = 0; d < S && ok; d++) {
-            if (!mbar_wait(smem_u32(bar + d), 0, wait_limit)) {
+        for (int i = 0; i < RING && i < S; i++) load_a(i);
+        bool ok = mbar_wait(smem_u32(b_full), 0, wait_limit);
+        for (int i = 0; i < S && ok; i++) {
+            const int slot = i % RING;
+            if (!mbar_wait(smem_u32(a_full + slot), (unsigned)((i / RING) & 1), wait_limit)) {
                 ok = false;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const unsigned acc = tmem + (unsigned)(d * BN);
-            for (int i = 0; i <= d; i++) {
+            for (int l = 0; l + i < S; l++) {
+                const unsigned acc = tmem + (unsigned)((i + l) * BN);
 #pragma unroll
                 for (int ks = 0; ks < KI / 16; ks++)
-                    mma_bf16(acc, op_desc(smem_u32(sA + i * AIMG + ks * 256)),
-                             op_desc(smem_u32(sB + (d - i) * BIMG + ks * 256)), (i > 0 || ks > 0) ? 1u : 0u);
+                    mma_bf16(acc, op_desc(smem_u32(ring + slot * AIMG + ks * 256)),
+                             op_desc(smem_u32(sB + l * BIMG + ks * 256)), (i > 0 || ks > 0) ? 1u : 0u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(a_empty + slot))
+                         : "memory");
+            /* the buffer of slice i - 1 takes slice i - 1 + RING once its products are done */
+            const int nx = i - 1 + RING;
+            if (i >= 1 && nx < S) {
+                const int ps = (i - 1) % RING;
+                if (!mbar_wait(smem_u32(a_empty + ps), (unsigned)(((i - 1) / RING) & 1), wait_limit)) {
+                    ok = false;
+                    break;
+                }
+                load_a(nx);
             }
         }
         if (!ok) {
-            /* a slice that never landed: record it, and let the copies still
-             * in flight finish (bounded) before the CTA exits */
+            /* record it, and let the copies still in flight land (bounded) */
             atomicExch(err, 1);
-            for (int i = 0; i < S; i++) mbar_wait(smem_u32(bar + i), 0, wait_limit);
+            mbar_wait(smem_u32(b_full), 0, wait_limit);
+            for (int r = 0; r < RING; r++)
+                if (last[r] >= 0) mbar_wait(smem_u32(a_full + r), (unsigned)((last[r] / RING) & 1), wait_limit);
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         smem_u32(bar + S))
+                         smem_u32(acc_full))
                      : "memory");
     }
     __syncwarp();
-    const bool done = mbar_wait(smem_u32(bar + S), 0, wait_limit);
+    const bool done = mbar_wait(smem_u32(acc_full), 0, wait_limit);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!done) {
         if (lane == 0) atomicExch(err, 2);
