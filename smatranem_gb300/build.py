@@ -89,7 +89,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for f in [ex.submit(_run, j, log) for j in jobs]:
             f.result()
     if force or _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm"], log)
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm", "-lpthread"], log)
     main_c = os.path.join(CSRC, "fdtd_main.c")
     if os.path.exists(main_c) and (force or _stale(EXE, [main_c, LIB] + headers)):
         _run(["gcc"] + CFLAGS + [main_c, "-o", EXE, "-L" + OUT, "-lsmatran_fdtd", "-Wl,-rpath,$ORIGIN", "-lm"], log)

@@ -425,10 +425,11 @@ __global__ void __launch_bounds__(PCT) k_panel_cl(double2 *A, int lda, int m, in
  * memory, or 0 where it does not fit (the one-CTA k_panel then) */
 static int panel_cluster(int m, size_t *smem)
 {
-    static int cached = -1;
-    if (cached < 0) {
-        cached = 0;
-        int dev = 0, optin = 0;
+    /* the cluster size (16, else 8) and the shared-memory limit in KB, found
+     * once per process (thread-safe initialisation: passes of smat_scalc may
+     * run on two host threads) */
+    static const int cached = [] {
+        int c = 0, dev = 0, optin = 0;
         if (cudaGetDevice(&dev) == cudaSuccess &&
             cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
             cudaFuncSetAttribute(k_panel_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
@@ -447,14 +448,15 @@ static int panel_cluster(int m, size_t *smem)
                 cfg.numAttrs = 1;
                 int n = 0;
                 if (cudaOccupancyMaxActiveClusters(&n, k_panel_cl, &cfg) == cudaSuccess && n > 0) {
-                    cached = cs;
+                    c = cs;
                     break;
                 }
             }
-            cached = cached * 100000 + (optin - 8192) / 1024; /* cluster size, then the smem limit in KB */
+            c = c * 100000 + (optin - 8192) / 1024;
         }
         cudaGetLastError();
-    }
+        return c;
+    }();
     const int cs = cached / 100000;
     const size_t limit = (size_t)(cached % 100000) * 1024;
     if (cs == 0) return 0;

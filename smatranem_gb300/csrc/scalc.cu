@@ -21,6 +21,8 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "dense_z.cuh"
@@ -335,41 +337,52 @@ extern "C" int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int
     if (nB < 1 || nT < 1 || nB > NA || nT > NA) return smat_fail(SMAT_EINVAL, "smat_scalc: modes %d, %d", nB, nT);
     if (!(omega > 0) || !std::isfinite(omega)) return smat_fail(SMAT_EINVAL, "smat_scalc: omega = %g", omega);
     const int Nmax = std::max(nB, nT);
-    Transfer T;
-    T.NA = NA;
-    T.g.L0 = L0;
-    T.g.L1 = L1;
-    T.g.NA1 = NA1;
-    T.g.s0 = L0 > 1 ? -1.0 : (double)BoundC[0];
-    T.g.s1 = L1 > 1 ? -1.0 : (double)BoundC[1];
-    T.g.e0 = L0 > 1 ? (double)BoundC[0] : 0.0;
-    T.g.e1 = L1 > 1 ? (double)BoundC[1] : 0.0;
-    SCK(cudaStreamCreateWithFlags(&T.st, cudaStreamNonBlocking));
     const size_t ldF = (size_t)Nmax + NA;
-    auto alloc = [&](double2 **p, size_t n) {
-        if (cudaMalloc((void **)p, n * sizeof(double2)) != cudaSuccess) {
-            cudaGetLastError();
-            return smat_fail(SMAT_ENOMEM, "smat_scalc: %zu bytes of device memory", n * sizeof(double2));
-        }
-        return SMAT_OK;
+    /* one transfer state per direction: device matrices, stream, product workspace */
+    auto setup = [&](Transfer &T) {
+        T.NA = NA;
+        T.g.L0 = L0;
+        T.g.L1 = L1;
+        T.g.NA1 = NA1;
+        T.g.s0 = L0 > 1 ? -1.0 : (double)BoundC[0];
+        T.g.s1 = L1 > 1 ? -1.0 : (double)BoundC[1];
+        T.g.e0 = L0 > 1 ? (double)BoundC[0] : 0.0;
+        T.g.e1 = L1 > 1 ? (double)BoundC[1] : 0.0;
+        SCK(cudaStreamCreateWithFlags(&T.st, cudaStreamNonBlocking));
+        auto alloc = [&](double2 **p, size_t n) {
+            if (cudaMalloc((void **)p, n * sizeof(double2)) != cudaSuccess) {
+                cudaGetLastError();
+                return smat_fail(SMAT_ENOMEM, "smat_scalc: %zu bytes of device memory", n * sizeof(double2));
+            }
+            return SMAT_OK;
+        };
+        RC(alloc(&T.F01, ldF * Nmax));
+        RC(alloc(&T.B01, ldF * NA));
+        RC(alloc(&T.F2, (size_t)NA * Nmax));
+        RC(alloc(&T.B2, (size_t)NA * NA));
+        RC(alloc(&T.W1, (size_t)NA * NA));
+        RC(alloc(&T.W2, (size_t)NA * ldF));
+        RC(alloc(&T.Xi, (size_t)N2 * N2));
+        RC(alloc(&T.P, (size_t)N2 * N2));
+        RC(alloc(&T.PH, (size_t)N2 * N2));
+        RC(alloc(&T.FB, (size_t)N2 * ldF));
+        RC(alloc(&T.Cm, (size_t)N2 * ldF));
+        RC(alloc(&T.V, 6 * (size_t)NA1));
+        SCK(cudaMalloc(&T.ipiv, sizeof(int) * NA));
+        SCK(cudaMalloc(&T.dinfo, sizeof(int)));
+        SCK(cudaMemsetAsync(T.dinfo, 0, sizeof(int), T.st));
+        /* products up to 2NA x (Nmax + NA) (the projection on the dual modes) */
+        return smat::dense::gemm_ctx_alloc(T.gm, N2, (int)ldF, T.st);
     };
-    RC(alloc(&T.F01, ldF * Nmax));
-    RC(alloc(&T.B01, ldF * NA));
-    RC(alloc(&T.F2, (size_t)NA * Nmax));
-    RC(alloc(&T.B2, (size_t)NA * NA));
-    RC(alloc(&T.W1, (size_t)NA * NA));
-    RC(alloc(&T.W2, (size_t)NA * ldF));
-    RC(alloc(&T.Xi, (size_t)N2 * N2));
-    RC(alloc(&T.P, (size_t)N2 * N2));
-    RC(alloc(&T.PH, (size_t)N2 * N2));
-    RC(alloc(&T.FB, (size_t)N2 * ldF));
-    RC(alloc(&T.Cm, (size_t)N2 * ldF));
-    RC(alloc(&T.V, 6 * (size_t)NA1));
-    SCK(cudaMalloc(&T.ipiv, sizeof(int) * NA));
-    SCK(cudaMalloc(&T.dinfo, sizeof(int)));
-    SCK(cudaMemsetAsync(T.dinfo, 0, sizeof(int), T.st));
-    /* products up to 2NA x (Nmax + NA) (the projection on the dual modes) */
-    RC(smat::dense::gemm_ctx_alloc(T.gm, N2, (int)ldF, T.st));
+    Transfer T;
+    RC(setup(T));
+    /* the backward pass on a state, stream and host thread of its own, so
+     * that the two directions' latency-bound panel factorisations (a cluster
+     * of 16 SMs) run beside each other's products; if the second state does
+     * not fit the device, the passes run one after the other on the first */
+    Transfer T2;
+    const bool concurrent = both_ways && setup(T2) == SMAT_OK;
+    if (both_ways && !concurrent) smat_clear_error();
     const size_t lstride = (size_t)2 * 6 * NA1;
     std::vector<const double *> up(nlayers), down(nlayers);
     for (int l = 0; l < nlayers; l++) {
@@ -377,18 +390,41 @@ extern "C" int smat_scalc(int L0, int L1, const int BoundC[2], double omega, int
         down[l] = meds + lstride * (nlayers - 1 - l);
     }
     const int N = nB + nT;
-    std::vector<std::complex<double>> Sm((size_t)N * N, 0.0), F01h, B01h;
+    std::vector<std::complex<double>> Sm((size_t)N * N, 0.0), F01h, B01h, F01b, B01b;
+    int rc_back = SMAT_OK;
+    std::string msg_back;
+    std::thread back;
+    if (concurrent) {
+        int dev = 0;
+        SCK(cudaGetDevice(&dev));
+        back = std::thread([&, dev] {
+            cudaSetDevice(dev);
+            rc_back = one_way(T2, -1, nlayers, down.data(), omega, XiT, XiB, nT, nB, F01b, B01b);
+            if (rc_back) msg_back = smat_last_error();
+        });
+    }
     /* forward: Smat_calc :148-158 */
-    RC(one_way(T, 1, nlayers, up.data(), omega, XiB, XiT, nB, nT, F01h, B01h));
+    const int rc_fwd = one_way(T, 1, nlayers, up.data(), omega, XiB, XiT, nB, nT, F01h, B01h);
+    if (back.joinable()) back.join();
+    RC(rc_fwd);
+    if (rc_back) return smat_fail(rc_back, "%s", msg_back.c_str());
     for (int c = 0; c < N; c++)
         for (int r = 0; r < N; r++)
             Sm[r + (size_t)N * c] = c < nB ? F01h[r + (size_t)N * c] : B01h[r + (size_t)N * (c - nB)];
     if (both_ways) { /* backward: Smat_calc :159-168 */
-        RC(one_way(T, -1, nlayers, down.data(), omega, XiT, XiB, nT, nB, F01h, B01h));
+        if (!concurrent) RC(one_way(T, -1, nlayers, down.data(), omega, XiT, XiB, nT, nB, F01b, B01b));
         for (int c = nB; c < N; c++) {
-            for (int r = nB; r < N; r++) Sm[r + (size_t)N * c] = F01h[(r - nB) + (size_t)N * (c - nB)];
-            for (int r = 0; r < nB; r++) Sm[r + (size_t)N * c] = F01h[(r + nT) + (size_t)N * (c - nB)];
+            for (int r = nB; r < N; r++) Sm[r + (size_t)N * c] = F01b[(r - nB) + (size_t)N * (c - nB)];
+            for (int r = 0; r < nB; r++) Sm[r + (size_t)N * c] = F01b[(r + nT) + (size_t)N * (c - nB)];
         }
+    }
+    if (concurrent) {
+        int hinfo2 = 0;
+        SCK(cudaMemcpyAsync(&hinfo2, T2.dinfo, sizeof(int), cudaMemcpyDeviceToHost, T2.st));
+        SCK(cudaStreamSynchronize(T2.st));
+        RC(smat::dense::gemm_ctx_check(T2.gm));
+        if (hinfo2 != 0) return smat_fail(SMAT_ENUMERIC, "smat_scalc: singular matrix in the layer transfer (zgesv info)");
+        T.solves += T2.solves;
     }
     int hinfo = 0;
     SCK(cudaMemcpyAsync(&hinfo, T.dinfo, sizeof(int), cudaMemcpyDeviceToHost, T.st));
