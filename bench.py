@@ -518,7 +518,8 @@ def run_ours(args):
                 "adjoint": ("config_adjoint_160x160x120", 70, lambda: config_adjoint(6000, args.extra_fd_cells)),
                 "group": ("config_group_bend8_slabs16", 120,
                           lambda: config_group(args.warmup, 40, 0, 300, bend_workload=(bend, pr, modes))),
-                "large": ("config_large_640x640x512", 150, lambda: config_large(args.warmup, 20, 300))}
+                "large": ("config_large_640x640x512", 150, lambda: config_large(args.warmup, 20, 300)),
+                "scalc": ("config_scalc_grating32x32", 40, lambda: config_scalc(32, 32, 10, 2, "both", True))}
         for name in todo:
             key, est, fn = runs[name]
             left = args.extras_budget - (time.perf_counter() - t_start)
@@ -1019,9 +1020,9 @@ def run_modes(args):
         "cpu_baseline": cpu}))
 
 
-def run_scalc(args):
+def config_scalc(L0=32, L1=32, nl=10, steps=2, dense="both", cpu=True):
     """Layer-transfer S matrix (Scalc, (f)-4) on the GPU: a periodic grating
-    between uniform ports, --shape L0,L1,nlayers (default 32x32, 10 layers:
+    between uniform ports, L0 x L1 cells, nl layers (default 32x32, 10 layers:
     dense matrices of order NA = 2*L0*L1 = 2048, all propagating modes of the
     ports in S), both directions.  CPU side: the same dense steps (zgesv of
     B2^T with NA + N_real right-hand sides, the projection zgemm) through
@@ -1030,8 +1031,6 @@ def run_scalc(args):
     import torch
     from smatranem_gb300 import scalc as SC
     from smatranem_gb300 import workloads as W
-    parts = [int(x) for x in args.shape.split(",")] if args.shape != "256,192,48" else [32, 32, 10]
-    L0, L1, nl = parts[:3]
     om = 0.405
     t0 = time.perf_counter()
     theta, Xi, nr = W.plane_wave_basis(L0, L1, omega=om)
@@ -1040,14 +1039,14 @@ def run_scalc(args):
     NA = 2 * L0 * L1
     res = {}
     modes = [(1, "tensor_cores"), (0, "fp64_kernel")]
-    if args.dense != "both":
-        modes = [m for m in modes if m[1].startswith(args.dense[:2])]
+    if dense != "both":
+        modes = [m for m in modes if m[1].startswith(dense[:2])]
     for mode, name in modes:
         SC.dense_mode(mode)
         SC.smatrix(meds[:2], om, L0, L1, (1, 1), Xi, nr, Xi, nr)  # warm-up (allocations, module load)
         torch.cuda.synchronize()
         times = []
-        for _ in range(max(1, args.steps)):
+        for _ in range(max(1, steps)):
             t0 = time.perf_counter()
             S, info = SC.smatrix(meds, om, L0, L1, (1, 1), Xi, nr, Xi, nr)
             times.append(time.perf_counter() - t0)
@@ -1061,8 +1060,8 @@ def run_scalc(args):
     # two projections on the dual modes ((2NA)^2 x (NA + N_real))
     flops = solves * (8.0 / 3.0 * NA ** 3 + 8.0 * NA ** 2 * (NA + nr) + 8.0 * (NA + nr) * nr * NA) \
         + 2 * 8.0 * (2 * NA) ** 2 * (NA + nr)
-    cpu = None
-    if not args.no_cpu:
+    cpu_line = None
+    if cpu:
         import scipy.linalg as sl
         rng = np.random.default_rng(0)
         A = rng.standard_normal((NA, NA)) + 1j * rng.standard_normal((NA, NA))
@@ -1076,13 +1075,13 @@ def run_scalc(args):
         P.conj().T @ F
         t_mm = time.perf_counter() - t0
         est = solves * t_solve + 2 * t_mm
-        cpu = {"value": est, "unit": "s per S matrix (LAPACK zgesv x solves + 2 projection zgemm)",
-               "cores": os.cpu_count(), "kind": "port",
-               "sample": f"one zgesv of order {NA} with {NA + nr} right-hand sides: {t_solve:.2f} s (x {solves}); "
-                         f"one {2 * NA}^2 x {NA + nr} zgemm: {t_mm:.2f} s (x 2); threads of the host BLAS"}
-    print(json.dumps({
-        "mode": "scalc", "config": f"periodic grating {L0}x{L1}, {nl} layers, uniform ports eps 2.085, "
-                                   f"NA = {NA}, N_real = {nr} per port, both directions",
+        cpu_line = {"value": est, "unit": "s per S matrix (LAPACK zgesv x solves + 2 projection zgemm)",
+                    "cores": os.cpu_count(), "kind": "port",
+                    "sample": f"one zgesv of order {NA} with {NA + nr} right-hand sides: {t_solve:.2f} s (x {solves}); "
+                              f"one {2 * NA}^2 x {NA + nr} zgemm: {t_mm:.2f} s (x 2); threads of the host BLAS"}
+    return {
+        "config": f"periodic grating {L0}x{L1}, {nl} layers, uniform ports eps 2.085, "
+                  f"NA = {NA}, N_real = {nr} per port, both directions",
         "s_per_smatrix": best, "runs": nruns, "solves": solves,
         "fp64_tflops": flops / best / 1e12,
         "products": "FP64-accurate complex products on the tensor cores (7 bf16 slices per operand, Ozaki scheme, "
@@ -1091,7 +1090,14 @@ def run_scalc(args):
                                                     "speedup_tensor_cores": best64 / best},
         "s_max_abs_diff_vs_fp64_kernel": None if S64 is None else float(np.abs(S - S64).max()),
         "unitarity": info["unitarity"], "unitarity_fp64_kernel": None if info64 is None else info64["unitarity"],
-        "transpose": info["transpose"], "setup_s": t_setup, "cpu_baseline": cpu}))
+        "transpose": info["transpose"], "setup_s": t_setup, "cpu_baseline": cpu_line}
+
+
+def run_scalc(args):
+    """--mode scalc: config_scalc's line; --shape L0,L1,nlayers (default 32,32,10)."""
+    parts = [int(x) for x in args.shape.split(",")] if args.shape != "256,192,48" else [32, 32, 10]
+    print(json.dumps(dict({"mode": "scalc"}, **config_scalc(parts[0], parts[1], parts[2], args.steps, args.dense,
+                                                              not args.no_cpu))))
 
 
 def main():
@@ -1118,9 +1124,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--dense", default="both", choices=["both", "tensor_cores", "fp64_kernel"],
                     help="--mode scalc: the dense products timed (tensor cores, the FP64 kernel, or both)")
-    ap.add_argument("--extras", default="cube,adjoint,group,large",
+    ap.add_argument("--extras", default="cube,adjoint,group,large,scalc",
                     help="main mode: the other workloads summarised in the contract line (comma list of cube, "
-                         "adjoint, group, large; empty: none)")
+                         "adjoint, group, large, scalc; empty: none)")
     ap.add_argument("--extras-budget", type=float, default=420.0,
                     help="seconds the extras may take together; one that would not fit is reported as skipped")
     ap.add_argument("--extra-fd-cells", type=int, default=4,
