@@ -1045,6 +1045,7 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
         p->zc = zc;
         p->ctas_per_sm = ctas_per_sm;
         p->max_ctas = occ;
+        p->ns = 0; /* the fifth tuning value means nothing to kernel 6 */
         p->fused = 6;
         drop_graph(p);
         return SMAT_OK;
