@@ -13,20 +13,21 @@
  *   - complex as real: [Pr | Pi] = [Ar | Ai] * [[Br, Bi], [-Bi, Br]], one real
  *     product of inner size 2k.
  *   - each row r of [Ar | Ai] is scaled by 2^-e_r (e_r: the exponent of its
- *     largest entry, so every scaled entry lies in (-1, 1)) and cut into
- *     digits x = sum_i t_i 2^(-7-8i), t_i = rint of the remainder (integers in
- *     [-128, 128], exact in bf16); each column of the real B likewise (one
- *     exponent per complex column).  The cuts are exact in FP64.
+ *     largest entry, so every scaled entry x lies in (-1, 1)) and cut into
+ *     balanced base-256 digits of F = rint(x 2^55): x ~ sum_i t_i 2^(-7-8i),
+ *     t_i integers in [-128, 128], exact in bf16; each column of the real B
+ *     likewise (one exponent per complex column).
  *   - products t * t' are at most 2^14 in magnitude; with 2k <= 64 and at most
  *     S pairs per sum, every partial sum is an integer below 2^24 and the FP32
  *     accumulation of the tensor cores is exact.  The pairs (i, l) with the
  *     same i + l = d share the scale 2^(-14-8d) and one TMEM accumulator.
- *   - the d-accumulators are summed in FP64 (smallest first), scaled by
- *     2^(e_r + e_c) (exact), multiplied by alpha and added to C.
- *   Error: the slices hold 8S - 1 bits of each scaled entry and the pairs
- *   with i + l >= S are dropped, about 2k * S * 2^(-8S) of |row max| * |col
- *   max| per entry: 2^-47 relative for S = 7 at 2k = 64, the size of the
- *   FP64 product's own rounding bound over that inner size.
+ *   - the d-accumulators are combined exactly in integers, X = sum_d acc_d
+ *     256^(S-1-d), rounded once to the nearest double, scaled by
+ *     2^(e_r + e_c - 14 - 8(S-1)) (exact), multiplied by alpha and added to C.
+ *   Error: the cuts keep 55 bits below each row's (column's) leading bit and
+ *   the pairs with i + l >= S are dropped, about 2k * S * 2^(-8S) of |row
+ *   max| * |col max| per entry: 2^-47 relative for S = 7 at 2k = 64, the size
+ *   of the FP64 product's own rounding bound over that inner size.
  *
  * GB300 form.  Output tiles of 128 rows x 16 complex columns, two CTAs of
  * 256 threads per SM (224 TMEM columns each), so that one CTA's epilogue runs
