@@ -865,15 +865,17 @@ __device__ __forceinline__ double widen(float f)
     return e == 0u ? 0.0 : __hiloint2double((int)hi, (int)lo);
 }
 
-/* COUNT: the window length when it is the full ring (the common case, no
- * per-sample predicate), 0 for a shorter window at the end of a run */
-template <int COUNT>
+/* CMAX: the window length rounded up to a multiple of 8 (a full ring: 32,
+ * no per-sample predicate); a shorter window at the end of a run skips the
+ * samples past its length, so its cost follows its length */
+template <int CMAX>
 __global__ void __launch_bounds__(128, 6) k_flush32(const P32 p, const int rel_end, const int count_rt)
 {
     /* [nfreq][count] {hi re, hi im, lo re, lo im} of this block's half (H or E
      * phases) */
     extern __shared__ float4 sph[];
-    const int count = COUNT > 0 ? COUNT : count_rt;
+    constexpr bool FULL = CMAX == RING_MAX;
+    const int count = FULL ? RING_MAX : count_rt;
     const Dft &d = p.d;
     const int k0 = *p.s.base + rel_end - count;
     const int qv = blockIdx.y, b = blockIdx.z;
@@ -887,9 +889,9 @@ __global__ void __launch_bounds__(128, 6) k_flush32(const P32 p, const int rel_e
     __syncthreads();
     const int px = blockIdx.x * blockDim.x + threadIdx.x;
     if (px >= p.g.pl) return;
-    float x[RING_MAX];
+    float x[CMAX];
 #pragma unroll
-    for (int s = 0; s < RING_MAX; s++) x[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, v)[px] : 0.0f;
+    for (int s = 0; s < CMAX; s++) x[s] = (s < count) ? ring_at(d, p.g.pl, b, k0 + s, q, v)[px] : 0.0f;
     double *acc = d.acc + 2 * (((((long long)b * d.nfreq) * d.nq + q) * 4 + v) * p.g.pl + px);
     const long long fstride = 2 * (long long)d.nq * 4 * p.g.pl; /* doubles from one frequency to the next */
     int f = 0;
@@ -897,8 +899,8 @@ __global__ void __launch_bounds__(128, 6) k_flush32(const P32 p, const int rel_e
         const float4 *pa = sph + f * count, *pb = pa + count;
         float sa = 0.f, na = 0.f, sai = 0.f, nai = 0.f, sb = 0.f, nb = 0.f, sbi = 0.f, nbi = 0.f;
 #pragma unroll
-        for (int s = 0; s < RING_MAX; s++) {
-            if (COUNT > 0 || s < count) {
+        for (int s = 0; s < CMAX; s++) {
+            if (FULL || s < count) {
                 const float4 ha = pa[s], hb = pb[s];
                 kahan_term(x[s], ha.x, ha.z, sa, na);
                 kahan_term(x[s], ha.y, ha.w, sai, nai);
@@ -916,8 +918,8 @@ __global__ void __launch_bounds__(128, 6) k_flush32(const P32 p, const int rel_e
         const float4 *pa = sph + f * count;
         float sa = 0.f, na = 0.f, sai = 0.f, nai = 0.f;
 #pragma unroll
-        for (int s = 0; s < RING_MAX; s++) {
-            if (COUNT > 0 || s < count) {
+        for (int s = 0; s < CMAX; s++) {
+            if (FULL || s < count) {
                 const float4 ha = pa[s];
                 kahan_term(x[s], ha.x, ha.z, sa, na);
                 kahan_term(x[s], ha.y, ha.w, sai, nai);
@@ -996,10 +998,15 @@ void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st)
     if (p.d.nfreq <= 0 || p.d.nq <= 0 || count <= 0) return;
     dim3 blk(128), grd((p.g.pl + 127) / 128, p.d.nq * 4, p.batch);
     const size_t sm = sizeof(float4) * (size_t)count * p.d.nfreq;
-    const void *fn = count == RING_MAX ? (const void *)k_flush32<RING_MAX> : (const void *)k_flush32<0>;
+    static_assert(RING_MAX == 32, "flush instantiations: windows rounded up to 8, 16, 24, 32");
+    const int cmax = (count + 7) / 8 * 8;
+    const void *fn = cmax == 8    ? (const void *)k_flush32<8>
+                     : cmax == 16 ? (const void *)k_flush32<16>
+                     : cmax == 24 ? (const void *)k_flush32<24>
+                                  : (const void *)k_flush32<32>;
     if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (count == RING_MAX) k_flush32<RING_MAX><<<grd, blk, sm, st>>>(p, rel_end, count);
-    else k_flush32<0><<<grd, blk, sm, st>>>(p, rel_end, count);
+    void *args[] = {(void *)&p, (void *)&rel_end, (void *)&count};
+    cudaLaunchKernel(fn, grd, blk, args, sm, st);
 }
 
 } // namespace smat
