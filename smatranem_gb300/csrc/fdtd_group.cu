@@ -103,9 +103,9 @@ int setup_persistent(smat_fdtd_group *g, int threads)
     int used = 0;
     for (int i = 0; i < n; i++) {
         const smat_fdtd_plan *p = g->m[i];
-        if (p->nrec_metal > 0 || p->nrec_split > 0)
-            return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 needs members without stable-form metal or "
-                                          "lossy split cells (member %d has them)", i);
+        if (p->nrec_metal > 0)
+            return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 needs members without stable-form metal "
+                                          "cells (member %d has them)", i);
         const int nq = p->L[0] / 4;
         int t = 0;
         for (int c = 16; c >= 1 && !t; c--)

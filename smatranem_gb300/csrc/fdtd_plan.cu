@@ -1029,9 +1029,9 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
                                       "rows)");
     if (fused == 6) {
         /* whole-row fused step: tile_y rows per CTA, z chunks, ctas_per_sm = register bound 1..3 */
-        if (p->L[0] % 4 != 0 || p->nrec_metal > 0 || p->nrec_split > 0)
+        if (p->L[0] % 4 != 0 || p->nrec_metal > 0)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 needs L0 %% 4 == 0 and a plan without stable-form "
-                                          "metal cells or lossy split cells");
+                                          "metal cells");
         if (tile_y < 1 || tile_y > 16 || z_chunk < 0 || ctas_per_sm < 1 || ctas_per_sm > 3)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 takes tile_y in 1..16, z_chunk >= 0 (0: persistent "
                                           "CTAs) and ctas_per_sm (register bound) 1..3");
@@ -1099,8 +1099,8 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
                 if (zc > 0 && zc < L2) cands.push_back({2, by, zc, 5, 4});
         cands.push_back({2, 4, 0, 5, 4});
     }
-    /* whole-row fused step (plans without record cells) */
-    if (p->L[0] % 4 == 0 && p->nrec_metal == 0 && p->nrec_split == 0)
+    /* whole-row fused step (plans without stable-form metal cells) */
+    if (p->L[0] % 4 == 0 && p->nrec_metal == 0)
         for (int ty : {1, 2, 4, 5})
             for (int mb : {1, 2})
                 for (int zc : {0, L2, 40, 32, 24, 20})

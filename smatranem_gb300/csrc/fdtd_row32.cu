@@ -5,8 +5,8 @@
  * Same update as the two FP32 sweeps of fdtd_f32.cu (the reference main_calc,
  * FDTDcalc/FDTDsplitfieldMetal.c:242-329, in total-field form), with the same
  * floating point expressions, so the results are bit-identical to them.  For
- * plans with L0 % 4 == 0 and without stable-form metal or lossy split cells
- * (lossy and PEC ordinary cells run a compile-time variant, REC).
+ * plans with L0 % 4 == 0 and without stable-form metal cells (lossy and PEC
+ * ordinary cells and lossy split cells run a compile-time variant, REC).
  *
  *   - a CTA owns TY whole x rows (y0 .. y0+TY-1) of one excitation and marches
  *     along z through a range of planes [z0, z1).  At stage z it computes
@@ -103,18 +103,30 @@ struct QuadTab {
     unsigned xm;
 };
 
-/* A record cell of an ordinary ('n') cell -- lossy or PEC: the update of the
- * sweeps' general-cell path (fdtd_f32.cu, general32_cell) from the same
- * curls; t is the cell's total field, updated in place.  The host admits no
- * other record kind to this kernel.  Out of line: record cells are rare and
- * must not cost the quads registers. */
+/* A record cell -- an ordinary ('n') cell that is lossy or PEC, or a split
+ * cell with lossy media (RK_A): the update of the sweeps' general-cell path
+ * (fdtd_f32.cu, general32_cell) from the same curls; t is the cell's total
+ * field, ta its aux slot (read and written for RK_A only), both updated in
+ * place.  The host admits no other record kind to this kernel.  Out of line:
+ * record cells are rare and must not cost the quads registers. */
 template <bool EF>
 __device__ __noinline__ void row_record(const P32 &p, const int k, const int b, const bool on_src, const int px,
-                                        const int ridx, const float *pl, const float *mi, float *t)
+                                        const int ridx, const float *pl, const float *mi, float *t, float *ta)
 {
     const Geo &g = p.g;
     const float sg = EF ? 1.0f : -1.0f;
     const Rec32 r = (EF ? p.erec : p.hrec)[ridx];
+    if (r.kind == RK_A) { /* the two halves of a split cell, record coefficients */
+        for (int c = 0; c < 3; c++) {
+            const float m = ta[c];
+            const float pp = t[c] - m;
+            const float np = fmaf(sg * r.B0[c], pl[c], r.A0[c] * pp);
+            const float nm = fmaf(sg * r.B1[c], mi[c], r.A1[c] * m);
+            t[c] = np + nm;
+            ta[c] = nm;
+        }
+        return;
+    }
     float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
     if (on_src) {
         W[0] += (float)(p.s.sgn[b] * row_sheet(p.s, g.pl, b, k, !EF, 1, px));
@@ -170,9 +182,13 @@ __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b,
         const float bn[3] = {el(c[0], i), el(c[1], i), el(c[2], i)};
         if (REC && isnan(bn[0])) { /* a record cell (marked by NaN in its first coefficient) */
             float t[3] = {el(out[0], i), el(out[1], i), el(out[2], i)};
-            row_record<EF>(p, k, b, on_src, px0 + i, __float_as_int(bn[1]), pl, mi, t);
+            float ta[3] = {el(aux[0], i), el(aux[1], i), el(aux[2], i)}; /* staged where the quad is split */
+            row_record<EF>(p, k, b, on_src, px0 + i, __float_as_int(bn[1]), pl, mi, t, ta);
 #pragma unroll
-            for (int cc = 0; cc < 3; cc++) set_el(out[cc], i, t[cc]);
+            for (int cc = 0; cc < 3; cc++) {
+                set_el(out[cc], i, t[cc]);
+                set_el(aux[cc], i, ta[cc]);
+            }
         } else if (!(((tq.xm >> i) & 1u) | pyz)) {
             float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
             if (on_src) {
@@ -429,6 +445,9 @@ __device__ __forceinline__ void row_march(const Row32 &r, const int rel, const i
                 if (qs) {
 #pragma unroll
                     for (int i = 0; i < 3; i++) a[i] = (&PH(2, i))[sid];
+                } else if (REC) { /* record cells read the aux values; none is split here */
+#pragma unroll
+                    for (int i = 0; i < 3; i++) a[i] = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
                 float4 gy0, gy2;
                 if (ry == 0) {
@@ -478,6 +497,9 @@ __device__ __forceinline__ void row_march(const Row32 &r, const int rel, const i
                 if (qse) {
 #pragma unroll
                     for (int i = 0; i < 3; i++) ae[i] = (&PE(1, i))[sid];
+                } else if (REC) {
+#pragma unroll
+                    for (int i = 0; i < 3; i++) ae[i] = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
                 /* H_new of plane z-1 (own quad, row above, quad to the right) from
                  * shared memory, of plane z from registers */

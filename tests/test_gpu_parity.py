@@ -413,8 +413,12 @@ def test_row_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
 
 
 ROW_REC_CASES = [
-    # record cells other than stable-form metal: lossy and PEC ordinary cells
+    # record cells other than stable-form metal: lossy and PEC ordinary cells,
+    # split cells with lossy media
     ((40, 17, 19, 3), 41, dict(pml=(4, 4, 4), lossy=0.05, iBc=(1, 1, -1)), (5, 13, 7, -1)),
+    ((48, 19, 21, 3), 44, dict(pml=(4, 4, 4), lossy=0.03, lossy_pml=0.2, iBc=(1, -1, 1)), (5, 15, 8, 1)),
+    ((36, 10, 16, 2), 45, dict(pml=(0, 0, 4), pml_z_only=True, lossy_pml=0.3, pec=0.03, iBc=(0, 0, -1)),
+     (5, 11, 8, -1)),
     ((136, 13, 17, 2), 42, dict(pml=(4, 3, 3), lossy=0.05, pec=0.03, iBc=(0, 0, 0)), (4, 12, 6, 1)),
     ((36, 9, 12, 2), 43, dict(pml=(0, 0, 3), pml_z_only=True, pec=0.05, iBc=(0, -1, 0)), (4, 8, 5, 1)),
 ]
@@ -423,12 +427,22 @@ ROW_REC_CASES = [
 @pytest.mark.parametrize("case", range(len(ROW_REC_CASES)))
 def test_row_fused_record_cells_bit_identical(built, case):
     """Record cells in kernel 6 (the sweeps' general-cell update, out of
-    line): lossy and PEC ordinary cells, bit for bit as the scalar sweeps,
-    chunked and persistent."""
+    line): lossy and PEC ordinary cells and split cells with lossy media, bit
+    for bit as the scalar sweeps, chunked and persistent."""
     from smatranem_gb300 import workloads as W
     L, seed, kw, iBTIin = ROW_REC_CASES[case]
+    kw = dict(kw)
+    lossy_pml = kw.pop("lossy_pml", 0.0)
     s = W.random_structure(L, seed=seed, **kw)
     pr = W.prepare(s)
+    if lossy_pml:
+        # absorbing media in a share of the split cells (the reference's
+        # remove_sigma refuses such decks; the plan API takes them)
+        rng = np.random.default_rng(seed)
+        cells = np.flatnonzero(np.asarray(pr.cont).view(np.uint8) == ord("a"))
+        pick = rng.choice(cells, size=max(1, int(lossy_pml * cells.size)), replace=False)
+        for c in range(3):
+            pr.epsi[3 * pick + c] += 1j * np.abs(pr.epsi[3 * pick + c].real) * rng.uniform(0.01, 0.3, pick.size)
     nsteps = 33
     ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
     # plans with record cells run kernel 6 at one CTA per SM only
