@@ -14,6 +14,9 @@
 #include <cstdlib>
 #include <algorithm>
 #include <cstring>
+#include <functional>
+#include <memory>
+#include <new>
 #include <vector>
 
 #include "trace.cuh"
@@ -438,63 +441,105 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
     const long long n3 = p->n3;
     const double iR = d->invtau_R, iI = d->invtau_I;
     const double *mu = d->mu, *ep = d->epsi;
-    std::vector<float> bh(3 * n3), be(3 * n3);
-    std::vector<Rec32> hrec, erec;
+    std::unique_ptr<float[]> bh(new (std::nothrow) float[3 * n3]), be(new (std::nothrow) float[3 * n3]);
+    if (!bh || !be) return smat_fail(SMAT_ENOMEM, "create: out of host memory for the packed coefficients");
     auto aux = [&](long long l, int c) { return (size_t)c + 3 * (size_t)(n3 + p->addr[l]); };
-    auto put_rec = [&](std::vector<float> &cf, std::vector<Rec32> &recs, long long l, const Rec32 &r) {
-        cf[l] = std::nanf("");
-        int idx = (int)recs.size();
-        float f;
-        memcpy(&f, &idx, 4);
-        cf[n3 + l] = f;
-        cf[2 * n3 + l] = 0.0f;
-        recs.push_back(r);
+    /* The cells go over host worker threads in runs of whole z planes.  Each
+     * run numbers its records from 0 in cell order and keeps the cells they
+     * belong to; joining the runs in order afterwards gives the numbering of
+     * one pass over all cells, so the packed arrays do not depend on the
+     * number of threads. */
+    struct Run {
+        std::vector<Rec32> rec[2]; /* 0: H (mu), 1: E (epsi) */
+        std::vector<int> cell[2];
     };
-    for (long long l = 0; l < n3; l++) {
-        const char k = p->cont[l];
-        const bool pec = d->pec && d->pec[l];
-        for (int side = 0; side < 2; side++) { /* 0: H (mu), 1: E (epsi) */
-            std::vector<float> &cf = side ? be : bh;
-            std::vector<Rec32> &recs = side ? erec : hrec;
-            const double *m = side ? ep : mu;
-            const double *A = side ? Ae : Ah, *B = side ? Be : Bh;
-            const bool lossless = m[2 * (3 * l + 0) + 1] == 0.0 && m[2 * (3 * l + 1) + 1] == 0.0 &&
-                                  m[2 * (3 * l + 2) + 1] == 0.0;
-            bool simple = false;
-            if (k == 'n')
-                simple = lossless && !(side == 1 && pec) && (float)A[3 * l] == 1.0f && (float)A[1 + 3 * l] == 1.0f &&
-                         (float)A[2 + 3 * l] == 1.0f;
-            else if (k == 'a')
-                simple = lossless;
-            if (simple) {
-                for (int c = 0; c < 3; c++) cf[c * n3 + l] = (float)(1. / (iR * m[2 * (3 * l + c)]));
-                continue;
-            }
-            /* a record: everything else (a few per mille of the cells) */
-            Rec32 r;
-            memset(&r, 0, sizeof r);
-            for (int c = 0; c < 3; c++) {
-                r.A0[c] = (float)A[c + 3 * l];
-                r.B0[c] = (float)B[c + 3 * l];
-                if (k != 'n') {
-                    r.A1[c] = (float)A[aux(l, c)];
-                    r.B1[c] = (float)B[aux(l, c)];
+    const int nrun = std::min(host_threads(n3), p->L[2]);
+    std::vector<Run> runs(nrun);
+    struct PackCtx {
+        std::vector<Run> *runs;
+        std::function<void(Run &, long long, long long)> pack;
+        int nrun, L2;
+        long long pl;
+    } ctx{&runs, nullptr, nrun, p->L[2], p->pl};
+    ctx.pack = [&](Run &run, long long l0, long long l1) {
+        for (long long l = l0; l < l1; l++) {
+            const char k = p->cont[l];
+            const bool pec = d->pec && d->pec[l];
+            for (int side = 0; side < 2; side++) {
+                float *cf = side ? be.get() : bh.get();
+                const double *m = side ? ep : mu;
+                const double *A = side ? Ae : Ah, *B = side ? Be : Bh;
+                const bool lossless = m[2 * (3 * l + 0) + 1] == 0.0 && m[2 * (3 * l + 1) + 1] == 0.0 &&
+                                      m[2 * (3 * l + 2) + 1] == 0.0;
+                bool simple = false;
+                if (k == 'n')
+                    simple = lossless && !(side == 1 && pec) && (float)A[3 * l] == 1.0f &&
+                             (float)A[1 + 3 * l] == 1.0f && (float)A[2 + 3 * l] == 1.0f;
+                else if (k == 'a')
+                    simple = lossless;
+                if (simple) {
+                    for (int c = 0; c < 3; c++) cf[c * n3 + l] = (float)(1. / (iR * m[2 * (3 * l + c)]));
+                    continue;
                 }
+                /* a record: everything else (a few per mille of the cells) */
+                Rec32 r;
+                memset(&r, 0, sizeof r);
+                for (int c = 0; c < 3; c++) {
+                    r.A0[c] = (float)A[c + 3 * l];
+                    r.B0[c] = (float)B[c + 3 * l];
+                    if (k != 'n') {
+                        r.A1[c] = (float)A[aux(l, c)];
+                        r.B1[c] = (float)B[aux(l, c)];
+                    }
+                }
+                if (k == 'n') {
+                    r.kind = RK_N;
+                } else if (k == 'a') {
+                    r.kind = RK_A;
+                } else {
+                    const bool stable_here = side == 0 ? (k == 'h' || k == 'b') : (k == 'e' || k == 'b');
+                    r.kind = stable_here ? RK_STABLE : RK_FROZEN;
+                }
+                if (side == 1 && pec) {
+                    for (int c = 0; c < 3; c++) r.A0[c] = r.B0[c] = 0.0f;
+                }
+                /* the coefficient slot holds NaN, the next one the record number */
+                const int idx = (int)run.rec[side].size();
+                cf[l] = std::nanf("");
+                memcpy(&cf[n3 + l], &idx, 4);
+                cf[2 * n3 + l] = 0.0f;
+                run.rec[side].push_back(r);
+                run.cell[side].push_back((int)l);
             }
-            if (k == 'n') {
-                r.kind = RK_N;
-            } else if (k == 'a') {
-                r.kind = RK_A;
-            } else {
-                const bool stable_here = side == 0 ? (k == 'h' || k == 'b') : (k == 'e' || k == 'b');
-                r.kind = stable_here ? RK_STABLE : RK_FROZEN;
-            }
-            if (side == 1 && pec) {
-                for (int c = 0; c < 3; c++) r.A0[c] = r.B0[c] = 0.0f;
-            }
-            put_rec(cf, recs, l, r);
         }
-    }
+    };
+    host_parallel_for(
+        nrun, nrun,
+        [](void *c, long long t0, long long t1) {
+            PackCtx &x = *static_cast<PackCtx *>(c);
+            for (long long t = t0; t < t1; t++) {
+                const long long z0 = x.L2 * t / x.nrun, z1 = x.L2 * (t + 1) / x.nrun;
+                x.pack((*x.runs)[t], z0 * x.pl, z1 * x.pl);
+            }
+        },
+        &ctx);
+    std::vector<Rec32> hrec, erec;
+    std::vector<int> hgen, egen;
+    for (const Run &run : runs)
+        for (int side = 0; side < 2; side++) {
+            std::vector<Rec32> &recs = side ? erec : hrec;
+            std::vector<int> &gen = side ? egen : hgen;
+            float *cf = side ? be.get() : bh.get();
+            const int base = (int)recs.size();
+            if (base)
+                for (size_t i = 0; i < run.cell[side].size(); i++) {
+                    const int idx = base + (int)i;
+                    memcpy(&cf[n3 + run.cell[side][i]], &idx, 4);
+                }
+            recs.insert(recs.end(), run.rec[side].begin(), run.rec[side].end());
+            gen.insert(gen.end(), run.cell[side].begin(), run.cell[side].end());
+        }
+    runs.clear();
     /* 1-D sigma tables: rows A_h, G_h, A_e, G_e over the three axes */
     const int S = p->L[0] + p->L[1] + p->L[2];
     std::vector<float> tab(4 * (size_t)S);
@@ -518,21 +563,8 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
     if ((rc = p->alloc(&p->d_Ha32, fs)) || (rc = p->alloc(&p->d_Ea32, fs))) return rc;
     if ((rc = p->alloc(&p->d_H32b, fs)) || (rc = p->alloc(&p->d_E32b, fs))) return rc;
     if ((rc = p->alloc(&p->d_Ha32b, fs)) || (rc = p->alloc(&p->d_Ea32b, fs))) return rc;
-    std::vector<int> stable;
-    for (long long l = 0; l < n3; l++) {
-        float c0 = be[l];
-        if (std::isnan(c0)) {
-            int idx;
-            memcpy(&idx, &be[n3 + l], 4);
-            if (erec[idx].kind == RK_STABLE) stable.push_back((int)l);
-        }
-    }
-    p->nstable = (int)stable.size();
-    std::vector<int> hgen, egen;
-    for (long long l = 0; l < n3; l++) {
-        if (std::isnan(bh[l])) hgen.push_back((int)l);
-        if (std::isnan(be[l])) egen.push_back((int)l);
-    }
+    p->nstable = 0;
+    for (const Rec32 &r : erec) p->nstable += r.kind == RK_STABLE;
     p->nhgen = (int)hgen.size();
     p->negen = (int)egen.size();
     p->hgen_host = hgen;
@@ -550,18 +582,11 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
     if (!egen.empty())
         CK(p->cpy(p->d_egen, egen.data(), egen.size() * sizeof(int), cudaMemcpyHostToDevice));
     /* record kinds kernel 6 can or cannot take */
-    for (int side = 0; side < 2; side++) {
-        const std::vector<float> &cf = side ? be : bh;
-        const std::vector<Rec32> &recs = side ? erec : hrec;
-        for (long long l = 0; l < n3; l++) {
-            if (!std::isnan(cf[l])) continue;
-            int idx;
-            memcpy(&idx, &cf[n3 + l], 4);
-            const int kind = recs[idx].kind;
-            if (kind == RK_STABLE || kind == RK_FROZEN) p->nrec_metal++;
-            if (kind == RK_A) p->nrec_split++;
+    for (int side = 0; side < 2; side++)
+        for (const Rec32 &r : side ? erec : hrec) {
+            if (r.kind == RK_STABLE || r.kind == RK_FROZEN) p->nrec_metal++;
+            if (r.kind == RK_A) p->nrec_split++;
         }
-    }
     if (p->L[0] % 4 == 0) {
         p->fused = 2; /* default: vectorised sweeps where they apply */
         p->by32 = 2;
@@ -577,8 +602,8 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
         if ((rc = p->alloc(&p->d_qorder, (size_t)nq))) return rc;
         CK(p->cpy(p->d_qorder, qorder.data(), nq * sizeof(int), cudaMemcpyHostToDevice));
     }
-    CK(p->cpy(p->d_bh, bh.data(), bh.size() * 4, cudaMemcpyHostToDevice));
-    CK(p->cpy(p->d_be, be.data(), be.size() * 4, cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_bh, bh.get(), 3 * (size_t)n3 * 4, cudaMemcpyHostToDevice));
+    CK(p->cpy(p->d_be, be.get(), 3 * (size_t)n3 * 4, cudaMemcpyHostToDevice));
     CK(p->cpy(p->d_tab, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
     CK(p->cpy(p->d_pmask, pmask.data(), pmask.size(), cudaMemcpyHostToDevice));
     if (!hrec.empty())
@@ -639,10 +664,18 @@ extern "C" int smat_fdtd_create(const smat_fdtd_desc *d, void *stream, smat_fdtd
                 smat_fdtd_destroy(p);
                 return smat_fail(SMAT_EINVAL, "PEC cell %lld is not an ordinary ('n') cell", l);
             }
+    /* smat_coefficients fills every entry (its zero fill runs on the host
+     * worker threads, which also takes the first touch of the pages off the
+     * calling thread), so the arrays start uninitialised */
     const size_t nc = 3 * (size_t)(n3 + p->lnotn);
-    std::vector<double> Ah(nc), Bh(nc), Ae(nc), Be(nc);
+    std::unique_ptr<double[]> Ah(new (std::nothrow) double[nc]), Bh(new (std::nothrow) double[nc]),
+        Ae(new (std::nothrow) double[nc]), Be(new (std::nothrow) double[nc]);
+    if (!Ah || !Bh || !Ae || !Be) {
+        smat_fdtd_destroy(p);
+        return smat_fail(SMAT_ENOMEM, "create: out of host memory for the coefficients");
+    }
     rc = smat_coefficients(d->L, p->lnotn, d->sigma, d->mu, d->epsi, p->cont.data(), p->addr.data(), d->invtau_R,
-                           d->invtau_I, Ah.data(), Bh.data(), Ae.data(), Be.data());
+                           d->invtau_I, Ah.get(), Bh.get(), Ae.get(), Be.get());
     if (rc) {
         smat_fdtd_destroy(p);
         return rc;
@@ -651,8 +684,8 @@ extern "C" int smat_fdtd_create(const smat_fdtd_desc *d, void *stream, smat_fdtd
         for (long long l = 0; l < n3; l++)
             if (d->pec[l])
                 for (int c = 0; c < 3; c++) Ae[c + 3 * l] = Be[c + 3 * l] = 0.0;
-    rc = p->precision == SMAT_FP64 ? upload_f64(p, Ah.data(), Bh.data(), Ae.data(), Be.data())
-                                   : upload_f32(p, d, Ah.data(), Bh.data(), Ae.data(), Be.data());
+    rc = p->precision == SMAT_FP64 ? upload_f64(p, Ah.get(), Bh.get(), Ae.get(), Be.get())
+                                   : upload_f32(p, d, Ah.get(), Bh.get(), Ae.get(), Be.get());
     return finish_create(p, rc, out);
 }
 

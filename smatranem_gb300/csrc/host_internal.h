@@ -16,6 +16,17 @@ int host_expn(int N, double *out);
  * per step, stop-period*N steps (main :153-167). */
 int host_cw_schedule(int N, const int time_period[3], double *src, double *phase);
 
+/* Host worker threads for a loop over `work` cells: SMAT_HOST_THREADS when it
+ * is set to 1..HOST_MAX_THREADS, else one per online core (at most 16) for a
+ * million cells or more, else 1. */
+#define HOST_MAX_THREADS 64
+int host_threads(long long work);
+/* fn(ctx, lo, hi) over [0, n) cut into nt contiguous ranges, range 0 on the
+ * calling thread; returns when all have run.  A range whose thread cannot be
+ * created runs on the calling thread afterwards. */
+typedef void (*host_range_fn)(void *ctx, long long lo, long long hi);
+void host_parallel_for(long long n, int nt, host_range_fn fn, void *ctx);
+
 struct smat_fdtd_plan;
 int smat_fdtd_dft_count(const struct smat_fdtd_plan *plan, int *nfreq, int *nplanes);
 

@@ -8,14 +8,18 @@
  * bit-identical to the reference's on the same host.  That is what lets the
  * FP64 GPU path reproduce the reference's fields exactly.
  */
+#define _POSIX_C_SOURCE 200809L /* sysconf under -std=c11 */
+
 #include "smatran_fdtd.h"
 #include "host_internal.h"
 
 #include <complex.h>
 #include <float.h>
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #define TWO_PI_LD (2.0L * 3.1415926535897932384626433832795028841971L) /* constant.h:13-15 */
 #define TINY (10.0 * DBL_EPSILON)                                      /* constant.h:7 */
@@ -181,6 +185,58 @@ int smat_set_address(const int L[4], const double *sigma, const double *mu_, con
     return SMAT_OK;
 }
 
+/* ---- host worker threads ------------------------------------------------ */
+
+int host_threads(long long work)
+{
+    const char *e = getenv("SMAT_HOST_THREADS");
+    if (e && *e) {
+        const int n = atoi(e);
+        if (n >= 1 && n <= HOST_MAX_THREADS) return n;
+    }
+    if (work < (1LL << 20)) return 1;
+    const long c = sysconf(_SC_NPROCESSORS_ONLN);
+    return c < 1 ? 1 : c < 16 ? (int)c : 16;
+}
+
+struct host_range {
+    host_range_fn fn;
+    void *ctx;
+    long long lo, hi;
+};
+
+static void *host_range_main(void *a)
+{
+    const struct host_range *r = (const struct host_range *)a;
+    r->fn(r->ctx, r->lo, r->hi);
+    return NULL;
+}
+
+void host_parallel_for(long long n, int nt, host_range_fn fn, void *ctx)
+{
+    if (nt > HOST_MAX_THREADS) nt = HOST_MAX_THREADS;
+    if ((long long)nt > n) nt = (int)n;
+    if (nt <= 1) {
+        if (n > 0) fn(ctx, 0, n);
+        return;
+    }
+    pthread_t th[HOST_MAX_THREADS];
+    struct host_range r[HOST_MAX_THREADS];
+    int started[HOST_MAX_THREADS];
+    for (int t = 0; t < nt; t++) {
+        r[t].fn = fn;
+        r[t].ctx = ctx;
+        r[t].lo = n * t / nt;
+        r[t].hi = n * (t + 1) / nt;
+        started[t] = t > 0 && pthread_create(&th[t], NULL, host_range_main, &r[t]) == 0;
+    }
+    host_range_main(&r[0]);
+    /* a range whose thread could not be created runs here */
+    for (int t = 1; t < nt; t++)
+        if (started[t]) pthread_join(th[t], NULL);
+        else host_range_main(&r[t]);
+}
+
 /* ---- coefficients, main :106-143 ---------------------------------------- */
 
 /* lossless / lossy update factors with stretch sigma (main :118-127) */
@@ -197,33 +253,47 @@ static void ab_stable(double iR, double iI, double re, double im, double *A, dou
     *A = -(0.5 * re + iR * (0.5 * im / iI)) * *B;
 }
 
-int smat_coefficients(const int L[4], int Lnotn, const double *sigma, const double *mu_,
-                      const double *epsi_, const char *Cont, const int *address_notn,
-                      double iR, double iI, double *Ah, double *Bh, double *Ae, double *Be)
+struct coeff_job {
+    const int *L;
+    long n3;
+    size_t len; /* doubles per output array */
+    const double *sigma;
+    const double complex *mu, *ep;
+    const char *Cont;
+    const int *address_notn;
+    double iR, iI;
+    double *Ah, *Bh, *Ae, *Be;
+};
+
+static void coeff_zero(void *ctx, long long lo, long long hi)
 {
-    if (!dims_ok(L) || Lnotn < 0 || !sigma || !mu_ || !epsi_ || !Cont || !address_notn || !Ah || !Bh ||
-        !Ae || !Be)
-        return smat_fail(SMAT_EINVAL, "coefficients: bad arguments");
-    const double complex *mu = (const double complex *)mu_;
-    const double complex *ep = (const double complex *)epsi_;
-    const long n3 = (long)L[0] * L[1] * L[2];
-    const size_t bytes = sizeof(double) * 3 * (size_t)(n3 + Lnotn);
-    memset(Ah, 0, bytes);
-    memset(Bh, 0, bytes);
-    memset(Ae, 0, bytes);
-    memset(Be, 0, bytes);
+    const struct coeff_job *j = (const struct coeff_job *)ctx;
+    double *out[4] = {j->Ah, j->Bh, j->Ae, j->Be};
+    for (int w = 0; w < 4; w++) memset(out[w] + lo, 0, sizeof(double) * (size_t)(hi - lo));
+}
+
+/* the cells of planes [z0, z1): every cell writes its own three main entries
+ * and the aux entries of its own address */
+static void coeff_planes(void *ctx, long long z0, long long z1)
+{
+    const struct coeff_job *J = (const struct coeff_job *)ctx;
+    const int *L = J->L;
+    const long n3 = J->n3;
+    const double iR = J->iR, iI = J->iI;
+    const double *sigma = J->sigma;
+    double *Ah = J->Ah, *Bh = J->Bh, *Ae = J->Ae, *Be = J->Be;
     const int off[3] = {0, 2 * L[0], 2 * (L[0] + L[1])};
-    long l = 0;
-    for (int j2 = 0; j2 < L[2]; j2++)
+    long l = (long)z0 * L[0] * L[1];
+    for (int j2 = (int)z0; j2 < (int)z1; j2++)
         for (int j1 = 0; j1 < L[1]; j1++)
             for (int j0 = 0; j0 < L[0]; j0++, l++) {
                 const int jj[3] = {j0, j1, j2};
-                const char k = Cont[l];
+                const char k = J->Cont[l];
                 for (int c = 0; c < 3; c++) {
                     const long m = c + 3 * l;
-                    const long x = c + 3L * address_notn[l] + 3 * n3;
-                    const double mr = creal(mu[m]), mi = cimag(mu[m]);
-                    const double er = creal(ep[m]), ei = cimag(ep[m]);
+                    const long x = c + 3L * J->address_notn[l] + 3 * n3;
+                    const double mr = creal(J->mu[m]), mi = cimag(J->mu[m]);
+                    const double er = creal(J->ep[m]), ei = cimag(J->ep[m]);
                     const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
                     ab_split(iR, iI, mr, mi, sigma[off[a1] + 0 + 2 * jj[a1]], &Ah[m], &Bh[m]);
                     ab_split(iR, iI, er, ei, sigma[off[a1] + 1 + 2 * jj[a1]], &Ae[m], &Be[m]);
@@ -235,6 +305,36 @@ int smat_coefficients(const int L[4], int Lnotn, const double *sigma, const doub
                     if (k == 'h' || k == 'b') ab_stable(iR, iI, mr, mi, &Ah[x], &Bh[x]);
                 }
             }
+}
+
+int smat_coefficients(const int L[4], int Lnotn, const double *sigma, const double *mu_,
+                      const double *epsi_, const char *Cont, const int *address_notn,
+                      double iR, double iI, double *Ah, double *Bh, double *Ae, double *Be)
+{
+    if (!dims_ok(L) || Lnotn < 0 || !sigma || !mu_ || !epsi_ || !Cont || !address_notn || !Ah || !Bh ||
+        !Ae || !Be)
+        return smat_fail(SMAT_EINVAL, "coefficients: bad arguments");
+    struct coeff_job J;
+    J.L = L;
+    J.n3 = (long)L[0] * L[1] * L[2];
+    J.len = 3 * (size_t)(J.n3 + Lnotn);
+    J.sigma = sigma;
+    J.mu = (const double complex *)mu_;
+    J.ep = (const double complex *)epsi_;
+    J.Cont = Cont;
+    J.address_notn = address_notn;
+    J.iR = iR;
+    J.iI = iI;
+    J.Ah = Ah;
+    J.Bh = Bh;
+    J.Ae = Ae;
+    J.Be = Be;
+    /* every entry is a pure function of its own cell, so any split of the
+     * planes over threads gives the same bits; the zero fill finishes first
+     * because a thread's aux entries may lie in another thread's fill range */
+    const int nt = host_threads(J.n3);
+    host_parallel_for((long long)J.len, nt, coeff_zero, &J);
+    host_parallel_for(L[2], nt, coeff_planes, &J);
     return SMAT_OK;
 }
 

@@ -456,6 +456,29 @@ def test_row_fused_record_cells_bit_identical(built, case):
                 assert np.array_equal(a, b_), tuning
 
 
+def test_fp32_plan_independent_of_host_threads(built, monkeypatch):
+    """FP32 plan creation packs the coefficients and numbers the record cells
+    on host worker threads: plans made with 1, 3 and 16 threads step to the
+    same bits (every record kind: metal, lossy, PEC, lossy split cells)."""
+    from smatranem_gb300 import workloads as W
+    L, seed, kw, iBTIin = (40, 17, 19, 3), 46, dict(pml=(4, 4, 4), metals=0.03, lossy=0.05, pec=0.02), (5, 13, 7, 1)
+    s = W.random_structure(L, seed=seed, **kw)
+    pr = W.prepare(s)
+    rng = np.random.default_rng(seed)
+    cells = np.flatnonzero(np.asarray(pr.cont).view(np.uint8) == ord("a"))
+    pick = rng.choice(cells, size=cells.size // 5, replace=False)
+    for c in range(3):
+        pr.epsi[3 * pick + c] += 1j * np.abs(pr.epsi[3 * pick + c].real) * rng.uniform(0.01, 0.3, pick.size)
+    runs = []
+    for nt in (1, 3, 16):
+        monkeypatch.setenv("SMAT_HOST_THREADS", str(nt))
+        runs.append(_run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), 9))
+    for got in runs[1:]:
+        for rb, gb in zip(runs[0], got):
+            for a, b_ in zip(rb, gb):
+                assert np.array_equal(a, b_)
+
+
 def test_row_fused_refuses_metal_cells(built):
     """Kernel 6 has no stable-form path: a plan with metal ('h', 'e', 'b')
     cells is refused."""

@@ -60,3 +60,22 @@ def test_precompute_errors(built):
     sig[2 * 8 + 0] = 3.0
     with pytest.raises(fdtd.FdtdError):
         fdtd.remove_sigma(L, mu, ep, sig)
+
+
+def test_coefficients_independent_of_host_threads(built, monkeypatch):
+    """The coefficient build splits its planes over host worker threads: the
+    arrays are the same bits for every thread count (every cell class,
+    ragged plane splits)."""
+    from smatranem_gb300 import fdtd
+    from smatranem_gb300 import workloads as W
+    s = W.random_structure((23, 17, 29, 2), seed=7, pml=(3, 3, 4), metals=0.04, lossy=0.05, pec=0.02)
+    pr = W.prepare(s)
+    out = {}
+    for nt in (1, 2, 5, 29, 64):
+        monkeypatch.setenv("SMAT_HOST_THREADS", str(nt))
+        out[nt] = fdtd.coefficients(s.L, pr.lnotn, pr.sigma, pr.mu, pr.epsi, pr.cont, pr.addr, pr.invtau_R,
+                                    pr.invtau_I)
+    assert set(np.unique(pr.cont)) >= {ord(c) for c in "naheb"}
+    for nt in (2, 5, 29, 64):
+        for a, b in zip(out[1], out[nt]):
+            assert np.array_equal(a, b), nt
