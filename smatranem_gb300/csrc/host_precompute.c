@@ -137,54 +137,6 @@ int smat_remove_sigma(const int L[4], double *mu_, double *epsi_, const double *
     return rc;
 }
 
-/* ---- set_address :188-233 ---------------------------------------------- */
-
-int smat_set_address(const int L[4], const double *sigma, const double *mu_, const double *epsi_,
-                     char *Cont, int *Lnotn, int *address_notn)
-{
-    if (!dims_ok(L) || !sigma || !mu_ || !epsi_ || !Cont || !Lnotn || !address_notn)
-        return smat_fail(SMAT_EINVAL, "set_address: bad arguments");
-    const double complex *mu = (const double complex *)mu_;
-    const double complex *ep = (const double complex *)epsi_;
-    const int off[3] = {0, 2 * L[0], 2 * (L[0] + L[1])};
-    const long n3 = (long)L[0] * L[1] * L[2];
-    /* a cell is split ('a') when any of its six sub-point sigmas is nonzero */
-    unsigned char *pml[3];
-    for (int a = 0; a < 3; a++) {
-        pml[a] = malloc(L[a]);
-        if (!pml[a]) {
-            for (int b = 0; b < a; b++) free(pml[b]);
-            return smat_fail(SMAT_ENOMEM, "set_address: out of host memory");
-        }
-        for (int j = 0; j < L[a]; j++)
-            pml[a][j] = fabs(sigma[off[a] + 2 * j]) > TINY || fabs(sigma[off[a] + 1 + 2 * j]) > TINY;
-    }
-    int count = 0;
-    long l = 0;
-    for (int j2 = 0; j2 < L[2]; j2++)
-        for (int j1 = 0; j1 < L[1]; j1++)
-            for (int j0 = 0; j0 < L[0]; j0++, l++) {
-                char k = (pml[0][j0] || pml[1][j1] || pml[2][j2]) ? 'a' : 'n';
-                /* lossy media override, the last component deciding (:200-210) */
-                for (int c = 0; c < 3; c++) {
-                    /* with a zero imaginary part tan(carg()) is 0 or +-1.2e-16,
-                     * never below -TINY: skip the trigonometry (same answer) */
-                    const int m = cimag(mu[c + 3 * l]) != 0.0 && tan(carg(mu[c + 3 * l])) < -TINY;
-                    const int e = cimag(ep[c + 3 * l]) != 0.0 && tan(carg(ep[c + 3 * l])) < -TINY;
-                    if (m && e) k = 'b';
-                    else if (m) k = 'h';
-                    else if (e) k = 'e';
-                }
-                Cont[l] = k;
-                if (k != 'n') count++;
-            }
-    for (int a = 0; a < 3; a++) free(pml[a]);
-    int next = 0;
-    for (l = 0; l < n3; l++) address_notn[l] = Cont[l] != 'n' ? next++ : count;
-    *Lnotn = count;
-    return SMAT_OK;
-}
-
 /* ---- host worker threads ------------------------------------------------ */
 
 int host_threads(long long work)
@@ -235,6 +187,112 @@ void host_parallel_for(long long n, int nt, host_range_fn fn, void *ctx)
     for (int t = 1; t < nt; t++)
         if (started[t]) pthread_join(th[t], NULL);
         else host_range_main(&r[t]);
+}
+
+/* ---- set_address :188-233 ---------------------------------------------- */
+
+struct address_job {
+    const int *L;
+    const double complex *mu, *ep;
+    const unsigned char *pml[3];
+    char *Cont;
+    int *address_notn;
+    int nrun;
+    int *count; /* [nrun]: non-'n' cells of each run, then the first address of each */
+    int total;
+};
+
+/* run t: planes [z0, z1) */
+static void address_run(const struct address_job *J, long long t, int *z0, int *z1)
+{
+    *z0 = (int)(J->L[2] * t / J->nrun);
+    *z1 = (int)(J->L[2] * (t + 1) / J->nrun);
+}
+
+/* classify the cells of runs [t0, t1) and count the split ones */
+static void address_classify(void *ctx, long long t0, long long t1)
+{
+    struct address_job *J = (struct address_job *)ctx;
+    const int *L = J->L;
+    for (long long t = t0; t < t1; t++) {
+        int z0, z1;
+        address_run(J, t, &z0, &z1);
+        long l = (long)z0 * L[0] * L[1];
+        int count = 0;
+        for (int j2 = z0; j2 < z1; j2++)
+            for (int j1 = 0; j1 < L[1]; j1++)
+                for (int j0 = 0; j0 < L[0]; j0++, l++) {
+                    char k = (J->pml[0][j0] || J->pml[1][j1] || J->pml[2][j2]) ? 'a' : 'n';
+                    /* lossy media override, the last component deciding (:200-210) */
+                    for (int c = 0; c < 3; c++) {
+                        /* with a zero imaginary part tan(carg()) is 0 or +-1.2e-16,
+                         * never below -TINY: skip the trigonometry (same answer) */
+                        const int m = cimag(J->mu[c + 3 * l]) != 0.0 && tan(carg(J->mu[c + 3 * l])) < -TINY;
+                        const int e = cimag(J->ep[c + 3 * l]) != 0.0 && tan(carg(J->ep[c + 3 * l])) < -TINY;
+                        if (m && e) k = 'b';
+                        else if (m) k = 'h';
+                        else if (e) k = 'e';
+                    }
+                    J->Cont[l] = k;
+                    if (k != 'n') count++;
+                }
+        J->count[t] = count;
+    }
+}
+
+/* addresses in cell order: a run starts at the split cells of the runs before it */
+static void address_number(void *ctx, long long t0, long long t1)
+{
+    struct address_job *J = (struct address_job *)ctx;
+    for (long long t = t0; t < t1; t++) {
+        int z0, z1;
+        address_run(J, t, &z0, &z1);
+        const long pl = (long)J->L[0] * J->L[1];
+        int next = J->count[t];
+        for (long l = z0 * pl; l < z1 * pl; l++) J->address_notn[l] = J->Cont[l] != 'n' ? next++ : J->total;
+    }
+}
+
+int smat_set_address(const int L[4], const double *sigma, const double *mu_, const double *epsi_,
+                     char *Cont, int *Lnotn, int *address_notn)
+{
+    if (!dims_ok(L) || !sigma || !mu_ || !epsi_ || !Cont || !Lnotn || !address_notn)
+        return smat_fail(SMAT_EINVAL, "set_address: bad arguments");
+    const int off[3] = {0, 2 * L[0], 2 * (L[0] + L[1])};
+    const long n3 = (long)L[0] * L[1] * L[2];
+    /* a cell is split ('a') when any of its six sub-point sigmas is nonzero */
+    unsigned char *pml[3];
+    for (int a = 0; a < 3; a++) {
+        pml[a] = malloc(L[a]);
+        if (!pml[a]) {
+            for (int b = 0; b < a; b++) free(pml[b]);
+            return smat_fail(SMAT_ENOMEM, "set_address: out of host memory");
+        }
+        for (int j = 0; j < L[a]; j++)
+            pml[a][j] = fabs(sigma[off[a] + 2 * j]) > TINY || fabs(sigma[off[a] + 1 + 2 * j]) > TINY;
+    }
+    struct address_job J;
+    J.L = L;
+    J.mu = (const double complex *)mu_;
+    J.ep = (const double complex *)epsi_;
+    for (int a = 0; a < 3; a++) J.pml[a] = pml[a];
+    J.Cont = Cont;
+    J.address_notn = address_notn;
+    J.nrun = host_threads(n3);
+    if (J.nrun > L[2]) J.nrun = L[2];
+    int count[HOST_MAX_THREADS];
+    J.count = count;
+    host_parallel_for(J.nrun, J.nrun, address_classify, &J);
+    J.total = 0;
+    for (int t = 0; t < J.nrun; t++) {
+        const int c = count[t];
+        count[t] = J.total;
+        J.total += c;
+    }
+    host_parallel_for(J.nrun, J.nrun, address_number, &J);
+    for (int a = 0; a < 3; a++) free(pml[a]);
+    *Lnotn = J.total;
+    return SMAT_OK;
 }
 
 /* ---- coefficients, main :106-143 ---------------------------------------- */

@@ -62,10 +62,11 @@ def test_precompute_errors(built):
         fdtd.remove_sigma(L, mu, ep, sig)
 
 
-def test_coefficients_independent_of_host_threads(built, monkeypatch):
-    """The coefficient build splits its planes over host worker threads: the
-    arrays are the same bits for every thread count (every cell class,
-    ragged plane splits)."""
+def test_precompute_independent_of_host_threads(built, monkeypatch):
+    """set_address and the coefficient build split their planes over host
+    worker threads: cell classes, addresses and coefficients are the same
+    bits for every thread count (every cell class, ragged plane splits, more
+    threads than planes)."""
     from smatranem_gb300 import fdtd
     from smatranem_gb300 import workloads as W
     s = W.random_structure((23, 17, 29, 2), seed=7, pml=(3, 3, 4), metals=0.04, lossy=0.05, pec=0.02)
@@ -73,9 +74,12 @@ def test_coefficients_independent_of_host_threads(built, monkeypatch):
     out = {}
     for nt in (1, 2, 5, 29, 64):
         monkeypatch.setenv("SMAT_HOST_THREADS", str(nt))
-        out[nt] = fdtd.coefficients(s.L, pr.lnotn, pr.sigma, pr.mu, pr.epsi, pr.cont, pr.addr, pr.invtau_R,
-                                    pr.invtau_I)
-    assert set(np.unique(pr.cont)) >= {ord(c) for c in "naheb"}
+        cont, addr, ln = fdtd.set_address(s.L, pr.sigma, pr.mu, pr.epsi)
+        coef = fdtd.coefficients(s.L, ln, pr.sigma, pr.mu, pr.epsi, cont, addr, pr.invtau_R, pr.invtau_I)
+        out[nt] = (cont, addr, ln, coef)
+    assert set(np.unique(out[1][0])) >= {ord(c) for c in "naheb"}
     for nt in (2, 5, 29, 64):
-        for a, b in zip(out[1], out[nt]):
+        assert np.array_equal(out[1][0], out[nt][0]) and np.array_equal(out[1][1], out[nt][1])
+        assert out[1][2] == out[nt][2]
+        for a, b in zip(out[1][3], out[nt][3]):
             assert np.array_equal(a, b), nt
