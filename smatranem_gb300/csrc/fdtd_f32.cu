@@ -865,16 +865,18 @@ __device__ __forceinline__ double widen(float f)
     return e == 0u ? 0.0 : __hiloint2double((int)hi, (int)lo);
 }
 
-/* CMAX: the window length rounded up to a multiple of 8 (a full ring: 32,
- * no per-sample predicate); a shorter window at the end of a run skips the
- * samples past its length, so its cost follows its length */
-template <int CMAX>
+/* CMAX: the window length rounded up to a multiple of 8; FULL: the window is
+ * the whole ring (CMAX = RING_MAX samples, no per-sample predicate).  A
+ * shorter window at the end of a run skips the samples past its length, so
+ * its cost follows its length; only a window of exactly RING_MAX samples may
+ * take FULL (the phase table in shared memory holds count_rt samples). */
+template <int CMAX, bool FULL>
 __global__ void __launch_bounds__(128, 6) k_flush32(const P32 p, const int rel_end, const int count_rt)
 {
     /* [nfreq][count] {hi re, hi im, lo re, lo im} of this block's half (H or E
      * phases) */
     extern __shared__ float4 sph[];
-    constexpr bool FULL = CMAX == RING_MAX;
+    static_assert(!FULL || CMAX == RING_MAX, "a full window is the whole ring");
     const int count = FULL ? RING_MAX : count_rt;
     const Dft &d = p.d;
     const int k0 = *p.s.base + rel_end - count;
@@ -995,15 +997,17 @@ void launch_e32v(const P32 &p, int rel, int by, int mb, int z0, int z1, const in
 
 void launch_flush32(const P32 &p, int rel_end, int count, cudaStream_t st)
 {
-    if (p.d.nfreq <= 0 || p.d.nq <= 0 || count <= 0) return;
+    /* callers flush at least once every RING_MAX steps (the ring's length) */
+    if (p.d.nfreq <= 0 || p.d.nq <= 0 || count <= 0 || count > RING_MAX) return;
     dim3 blk(128), grd((p.g.pl + 127) / 128, p.d.nq * 4, p.batch);
     const size_t sm = sizeof(float4) * (size_t)count * p.d.nfreq;
     static_assert(RING_MAX == 32, "flush instantiations: windows rounded up to 8, 16, 24, 32");
     const int cmax = (count + 7) / 8 * 8;
-    const void *fn = cmax == 8    ? (const void *)k_flush32<8>
-                     : cmax == 16 ? (const void *)k_flush32<16>
-                     : cmax == 24 ? (const void *)k_flush32<24>
-                                  : (const void *)k_flush32<32>;
+    const void *fn = count == RING_MAX ? (const void *)k_flush32<32, true>
+                     : cmax == 8       ? (const void *)k_flush32<8, false>
+                     : cmax == 16      ? (const void *)k_flush32<16, false>
+                     : cmax == 24      ? (const void *)k_flush32<24, false>
+                                       : (const void *)k_flush32<32, false>;
     if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     void *args[] = {(void *)&p, (void *)&rel_end, (void *)&count};
     cudaLaunchKernel(fn, grd, blk, args, sm, st);

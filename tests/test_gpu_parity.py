@@ -696,16 +696,23 @@ def test_checkpoint_and_resume(built, tmp_path, precision):
             p.load_state(path)
 
 
-def test_fp32_dft_flush_is_compensated(built):
+# runs of the FP32 plan: each is cut into windows of 32 steps from its start,
+# the last one partial (6, 29, 31, 25 and 8 steps: every flush instantiation)
+FLUSH_RUNS = [[(0, 70)], [(0, 29), (29, 90)], [(0, 31), (31, 56), (56, 81), (81, 89)]]
+
+
+@pytest.mark.parametrize("runs", FLUSH_RUNS)
+def test_fp32_dft_flush_is_compensated(built, runs):
     """The FP32 running DFT (ring of field samples folded into FP64
     accumulators, the reference's DFT of :318-328 on FP32 samples) is summed
     in compensated FP32: against the exact FP64 sum of the same samples with
     the same FP64 phases, its error stays under 2 units of 2^-24 of the
     summed magnitudes and its RMS under half that of a plain FP32 sum of the
     window (FP32 phases, one fused multiply-add per sample, as an
-    uncompensated flush would do).  The samples come from a twin plan stepped one step per run (the
-    field updates do not depend on how steps are grouped); its monitor planes
-    hold no split cell, so a sample is the cell's field itself."""
+    uncompensated flush would do), for full and partial windows of every
+    length class.  The samples come from a twin plan stepped one step per run
+    (the field updates do not depend on how steps are grouped); its monitor
+    planes hold no split cell, so a sample is the cell's field itself."""
     from smatranem_gb300 import workloads as W
     f = _fdtd()
     L = (16, 12, 24, 2)
@@ -713,7 +720,8 @@ def test_fp32_dft_flush_is_compensated(built):
     pr = W.prepare(s)
     planes = (7, 15)
     iBTIin = (7, 15, 10, 1)
-    nsteps = 70  # flush windows of 32, 32 and 6 steps
+    nsteps = runs[-1][1]
+    windows = [(w0, min(w0 + 32, r1)) for r0, r1 in runs for w0 in range(r0, r1, 32)]
     src, ph = W.pulse_schedule(nsteps, pr.dt, lams_um=[1.3, 1.55, 1.9])
     H0, E0 = W.random_fields(s.n3, pr.lnotn, seed=3, scale=1e-2)
     Hinc, Einc = W.random_incident(L[0] * L[1], seed=4)
@@ -728,7 +736,8 @@ def test_fp32_dft_flush_is_compensated(built):
 
     pl = L[0] * L[1]
     with plan() as a, plan() as b:
-        a.run(0, nsteps)
+        for r0, r1 in runs:
+            a.run(r0, r1)
         got = np.array([[a.get_dft(0, fi, q) for q in range(2)] for fi in range(3)])  # [f][q][Hx,Hy,Ex,Ey][px]
         samples = np.zeros((nsteps, 2, 4, pl))
         for k in range(nsteps):
@@ -744,7 +753,7 @@ def test_fp32_dft_flush_is_compensated(built):
     exact = np.zeros((3, 2, 4, pl), np.complex128)
     plain = np.zeros_like(exact)
     scale = np.zeros((3, 2, 4, pl))
-    for w0, w1 in ((0, 32), (32, 64), (64, 70)):
+    for w0, w1 in windows:
         for fi in range(3):
             for v in range(4):
                 z = phz[w0:w1, fi, v // 2]
