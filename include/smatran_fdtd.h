@@ -270,8 +270,8 @@ int smat_fdtd_group_destroy(smat_fdtd_group *group);
  * smat_fdtd_set_tuning: the whole-row fused step or the sweeps) on the
  * member's own stream, forked from the group's stream and joined back, so the
  * members run side by side; mode 3: one persistent launch of the whole-row
- * fused step per step for every member (members without stable-form metal
- * cells, at most one excitation per resident CTA in all): the
+ * fused step per step for every member (at most one excitation per
+ * resident CTA in all; members with metal cells add their second launch): the
  * resident CTAs are shared out in groups of one CTA per excitation, each
  * member's groups marching its own persistent schedule.  All are captured as
  * one graph per 32 steps.  block_y: rows per sweep block, 1..4 (modes 0, 1);
@@ -367,9 +367,11 @@ int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double
  *             along z through z_chunk planes (0: persistent CTAs), four cells
  *             a thread, the next plane's inputs staged by cp.async;
  *             ctas_per_sm is its register bound (1..3 resident CTAs per SM);
- *             slots is not used; for plans with L0 % 4 == 0 and no
- *             stable-form metal cells (lossy and PEC ordinary cells and lossy
- *             split cells run an out-of-line record update).
+ *             slots is not used; for plans with L0 % 4 == 0 (lossy and PEC
+ *             ordinary cells, lossy split cells and metal cells run an
+ *             out-of-line record update; plans with metal cells add a second,
+ *             small launch per step for their stable-form E update and their
+ *             monitor samples).
  * Other kernel codes are refused (SMAT_EINVAL).  Results are bit-identical
  * across configurations. */
 int smat_fdtd_set_tuning(smat_fdtd_plan *plan, int kernel, int tile_y, int z_chunk, int ctas_per_sm,

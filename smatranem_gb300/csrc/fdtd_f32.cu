@@ -30,48 +30,6 @@
 
 namespace smat {
 
-struct Stn32 {
-    long long o[3];
-    float f[3]; /* boundary factor iBc at the wrapped neighbour, else 1 */
-};
-
-__device__ __forceinline__ Stn32 make_stn32(const Geo &g, int j0, int j1, int j2, bool fwd)
-{
-    Stn32 st;
-    const int j[3] = {j0, j1, j2};
-    const int L[3] = {g.L0, g.L1, g.L2};
-    long long stride = 1;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const bool edge = fwd ? (j[a] + 1 == L[a]) : (j[a] == 0);
-        const int jn = fwd ? (edge ? 0 : j[a] + 1) : (edge ? L[a] - 1 : j[a] - 1);
-        st.o[a] = (long long)(jn - j[a]) * stride;
-        st.f[a] = edge ? (float)g.bc[a] : 1.0f;
-        stride *= L[a];
-    }
-    return st;
-}
-
-/* Half curls of a field given by an accessor get(c, offset). */
-template <bool FWD, class Get>
-__device__ __forceinline__ void curl32(const Get &get, const Stn32 &st, float pl[3], float mi[3])
-{
-    const float here[3] = {get(0, 0), get(1, 0), get(2, 0)};
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-        const float n2 = st.f[a1] * get(a2, st.o[a1]);
-        const float n1 = st.f[a2] * get(a1, st.o[a2]);
-        if (!FWD) {
-            pl[c] = here[a2] - n2;
-            mi[c] = n1 - here[a1];
-        } else {
-            pl[c] = n2 - here[a2];
-            mi[c] = here[a1] - n1;
-        }
-    }
-}
-
 __device__ __forceinline__ double sheet32(const Src &s, int pl, int b, int k, bool efield, int v, int p)
 {
     if (s.xsrc) return s.xsrc[(efield ? 2 * pl : 0) + v + 2 * p];

@@ -103,9 +103,6 @@ int setup_persistent(smat_fdtd_group *g, int threads)
     int used = 0;
     for (int i = 0; i < n; i++) {
         const smat_fdtd_plan *p = g->m[i];
-        if (p->nrec_metal > 0)
-            return smat_fail(SMAT_EINVAL, "group_set_tuning: mode 3 needs members without stable-form metal "
-                                          "cells (member %d has them)", i);
         const int nq = p->L[0] / 4;
         int t = 0;
         for (int c = 16; c >= 1 && !t; c--)
@@ -192,6 +189,11 @@ void enqueue_group(smat_fdtd_group *g, int rel0, int n)
                 r.nitems = g->groups3[j] * p->batch;
             }
             launch_row32_group(G, rel0 + i, g->threads3, g->grid3, g->smem3, g->rec3, g->stream);
+            /* members with metal cells: their second launch, before the sets swap */
+            for (int j = 0; j < G.n; j++) {
+                const smat_fdtd_plan *p = g->m[j];
+                launch_row_metal(G.r[j], rel0 + i, p->d_hmetal, p->nhmetal, p->d_emetal, p->nemetal, g->stream);
+            }
             for (smat_fdtd_plan *p : g->m) p->cur ^= 1;
         }
     } else if (g->mode == 0) {

@@ -171,7 +171,7 @@ struct Row32 {
     int ngroups;                /* persistent: groups of one CTA per excitation */
     const int *qorder;          /* [L0/4]: quads whose x index lies in a PML, then the others */
     int nqp;                    /* how many of the first kind */
-    int has_rec;                /* the plan has record cells (lossy or PEC cells; no stable-form metal) */
+    int has_rec;                /* the plan has record cells (lossy, PEC or metal cells) */
 };
 
 /* Several plans in one persistent launch of form 6 (a group's form 3): CTAs
@@ -185,6 +185,51 @@ struct RowGroup32 {
     Row32 r[MAX_GROUP];
 };
 
+
+/* The curl stencil of a cell: offsets of its forward (fwd) or backward
+ * neighbour along each axis, wrapped at the grid's faces, and the boundary
+ * factor iBc at a wrapped neighbour (else 1). */
+struct Stn32 {
+    long long o[3];
+    float f[3];
+};
+
+__device__ __forceinline__ Stn32 make_stn32(const Geo &g, int j0, int j1, int j2, bool fwd)
+{
+    Stn32 st;
+    const int j[3] = {j0, j1, j2};
+    const int L[3] = {g.L0, g.L1, g.L2};
+    long long stride = 1;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const bool edge = fwd ? (j[a] + 1 == L[a]) : (j[a] == 0);
+        const int jn = fwd ? (edge ? 0 : j[a] + 1) : (edge ? L[a] - 1 : j[a] - 1);
+        st.o[a] = (long long)(jn - j[a]) * stride;
+        st.f[a] = edge ? (float)g.bc[a] : 1.0f;
+        stride *= L[a];
+    }
+    return st;
+}
+
+/* Half curls of a field given by an accessor get(c, offset). */
+template <bool FWD, class Get>
+__device__ __forceinline__ void curl32(const Get &get, const Stn32 &st, float pl[3], float mi[3])
+{
+    const float here[3] = {get(0, 0), get(1, 0), get(2, 0)};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+        const float n2 = st.f[a1] * get(a2, st.o[a1]);
+        const float n1 = st.f[a2] * get(a1, st.o[a2]);
+        if (!FWD) {
+            pl[c] = here[a2] - n2;
+            mi[c] = n1 - here[a1];
+        } else {
+            pl[c] = n2 - here[a2];
+            mi[c] = here[a1] - n1;
+        }
+    }
+}
 
 /* launchers (one translation unit per precision) */
 void launch_h64(const P64 &p, int rel, cudaStream_t st);
@@ -206,6 +251,9 @@ int row32_threads(int L0, int ty);
 size_t row32_smem(int L0, int ty, int zc);
 int row32_max_ctas_per_sm(int L0, int ty, int mb, int zc, bool rec);
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st);
+/* the metal cells of a form-6 step, after it: nh H cells, ne E cells (lists
+ * of cell indices with stable-form or frozen records) */
+void launch_row_metal(const Row32 &r, int rel, const int *hcells, int nh, const int *ecells, int ne, cudaStream_t st);
 /* the grouped launch, CTAs of `threads` = 384 (one per SM) or 192 (two per
  * SM): its resident CTAs per SM at smem bytes of shared memory (0: does not
  * fit), and the launch itself */

@@ -161,10 +161,7 @@ void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp)
             launch_dft64(q, rel0 + i, p->stream);
         }
     } else if (p->fused == 6) {
-        for (int i = 0; i < n; i++) {
-            launch_row32(make_row(p, xp), rel0 + i, p->ctas_per_sm, p->stream);
-            p->cur ^= 1;
-        }
+        for (int i = 0; i < n; i++) launch_row_step(p, xp, rel0 + i, p->stream);
         launch_flush32(make_p32(p, xp), rel0 + n, n, p->stream);
     } else {
         const P32 q = make_p32(p, xp);
@@ -180,11 +177,18 @@ void enqueue_update(smat_fdtd_plan *p, int rel, cudaStream_t st)
 {
     if (p->precision != SMAT_FP32) return;
     if (p->fused == 6) {
-        launch_row32(make_row(p, false), rel, p->ctas_per_sm, st);
-        p->cur ^= 1;
+        launch_row_step(p, false, rel, st);
         return;
     }
     sweep_step(p, make_p32(p, false), rel, st);
+}
+
+void launch_row_step(smat_fdtd_plan *p, bool xp, int rel, cudaStream_t st)
+{
+    const Row32 r = make_row(p, xp);
+    launch_row32(r, rel, p->ctas_per_sm, st);
+    launch_row_metal(r, rel, p->d_hmetal, p->nhmetal, p->d_emetal, p->nemetal, st);
+    p->cur ^= 1;
 }
 
 /* One FP32 step as two sweeps (kernels 0 and 2), in z-chunks of szc planes:
@@ -581,12 +585,29 @@ int upload_f32(smat_fdtd_plan *p, const smat_fdtd_desc *d, const double *Ah, con
         CK(p->cpy(p->d_hgen, hgen.data(), hgen.size() * sizeof(int), cudaMemcpyHostToDevice));
     if (!egen.empty())
         CK(p->cpy(p->d_egen, egen.data(), egen.size() * sizeof(int), cudaMemcpyHostToDevice));
-    /* record kinds kernel 6 can or cannot take */
-    for (int side = 0; side < 2; side++)
-        for (const Rec32 &r : side ? erec : hrec) {
-            if (r.kind == RK_STABLE || r.kind == RK_FROZEN) p->nrec_metal++;
-            if (r.kind == RK_A) p->nrec_split++;
+    /* record kinds; the cells of metal records (stable-form or frozen
+     * components), which kernel 6 finishes in a second launch */
+    std::vector<int> metal[2];
+    for (int side = 0; side < 2; side++) {
+        const std::vector<Rec32> &recs = side ? erec : hrec;
+        const std::vector<int> &gen = side ? egen : hgen;
+        for (size_t i = 0; i < recs.size(); i++) {
+            const int kind = recs[i].kind;
+            if (kind == RK_STABLE || kind == RK_FROZEN) {
+                p->nrec_metal++;
+                metal[side].push_back(gen[i]);
+            }
+            if (kind == RK_A) p->nrec_split++;
         }
+    }
+    p->nhmetal = (int)metal[0].size();
+    p->nemetal = (int)metal[1].size();
+    if ((rc = p->alloc(&p->d_hmetal, metal[0].size() + 1)) || (rc = p->alloc(&p->d_emetal, metal[1].size() + 1)))
+        return rc;
+    if (!metal[0].empty())
+        CK(p->cpy(p->d_hmetal, metal[0].data(), metal[0].size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!metal[1].empty())
+        CK(p->cpy(p->d_emetal, metal[1].data(), metal[1].size() * sizeof(int), cudaMemcpyHostToDevice));
     if (p->L[0] % 4 == 0) {
         p->fused = 2; /* default: vectorised sweeps where they apply */
         p->by32 = 2;
@@ -1015,8 +1036,7 @@ extern "C" int smat_fdtd_time_kernels(smat_fdtd_plan *p, int k_begin, int nsteps
         CK(cudaEventRecord(ev[0], p->stream));
         if (p->precision == SMAT_FP64) launch_h64(q64, i, p->stream);
         else if (p->fused == 6) {
-            launch_row32(make_row(p, false), i, p->ctas_per_sm, p->stream);
-            p->cur ^= 1;
+            launch_row_step(p, false, i, p->stream);
         } else if (p->szc > 0 && p->szc < p->L[2]) {
             sweep_step(p, q32, i, p->stream); /* chunked sweeps: the whole step in ms[0] */
         } else if (p->fused == 2) {
@@ -1062,9 +1082,7 @@ extern "C" int smat_fdtd_set_tuning(smat_fdtd_plan *p, int fused, int tile_y, in
                                       "rows)");
     if (fused == 6) {
         /* whole-row fused step: tile_y rows per CTA, z chunks, ctas_per_sm = register bound 1..3 */
-        if (p->L[0] % 4 != 0 || p->nrec_metal > 0)
-            return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 needs L0 %% 4 == 0 and a plan without stable-form "
-                                          "metal cells");
+        if (p->L[0] % 4 != 0) return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 needs L0 %% 4 == 0");
         if (tile_y < 1 || tile_y > 16 || z_chunk < 0 || ctas_per_sm < 1 || ctas_per_sm > 3)
             return smat_fail(SMAT_EINVAL, "set_tuning: kernel 6 takes tile_y in 1..16, z_chunk >= 0 (0: persistent "
                                           "CTAs) and ctas_per_sm (register bound) 1..3");
@@ -1132,8 +1150,8 @@ extern "C" int smat_fdtd_autotune(smat_fdtd_plan *p, int nsteps, int best[5], do
                 if (zc > 0 && zc < L2) cands.push_back({2, by, zc, 5, 4});
         cands.push_back({2, 4, 0, 5, 4});
     }
-    /* whole-row fused step (plans without stable-form metal cells) */
-    if (p->L[0] % 4 == 0 && p->nrec_metal == 0)
+    /* whole-row fused step */
+    if (p->L[0] % 4 == 0)
         for (int ty : {1, 2, 4, 5})
             for (int mb : {1, 2})
                 for (int zc : {0, L2, 40, 32, 24, 20})

@@ -5,8 +5,10 @@
  * Same update as the two FP32 sweeps of fdtd_f32.cu (the reference main_calc,
  * FDTDcalc/FDTDsplitfieldMetal.c:242-329, in total-field form), with the same
  * floating point expressions, so the results are bit-identical to them.  For
- * plans with L0 % 4 == 0 and without stable-form metal cells (lossy and PEC
- * ordinary cells and lossy split cells run a compile-time variant, REC).
+ * plans with L0 % 4 == 0 (record cells -- lossy and PEC ordinary cells, lossy
+ * split cells, metal cells -- run a compile-time variant, REC; the
+ * stable-form E update of metal cells and the monitor samples of metal cells
+ * run in a second, small launch after the step, k_row_metal).
  *
  *   - a CTA owns TY whole x rows (y0 .. y0+TY-1) of one excitation and marches
  *     along z through a range of planes [z0, z1).  At stage z it computes
@@ -103,15 +105,55 @@ struct QuadTab {
     unsigned xm;
 };
 
-/* A record cell -- an ordinary ('n') cell that is lossy or PEC, or a split
- * cell with lossy media (RK_A): the update of the sweeps' general-cell path
- * (fdtd_f32.cu, general32_cell) from the same curls; t is the cell's total
- * field, ta its aux slot (read and written for RK_A only), both updated in
- * place.  The host admits no other record kind to this kernel.  Out of line:
- * record cells are rare and must not cost the quads registers. */
+/* A metal cell's stable-form or frozen component in the march: the aux slot
+ * from the old set (it is staged only where the quad is split; the caller
+ * stores the aux slots of every quad with a record cell) into ta; an H
+ * stable-form component updates t and ta from the backward curl of E's main
+ * slot (E - Ea, old set, from global memory), as the sweeps do; an E
+ * stable-form component is left for k_row_metal after the step, and a frozen
+ * one keeps its values.  Out of line from the record path (metal cells are
+ * rarer still). */
+template <bool EF>
+__device__ __noinline__ void row_metal_record(const P32 &p, const int b, const int px, const int j2, const Rec32 &r,
+                                              float *t, float *ta)
+{
+    const Geo &g = p.g;
+    const long long n3 = g.n3, bs = 3 * n3, l = px + (long long)g.pl * j2;
+    const float *Fa = (EF ? p.Ea : p.Ha) + b * bs;
+    float x[3] = {Fa[l], Fa[n3 + l], Fa[2 * n3 + l]};
+    if (!EF && r.kind == RK_STABLE) {
+        /* the stable form differentiates the MAIN slot of the other field */
+        const float sg = -1.0f;
+        const float *G = p.E + b * bs, *Ga = p.Ea + b * bs;
+        const Stn32 st = make_stn32(g, px % g.L0, px / g.L0, j2, false);
+        auto get = [&](int c, long long o) { return G[c * n3 + l + o] - Ga[c * n3 + l + o]; };
+        float ps[3], ms[3];
+        curl32<false>(get, st, ps, ms);
+        for (int c = 0; c < 3; c++) {
+            const float W = ps[c] + ms[c];
+            float xc = x[c];
+            float f = t[c] - xc;
+            f += 0.5f * xc;
+            xc = fmaf(sg * r.B1[c], W, r.A1[c] * xc);
+            f += 0.5f * xc;
+            t[c] = f + xc;
+            x[c] = xc;
+        }
+    }
+    for (int c = 0; c < 3; c++) ta[c] = x[c];
+}
+
+/* A record cell -- an ordinary ('n') cell that is lossy or PEC, a split cell
+ * with lossy media (RK_A), or a metal cell's stable-form or frozen component
+ * (row_metal_record) -- updated as the sweeps' general-cell path does
+ * (fdtd_f32.cu, general32_cell); t is the cell's total field, ta its aux
+ * slot, both updated in place; pl, mi the half curls of the other field's
+ * total.  Out of line: record cells are rare and must not cost the quads
+ * registers. */
 template <bool EF>
 __device__ __noinline__ void row_record(const P32 &p, const int k, const int b, const bool on_src, const int px,
-                                        const int ridx, const float *pl, const float *mi, float *t, float *ta)
+                                        const int j2, const int ridx, const float *pl, const float *mi, float *t,
+                                        float *ta)
 {
     const Geo &g = p.g;
     const float sg = EF ? 1.0f : -1.0f;
@@ -125,6 +167,10 @@ __device__ __noinline__ void row_record(const P32 &p, const int k, const int b, 
             t[c] = np + nm;
             ta[c] = nm;
         }
+        return;
+    }
+    if (r.kind == RK_STABLE || r.kind == RK_FROZEN) {
+        row_metal_record<EF>(p, b, px, j2, r, t, ta);
         return;
     }
     float W[3] = {pl[0] + mi[0], pl[1] + mi[1], pl[2] + mi[2]};
@@ -183,7 +229,7 @@ __device__ __forceinline__ void row_quad(const P32 &p, const int k, const int b,
         if (REC && isnan(bn[0])) { /* a record cell (marked by NaN in its first coefficient) */
             float t[3] = {el(out[0], i), el(out[1], i), el(out[2], i)};
             float ta[3] = {el(aux[0], i), el(aux[1], i), el(aux[2], i)}; /* staged where the quad is split */
-            row_record<EF>(p, k, b, on_src, px0 + i, __float_as_int(bn[1]), pl, mi, t, ta);
+            row_record<EF>(p, k, b, on_src, px0 + i, j2, __float_as_int(bn[1]), pl, mi, t, ta);
 #pragma unroll
             for (int cc = 0; cc < 3; cc++) {
                 set_el(out[cc], i, t[cc]);
@@ -462,6 +508,9 @@ __device__ __forceinline__ void row_march(const Row32 &r, const int rel, const i
                 const float4 gz0 = scale4(Ep[0], fzw), gz1 = scale4(Ep[1], fzw);
                 th.az = zi.ah;
                 th.gz = zi.gh;
+                /* the aux slots leave for split quads and quads with a record
+                 * cell (a metal cell's aux slot; zeros elsewhere) */
+                const bool qa = qs || (REC && (isnan(c[0].x) | isnan(c[0].y) | isnan(c[0].z) | isnan(c[0].w)));
                 row_quad<false, REC>(p, k, b, gy, zr, x0, zr == iIb, th, c, o, e, a, gy0, gy2, gz0, gz1, xn1, xn2, pyz);
                 /* the private slot is free: plane z+1's bh, H, aux leave */
                 if (z < z1) stage_h(z + 1);
@@ -469,7 +518,7 @@ __device__ __forceinline__ void row_march(const Row32 &r, const int rel, const i
                 if (own && z < z1) {
 #pragma unroll
                     for (int i = 0; i < 3; i++) st4(r.Hn + i * n3 + l, o[i]);
-                    if (qs) {
+                    if (qa) {
 #pragma unroll
                         for (int i = 0; i < 3; i++) st4(r.Han + i * n3 + l, a[i]);
                     }
@@ -510,10 +559,11 @@ __device__ __forceinline__ void row_march(const Row32 &r, const int rel, const i
                 const float xp1 = fxp * lds4(&HS(ze, ry, 1) + xqn).x, xp2 = fxp * lds4(&HS(ze, ry, 2) + xqn).x;
                 te.az = zi.ae;
                 te.gz = zi.ge;
+                const bool qae = qse || (REC && (isnan(ce[0].x) | isnan(ce[0].y) | isnan(ce[0].z) | isnan(ce[0].w)));
                 row_quad<true, REC>(p, k, b, gy, ze, x0, ze == iIb, te, ce, Ep, hp, ae, ey0, ey2, ez0, ez1, xp1, xp2, pyze);
 #pragma unroll
                 for (int i = 0; i < 3; i++) st4(r.En + i * n3 + le, Ep[i]);
-                if (qse) {
+                if (qae) {
 #pragma unroll
                     for (int i = 0; i < 3; i++) st4(r.Ean + i * n3 + le, ae[i]);
                 }
@@ -540,6 +590,63 @@ __device__ __forceinline__ void row_march(const Row32 &r, const int rel, const i
 #undef PE
 #undef TOP
 #undef HS
+}
+
+/* The metal cells of a step of form 6, after it: the stable-form E update,
+ * whose backward curls read H_new of the plane below and of the row above
+ * the cell (values the march no longer holds, or another CTA's), and the
+ * monitor samples of stable-form and frozen components, which are the main
+ * slot rather than the total field -- the sweeps' general-cell path
+ * (fdtd_f32.cu, general32_cell) on the old set (E, H aux, E aux) and the new
+ * one (H, H aux).  One thread per cell and excitation (blockIdx.y): the nh
+ * H cells, then the ne E cells. */
+__global__ void __launch_bounds__(128) k_row_metal(const Row32 r, const int rel, const int *hcells, const int nh,
+                                                   const int *ecells, const int ne)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nh + ne) return;
+    const P32 &p = r.p;
+    const Geo &g = p.g;
+    const int b = blockIdx.y;
+    const bool ef = i >= nh;
+    const long long l = ef ? ecells[i - nh] : hcells[i];
+    const long long n3 = g.n3, bs = 3 * n3;
+    const int j0 = (int)(l % g.L0), j1 = (int)((l / g.L0) % g.L1), j2 = (int)(l / g.pl);
+    const int q = row_monitor(p.d, j2);
+    const Rec32 rc = (ef ? p.erec : p.hrec)[__float_as_int((ef ? p.be : p.bh)[n3 + l])];
+    if (q < 0 && !(ef && rc.kind == RK_STABLE)) return; /* nothing else to do off the monitor planes */
+    const float sg = ef ? 1.0f : -1.0f;
+    const float *F = (ef ? p.E : p.H) + b * bs, *Fa = (ef ? p.Ea : p.Ha) + b * bs; /* the old set */
+    float mo[3];
+    if (rc.kind == RK_FROZEN) {
+        for (int c = 0; c < 3; c++) mo[c] = F[c * n3 + l] - Fa[c * n3 + l];
+    } else {
+        /* the stable form differentiates the MAIN slot of the other field */
+        const float *G = ef ? r.Hn + b * bs : p.E + b * bs, *Ga = ef ? r.Han + b * bs : p.Ea + b * bs;
+        const Stn32 st = make_stn32(g, j0, j1, j2, false);
+        auto get = [&](int c, long long o) { return G[c * n3 + l + o] - Ga[c * n3 + l + o]; };
+        float pl[3], mi[3];
+        curl32<false>(get, st, pl, mi);
+        for (int c = 0; c < 3; c++) {
+            const float W = pl[c] + mi[c];
+            float x = Fa[c * n3 + l];
+            float f = F[c * n3 + l] - x;
+            f += 0.5f * x;
+            x = fmaf(sg * rc.B1[c], W, rc.A1[c] * x);
+            f += 0.5f * x;
+            mo[c] = f;
+            if (ef) {
+                r.En[b * bs + c * n3 + l] = f + x;
+                r.Ean[b * bs + c * n3 + l] = x;
+            }
+        }
+    }
+    if (q >= 0) {
+        const int k = *p.s.base + rel;
+        const int px = j0 + g.L0 * j1;
+        row_ring(p.d, g.pl, b, k, q, ef ? 2 : 0)[px] = mo[0];
+        row_ring(p.d, g.pl, b, k, q, ef ? 3 : 1)[px] = mo[1];
+    }
 }
 
 template <int MAXT, int MB, bool REC>
@@ -707,6 +814,12 @@ void launch_row32_group(const RowGroup32 &g, int rel, int threads, int grid, siz
 {
     void *args[] = {(void *)&g, (void *)&rel};
     cudaLaunchKernel(row_group_kernel(threads, rec), dim3(grid), dim3(threads), args, smem, st);
+}
+
+void launch_row_metal(const Row32 &r, int rel, const int *hcells, int nh, const int *ecells, int ne, cudaStream_t st)
+{
+    if (nh + ne <= 0) return;
+    k_row_metal<<<dim3((nh + ne + 127) / 128, r.p.batch), 128, 0, st>>>(r, rel, hcells, nh, ecells, ne);
 }
 
 void launch_row32(const Row32 &r, int rel, int mb, cudaStream_t st)

@@ -99,6 +99,8 @@ struct smat_fdtd_plan {
     int *d_qorder = nullptr; /* kernel 6: quads with a PML x index first (nqp of them), then the others */
     int nqp = 0;
     int nrec_metal = 0;   /* records of stable-form or frozen components (metal cells) */
+    int *d_hmetal = nullptr, *d_emetal = nullptr; /* kernel 6: cells of those records, H and E side */
+    int nhmetal = 0, nemetal = 0;
     int nrec_split = 0;   /* records of split cells (lossy media in a PML) */
     int nstable = 0;
     int *d_hgen = nullptr, *d_egen = nullptr; /* record (general) cells of each sweep, in cell order */
@@ -153,6 +155,9 @@ Row32 make_row(const smat_fdtd_plan *p, bool xp);
 void enqueue_steps(smat_fdtd_plan *p, int rel0, int n, bool xp);
 void sweep_step(smat_fdtd_plan *p, const P32 &q, int rel, cudaStream_t st);
 void enqueue_update(smat_fdtd_plan *p, int rel, cudaStream_t st);
+/* one step of form 6 on stream st: the fused launch, the metal-cell launch
+ * after it (plans with metal cells), then the field sets swap */
+void launch_row_step(smat_fdtd_plan *p, bool xp, int rel, cudaStream_t st);
 int sm_count();
 void drop_graph(smat_fdtd_plan *p);
 } // namespace plan

@@ -221,28 +221,46 @@ def test_group_persistent_launch_needs_a_cta_per_excitation(built):
             assert np.array_equal(a, b_)
 
 
-def test_group_persistent_launch_refuses_metal(built):
-    """Mode 3 has no stable-form path: a member with metal cells is refused
-    and the group keeps its form."""
+def test_group_persistent_launch_with_metal_member(built):
+    """Mode 3 with a member holding metal cells (its stable-form E update and
+    metal monitor samples in a second launch after the group's step) and a
+    record-free member: each ends with the bits of the member stepped alone;
+    an out-of-range shape is refused and the group keeps its form."""
     from smatranem_gb300 import fdtd as f
     from smatranem_gb300 import workloads as W
-    L, seed, kw, iBTIin, batch = MEMBERS[3]
-    s = W.random_structure(L, seed=seed, **kw)
-    pr = W.prepare(s)
-    sm = W.random_structure((40, 17, 19, 3), seed=7, pml=(4, 4, 4), metals=0.02)
-    prm = W.prepare(sm)
-    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma,
-                       precision=f.FP32) as p, \
-            f.Plan.create(sm.L, sm.iBc, (5, 13, 7, 1), prm.invtau_R, prm.invtau_I, prm.mu, prm.epsi, prm.sigma,
-                          precision=f.FP32, pec=sm.pec) as pm:
-        with f.Group([p]) as g:
-            g.set_tuning(3, 2)
+    members = [
+        ((40, 17, 19, 3), 7, dict(pml=(4, 4, 4), metals=0.03, pec=0.02, iBc=(1, 1, -1)), (6, 12, 8, 1), 2),
+        MEMBERS[3],
+    ]
+    nsteps = 9
+    windows = [(0, 4), (4, 9)]
+    structs = []
+    for L, seed, kw, iBTIin, batch in members:
+        s = W.random_structure(L, seed=seed, **kw)
+        structs.append((s, W.prepare(s), iBTIin, batch, seed))
+    alone = []
+    for s, pr, iBTIin, batch, seed in structs:
+        with _setup(f, W, s, pr, iBTIin, batch, seed, nsteps) as p:
+            p.set_tuning(0, 4, 0, 0, 4)
+            for a, b in windows:
+                p.run(a, b)
+            alone.append(_result(p, batch))
+    plans = [_setup(f, W, s, pr, iBTIin, batch, seed, nsteps) for s, pr, iBTIin, batch, seed in structs]
+    try:
+        with f.Group(plans) as g:
             with pytest.raises(f.FdtdError):
                 g.set_tuning(3, 3)
-        with f.Group([p, pm]) as g:
-            with pytest.raises(f.FdtdError):
-                g.set_tuning(3, 1)
-            g.set_tuning(1, 1)
+            g.set_tuning(3, 1)
+            for a, b in windows:
+                g.run(a, b)
+        for p, ref, (_, _, _, batch, _) in zip(plans, alone, structs):
+            got = _result(p, batch)
+            for rb, gb in zip(ref, got):
+                for a, b_ in zip(rb, gb):
+                    assert np.all(np.isfinite(a)) and np.array_equal(a, b_)
+    finally:
+        for p in plans:
+            p.close()
 
 
 def test_group_autotune_and_errors(built):

@@ -413,8 +413,8 @@ def test_row_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
 
 
 ROW_REC_CASES = [
-    # record cells other than stable-form metal: lossy and PEC ordinary cells,
-    # split cells with lossy media
+    # record cells other than metal: lossy and PEC ordinary cells, split cells
+    # with lossy media
     ((40, 17, 19, 3), 41, dict(pml=(4, 4, 4), lossy=0.05, iBc=(1, 1, -1)), (5, 13, 7, -1)),
     ((48, 19, 21, 3), 44, dict(pml=(4, 4, 4), lossy=0.03, lossy_pml=0.2, iBc=(1, -1, 1)), (5, 15, 8, 1)),
     ((36, 10, 16, 2), 45, dict(pml=(0, 0, 4), pml_z_only=True, lossy_pml=0.3, pec=0.03, iBc=(0, 0, -1)),
@@ -479,18 +479,40 @@ def test_fp32_plan_independent_of_host_threads(built, monkeypatch):
                 assert np.array_equal(a, b_)
 
 
-def test_row_fused_refuses_metal_cells(built):
-    """Kernel 6 has no stable-form path: a plan with metal ('h', 'e', 'b')
-    cells is refused."""
+ROW_METAL_CASES = [
+    # metal cells ('h', 'e', 'b': stable-form and frozen components) with lossy
+    # and PEC cells; monitor planes through the metal; iBc wraps on every axis
+    ((40, 17, 19, 3), 47, dict(pml=(4, 4, 4), metals=0.04, lossy=0.03, pec=0.02, iBc=(1, -1, 1)), (6, 12, 8, 1)),
+    ((36, 14, 16, 2), 48, dict(pml=(0, 0, 3), pml_z_only=True, metals=0.05, iBc=(-1, 1, -1)), (4, 9, 6, -1)),
+    ((64, 12, 14, 2), 49, dict(pml=(5, 3, 3), metals=0.03, pec=0.03, iBc=(0, 0, 0)), (4, 9, 5, 1)),
+]
+
+
+@pytest.mark.parametrize("case", range(len(ROW_METAL_CASES)))
+def test_row_fused_metal_cells_bit_identical(built, case):
+    """Metal cells in kernel 6: the H stable-form update in the march (the
+    backward curl of E's main slot from the old set), the E stable-form update
+    and the monitor samples of stable-form and frozen components in the second
+    launch after the step -- bit for bit as the scalar sweeps, for whole
+    grids, z chunks and persistent CTAs, across field-set swaps."""
     from smatranem_gb300 import workloads as W
-    f = _fdtd()
-    L, seed, kw, iBTIin = FUSED_CASES[0]
+    L, seed, kw, iBTIin = ROW_METAL_CASES[case]
     s = W.random_structure(L, seed=seed, **kw)
     pr = W.prepare(s)
-    with f.Plan.create(s.L, s.iBc, iBTIin, pr.invtau_R, pr.invtau_I, pr.mu, pr.epsi, pr.sigma, precision=f.FP32,
-                       pec=s.pec) as p:
-        with pytest.raises(f.FdtdError):
-            p.set_tuning(6, 2, 4, 1, 0)
+    cont = np.asarray(pr.cont).view(np.uint8)
+    pl = L[0] * L[1]
+    metal = np.isin(cont, [ord("e"), ord("h"), ord("b")])
+    assert metal.any() and any(metal[z * pl:(z + 1) * pl].any() for z in iBTIin[:2])
+    nsteps = 9  # the stable form is not unconditionally stable: few steps
+    ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
+    tunings = [(6, ty, zc, 1, 0) for ty, zc in [(2, 5), (5, 0), (1, 3), (3, 0), (4, L[2])]
+               if _row_fits(L[0], ty, 1, min(zc, L[2]) if zc else L[2])]
+    assert len(tunings) >= 4
+    for tuning in tunings:
+        got = _run_fp32(s, pr, iBTIin, tuning, nsteps)
+        for rb, gb in zip(ref, got):
+            for a, b_ in zip(rb, gb):
+                assert np.all(np.isfinite(a)) and np.array_equal(a, b_), tuning
 
 
 def test_row_fused_refuses_bad_tunings(built):
