@@ -16,7 +16,7 @@ int host_expn(int N, double *out);
  * per step, stop-period*N steps (main :153-167). */
 int host_cw_schedule(int N, const int time_period[3], double *src, double *phase);
 
-/* Host worker threads for a loop over `work` cells: SMAT_HOST_THREADS when it
+/* Host worker threads for a loop over `work` cells: SMATRAN_HOST_THREADS when it
  * is set to 1..HOST_MAX_THREADS, else one per online core (at most 16) for a
  * million cells or more, else 1. */
 #define HOST_MAX_THREADS 64

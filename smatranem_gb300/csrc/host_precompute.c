@@ -141,7 +141,7 @@ int smat_remove_sigma(const int L[4], double *mu_, double *epsi_, const double *
 
 int host_threads(long long work)
 {
-    const char *e = getenv("SMAT_HOST_THREADS");
+    const char *e = getenv("SMATRAN_HOST_THREADS");
     if (e && *e) {
         const int n = atoi(e);
         if (n >= 1 && n <= HOST_MAX_THREADS) return n;

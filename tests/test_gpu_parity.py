@@ -471,7 +471,7 @@ def test_fp32_plan_independent_of_host_threads(built, monkeypatch):
         pr.epsi[3 * pick + c] += 1j * np.abs(pr.epsi[3 * pick + c].real) * rng.uniform(0.01, 0.3, pick.size)
     runs = []
     for nt in (1, 3, 16):
-        monkeypatch.setenv("SMAT_HOST_THREADS", str(nt))
+        monkeypatch.setenv("SMATRAN_HOST_THREADS", str(nt))
         runs.append(_run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), 9))
     for got in runs[1:]:
         for rb, gb in zip(runs[0], got):

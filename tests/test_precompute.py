@@ -73,7 +73,7 @@ def test_precompute_independent_of_host_threads(built, monkeypatch):
     pr = W.prepare(s)
     out = {}
     for nt in (1, 2, 5, 29, 64):
-        monkeypatch.setenv("SMAT_HOST_THREADS", str(nt))
+        monkeypatch.setenv("SMATRAN_HOST_THREADS", str(nt))
         cont, addr, ln = fdtd.set_address(s.L, pr.sigma, pr.mu, pr.epsi)
         coef = fdtd.coefficients(s.L, ln, pr.sigma, pr.mu, pr.epsi, cont, addr, pr.invtau_R, pr.invtau_I)
         out[nt] = (cont, addr, ln, coef)
@@ -83,3 +83,24 @@ def test_precompute_independent_of_host_threads(built, monkeypatch):
         assert out[1][2] == out[nt][2]
         for a, b in zip(out[1][3], out[nt][3]):
             assert np.array_equal(a, b), nt
+
+
+def test_host_threads_setting(built, monkeypatch):
+    """SMATRAN_HOST_THREADS sets the precompute's worker threads (1..64);
+    unset or out of range, small grids take one thread and large ones one per
+    core, at most 16."""
+    import ctypes
+    import os
+    from smatranem_gb300 import fdtd
+    ht = fdtd.lib().host_threads
+    ht.argtypes = [ctypes.c_longlong]
+    ht.restype = ctypes.c_int
+    for v, small in (("1", 1), ("5", 5), ("64", 64)):
+        monkeypatch.setenv("SMATRAN_HOST_THREADS", v)
+        assert ht(10) == small and ht(1 << 22) == small
+    cores = min(os.cpu_count() or 1, 16)
+    for v in ("65", "0", "x"):
+        monkeypatch.setenv("SMATRAN_HOST_THREADS", v)
+        assert ht(10) == 1 and 1 <= ht(1 << 22) <= 16
+    monkeypatch.delenv("SMATRAN_HOST_THREADS")
+    assert ht(10) == 1 and ht(1 << 22) == cores
