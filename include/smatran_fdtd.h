@@ -367,7 +367,11 @@ int smat_fdtd_time_kernels(smat_fdtd_plan *plan, int k_begin, int nsteps, double
  *             along z through z_chunk planes (0: persistent CTAs), four cells
  *             a thread, the next plane's inputs staged by cp.async;
  *             ctas_per_sm is its register bound (1..3 resident CTAs per SM);
- *             slots is not used; for plans with L0 % 4 == 0 (lossy and PEC
+ *             slots is the warp order (0: quads in order; 1: in blocks of a
+ *             multiple of 128 threads, at least 256, the last two warps --
+ *             mostly the halo row's -- trade places with the two before
+ *             them, so they share the SM sub-partitions of the split quads'
+ *             warps; the autotuner's choice); for plans with L0 % 4 == 0 (lossy and PEC
  *             ordinary cells, lossy split cells and metal cells run an
  *             out-of-line record update; plans with metal cells add a second,
  *             small launch per step for their stable-form E update and their

@@ -187,6 +187,7 @@ void enqueue_group(smat_fdtd_group *g, int rel0, int n)
                 r.nzc = 1;
                 r.ngroups = g->groups3[j];
                 r.nitems = g->groups3[j] * p->batch;
+                r.worder = 0;
             }
             launch_row32_group(G, rel0 + i, g->threads3, g->grid3, g->smem3, g->rec3, g->stream);
             /* members with metal cells: their second launch, before the sets swap */

@@ -172,6 +172,7 @@ struct Row32 {
     const int *qorder;          /* [L0/4]: quads whose x index lies in a PML, then the others */
     int nqp;                    /* how many of the first kind */
     int has_rec;                /* the plan has record cells (lossy, PEC or metal cells) */
+    int worder;                 /* 1: the last two warps trade places with the two before them */
 };
 
 /* Several plans in one persistent launch of form 6 (a group's form 3): CTAs

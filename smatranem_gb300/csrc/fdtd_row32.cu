@@ -332,13 +332,23 @@ __device__ __forceinline__ void row_march(const Row32 &r, const int rel, const i
      * rest, so that whole warps run the ordinary update with no split-cell
      * branch (in x order within each group: r.qorder) */
     const int nqp = r.nqp, nqi = NQ - nqp;
+    /* the thread's place in that order: with r.worder the last two warps
+     * (mostly the halo row's quads, which skip the E update) trade places
+     * with the two before them, so that they share the SM sub-partitions of
+     * warps 0 and 1 (the split quads); warps go to the four sub-partitions
+     * by warp index mod 4 */
+    int qt = tid;
+    if (r.worder && (T & 127) == 0 && T >= 256) {
+        const int w = qt >> 5, W = T >> 5;
+        if (w >= W - 4) qt += w < W - 2 ? 64 : -64;
+    }
     int ry = TY, xq = NQ - 1;
-    const bool xlive = tid < NC; /* threads past the tile's quads idle */
-    if (tid < NR * nqp) {
-        ry = tid / nqp;
-        xq = r.qorder[tid % nqp];
+    const bool xlive = qt < NC; /* threads past the tile's quads idle */
+    if (qt < NR * nqp) {
+        ry = qt / nqp;
+        xq = r.qorder[qt % nqp];
     } else if (xlive) {
-        const int u = tid - NR * nqp;
+        const int u = qt - NR * nqp;
         ry = u / nqi;
         xq = r.qorder[nqp + u % nqi];
     }

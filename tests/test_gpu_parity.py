@@ -400,9 +400,12 @@ def test_row_fused_fp32_is_bit_identical_to_the_sweeps(built, case):
     pr = W.prepare(s)
     nsteps = 37
     ref = _run_fp32(s, pr, iBTIin, (0, 4, 0, 0, 4), nsteps)
-    tunings = [(6, ty, zc, mb, 0) for ty, zc, mb in
-               [(1, L[2], 1), (2, 5, 2), (4, 3, 1), (3, 1, 3), (4, 7, 2), (8, 40, 1), (2, 2, 3), (5, L[2], 1),
-                (1, 4, 3), (1, 2, 2), (1, 0, 1), (2, 0, 2), (5, 0, 1), (3, 0, 3)]
+    # the fifth value: the warp order (1: the last two warps trade places with
+    # the two before them, in blocks of a multiple of 128 threads, >= 256)
+    tunings = [(6, ty, zc, mb, wo) for ty, zc, mb, wo in
+               [(1, L[2], 1, 0), (2, 5, 2, 0), (4, 3, 1, 0), (3, 1, 3, 0), (4, 7, 2, 0), (8, 40, 1, 0), (2, 2, 3, 0),
+                (5, L[2], 1, 0), (1, 4, 3, 0), (1, 2, 2, 0), (1, 0, 1, 0), (2, 0, 2, 0), (5, 0, 1, 0), (3, 0, 3, 0),
+                (15, 0, 1, 1), (15, 7, 1, 1), (5, 0, 1, 1)]
                if _row_fits(L[0], ty, mb, min(zc, L[2]) if zc else L[2])]
     assert len(tunings) >= 5
     for tuning in tunings:
@@ -528,8 +531,8 @@ def test_row_fused_refuses_bad_tunings(built):
         p.set_tuning(6, 2, 0, 1, 0)
         assert tuple(p.get_tuning())[:4] == (6, 2, 0, 1)
         for bad in [(6, 0, 0, 1, 0), (6, 17, 0, 1, 0), (6, 2, -1, 1, 0), (6, 2, 0, 0, 0), (6, 2, 0, 4, 0),
-                    (6, 200, 0, 1, 0), (7, 2, 0, 1, 0), (-1, 2, 0, 1, 0), (1, 8, 40, 0, 5), (3, 8, 40, 0, 5),
-                    (4, 2, 2, 0, 0), (5, 4, 40, 1, 4)]:
+                    (6, 200, 0, 1, 0), (6, 2, 0, 1, 2), (6, 2, 0, 1, -1), (7, 2, 0, 1, 0), (-1, 2, 0, 1, 0),
+                    (1, 8, 40, 0, 5), (3, 8, 40, 0, 5), (4, 2, 2, 0, 0), (5, 4, 40, 1, 4)]:
             with pytest.raises(f.FdtdError):
                 p.set_tuning(*bad)
             assert tuple(p.get_tuning())[:4] == (6, 2, 0, 1)
