@@ -104,3 +104,26 @@ def test_host_threads_setting(built, monkeypatch):
         assert ht(10) == 1 and 1 <= ht(1 << 22) <= 16
     monkeypatch.delenv("SMATRAN_HOST_THREADS")
     assert ht(10) == 1 and ht(1 << 22) == cores
+
+
+def test_host_parallel_for_covers_each_index_once(built):
+    """The precompute's range splitter: for any count and thread count
+    (more threads than items, none, past the cap) every index of [0, n) is
+    handed out exactly once, in contiguous ranges."""
+    import ctypes
+    from smatranem_gb300 import fdtd
+    fn_t = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong)
+    pf = fdtd.lib().host_parallel_for
+    pf.argtypes = [ctypes.c_longlong, ctypes.c_int, fn_t, ctypes.c_void_p]
+    pf.restype = None
+    for n, nt in [(0, 4), (1, 1), (1, 8), (7, 3), (100, 16), (5, 64), (1000, 100), (33, 0), (33, -2)]:
+        seen = np.zeros(n, np.int64)
+        ranges = []
+
+        def cb(ctx, lo, hi):
+            ranges.append((lo, hi))
+            seen[lo:hi] += 1
+
+        pf(n, nt, fn_t(cb), None)
+        assert np.all(seen == 1), (n, nt)
+        assert all(lo < hi for lo, hi in ranges) and len(ranges) <= max(1, min(nt, 64, n))
